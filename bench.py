@@ -1,0 +1,344 @@
+"""Benchmark: P1-tet diffusion + mass assembly (FP64) on the Kuhn-split unit
+cube, 64^3 cubes x 6 (1,572,864 elements, 274,625 nodes), per-element kappa
+~ lognormal(0,1), jittered interior nodes -- the workload the headline metric
+"P1-tet elements assembled/s" is quoted on.
+
+One step = one assembly pass producing the CSR values of K(kappa) and M.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm prints ``value`` (elements/s, inputs resident in HBM, L2 flushed
+between steps), ``e2e`` (the same through the public API with the inputs
+copied from pinned host memory and both value arrays copied back, every
+step), the roofline of the assembly pass, the CPU baseline (the oracle on
+the host cores) and the SM clocks seen during the timed region.  The
+reference arm times the reference's op sequence (a restatement in torch) on
+the host cores.  With torchrun, every rank assembles its own copy of the
+mesh ("replicas only": the path has no exchange step).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "P1-tet elements assembled/s vs ref torch-GPU (FP64, <=1e-12 rel); batched solves/s"
+WORKLOAD = "diffusion_mass_tet_64: P1 tet K(kappa)+M, 64^3 cubes x 6 Kuhn, 1,572,864 elements, 274,625 nodes, FP64"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1 and not torch.distributed.is_initialized():
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        torch.distributed.init_process_group(backend)
+    return ws, rank, local
+
+
+def _barrier(ws):
+    if ws > 1:
+        torch.distributed.barrier()
+
+
+def _max_over_ranks(x, ws, dev):
+    if ws == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) of the SM clock and throttle reasons."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "",
+                                 f".clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax.append(float(f[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic():
+    """DRAM bytes per assembly pass from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_matrix_tet4_diffusion_mass.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh).get("dram_bytes_per_pass")
+    return None
+
+
+def algorithmic_bytes(N, E, nnz):
+    """Inputs read once, outputs written once, int32 indices, slot map
+    included: 24N (points) + 16E (connectivity) + 8E (kappa) + 64E (4x4 int32
+    slot map) + 2 x 8 nnz (K and M values)."""
+    return 24 * N + 16 * E + 8 * E + 64 * E + 16 * nnz
+
+
+def cpu_baseline(wl, budget_s=12.0):
+    from oracle import fem_oracle as O
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    pts = wl.mesh.points
+    conn = wl.mesh.elements()
+    edges, slot = O.element_pattern(conn, wl.mesh.n_points)
+    kappa = wl.data["kappa"]
+    O.reference_call_diffusion_mass(pts[:0], conn[:0], kappa[:0], slot[:0], edges[:, :0], with_hash=False)
+    runs, t0 = 0, time.perf_counter()
+    while True:
+        O.reference_call_diffusion_mass(pts, conn, kappa, slot, edges)
+        runs += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or runs >= 5:
+            break
+    E = conn.shape[0]
+    return {"value": E * runs / el, "unit": "elements/s", "cores": threads, "kind": "port",
+            "sample": f"{runs} full passes ({E} elements each, K+M incl. per-call SparseMatrix hashing) "
+                      f"of the reference op sequence in torch on {threads} host threads, {el:.1f} s"}
+
+
+def run_ours(args, ws, rank, local):
+    import tensormesh_gb300 as tg
+    from tensormesh_gb300 import _lib, workloads as W
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    wl = W.diffusion_mass_tet(64)
+    mesh = wl.mesh.to(dev)
+    kappa = wl.data["kappa"].to(dev)
+    K_asm = tg.LaplaceElementAssembler.from_mesh(mesh)
+    M_asm = tg.MassElementAssembler.from_assembler(K_asm)
+    N, E, nnz = mesh.n_points, mesh.n_elements, K_asm.edges.shape[1]
+    ed = {"kappa": kappa}
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)      # > 129 MB of L2
+    kb, ke = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for ev in (kb, ke):
+        ev.record()
+    for _ in range(args.warmup):
+        tg.assemble_forms([K_asm, M_asm], mesh.points, ed)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kbeg = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kend = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for ev in kbeg + kend:
+        ev.record()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    _barrier(ws)
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record()
+        tg.assemble_forms([K_asm, M_asm], mesh.points, ed, _events=(kbeg[k], kend[k]))
+        ends[k].record()
+    torch.cuda.synchronize()
+    _barrier(ws)
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    kern_ms = [s.elapsed_time(e) for s, e in zip(kbeg, kend)]
+    ms = _max_over_ranks(statistics.mean(step_ms), ws, dev)
+    kms = statistics.mean(kern_ms)
+
+    # e2e: public API, host buffers, copies inside the timed region
+    pts_h = wl.mesh.points.clone().pin_memory()
+    kap_h = wl.data["kappa"].clone().pin_memory()
+    pts_d = torch.empty_like(mesh.points)
+    kap_d = torch.empty_like(kappa)
+    K_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    M_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    for _ in range(max(1, args.warmup)):
+        pts_d.copy_(pts_h, non_blocking=True)
+        kap_d.copy_(kap_h, non_blocking=True)
+        K, M = tg.assemble_forms([K_asm, M_asm], pts_d, {"kappa": kap_d})
+        K_h.copy_(K, non_blocking=True)
+        M_h.copy_(M, non_blocking=True)
+    torch.cuda.synchronize()
+    e_s = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    e_e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    _barrier(ws)
+    for k in range(args.steps):
+        flush.zero_()
+        e_s[k].record()
+        pts_d.copy_(pts_h, non_blocking=True)
+        kap_d.copy_(kap_h, non_blocking=True)
+        K, M = tg.assemble_forms([K_asm, M_asm], pts_d, {"kappa": kap_d})
+        K_h.copy_(K, non_blocking=True)
+        M_h.copy_(M, non_blocking=True)
+        e_e[k].record()
+    torch.cuda.synchronize()
+    e2e_ms = _max_over_ranks(statistics.mean(s.elapsed_time(e) for s, e in zip(e_s, e_e)), ws, dev)
+    h2d = pts_h.numel() * 8 + kap_h.numel() * 8
+    d2h = 2 * nnz * 8
+
+    peak, peak_kind = _peaks()
+    abytes = algorithmic_bytes(N, E, nnz)
+    achieved = abytes / (ms * 1e-3) / 1e9
+    traffic = _traffic()
+    line = {
+        "metric": METRIC,
+        "value": E * ws / (ms * 1e-3),
+        "unit": "elements/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded jittered Kuhn-split cube, lognormal kappa)",
+        "config": {"workload": WORKLOAD, "elements": E, "nodes": N, "nnz": nnz, "forms": ["diffusion", "mass"],
+                   "quadrature_order": 2, "l2": "flushed between steps (512 MB write)",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": E * ws / (e2e_ms * 1e-3), "unit": "elements/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "k_matrix + k_matrix_finalize (one assembly pass)",
+                     "algorithmic_bytes": abytes, "k_matrix_ms": kms,
+                     "fp64_gflops": 125.0 * E / (ms * 1e-3) / 1e9},
+        "clocks": clocks,
+        "gpu_launches": 2 * args.steps,
+        "wall_s_timed_region": wall,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(wl)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_reference(args, ws, rank, local):
+    if rank != 0:
+        return
+    from oracle import fem_oracle as O
+    from tensormesh_gb300 import workloads as W
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    wl = W.diffusion_mass_tet(64)
+    pts, conn, kappa = wl.mesh.points, wl.mesh.elements(), wl.data["kappa"]
+    edges, slot = O.element_pattern(conn, wl.mesh.n_points)
+    E = conn.shape[0]
+    for _ in range(args.warmup):
+        O.reference_call_diffusion_mass(pts[:E // 16], conn[:E // 16], kappa[:E // 16], slot[:E // 16 * 16],
+                                        edges, with_hash=False)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.reference_call_diffusion_mass(pts, conn, kappa, slot, edges)
+        times.append(time.perf_counter() - t0)
+    s = statistics.mean(times)
+    line = {"metric": METRIC, "impl": "reference", "value": E / s, "unit": "elements/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded jittered Kuhn-split cube, lognormal kappa)",
+            "config": {"workload": WORKLOAD, "elements": E, "parallelism": "host cores"},
+            "cpu_baseline": {"value": E / s, "unit": "elements/s", "cores": threads, "kind": "port",
+                             "sample": f"full workload per step, reference op sequence restated in torch "
+                                       f"(CPU, {threads} threads), incl. per-call SparseMatrix hashing"},
+            "e2e": {"value": E / s, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if torch.cuda.is_available() and not args.no_gpu_reference:
+        dev = torch.device("cuda", local)
+        pd, cd, kd, sd, ed = pts.to(dev), conn.to(dev), kappa.to(dev), slot.to(dev), edges.to(dev)
+        for _ in range(max(3, args.warmup)):
+            O.reference_call_diffusion_mass(pd, cd, kd, sd, ed)
+        torch.cuda.synchronize()
+        res = {}
+        for with_hash in (True, False):
+            ts = []
+            for _ in range(max(3, min(args.steps, 10))):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                O.reference_call_diffusion_mass(pd, cd, kd, sd, ed, with_hash=with_hash)
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+            res["with_hash" if with_hash else "without_hash"] = E / statistics.median(ts)
+        line["torch_gpu"] = {"value": res["with_hash"], "value_without_hash": res["without_hash"],
+                             "unit": "elements/s",
+                             "note": "the reference op sequence (torch einsum/inverse/det/index_add_) on the GPU"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-gpu-reference", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = _dist()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, local)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

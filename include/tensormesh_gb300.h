@@ -1,0 +1,271 @@
+/*
+ * tensormesh_gb300 -- C ABI of the GB300 (sm_103a) tensorized FEM assembly path.
+ *
+ * Plain pointers and sizes only.  Every array argument named "device" lives
+ * in GPU memory owned by the caller; the library allocates nothing on the
+ * GPU inside these calls and keeps no state between them.  Calls are
+ * stream-ordered on the stream passed in (0 = legacy default stream) and
+ * return a status code (TM_OK = 0).  A launch error is reported as
+ * TM_ERR_CUDA; tm_last_error_message() gives the text.
+ *
+ * The reference (TensorMesh) is pure Python on PyTorch and has no native
+ * interface; each entry point below cites the reference function whose work
+ * it replaces.  The Python package tensormesh_gb300 binds these with ctypes
+ * (tensormesh_gb300/_lib.py).
+ */
+#ifndef TENSORMESH_GB300_H
+#define TENSORMESH_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* tm_stream_t;   /* == cudaStream_t */
+
+/* ---- status codes ------------------------------------------------------ */
+#define TM_OK                 0
+#define TM_ERR_INVALID_ARG    1   /* bad size, null pointer, unsupported combination */
+#define TM_ERR_UNSUPPORTED    2   /* element type / form not built */
+#define TM_ERR_CUDA           3   /* kernel launch or runtime error */
+#define TM_ERR_PLAN           4   /* plan construction failed (host) */
+#define TM_ERR_TOO_LARGE      5   /* size above a documented limit */
+
+/* ---- element types (element/element_type.py:57-87) --------------------- */
+#define TM_TRI3   0   /* "triangle"  */
+#define TM_TET4   1   /* "tetra"     */
+#define TM_TRI6   2   /* "triangle6" */
+#define TM_TET10  3   /* "tetra10"   */
+
+/* ---- floating types ---------------------------------------------------- */
+#define TM_F64 0
+#define TM_F32 1
+
+/* ---- bilinear forms (bit mask) ----------------------------------------- */
+#define TM_FORM_DIFFUSION   1   /* kappa_e grad u . grad v  (assemble/builtin.py:61-62) */
+#define TM_FORM_MASS        2   /* rho u v                  (assemble/builtin.py:99-100) */
+#define TM_FORM_ELASTICITY  4   /* B^T C(E_e, nu) B         (assemble/builtin.py:172-178) */
+
+/* ---- linear-form sources ------------------------------------------------ */
+#define TM_SOURCE_NODAL  0   /* f given at nodes, interpolated with phi (node_assembler.py:389) */
+#define TM_SOURCE_CONST  1   /* constant c                  (builtin.py:730-771) */
+#define TM_SOURCE_QUAD   2   /* f given per quadrature point (builtin.py:773-813) */
+
+const char* tm_error_string(int status);
+const char* tm_last_error_message(void);
+int tm_version(void);
+
+/*
+ * Reference-element tables of one (element type, quadrature order): a flat
+ * float64 device array [w(Q) | phi(Q*B) | dphi(Q*D*B) | mass_hat(B*B) |
+ * load_hat(B) | wsum], see tensormesh_gb300/element.py packed_tables().
+ * Replaces the quadrature / shape-function caches of
+ * element/transformation.py:266-367 and element/element.py:557-872.
+ */
+typedef struct tm_element_tables {
+    int32_t element_type;      /* TM_TRI3 ... */
+    int32_t n_quad;            /* Q */
+    const double* packed;      /* device */
+} tm_element_tables;
+
+/*
+ * Element-chunk reduction plan (built once per mesh by tm_plan_build and
+ * copied to the device).  Elements are processed in chunks of chunk_elems
+ * consecutive entries of the processing order; each chunk reduces the
+ * contributions its elements make to a target (a CSR position for matrix
+ * plans, a node for node plans) in shared memory, in a fixed order, and
+ * writes either the final value (the target is touched by this chunk only)
+ * or a partial that tm finalisation sums in chunk order.  No atomics: the
+ * result is bitwise reproducible.
+ */
+typedef struct tm_chunk_plan {
+    int64_t n_elements;
+    int32_t n_basis;
+    int32_t n_local;           /* entries per element: B(B+1)/2 (matrix) or B (node) */
+    int32_t chunk_elems;
+    int32_t n_chunks;
+    int64_t n_targets;         /* nnz (matrix) or n_points (node) */
+    int32_t n_shared;          /* targets with contributions from >1 chunk */
+    int32_t n_partials;
+    const int32_t* elem_perm;      /* [E] processing position -> element id */
+    const int32_t* conn;           /* [E*B] connectivity in processing order */
+    const int32_t* chunk_begin;    /* [n_chunks+1] */
+    const int32_t* slot_ptr;       /* [n_chunk_slots+1] */
+    const uint16_t* contrib;       /* [n_contrib] ((e_local*n_local + l) << 1) | transpose */
+    const int32_t* slot_target;    /* [n_chunk_slots] >= 0 target; < 0: -(partial+1) */
+    const int32_t* slot_mirror;    /* [n_chunk_slots] transposed CSR position or -1 */
+    const int32_t* shared_ptr;     /* [n_shared+1] partial ranges, chunk order */
+    const int32_t* shared_target;  /* [n_shared] */
+    const int32_t* shared_mirror;  /* [n_shared] */
+} tm_chunk_plan;
+
+/*
+ * Host-side plan construction (replaces ElementAssembler.from_mesh,
+ * assemble/element_assembler.py:811-851, and NodeAssembler.from_elements,
+ * assemble/node_assembler.py:665-670).  conn is a host int64 [E*B] array,
+ * perm an optional host int32 [E] processing order (NULL = identity).
+ * kind: 0 = matrix (CSR pattern + element->CSR slot map + chunk plan),
+ *       1 = node   (chunk plan onto nodes).
+ * slot_map: optional host int64 [E*B*B] slot map of an earlier matrix plan of
+ * the same mesh (NULL = build the pattern); lets one mesh carry chunk plans
+ * of several chunk sizes.
+ * The CSR pattern is the reference's: unique (row, col) pairs sorted
+ * row-major, and the slot map is the element-major, i-major, j-minor
+ * position of every local pair in that pattern.
+ */
+typedef struct tm_host_plan tm_host_plan;
+#define TM_PLAN_KIND_MATRIX 0
+#define TM_PLAN_KIND_NODE   1
+int tm_plan_build(const int64_t* conn, int64_t n_elements, int32_t n_basis, int64_t n_points,
+                  int32_t kind, int32_t chunk_elems, const int32_t* perm, const int64_t* slot_map,
+                  tm_host_plan** out);
+/* array ids for tm_plan_array_size / tm_plan_copy_array */
+#define TM_PLAN_EDGE_ROW      0   /* int32  [nnz]       */
+#define TM_PLAN_EDGE_COL      1   /* int32  [nnz]       */
+#define TM_PLAN_SLOT          2   /* int64  [E*B*B]     */
+#define TM_PLAN_CHUNK_BEGIN   3   /* int32               */
+#define TM_PLAN_SLOT_PTR      4   /* int32               */
+#define TM_PLAN_CONTRIB       5   /* uint16              */
+#define TM_PLAN_SLOT_TARGET   6   /* int32               */
+#define TM_PLAN_SLOT_MIRROR   7   /* int32               */
+#define TM_PLAN_SHARED_PTR    8   /* int32               */
+#define TM_PLAN_SHARED_TARGET 9   /* int32               */
+#define TM_PLAN_SHARED_MIRROR 10  /* int32               */
+#define TM_PLAN_CONN          11  /* int32  [E*B]        */
+#define TM_PLAN_PERM          12  /* int32  [E]          */
+int64_t tm_plan_array_size(const tm_host_plan* plan, int32_t array_id);   /* elements */
+int tm_plan_copy_array(const tm_host_plan* plan, int32_t array_id, void* host_dst);
+/* scalars: 0 nnz, 1 n_chunks, 2 n_chunk_slots, 3 n_contrib, 4 n_shared, 5 n_partials, 6 n_local */
+int64_t tm_plan_scalar(const tm_host_plan* plan, int32_t which);
+void tm_plan_free(tm_host_plan* plan);
+
+/*
+ * Bilinear-form assembly into CSR values (ElementAssembler.__call__,
+ * assemble/element_assembler.py:231-445, with Transformation.batch_shape_grad_jxw,
+ * element/transformation.py:1219-1276, Element.eval_shape_grad,
+ * element/element.py:875-968, and ReduceProjector.__call__,
+ * assemble/projector.py:95-123, fused in one pass).
+ * Outputs: out_* [nnz] (diffusion, mass) and [nnz*D*D] (elasticity, blocks
+ * in [edge, a, b] order as SparseMatrix.from_block_coo expects,
+ * sparse/matrix.py:332-381).  workspace: device, >= tm_matrix_workspace_bytes().
+ */
+typedef struct tm_matrix_args {
+    int32_t dtype;             /* TM_F64 / TM_F32: points, coefficients and outputs */
+    int32_t forms;             /* TM_FORM_* mask; ELASTICITY cannot be combined */
+    int64_t n_points;
+    const void* points;        /* device [N*D] */
+    const void* kappa;         /* device [E] per-element diffusion coefficient, or NULL */
+    double kappa_scale;        /* multiplies kappa (or is kappa when NULL) */
+    double mass_scale;         /* rho */
+    const void* young;         /* device [E] per-element Young's modulus, or NULL */
+    double young_scale;        /* multiplies young (or is E when NULL) */
+    double poisson;            /* nu */
+    void* out_diffusion;
+    void* out_mass;
+    void* out_elasticity;
+    void* workspace;
+    tm_element_tables tables;
+    tm_chunk_plan plan;
+    void* event_begin;         /* optional cudaEvent_t recorded before the element-chunk kernel */
+    void* event_end;           /* optional cudaEvent_t recorded after it (before finalisation) */
+} tm_matrix_args;
+size_t tm_matrix_workspace_bytes(const tm_matrix_args* args);
+int tm_assemble_matrix(const tm_matrix_args* args, tm_stream_t stream);
+
+/*
+ * Linear-form assembly into a nodal vector (NodeAssembler.__call__,
+ * assemble/node_assembler.py:242-409, with const_node_assembler /
+ * func_node_assembler, assemble/builtin.py:730-813).
+ * values: TM_SOURCE_NODAL [N*width], TM_SOURCE_QUAD [E*Q*width] in element
+ * order, ignored for TM_SOURCE_CONST (constant[width]).  out [N*width].
+ */
+typedef struct tm_vector_args {
+    int32_t dtype;
+    int32_t source;
+    int32_t width;             /* components per node, 1..3 */
+    int64_t n_points;
+    const void* points;
+    const void* values;
+    double constant[3];
+    void* out;
+    void* workspace;
+    tm_element_tables tables;
+    tm_chunk_plan plan;        /* node plan */
+} tm_vector_args;
+size_t tm_vector_workspace_bytes(const tm_vector_args* args);
+int tm_assemble_vector(const tm_vector_args* args, tm_stream_t stream);
+
+/*
+ * Physical shape gradients and |det J| w per element and quadrature point
+ * (Transformation.batch_shape_grad_jxw, element/transformation.py:1219-1276).
+ * grad [E*Q*B*D], jxw [E*Q], element order, float64.
+ */
+int tm_shape_grad_jxw(int64_t n_elements, const int32_t* conn, const double* points,
+                      tm_element_tables tables, double* grad, double* jxw, tm_stream_t stream);
+
+/*
+ * Deterministic scatter-add (ReduceProjector.__call__, assemble/projector.py:95-123,
+ * and SparseProjector.__call__, :217-242): out[t, :] = sum over k in
+ * [seg_ptr[t], seg_ptr[t+1]) of x[src[k], :], in src order.
+ * src/seg_ptr are the inverse of the projector's index map (tm_project_plan).
+ */
+int tm_project_reduce(int32_t dtype, int64_t n_to, int64_t width, const int64_t* seg_ptr,
+                      const int64_t* src, const void* x, void* out, tm_stream_t stream);
+
+/*
+ * Physical coordinates of the quadrature points, x_q = sum_b phi_b(q) X_b
+ * (the "x" argument of NodeAssembler forms, node_assembler.py:302-303),
+ * xq [E*Q*D], element order.  Used to evaluate func_node_assembler sources.
+ */
+int tm_quadrature_points(int32_t dtype, int64_t n_elements, const int32_t* conn, const void* points,
+                         tm_element_tables tables, void* xq, tm_stream_t stream);
+
+/* ---- sparse linear algebra (SparseMatrix @ and solve) ------------------- */
+/*
+ * CSR (block == 1) or block-CSR (block == H, HxH row-major blocks) operator.
+ * Rows sorted by column are not required.
+ */
+typedef struct tm_linear_operator {
+    int32_t dtype;             /* TM_F64 / TM_F32 */
+    int32_t block;             /* 1, 2 or 3 */
+    int64_t n_rows;            /* block rows */
+    const int64_t* row_ptr;    /* device [n_rows+1] */
+    const int32_t* col;        /* device [nnz_blocks] block columns */
+    const void* values;        /* device [nnz_blocks*block*block] */
+} tm_linear_operator;
+
+/* y = alpha A x + beta y  (SparseMatrix.__matmul__, inherited from torch-sla) */
+int tm_spmv(const tm_linear_operator* A, const void* x, void* y, double alpha, double beta,
+            tm_stream_t stream);
+
+/*
+ * Jacobi-preconditioned CG for SPD A (replaces SparseMatrix.solve for SPD
+ * systems; in-tree templates: sparse/solve/torch_solve.py:70-248).
+ * tm_pcg_start computes diag(A)^-1, r = b - A x, z, p and the scalars;
+ * tm_pcg_iterate runs n_iter iterations without host synchronisation.
+ * scalars (device float64 [8]): 0 rz, 1 pAp, 2 rz_new, 3 r.r, 4 b.b,
+ * 5 iterations done, 6 flag (0 running, 2 breakdown: pAp <= 0 or NaN).
+ * A breakdown freezes x; convergence is decided by the caller from r.r/b.b.
+ */
+typedef struct tm_pcg_args {
+    tm_linear_operator A;
+    const void* b;
+    void* x;                   /* initial guess on entry, solution on exit */
+    void* r;
+    void* z;
+    void* p;
+    void* q;
+    void* dinv;
+    double* scalars;
+    double* partials;          /* device, tm_pcg_partials_bytes() */
+} tm_pcg_args;
+size_t tm_pcg_partials_bytes(void);
+int tm_pcg_start(const tm_pcg_args* args, tm_stream_t stream);
+int tm_pcg_iterate(const tm_pcg_args* args, int32_t n_iter, tm_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TENSORMESH_GB300_H */

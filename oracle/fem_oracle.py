@@ -1,0 +1,375 @@
+"""Oracle for the tensorized-assembly path -- TEST INFRASTRUCTURE ONLY.
+
+A CPU restatement, in plain torch/numpy FP64, of the reference's assembly
+algorithm (TensorMesh).  It follows the reference's own op sequence --
+gather of element coordinates, transposed-Jacobian einsum, batched
+``torch.inverse``, gradient einsum, ``|det J| * w``, the integrand, the
+quadrature contraction and the ``index_add_`` scatter -- so that it can be
+compared with the reference on the golden fixtures and then used as the
+checker of the CUDA path.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
+``bench.py`` import this module.  The product (``tensormesh_gb300``) never
+does: it has no CPU path.
+"""
+from typing import Dict, Optional, Sequence, Tuple
+
+import hashlib
+import numpy as np
+import scipy.sparse
+import scipy.sparse.linalg
+import torch
+
+DT = torch.float64
+
+# ---------------------------------------------------------------------------
+# Quadrature rules (element/quadrature.py:68-166).  Same decimal tables as the
+# reference for orders 1-4, so that the oracle reproduces its rounding.
+# ---------------------------------------------------------------------------
+_TRI_W = {
+    1: [0.5],
+    2: [0.16666666666666666] * 3,
+    3: [-0.28125, 0.260416666666667, 0.260416666666667, 0.260416666666667],
+    4: [0.111690794839006, 0.054975871827661, 0.111690794839006,
+        0.054975871827661, 0.111690794839006, 0.054975871827661],
+}
+_TRI_P = {
+    1: [[0.3333333333333333, 0.3333333333333333]],
+    2: [[0.16666666666666666, 0.16666666666666666], [0.6666666666666666, 0.16666666666666666],
+        [0.16666666666666666, 0.6666666666666666]],
+    3: [[0.333333333333333, 0.333333333333333], [0.2, 0.6], [0.6, 0.2], [0.2, 0.2]],
+    4: [[0.445948490915965, 0.10810301816807], [0.0915762135097699, 0.816847572980459],
+        [0.10810301816807, 0.445948490915965], [0.816847572980459, 0.091576213509771],
+        [0.445948490915965, 0.445948490915965], [0.091576213509771, 0.0915762135097699]],
+}
+_TET_W = {
+    1: [0.16666666666666666],
+    2: [0.041666666666666664] * 4,
+    3: [-0.13333333333333333, 0.075, 0.075, 0.075, 0.075],
+    4: [-0.01315555555555555] + [0.007622222222222217] * 4 + [0.02488888888888888] * 6,
+}
+_TET_P = {
+    1: [[0.25, 0.25, 0.25]],
+    2: [[0.5854101966249685, 0.1381966011250105, 0.1381966011250105],
+        [0.1381966011250105, 0.1381966011250105, 0.1381966011250105],
+        [0.1381966011250105, 0.1381966011250105, 0.5854101966249685],
+        [0.1381966011250105, 0.5854101966249685, 0.1381966011250105]],
+    3: [[0.25, 0.25, 0.25], [0.5, 0.1666666666666667, 0.1666666666666667],
+        [0.1666666666666667, 0.1666666666666667, 0.1666666666666667],
+        [0.1666666666666667, 0.1666666666666667, 0.5],
+        [0.1666666666666667, 0.5, 0.1666666666666667]],
+    4: [[0.25, 0.25, 0.25], [0.7857142857142857, 0.0714285714285714, 0.0714285714285714],
+        [0.0714285714285714, 0.0714285714285714, 0.0714285714285714],
+        [0.0714285714285714, 0.0714285714285714, 0.7857142857142857],
+        [0.0714285714285714, 0.7857142857142857, 0.0714285714285714],
+        [0.1005964238332008, 0.3994035761667992, 0.3994035761667992],
+        [0.3994035761667992, 0.1005964238332008, 0.3994035761667992],
+        [0.3994035761667992, 0.3994035761667992, 0.1005964238332008],
+        [0.3994035761667992, 0.1005964238332008, 0.1005964238332008],
+        [0.1005964238332008, 0.3994035761667992, 0.1005964238332008],
+        [0.1005964238332008, 0.1005964238332008, 0.3994035761667992]],
+}
+
+ELEMENT = {  # type -> (dim, order, n_basis)   (element/element_type.py:57-87)
+    "triangle": (2, 1, 3), "triangle6": (2, 2, 6),
+    "tetra": (3, 1, 4), "tetra10": (3, 2, 10),
+}
+_TRI_EDGE = [[1, 2], [0, 2], [0, 1]]                          # element.py:1684
+_TET_EDGE = [[2, 3], [1, 3], [1, 2], [0, 3], [0, 2], [0, 1]]  # element.py:1949
+
+
+def quadrature(etype: str, order: int) -> Tuple[torch.Tensor, torch.Tensor]:
+    dim = ELEMENT[etype][0]
+    w, p = (_TRI_W, _TRI_P) if dim == 2 else (_TET_W, _TET_P)
+    return torch.tensor(w[order], dtype=DT), torch.tensor(p[order], dtype=DT)
+
+
+def basis_nodes(etype: str) -> torch.Tensor:
+    """Reference-element nodes: vertices, then edge mid-points in the
+    element's edge order (element/basis.py:639-695, 750-860)."""
+    dim, order, _ = ELEMENT[etype]
+    verts = torch.cat([torch.zeros(1, dim, dtype=DT), torch.eye(dim, dtype=DT)], 0)
+    if order == 1:
+        return verts
+    edges = _TRI_EDGE if dim == 2 else _TET_EDGE
+    mids = torch.stack([(verts[a] + verts[b]) / 2 for a, b in edges])
+    return torch.cat([verts, mids], 0)
+
+
+def _monomials(dim: int, order: int):
+    exps = []
+    for tot in range(order + 1):
+        if dim == 2:
+            for a in range(tot, -1, -1):
+                exps.append((a, tot - a))
+        else:
+            for a in range(tot, -1, -1):
+                for b in range(tot - a, -1, -1):
+                    exps.append((a, b, tot - a - b))
+    return exps
+
+
+def _eval_monomials(exps, pts: torch.Tensor) -> torch.Tensor:
+    return torch.stack([torch.prod(pts ** torch.tensor(e, dtype=DT), -1) for e in exps], -1)
+
+
+def _eval_monomial_grads(exps, pts: torch.Tensor) -> torch.Tensor:
+    """[Q, dim, n_mono] derivatives of the monomials."""
+    out = []
+    dim = pts.shape[-1]
+    for d in range(dim):
+        cols = []
+        for e in exps:
+            if e[d] == 0:
+                cols.append(torch.zeros(pts.shape[0], dtype=DT))
+            else:
+                e2 = list(e)
+                e2[d] -= 1
+                cols.append(e[d] * torch.prod(pts ** torch.tensor(e2, dtype=DT), -1))
+        out.append(torch.stack(cols, -1))
+    return torch.stack(out, 1)
+
+
+def shape_tables(etype: str, qorder: int):
+    """(w [Q], phi [Q,B], dphi [Q,D,B]) via the inverse monomial Vandermonde
+    matrix at the basis nodes (element/element.py:557-716, 804-872)."""
+    dim, order, nb = ELEMENT[etype]
+    w, q = quadrature(etype, qorder)
+    exps = _monomials(dim, order)
+    V = _eval_monomials(exps, basis_nodes(etype))        # [B, n_mono]
+    coef = torch.linalg.inv(V).T                          # element.py:657
+    phi = _eval_monomials(exps, q) @ coef.T               # [Q, B]
+    dphi = torch.einsum("qdm,bm->qdb", _eval_monomial_grads(exps, q), coef)
+    return w, phi, dphi
+
+
+# ---------------------------------------------------------------------------
+# Geometry: element.py:875-968 and transformation.py:1219-1276
+# ---------------------------------------------------------------------------
+def shape_grad_jxw(points: torch.Tensor, conn: torch.Tensor, etype: str, qorder: int = 2):
+    w, _, dphi = shape_tables(etype, qorder)
+    X = points[conn]                                                 # transformation.py:219
+    J = torch.einsum("ebj,qib->eqij", X, dphi)                        # element.py:962
+    Jinv = torch.inverse(J)                                          # element.py:964
+    grad = torch.einsum("qib,eqji->eqbj", dphi, Jinv)                 # element.py:966
+    jxw = torch.einsum("q,eq->eq", w, torch.linalg.det(J).abs())      # transformation.py:1272
+    return grad, jxw
+
+
+# ---------------------------------------------------------------------------
+# Sparsity pattern and slot map: element_assembler.py:811-830
+# ---------------------------------------------------------------------------
+def element_pattern(conn: torch.Tensor, n_points: int):
+    """Return (edges int32 [2,nnz], slot map int64 [E*B*B])."""
+    c = conn.cpu().numpy().astype(np.int64)
+    E, B = c.shape
+    eu = np.repeat(c[:, :, None], B, axis=2).reshape(-1)
+    ev = np.repeat(c[:, None, :], B, axis=1).reshape(-1)
+    tmp = scipy.sparse.coo_matrix((np.ones_like(eu), (eu, ev)),
+                                  shape=(n_points, n_points)).tocsr().tocoo()
+    edge_u, edge_v = tmp.row, tmp.col
+    eids = scipy.sparse.coo_matrix((np.arange(len(edge_u)), (edge_u, edge_v)),
+                                   shape=(n_points, n_points)).tocsr()
+    slot = np.asarray(eids[eu, ev]).ravel().astype(np.int64)
+    edges = np.stack([edge_u, edge_v], 0).astype(np.int32)
+    return torch.from_numpy(edges), torch.from_numpy(slot)
+
+
+def reduce_project(indices: torch.Tensor, x: torch.Tensor, to_size: int) -> torch.Tensor:
+    """projector.py:95-123: zeros(to).index_add_(0, indices, x)."""
+    x = x.reshape(indices.shape[0], *x.shape[indices.dim():]) if x.dim() > 1 else x
+    out = torch.zeros(to_size, *x.shape[1:], dtype=x.dtype)
+    return out.index_add_(0, indices, x)
+
+
+def layout_hash(row: torch.Tensor, col: torch.Tensor) -> str:
+    """sparse/matrix.py:82-86."""
+    return hashlib.sha256(row.detach().cpu().numpy().tobytes()
+                          + col.detach().cpu().numpy().tobytes()).hexdigest()
+
+
+def block_coo_indices(row: torch.Tensor, col: torch.Tensor, H: int):
+    """sparse/matrix.py:332-381: row*H+a, col*H+b in [edge, a, b] order."""
+    a = torch.arange(H).repeat_interleave(H)
+    b = torch.arange(H).repeat(H)
+    return ((row.long()[:, None] * H + a).reshape(-1), (col.long()[:, None] * H + b).reshape(-1))
+
+
+# ---------------------------------------------------------------------------
+# Forms (element_assembler.py:390-445 with the integrands of builtin.py)
+# ---------------------------------------------------------------------------
+def _chunks(E: int, chunk: int):
+    for s in range(0, E, chunk):
+        yield s, min(E, s + chunk)
+
+
+def element_locals_diffusion(points, conn, etype, kappa=None, qorder=2):
+    """K_e[i,j] = kappa_e sum_q jxw gradu_i . gradv_j  (builtin.py:61-62)."""
+    grad, jxw = shape_grad_jxw(points, conn, etype, qorder)
+    integ = torch.einsum("eqid,eqjd->eqij", grad, grad)
+    if kappa is not None:
+        integ = kappa[:, None, None, None] * integ
+    return torch.einsum("eqij,eq->eij", integ, jxw)                  # element_assembler.py:199
+
+
+def element_locals_mass(points, conn, etype, qorder=2):
+    """M_e[i,j] = sum_q jxw phi_i phi_j  (builtin.py:99-100, 'qij,eq->eij')."""
+    _, phi, _ = shape_tables(etype, qorder)
+    _, jxw = shape_grad_jxw(points, conn, etype, qorder)
+    integ = phi[:, :, None] * phi[:, None, :]
+    return torch.einsum("qij,eq->eij", integ, jxw)                   # element_assembler.py:208
+
+
+def voigt_B(grad: torch.Tensor) -> torch.Tensor:
+    """functional/elasticity.py:132-200: rows [xx,yy,(zz),(yz,xz),xy]."""
+    D = grad.shape[-1]
+    z = torch.zeros_like(grad[..., 0])
+    g = [grad[..., d] for d in range(D)]
+    if D == 2:
+        rows = [[g[0], z], [z, g[1]], [g[1], g[0]]]
+    else:
+        rows = [[g[0], z, z], [z, g[1], z], [z, z, g[2]],
+                [z, g[2], g[1]], [g[2], z, g[0]], [g[1], g[0], z]]
+    return torch.stack([torch.stack(r, -1) for r in rows], -2)       # [..., 3|6, D]
+
+
+def voigt_C(E: torch.Tensor, nu: float, D: int) -> torch.Tensor:
+    """functional/elasticity.py:202-284 for a batch of Young's moduli."""
+    mu = E / (2. * (1. + nu))
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    n = 3 if D == 2 else 6
+    C = torch.zeros(E.shape[0], n, n, dtype=DT)
+    for k in range(n):
+        C[:, k, k] = mu
+    for a in range(D):
+        for b in range(D):
+            C[:, a, b] = C[:, a, b] + lam
+        C[:, a, a] = C[:, a, a] + mu
+    return C
+
+
+def element_locals_elasticity(points, conn, etype, E, nu=0.3, qorder=2):
+    """Block [i,j,a,b] = sum_q jxw (B_i^T C B_j)[a,b]  (builtin.py:172-178)."""
+    grad, jxw = shape_grad_jxw(points, conn, etype, qorder)
+    D = grad.shape[-1]
+    if not torch.is_tensor(E):
+        E = torch.full((conn.shape[0],), float(E), dtype=DT)
+    Bm = voigt_B(grad)                                               # [e,q,b,k,a]
+    C = voigt_C(E, nu, D)
+    integ = torch.einsum("eqika,ekl,eqjlb->eqijab", Bm, C, Bm)
+    return torch.einsum("eqijab,eq->eijab", integ, jxw)
+
+
+def assemble_matrix(points, conn, n_points, local_fn, chunk=1 << 15, **kw):
+    """Run ``local_fn`` over element chunks and scatter with the slot map."""
+    edges, slot = element_pattern(conn, n_points)
+    nnz = edges.shape[1]
+    out = None
+    B = conn.shape[1]
+    for s, e in _chunks(conn.shape[0], chunk):
+        kwc = {k: (v[s:e] if torch.is_tensor(v) and v.dim() > 0 and v.shape[0] == conn.shape[0] else v)
+               for k, v in kw.items()}
+        loc = local_fn(points, conn[s:e], **kwc)
+        flat = loc.reshape((e - s) * B * B, *loc.shape[3:])
+        part = reduce_project(slot[s * B * B:e * B * B], flat, nnz)
+        out = part if out is None else out + part
+    return edges, slot, out
+
+
+def assemble_load(points, conn, etype, n_points, f_nodes=None, const=None, func=None, qorder=2,
+                  chunk=1 << 16):
+    """b_i = sum_e sum_q jxw phi_i(q) f(q)  (node_assembler.py:368-409):
+    ``f_nodes`` nodal values interpolated with phi (:389), ``const`` a
+    constant (builtin.py:730-771), ``func`` a function of the quadrature
+    point coordinates (builtin.py:773-813)."""
+    _, phi, _ = shape_tables(etype, qorder)
+    out = None
+    for s, e in _chunks(conn.shape[0], chunk):
+        c = conn[s:e]
+        _, jxw = shape_grad_jxw(points, c, etype, qorder)
+        if f_nodes is not None:
+            fq = torch.einsum("eb...,qb->eq...", f_nodes[c], phi)
+        elif func is not None:
+            xq = torch.einsum("ebd,qb->eqd", points[c], phi)
+            fq = func(xq)
+        else:
+            fq = torch.full(jxw.shape, float(1.0 if const is None else const), dtype=DT)
+        integ = phi[None, :, :] * fq[..., None] if fq.dim() == 2 else phi[None, :, :, None] * fq[:, :, None, :]
+        loc = torch.einsum("eqb...,eq->eb...", integ, jxw)
+        part = reduce_project(c.reshape(-1), loc.reshape(-1, *loc.shape[2:]), n_points)
+        out = part if out is None else out + part
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Dirichlet condensation (operator/condense.py:182-296) and a direct solve
+# ---------------------------------------------------------------------------
+def condense(values, row, col, n, mask, rhs, value=None):
+    row = row.long()
+    col = col.long()
+    inner = ~mask
+    ie = inner[row] & inner[col]
+    oe = inner[row] & mask[col]
+    loc = torch.full((n,), -1, dtype=torch.long)
+    loc[inner] = torch.arange(int(inner.sum()))
+    loc[mask] = torch.arange(int(mask.sum()))
+    ni, no = int(inner.sum()), int(mask.sum())
+    Kii = scipy.sparse.coo_matrix((values[ie].numpy(), (loc[row[ie]].numpy(), loc[col[ie]].numpy())),
+                                  shape=(ni, ni)).tocsr()
+    uo = torch.zeros(no, dtype=DT) if value is None else value
+    Kio = scipy.sparse.coo_matrix((values[oe].numpy(), (loc[row[oe]].numpy(), loc[col[oe]].numpy())),
+                                  shape=(ni, no)).tocsr()
+    rhs_i = rhs[inner].numpy() - Kio @ uo.numpy()
+    return Kii, rhs_i, inner
+
+
+def solve_dirichlet(values, row, col, n, mask, rhs):
+    Kii, ri, inner = condense(values, row, col, n, mask, rhs)
+    ui = scipy.sparse.linalg.spsolve(Kii.tocsc(), ri)
+    u = torch.zeros(n, dtype=DT)
+    u[inner] = torch.from_numpy(np.asarray(ui))
+    return u
+
+
+def checksum(values: torch.Tensor) -> Dict[str, float]:
+    """Size-independent fingerprints of an assembled value array: the
+    Frobenius norm and two positively weighted sums (weights in [0.5,1.5)
+    from a multiplicative hash of the flat index, so no cancellation)."""
+    v = values.reshape(-1).to(DT)
+    i = torch.arange(v.shape[0], dtype=torch.int64)
+    w1 = ((i * 2654435761) % 4294967296).to(DT) / 4294967296.0 + 0.5
+    w2 = ((i * 40503 + 12345) % 65536).to(DT) / 65536.0 + 0.5
+    return {"fro": float(torch.linalg.vector_norm(v)), "w1": float((w1 * v).sum()),
+            "w2": float((w2 * v).sum()), "abs": float(v.abs().sum()), "n": int(v.shape[0])}
+
+
+# ---------------------------------------------------------------------------
+# The reference's per-call work for the diffusion + mass benchmark, restated
+# op for op (element_assembler.py:390-445 with builtin.py:61-62 / :99-100 and
+# sparse/matrix.py:76-86), given the slot map of ``from_mesh``.  Used as the
+# reference arm of the benchmark, on the host cores and on the GPU.
+# ---------------------------------------------------------------------------
+def reference_call_diffusion_mass(points, conn, kappa, slot, edges, etype="tetra", qorder=2,
+                                  with_hash=True):
+    w, phi, dphi = shape_tables(etype, qorder)
+    w, phi, dphi = w.to(points.device), phi.to(points.device), dphi.to(points.device)
+    nnz = edges.shape[1]
+    X = points[conn]
+    J = torch.einsum("ebj,qib->eqij", X, dphi)
+    grad = torch.einsum("qib,eqji->eqbj", dphi, torch.inverse(J))
+    jxw = torch.einsum("q,eq->eq", w, torch.linalg.det(J).abs())
+    integ = kappa[:, None, None, None] * torch.einsum("eqid,eqjd->eqij", grad, grad)
+    Ke = torch.einsum("eqij,eq->eij", integ, jxw)
+    K = torch.zeros(nnz, dtype=points.dtype, device=points.device).index_add_(0, slot, Ke.reshape(-1))
+    # mass: the reference recomputes the geometry for every assembler call
+    J2 = torch.einsum("ebj,qib->eqij", X, dphi)
+    jxw2 = torch.einsum("q,eq->eq", w, torch.linalg.det(J2).abs())
+    Me = torch.einsum("qij,eq->eij", phi[:, :, None] * phi[:, None, :], jxw2)
+    M = torch.zeros(nnz, dtype=points.dtype, device=points.device).index_add_(0, slot, Me.reshape(-1))
+    hashes = []
+    if with_hash:
+        for _ in range(2):                       # one SparseMatrix per assembled form
+            r, c = edges[0], edges[1]
+            r.long(), c.long()
+            hashes.append(layout_hash(r, c))
+    return K, M, hashes

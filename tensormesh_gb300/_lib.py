@@ -1,0 +1,166 @@
+"""ctypes binding of ``libtmgb300.so`` (the C ABI declared in
+``include/tensormesh_gb300.h``).
+
+The library is loaded on first use.  If it is missing it is built with
+``tensormesh_gb300.build.build()``; if that is impossible the import fails
+with an error -- the package has no CPU or eager-PyTorch substitute for the
+kernels.
+"""
+import ctypes as C
+import os
+import threading
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LOCK = threading.Lock()
+_LIB = None
+
+TM_OK, TM_ERR_INVALID_ARG, TM_ERR_UNSUPPORTED, TM_ERR_CUDA, TM_ERR_PLAN, TM_ERR_TOO_LARGE = range(6)
+TM_F64, TM_F32 = 0, 1
+TM_FORM_DIFFUSION, TM_FORM_MASS, TM_FORM_ELASTICITY = 1, 2, 4
+TM_SOURCE_NODAL, TM_SOURCE_CONST, TM_SOURCE_QUAD = 0, 1, 2
+TM_PLAN_KIND_MATRIX, TM_PLAN_KIND_NODE = 0, 1
+(PLAN_EDGE_ROW, PLAN_EDGE_COL, PLAN_SLOT, PLAN_CHUNK_BEGIN, PLAN_SLOT_PTR, PLAN_CONTRIB,
+ PLAN_SLOT_TARGET, PLAN_SLOT_MIRROR, PLAN_SHARED_PTR, PLAN_SHARED_TARGET, PLAN_SHARED_MIRROR,
+ PLAN_CONN, PLAN_PERM) = range(13)
+
+
+class TmError(RuntimeError):
+    """A status code other than TM_OK returned by the native library."""
+
+
+class ElementTables(C.Structure):
+    _fields_ = [("element_type", C.c_int32), ("n_quad", C.c_int32), ("packed", C.c_void_p)]
+
+
+class ChunkPlan(C.Structure):
+    _fields_ = [
+        ("n_elements", C.c_int64), ("n_basis", C.c_int32), ("n_local", C.c_int32),
+        ("chunk_elems", C.c_int32), ("n_chunks", C.c_int32), ("n_targets", C.c_int64),
+        ("n_shared", C.c_int32), ("n_partials", C.c_int32),
+        ("elem_perm", C.c_void_p), ("conn", C.c_void_p), ("chunk_begin", C.c_void_p),
+        ("slot_ptr", C.c_void_p), ("contrib", C.c_void_p), ("slot_target", C.c_void_p),
+        ("slot_mirror", C.c_void_p), ("shared_ptr", C.c_void_p), ("shared_target", C.c_void_p),
+        ("shared_mirror", C.c_void_p),
+    ]
+
+
+class MatrixArgs(C.Structure):
+    _fields_ = [
+        ("dtype", C.c_int32), ("forms", C.c_int32), ("n_points", C.c_int64),
+        ("points", C.c_void_p), ("kappa", C.c_void_p), ("kappa_scale", C.c_double),
+        ("mass_scale", C.c_double), ("young", C.c_void_p), ("young_scale", C.c_double),
+        ("poisson", C.c_double), ("out_diffusion", C.c_void_p), ("out_mass", C.c_void_p),
+        ("out_elasticity", C.c_void_p), ("workspace", C.c_void_p),
+        ("tables", ElementTables), ("plan", ChunkPlan),
+        ("event_begin", C.c_void_p), ("event_end", C.c_void_p),
+    ]
+
+
+class VectorArgs(C.Structure):
+    _fields_ = [
+        ("dtype", C.c_int32), ("source", C.c_int32), ("width", C.c_int32), ("n_points", C.c_int64),
+        ("points", C.c_void_p), ("values", C.c_void_p), ("constant", C.c_double * 3),
+        ("out", C.c_void_p), ("workspace", C.c_void_p),
+        ("tables", ElementTables), ("plan", ChunkPlan),
+    ]
+
+
+class LinearOperator(C.Structure):
+    _fields_ = [("dtype", C.c_int32), ("block", C.c_int32), ("n_rows", C.c_int64),
+                ("row_ptr", C.c_void_p), ("col", C.c_void_p), ("values", C.c_void_p)]
+
+
+class PcgArgs(C.Structure):
+    _fields_ = [("A", LinearOperator), ("b", C.c_void_p), ("x", C.c_void_p), ("r", C.c_void_p),
+                ("z", C.c_void_p), ("p", C.c_void_p), ("q", C.c_void_p), ("dinv", C.c_void_p),
+                ("scalars", C.c_void_p), ("partials", C.c_void_p)]
+
+
+_SIGNATURES = {
+    "tm_error_string": (C.c_char_p, [C.c_int]),
+    "tm_last_error_message": (C.c_char_p, []),
+    "tm_version": (C.c_int, []),
+    "tm_plan_build": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32,
+                                C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "tm_plan_array_size": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "tm_plan_copy_array": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "tm_plan_scalar": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "tm_plan_free": (None, [C.c_void_p]),
+    "tm_matrix_workspace_bytes": (C.c_size_t, [C.POINTER(MatrixArgs)]),
+    "tm_assemble_matrix": (C.c_int, [C.POINTER(MatrixArgs), C.c_void_p]),
+    "tm_vector_workspace_bytes": (C.c_size_t, [C.POINTER(VectorArgs)]),
+    "tm_assemble_vector": (C.c_int, [C.POINTER(VectorArgs), C.c_void_p]),
+    "tm_shape_grad_jxw": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, ElementTables, C.c_void_p,
+                                    C.c_void_p, C.c_void_p]),
+    "tm_quadrature_points": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, ElementTables,
+                                       C.c_void_p, C.c_void_p]),
+    "tm_project_reduce": (C.c_int, [C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]),
+    "tm_spmv": (C.c_int, [C.POINTER(LinearOperator), C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                          C.c_void_p]),
+    "tm_pcg_partials_bytes": (C.c_size_t, []),
+    "tm_pcg_start": (C.c_int, [C.POINTER(PcgArgs), C.c_void_p]),
+    "tm_pcg_iterate": (C.c_int, [C.POINTER(PcgArgs), C.c_int32, C.c_void_p]),
+}
+
+EXPORTED = tuple(_SIGNATURES)
+
+
+def lib_path() -> str:
+    return os.path.join(_HERE, "libtmgb300.so")
+
+
+def load(build_if_missing: bool = True):
+    """Load (and if needed build) the native library."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = lib_path()
+        if build_if_missing:
+            from .build import build
+            build()
+        if not os.path.exists(path):
+            raise ImportError(f"tensormesh_gb300 native library not found at {path}; run "
+                              f"tensormesh_gb300.build.build()")
+        lib = C.CDLL(path)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+        return lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != TM_OK:
+        lib = load()
+        msg = lib.tm_last_error_message().decode(errors="replace")
+        kind = lib.tm_error_string(status).decode(errors="replace")
+        raise TmError(f"{what}: {kind}: {msg}" if what else f"{kind}: {msg}")
+
+
+def ptr(t) -> int:
+    return 0 if t is None else t.data_ptr()
+
+
+def stream_handle(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def dtype_code(dtype: torch.dtype) -> int:
+    if dtype == torch.float64:
+        return TM_F64
+    if dtype == torch.float32:
+        return TM_F32
+    raise TypeError(f"tensormesh_gb300 computes in float64 or float32, got {dtype}")
+
+
+def require_cuda(t: torch.Tensor, what: str) -> None:
+    if not t.is_cuda:
+        raise RuntimeError(f"{what} must be a CUDA tensor: tensormesh_gb300 assembles on the GPU only "
+                           f"(got device {t.device})")

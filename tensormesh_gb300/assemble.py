@@ -1,0 +1,547 @@
+"""``ElementAssembler`` and ``NodeAssembler`` with the reference's interfaces
+(assemble/element_assembler.py, assemble/node_assembler.py), running the
+fused GPU kernels of ``libtmgb300.so``.
+
+The reference lifts a Python ``forward`` integrand over elements,
+quadrature points and basis pairs with nested ``vmap`` and scatters with
+``index_add_``.  Here each built-in family is one kernel (see
+``csrc/tm_assemble.cu``); the class of the assembler selects it.  Calling an
+assembler whose ``forward`` is a custom Python integrand raises
+``NotImplementedError`` -- there is no CPU or vmap path.
+
+Linear forms are the exception that is kept general: any ``NodeAssembler``
+whose ``forward`` is a source term times the test function, ``g(x, data) * v``
+(the shape of every load form in the reference's documentation), is assembled
+by evaluating ``g`` on the device at the quadrature points (``forward`` called
+once with ``v = 1`` on [E, Q]-batched arguments, as the reference's own
+broadcast fast path does, node_assembler.py:173-240) and integrating and
+reducing it with the kernel.
+"""
+import inspect
+import math
+from typing import Callable, Dict, Mapping, Optional, Union
+
+import numpy as np
+import torch
+import torch.nn as nn
+
+from . import _lib
+from .element import element_info, element_tables, element_type2dimension
+from .plan import Topology
+from .sparse import SparseMatrix
+from .transformation import ReduceProjector, SparseProjector, Transformation
+
+
+class BufferDict(nn.Module):
+    """Named buffers that follow ``.to()`` (the reference's nn.BufferDict)."""
+
+    def __init__(self, d: Optional[Mapping[str, torch.Tensor]] = None):
+        super().__init__()
+        self._keys = []
+        for k, v in (d or {}).items():
+            self[k] = v
+
+    def __setitem__(self, k, v):
+        if k not in self._keys:
+            self._keys.append(k)
+        self.register_buffer(k, v)
+
+    def __getitem__(self, k):
+        return getattr(self, k)
+
+    def __contains__(self, k):
+        return k in self._keys
+
+    def __iter__(self):
+        return iter(self._keys)
+
+    def __len__(self):
+        return len(self._keys)
+
+    def keys(self):
+        return list(self._keys)
+
+    def values(self):
+        return [self[k] for k in self._keys]
+
+    def items(self):
+        return [(k, self[k]) for k in self._keys]
+
+
+def _single_type(elements) -> tuple:
+    if isinstance(elements, torch.Tensor):
+        raise TypeError("elements must be a {element_type: tensor} mapping")
+    keys = list(elements.keys())
+    if len(keys) != 1:
+        raise NotImplementedError(f"mixed-element meshes ({keys}) are not assembled by tensormesh_gb300")
+    element_info(keys[0])
+    return keys[0], elements[keys[0]]
+
+
+def _mesh_elements(mesh) -> Dict[str, torch.Tensor]:
+    elements = mesh.elements()
+    if isinstance(elements, torch.Tensor):
+        elements = {mesh.default_element_type: elements}
+    return dict(elements)
+
+
+class _AssemblerBase(nn.Module):
+    _topology: Optional[Topology] = None
+
+    def type(self, dtype: torch.dtype):
+        if dtype == torch.float64:
+            self.double()
+        elif dtype == torch.float32:
+            self.float()
+        else:
+            raise Exception(f"the dtype {dtype} is not supported")
+        return self
+
+    @property
+    def device(self) -> torch.device:
+        return next(iter(self.transformation.values())).device
+
+    @property
+    def dtype(self) -> torch.dtype:
+        return next(iter(self.transformation.values())).dtype
+
+    def _topo(self, matrix: bool) -> Topology:
+        if self._topology is None:
+            et = self.element_types[0]
+            trans = self.transformation[et]
+            self._topology = Topology(trans.points, self.elements[et], et, trans.quadrature_order, matrix=matrix)
+        return self._topology
+
+    def __post_init__(self, *args, **kwargs):
+        pass
+
+
+# ============================================================================
+# Bilinear forms
+# ============================================================================
+class ElementAssembler(_AssemblerBase):
+    """Assemble a bilinear form into a global ``SparseMatrix``.
+
+    Subclasses select the kernel through ``_tm_form``: ``"diffusion"``
+    (``LaplaceElementAssembler``), ``"mass"`` (``MassElementAssembler``) or
+    ``"elasticity"`` (``LinearElasticityElementAssembler``)."""
+
+    _tm_form: Optional[str] = None
+
+    def __init__(self, projector, transformation, elements, edges, *args, **kwargs):
+        super().__init__()
+        if not isinstance(projector, nn.ModuleDict):
+            projector = nn.ModuleDict(projector)
+        if not isinstance(transformation, nn.ModuleDict):
+            transformation = nn.ModuleDict(transformation)
+        if not isinstance(elements, BufferDict):
+            elements = BufferDict(elements)
+        element_types = list(projector.keys())
+        self.projector = projector
+        self.transformation = transformation
+        self.elements = elements
+        self.register_buffer("edges", edges)
+        self.dimension = element_type2dimension[element_types[0]]
+        self.element_types = list(elements.keys())
+        self.n_points = next(iter(self.transformation.values())).n_points
+        self.__post_init__(*args, **kwargs)
+
+    # -- construction ---------------------------------------------------------
+    @classmethod
+    def from_mesh(cls, mesh, quadrature_order: int = 2, project: str = "reduce", *args, **kwargs):
+        """Build from a mesh (assemble/element_assembler.py:769-878): the CSR
+        pattern ``edges`` (int32, unique pairs sorted row-major) and the
+        element->CSR slot map are the reference's, computed by the native
+        plan builder together with the kernels' reduction plan."""
+        assert project in ["reduce", "sparse"]
+        points = mesh.points
+        etype, conn = _single_type(_mesh_elements(mesh))
+        topo = Topology(points, conn, etype, quadrature_order, matrix=True)
+        E, B = conn.shape
+        if project == "reduce":
+            proj = ReduceProjector(indices=topo.slot, from_shape=(E, B, B), to_shape=(topo.nnz,))
+        else:
+            proj = SparseProjector(from_=torch.arange(E * B * B), to_=topo.slot, from_shape=(E, B, B),
+                                   to_shape=(topo.nnz,))
+        trans = Transformation(points=points, elements=conn.long(), element_type=etype,
+                               quadrature_order=quadrature_order)
+        asm = cls({etype: proj}, {etype: trans}, {etype: conn.long()}, topo.edges, *args, **kwargs)
+        asm._topology = topo
+        return asm.type(mesh.dtype).to(mesh.device)
+
+    @classmethod
+    def from_assembler(cls, obj, *args, **kwargs):
+        """Share the topology of another assembler (element_assembler.py:742-766)."""
+        assert isinstance(obj, ElementAssembler), f"obj must be an instance of ElementAssembler, but got {type(obj)}"
+        asm = cls(obj.projector, obj.transformation, obj.elements, obj.edges, *args, **kwargs)
+        asm._topology = obj._topology
+        return asm
+
+    # -- call -----------------------------------------------------------------
+    def _prepare(self, points, point_data, element_data, scalar_data):
+        assert isinstance(point_data, dict) or point_data is None, \
+            f"point_data should be a dict, but got {type(point_data)}"
+        et = self.element_types[0]
+        trans = self.transformation[et]
+        if points is None:
+            points = trans.points
+        else:
+            assert points.shape[1] == trans.dim, \
+                f"the dimension of points should be {trans.dim}, but got {points.shape[1]}"
+            trans.update_points(points)
+        _lib.require_cuda(points, "points")
+        self.type(points.dtype).to(points.device)
+        E = self.elements[et].shape[0]
+        ed = {}
+        if element_data:
+            for key, value in element_data.items():
+                if isinstance(value, dict):
+                    value = value[et]
+                assert value.shape[0] == E, f"the shape of {key} should be [{E}, ...], but got {tuple(value.shape)}"
+                ed[key] = value
+        sd = dict(scalar_data or {})
+        return et, points, ed, sd
+
+    def __call__(self, points: Optional[torch.Tensor] = None, func: Optional[Callable] = None,
+                 point_data=None, element_data=None, scalar_data=None, batch_size: int = -1):
+        """Assemble into a ``SparseMatrix`` of shape (N, N), or (N*D, N*D) for
+        elasticity.  ``batch_size`` (quadrature chunking in the reference)
+        does not change results and is accepted and ignored: the kernel
+        never materialises the integrand."""
+        if func is not None:
+            raise NotImplementedError("custom integrands (func=...) are not assembled by tensormesh_gb300")
+        form = type(self)._tm_form
+        if form is None:
+            raise NotImplementedError(
+                f"{type(self).__name__}.forward is a custom Python weak form; tensormesh_gb300 assembles the "
+                f"built-in families (LaplaceElementAssembler / DiffusionElementAssembler, "
+                f"MassElementAssembler, LinearElasticityElementAssembler)")
+        et, points, ed, sd = self._prepare(points, point_data, element_data, scalar_data)
+        (values,) = assemble_forms([self], points, ed, sd)
+        return self._build_output(values)
+
+    def _build_output(self, values: torch.Tensor) -> SparseMatrix:
+        topo = self._topo(True)
+        edges = self.edges
+        if values.dim() == 1:
+            return SparseMatrix(values, edges[0], edges[1], (self.n_points, self.n_points), _topology=topo,
+                                _sorted=True)
+        m = SparseMatrix.from_block_coo(values, edges[0], edges[1], (self.n_points, self.n_points),
+                                        _topology=topo)
+        m._sorted = True
+        return m
+
+    # -- form parameters (overridden by the built-ins) ------------------------
+    def _tm_coefficients(self, ed, sd, E):
+        return {}
+
+    def forward(self, *args, **kwargs):
+        raise NotImplementedError("forward is not implemented")
+
+    def __repr__(self):
+        return (f"{type(self).__name__}(element_types={self.element_types}, n_point={self.n_points}, "
+                f"n_element={[v.shape[0] for v in self.elements.values()]})")
+
+
+_FORM_BITS = {"diffusion": _lib.TM_FORM_DIFFUSION, "mass": _lib.TM_FORM_MASS,
+              "elasticity": _lib.TM_FORM_ELASTICITY}
+
+
+def _coef(value, dtype, device, E, name):
+    """(pointer tensor or None, scale) for a per-element or scalar coefficient."""
+    if value is None:
+        return None, 1.0
+    if isinstance(value, (int, float)):
+        return None, float(value)
+    t = torch.as_tensor(value)
+    if t.dim() == 0:
+        return None, float(t)
+    t = t.reshape(-1)
+    if t.shape[0] != E:
+        raise ValueError(f"{name} must have one value per element ({E}), got {tuple(t.shape)}")
+    return t.to(device=device, dtype=dtype).contiguous(), 1.0
+
+
+def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_data=None,
+                   scalar_data=None, _events=None):
+    """Assemble several built-in forms over one mesh in one fused launch when
+    they can share it (diffusion and mass do), else one launch per form.
+
+    Returns the value tensors ([nnz] per scalar form, [nnz, D, D] for
+    elasticity) in the order of ``assemblers``.  ``_events`` (two recorded
+    ``torch.cuda.Event``) are recorded around the element-chunk kernel of
+    the first launch, for timing."""
+    first = assemblers[0]
+    for a in assemblers[1:]:
+        if a._topology is not first._topology:
+            raise ValueError("fused assembly needs assemblers that share a topology (from_assembler)")
+    et = first.element_types[0]
+    trans = first.transformation[et]
+    if points is None:
+        points = trans.points
+    _lib.require_cuda(points, "points")
+    topo = first._topo(True)
+    ed = dict(element_data or {})
+    sd = dict(scalar_data or {})
+    E = topo.n_elements
+    dev, dt = points.device, points.dtype
+    pts = points.detach().contiguous()
+    if pts.dtype not in (torch.float64, torch.float32):
+        raise TypeError(f"points must be float64 or float32, got {pts.dtype}")
+    forms = [type(a)._tm_form for a in assemblers]
+    scalar_group = [i for i, f in enumerate(forms) if f in ("diffusion", "mass")]
+    out = [None] * len(assemblers)
+    groups = []
+    if len(scalar_group) == 2 and forms[scalar_group[0]] != forms[scalar_group[1]]:
+        groups.append(scalar_group)
+    else:
+        groups.extend([[i] for i in scalar_group])
+    groups.extend([[i] for i, f in enumerate(forms) if f == "elasticity"])
+    lib = _lib.load()
+    D = topo.info.dim
+    for g in groups:
+        bits = 0
+        args = _lib.MatrixArgs()
+        args.dtype = _lib.dtype_code(dt)
+        args.n_points = topo.n_points
+        args.points = _lib.ptr(pts)
+        args.kappa_scale = args.mass_scale = args.young_scale = 1.0
+        args.poisson = 0.3
+        keep = [pts]
+        block = False
+        for i in g:
+            a = assemblers[i]
+            f = forms[i]
+            bits |= _FORM_BITS[f]
+            c = a._tm_coefficients(ed, sd, E)
+            if f == "diffusion":
+                t, s = _coef(c.get("kappa"), dt, dev, E, "kappa")
+                args.kappa, args.kappa_scale = _lib.ptr(t), s
+                keep.append(t)
+                out[i] = torch.empty(topo.nnz, dtype=dt, device=dev)
+                args.out_diffusion = _lib.ptr(out[i])
+            elif f == "mass":
+                _, s = _coef(c.get("rho"), dt, dev, E, "rho")
+                args.mass_scale = s
+                out[i] = torch.empty(topo.nnz, dtype=dt, device=dev)
+                args.out_mass = _lib.ptr(out[i])
+            else:
+                block = True
+                t, s = _coef(c.get("E"), dt, dev, E, "E")
+                args.young, args.young_scale = _lib.ptr(t), s
+                args.poisson = float(c.get("nu", 0.3))
+                keep.append(t)
+                out[i] = torch.empty(topo.nnz, D, D, dtype=dt, device=dev)
+                args.out_elasticity = _lib.ptr(out[i])
+        args.forms = bits
+        plan = topo.matrix_plan(dev, block=block)
+        args.plan = plan.struct()
+        args.tables = topo.table_struct(dev)
+        ws_bytes = lib.tm_matrix_workspace_bytes(C_byref(args))
+        ws = torch.empty(max(1, ws_bytes), dtype=torch.uint8, device=dev)
+        args.workspace = _lib.ptr(ws)
+        if _events is not None:
+            args.event_begin, args.event_end = _events[0].cuda_event, _events[1].cuda_event
+            _events = None
+        _lib.check(lib.tm_assemble_matrix(C_byref(args), _lib.stream_handle(dev)), "tm_assemble_matrix")
+    return out
+
+
+def C_byref(x):
+    import ctypes
+    return ctypes.byref(x)
+
+
+# ============================================================================
+# Linear forms
+# ============================================================================
+class NodeAssembler(_AssemblerBase):
+    """Assemble a linear form into a nodal vector [N] (or [N*H])."""
+
+    def __init__(self, projector, transformation, elements, *args, **kwargs):
+        super().__init__()
+        if not isinstance(projector, nn.ModuleDict):
+            projector = nn.ModuleDict(projector)
+        if not isinstance(transformation, nn.ModuleDict):
+            transformation = nn.ModuleDict(transformation)
+        if not isinstance(elements, BufferDict):
+            elements = BufferDict(elements)
+        element_types = list(projector.keys())
+        self.projector = projector
+        self.transformation = transformation
+        self.elements = elements
+        self.dimension = element_type2dimension[element_types[0]]
+        self.element_types = element_types
+        # the reference stores the element count of the first type here
+        # (node_assembler.py:130)
+        self.n_points = next(iter(elements.values())).shape[0]
+        self._compile = False
+        self._compile_options = {}
+        self.__post_init__(*args, **kwargs)
+
+    @classmethod
+    def from_elements(cls, points: torch.Tensor, elements: Dict[str, torch.Tensor], quadrature_order: int = 2,
+                      device="cpu", dtype: torch.dtype = torch.float32, project: str = "reduce", *args, **kwargs):
+        """node_assembler.py:617-698: the scatter map is conn.flatten()."""
+        etype, conn = _single_type(elements)
+        N = points.shape[0]
+        E, B = conn.shape
+        if project == "reduce":
+            proj = ReduceProjector(indices=conn.flatten(), from_shape=(E, B), to_shape=(N,))
+        elif project == "sparse":
+            proj = SparseProjector(from_=torch.arange(E * B), to_=conn.flatten(), from_shape=(E, B), to_shape=(N,))
+        else:
+            raise ValueError(f"project should be either 'reduce' or 'sparse', but got {project}")
+        trans = Transformation(points, conn, etype, quadrature_order)
+        asm = cls({etype: proj}, {etype: trans}, {etype: conn}, *args, **kwargs)
+        asm._topology = Topology(points, conn, etype, quadrature_order, matrix=False)
+        return asm.type(dtype).to(device)
+
+    @classmethod
+    def from_mesh(cls, mesh, quadrature_order: int = 2, project: str = "reduce", *args, **kwargs):
+        elements = _mesh_elements(mesh)
+        return cls.from_elements(mesh.points, elements, quadrature_order, mesh.device, mesh.dtype, project,
+                                 *args, **kwargs)
+
+    @classmethod
+    def from_assembler(cls, obj, *args, **kwargs):
+        assert isinstance(obj, NodeAssembler), f"the object {obj} should inherit from NodeAssembler"
+        asm = cls(obj.projector, obj.transformation, obj.elements, *args, **kwargs)
+        asm._topology = obj._topology
+        return asm
+
+    # the reference's compile()/flat_mode switch between its vmap path and a
+    # broadcast path; the kernel path is the same either way
+    def compile(self, mode: str = "disable", **kwargs):
+        self._compile = True
+        self._compile_options = {"mode": mode, **kwargs}
+        return self
+
+    def flat_mode(self):
+        return self.compile(mode="disable")
+
+    def reset_compile(self):
+        self._compile = False
+        self._compile_options = {}
+        return self
+
+    @property
+    def is_compiled(self) -> bool:
+        return self._compile
+
+    def forward(self, *args, **kwargs):
+        raise NotImplementedError("forward is not implemented")
+
+    def __call__(self, points: Optional[torch.Tensor] = None, func: Optional[Callable] = None,
+                 point_data=None, scalar_data=None, batch_size: int = 1) -> torch.Tensor:
+        if point_data is None:
+            point_data = {}
+        if scalar_data is None:
+            scalar_data = {}
+        et = self.element_types[0]
+        trans = self.transformation[et]
+        if points is None:
+            points = trans.points
+        else:
+            assert points.shape[1] == trans.dim, \
+                f"the dimension of the points should be {trans.dim}, but got {points.shape[1]}"
+            trans.update_points(points)
+        _lib.require_cuda(points, "points")
+        self.type(points.dtype).to(points.device)
+        for key, value in point_data.items():
+            assert value.shape[0] == points.shape[0], \
+                f"the shape of {key} should be [n_point, ...], but got {tuple(value.shape)}"
+        fn = self.forward if func is None else func
+        return assemble_linear_form(self, fn, points, point_data, scalar_data)
+
+
+def assemble_linear_form(asm: NodeAssembler, fn: Callable, points: torch.Tensor, point_data, scalar_data):
+    topo = asm._topo(False)
+    dev, dt = points.device, points.dtype
+    pts = points.detach().contiguous()
+    params = list(inspect.signature(fn).parameters)
+    if "gradv" in params:
+        raise NotImplementedError("linear forms in gradv are not assembled by tensormesh_gb300")
+    for p in params:
+        if p not in ("v", "x") and p not in point_data and p not in scalar_data and \
+                not (p.startswith("grad") and p[4:] in point_data):
+            raise ValueError(f"{p} is not supported, please use `v`, `gradv` or more keys provided by "
+                             f"point_data or scalar_data")
+    source = getattr(asm, "_tm_source", None) if fn == asm.forward else None
+    Q = len(element_tables(topo.etype, topo.quadrature_order)["w"])
+    E = topo.n_elements
+    if source is not None and source[0] == "const":
+        c = torch.as_tensor(source[1], dtype=torch.float64).reshape(-1)
+        return _run_vector(topo, pts, _lib.TM_SOURCE_CONST, None, c.tolist(), int(c.numel()))
+    if source is not None and source[0] == "nodal" and source[1] in point_data:
+        f = point_data[source[1]].to(device=dev, dtype=dt)
+        width = 1 if f.dim() == 1 else int(np.prod(f.shape[1:]))
+        return _run_vector(topo, pts, _lib.TM_SOURCE_NODAL, f.reshape(f.shape[0], width).contiguous(), None, width)
+    # general source g(x, data) * v: evaluate g at the quadrature points
+    args = {}
+    need_x = "x" in params
+    if need_x or any(p.startswith("grad") for p in params):
+        xq = quadrature_points(topo, pts)                     # [E, Q, D]
+    phi = torch.from_numpy(element_tables(topo.etype, topo.quadrature_order)["phi"]).to(device=dev, dtype=dt)
+    conn = topo.conn32(dev).long()
+    for p in params:
+        if p == "v":
+            args[p] = torch.ones((), dtype=dt, device=dev)
+        elif p == "x":
+            args[p] = xq
+        elif p in point_data:
+            v = point_data[p].to(device=dev, dtype=dt)
+            args[p] = torch.einsum("eb...,qb->eq...", v[conn], phi)
+        elif p in scalar_data:
+            args[p] = torch.as_tensor(scalar_data[p], dtype=dt, device=dev)
+        else:
+            raise NotImplementedError(f"gradient of point data ({p}) in a linear form is not supported")
+    g = fn(**args)
+    g = torch.as_tensor(g, dtype=dt, device=dev)
+    if g.dim() >= 2 and g.shape[0] == E and g.shape[1] == Q:
+        trailing = g.shape[2:]
+    else:
+        trailing = g.shape
+        g = g.expand(E, Q, *trailing)
+    width = int(np.prod(trailing)) if len(trailing) else 1
+    fq = g.reshape(E, Q, width).contiguous()
+    return _run_vector(topo, pts, _lib.TM_SOURCE_QUAD, fq, None, width)
+
+
+def quadrature_points(topo: Topology, pts: torch.Tensor) -> torch.Tensor:
+    lib = _lib.load()
+    dev = pts.device
+    Q = len(element_tables(topo.etype, topo.quadrature_order)["w"])
+    xq = torch.empty(topo.n_elements, Q, topo.info.dim, dtype=pts.dtype, device=dev)
+    conn = topo.conn32(dev)
+    _lib.check(lib.tm_quadrature_points(_lib.dtype_code(pts.dtype), topo.n_elements, _lib.ptr(conn), _lib.ptr(pts),
+                                        topo.table_struct(dev), _lib.ptr(xq), _lib.stream_handle(dev)),
+               "tm_quadrature_points")
+    return xq
+
+
+def _run_vector(topo: Topology, pts: torch.Tensor, source: int, values: Optional[torch.Tensor],
+                const, width: int) -> torch.Tensor:
+    if width > 3:
+        raise NotImplementedError("linear forms with more than 3 components per node are not supported")
+    lib = _lib.load()
+    dev, dt = pts.device, pts.dtype
+    plan = topo.node_plan(dev)
+    args = _lib.VectorArgs()
+    args.dtype = _lib.dtype_code(dt)
+    args.source = source
+    args.width = width
+    args.n_points = topo.n_points
+    args.points = _lib.ptr(pts)
+    args.values = _lib.ptr(values)
+    if const is not None:
+        for k, c in enumerate(const):
+            args.constant[k] = float(c)
+    out = torch.empty(topo.n_points, width, dtype=dt, device=dev)
+    args.out = _lib.ptr(out)
+    args.plan = plan.struct()
+    args.tables = topo.table_struct(dev)
+    ws = torch.empty(max(1, lib.tm_vector_workspace_bytes(C_byref(args))), dtype=torch.uint8, device=dev)
+    args.workspace = _lib.ptr(ws)
+    _lib.check(lib.tm_assemble_vector(C_byref(args), _lib.stream_handle(dev)), "tm_assemble_vector")
+    return out.reshape(-1)

@@ -1,0 +1,849 @@
+// Fused FEM assembly kernels for sm_103a.
+//
+// One CTA per element chunk (tm_chunk_plan).  Phase 1 computes the element
+// locals of the chunk into shared memory: the geometry of
+// element/element.py:875-968 and element/transformation.py:1219-1276 (for P1
+// simplices once per element, the Jacobian being constant; for P2 per
+// quadrature point), then the integrand of the form summed over quadrature
+// points (assemble/element_assembler.py:190-209, builtin.py:61-178).
+// Phase 2 walks the chunk's targets (CSR positions or nodes) in increasing
+// order and adds their contributions from shared memory in a fixed order
+// (element, then local entry), replacing ReduceProjector's index_add_
+// (assemble/projector.py:95-123).  Targets touched by one chunk only are
+// written directly -- for symmetric forms the value is also written to the
+// transposed CSR position -- the others go to a partial that a second
+// kernel sums in chunk order.  There are no atomics: results are bitwise
+// reproducible run to run.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <cstdio>
+
+#include "../../include/tensormesh_gb300.h"
+#include "tm_element.cuh"
+#include "tm_status.h"
+
+namespace tmk {
+
+constexpr int kThreads = 256;
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+struct MatLayout {
+    size_t tab, mhl, x, g, jw, ld, lm, le, total;
+};
+
+template <typename R, int ET, int FORMS>
+__host__ __device__ inline MatLayout mat_layout(int CH, int Q) {
+    using T = Traits<ET>;
+    constexpr int D = T::D, B = T::B, NL = B * (B + 1) / 2;
+    constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
+    constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
+    constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
+    MatLayout L;
+    size_t o = 0;
+    L.tab = o;
+    o = align16(o + sizeof(double) * table_layout(Q, B, D).total);
+    L.mhl = o;
+    o = align16(o + sizeof(double) * NL);
+    L.x = L.g = L.jw = o;
+    if (!T::P1) {
+        L.x = o;
+        o = align16(o + sizeof(R) * CH * B * D);
+        L.g = o;
+        o = align16(o + sizeof(R) * CH * Q * B * D);
+        L.jw = o;
+        o = align16(o + sizeof(R) * CH * Q);
+    }
+    L.ld = o;
+    if (DIFF) o = align16(o + sizeof(R) * CH * NL);
+    L.lm = o;
+    if (MASS) o = align16(o + sizeof(R) * CH * (T::P1 ? 1 : NL));
+    L.le = o;
+    if (ELAST) o = align16(o + sizeof(R) * CH * NL * D * D);
+    L.total = o;
+    return L;
+}
+
+template <typename R>
+__device__ __forceinline__ R rabs(R x) { return x < R(0) ? -x : x; }
+
+template <typename R, int ET, int FORMS>
+__global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
+    using T = Traits<ET>;
+    constexpr int D = T::D, B = T::B, NL = B * (B + 1) / 2;
+    constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
+    constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
+    constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
+    constexpr int HH = ELAST ? D * D : 1;
+    const tm_chunk_plan& P = a.plan;
+    const int CH = P.chunk_elems, Q = a.tables.n_quad;
+    const MatLayout L = mat_layout<R, ET, FORMS>(CH, Q);
+    const TableLayout TL = table_layout(Q, B, D);
+    extern __shared__ __align__(16) unsigned char sm[];
+    double* tab = reinterpret_cast<double*>(sm + L.tab);
+    double* mhl = reinterpret_cast<double*>(sm + L.mhl);
+    R* LD = reinterpret_cast<R*>(sm + L.ld);
+    R* LM = reinterpret_cast<R*>(sm + L.lm);
+    R* LE = reinterpret_cast<R*>(sm + L.le);
+
+    for (int k = threadIdx.x; k < TL.total; k += blockDim.x) tab[k] = a.tables.packed[k];
+    __syncthreads();
+    if (MASS && T::P1)
+        for (int l = threadIdx.x; l < NL; l += blockDim.x) {
+            int pa, pb;
+            upper_pair<B>(l, pa, pb);
+            mhl[l] = tab[TL.mhat + pa * B + pb];
+        }
+
+    const int64_t i0 = (int64_t)blockIdx.x * CH;
+    const int ne = (int)min((int64_t)CH, P.n_elements - i0);
+    const R* pts = static_cast<const R*>(a.points);
+    const R* kap = static_cast<const R*>(a.kappa);
+    const R* yng = static_cast<const R*>(a.young);
+    const R kscale = (R)a.kappa_scale, mscale = (R)a.mass_scale, yscale = (R)a.young_scale;
+    const R nu = (R)a.poisson;
+    const R clam = nu / ((R(1) + nu) * (R(1) - R(2) * nu));
+    const R cmu = R(1) / (R(2) * (R(1) + nu));
+
+    if constexpr (T::P1 != 0) {
+        const R wsum = (R)tab[TL.wsum];
+        for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+            const int64_t i = i0 + el;
+            const int e = P.elem_perm[i];
+            R X[B][D];
+#pragma unroll
+            for (int b = 0; b < B; ++b) {
+                const int64_t node = P.conn[i * B + b];
+#pragma unroll
+                for (int d = 0; d < D; ++d) X[b][d] = ldg(pts + node * D + d);
+            }
+            R C[B][D];
+            const R det = p1_gradients<R, D>(X, C);
+            const R adet = rabs(det);
+            if constexpr (DIFF) {
+                const R kv = (kap ? ldg(kap + e) : R(1)) * kscale;
+                const R s = kv * wsum / adet;
+                int l = 0;
+#pragma unroll
+                for (int p = 0; p < B; ++p)
+#pragma unroll
+                    for (int q = p; q < B; ++q, ++l) LD[el * NL + l] = s * dot<R, D>(C[p], C[q]);
+            }
+            if constexpr (MASS) LM[el] = adet * mscale;
+            if constexpr (ELAST) {
+                const R Ey = (yng ? ldg(yng + e) : R(1)) * yscale;
+                const R s = wsum / adet;
+                int l = 0;
+#pragma unroll
+                for (int p = 0; p < B; ++p)
+#pragma unroll
+                    for (int q = p; q < B; ++q, ++l)
+                        elastic_block<R, D>(C[p], C[q], Ey * clam, Ey * cmu, s, LE + (el * NL + l) * HH, false);
+            }
+        }
+    } else {
+        R* X = reinterpret_cast<R*>(sm + L.x);
+        R* G = reinterpret_cast<R*>(sm + L.g);
+        R* JW = reinterpret_cast<R*>(sm + L.jw);
+        for (int k = threadIdx.x; k < ne * B; k += blockDim.x) {
+            const int64_t node = P.conn[i0 * B + k];
+#pragma unroll
+            for (int d = 0; d < D; ++d) X[k * D + d] = ldg(pts + node * D + d);
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < ne * Q; k += blockDim.x) {
+            const int el = k / Q, q = k - el * Q;
+            const double* dphi = tab + TL.dphi + q * D * B;
+            R J[D][D];
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    R s = 0;
+#pragma unroll
+                    for (int b = 0; b < B; ++b) s += (R)dphi[r * B + b] * X[(el * B + b) * D + c];
+                    J[r][c] = s;
+                }
+            R cof[D][D];
+            const R det = cofactors<R>(J, cof);
+            const R inv = R(1) / det;
+            R* g = G + (size_t)k * B * D;
+#pragma unroll
+            for (int b = 0; b < B; ++b)
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    R s = 0;
+#pragma unroll
+                    for (int r = 0; r < D; ++r) s += (R)dphi[r * B + b] * cof[r][c];
+                    g[b * D + c] = s * inv;
+                }
+            JW[k] = (R)tab[TL.w + q] * rabs(det);
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < ne * NL; k += blockDim.x) {
+            const int el = k / NL, l = k - el * NL;
+            int pa, pb;
+            upper_pair<B>(l, pa, pb);
+            const int e = P.elem_perm[i0 + el];
+            if constexpr (DIFF) {
+                R s = 0;
+                for (int q = 0; q < Q; ++q) {
+                    const R* g = G + (size_t)(el * Q + q) * B * D;
+                    s += JW[el * Q + q] * dot<R, D>(g + pa * D, g + pb * D);
+                }
+                LD[k] = s * ((kap ? ldg(kap + e) : R(1)) * kscale);
+            }
+            if constexpr (MASS) {
+                R s = 0;
+                for (int q = 0; q < Q; ++q)
+                    s += JW[el * Q + q] * (R)tab[TL.phi + q * B + pa] * (R)tab[TL.phi + q * B + pb];
+                LM[k] = s * mscale;
+            }
+            if constexpr (ELAST) {
+                const R Ey = (yng ? ldg(yng + e) : R(1)) * yscale;
+                R* blk = LE + (size_t)k * HH;
+                for (int q = 0; q < Q; ++q) {
+                    const R* g = G + (size_t)(el * Q + q) * B * D;
+                    elastic_block<R, D>(g + pa * D, g + pb * D, Ey * clam, Ey * cmu, JW[el * Q + q], blk, q > 0);
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // phase 2: fixed-order reduction of the chunk's targets
+    const int32_t s0 = P.chunk_begin[blockIdx.x], s1 = P.chunk_begin[blockIdx.x + 1];
+    R* oD = static_cast<R*>(a.out_diffusion);
+    R* oM = static_cast<R*>(a.out_mass);
+    R* oE = static_cast<R*>(a.out_elasticity);
+    R* part = static_cast<R*>(a.workspace);
+    const int64_t np = P.n_partials;
+    for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+        const int p0 = P.slot_ptr[s], p1 = P.slot_ptr[s + 1];
+        R ad = 0, am = 0;
+        R ae[HH];
+#pragma unroll
+        for (int k = 0; k < HH; ++k) ae[k] = 0;
+        for (int p = p0; p < p1; ++p) {
+            const int code = P.contrib[p];
+            const int idx = code >> 1;
+            if constexpr (DIFF) ad += LD[idx];
+            if constexpr (MASS) {
+                if constexpr (T::P1 != 0) {
+                    const int el = idx / NL;
+                    am += LM[el] * (R)mhl[idx - el * NL];
+                } else {
+                    am += LM[idx];
+                }
+            }
+            if constexpr (ELAST) {
+                const R* blk = LE + (size_t)idx * HH;
+                if (code & 1) {
+#pragma unroll
+                    for (int r = 0; r < D; ++r)
+#pragma unroll
+                        for (int c = 0; c < D; ++c) ae[r * D + c] += blk[c * D + r];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < HH; ++k) ae[k] += blk[k];
+                }
+            }
+        }
+        const int32_t tgt = P.slot_target[s];
+        if (tgt >= 0) {
+            const int32_t mir = P.slot_mirror[s];
+            if constexpr (DIFF) {
+                oD[tgt] = ad;
+                if (mir != tgt) oD[mir] = ad;
+            }
+            if constexpr (MASS) {
+                oM[tgt] = am;
+                if (mir != tgt) oM[mir] = am;
+            }
+            if constexpr (ELAST) {
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int c = 0; c < D; ++c) {
+                        oE[(int64_t)tgt * HH + r * D + c] = ae[r * D + c];
+                        if (mir != tgt) oE[(int64_t)mir * HH + c * D + r] = ae[r * D + c];
+                    }
+            }
+        } else {
+            const int64_t pi = -(int64_t)tgt - 1;
+            if constexpr (ELAST) {
+#pragma unroll
+                for (int k = 0; k < HH; ++k) part[pi * HH + k] = ae[k];
+            } else {
+                int f = 0;
+                if constexpr (DIFF) part[(f++) * np + pi] = ad;
+                if constexpr (MASS) part[(f++) * np + pi] = am;
+            }
+        }
+    }
+}
+
+// sum the partials of targets shared by several chunks, in chunk order
+template <typename R, int FORMS, int D>
+__global__ void __launch_bounds__(kThreads) k_matrix_finalize(const tm_matrix_args a) {
+    constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
+    constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
+    constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
+    constexpr int HH = ELAST ? D * D : 1;
+    const tm_chunk_plan& P = a.plan;
+    const R* part = static_cast<const R*>(a.workspace);
+    const int64_t np = P.n_partials;
+    R* oD = static_cast<R*>(a.out_diffusion);
+    R* oM = static_cast<R*>(a.out_mass);
+    R* oE = static_cast<R*>(a.out_elasticity);
+    for (int64_t sh = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sh < P.n_shared;
+         sh += (int64_t)gridDim.x * blockDim.x) {
+        const int p0 = P.shared_ptr[sh], p1 = P.shared_ptr[sh + 1];
+        const int64_t tgt = P.shared_target[sh], mir = P.shared_mirror[sh];
+        if constexpr (ELAST) {
+            R acc[HH];
+#pragma unroll
+            for (int k = 0; k < HH; ++k) acc[k] = 0;
+            for (int p = p0; p < p1; ++p)
+#pragma unroll
+                for (int k = 0; k < HH; ++k) acc[k] += part[(int64_t)p * HH + k];
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    oE[tgt * HH + r * D + c] = acc[r * D + c];
+                    if (mir != tgt) oE[mir * HH + c * D + r] = acc[r * D + c];
+                }
+        } else {
+            int f = 0;
+            if constexpr (DIFF) {
+                R acc = 0;
+                for (int p = p0; p < p1; ++p) acc += part[f * np + p];
+                oD[tgt] = acc;
+                if (mir != tgt) oD[mir] = acc;
+                ++f;
+            }
+            if constexpr (MASS) {
+                R acc = 0;
+                for (int p = p0; p < p1; ++p) acc += part[f * np + p];
+                oM[tgt] = acc;
+                if (mir != tgt) oM[mir] = acc;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- vectors
+struct VecLayout {
+    size_t tab, lv, total;
+};
+template <typename R, int ET, int W>
+__host__ __device__ inline VecLayout vec_layout(int CH, int Q) {
+    using T = Traits<ET>;
+    VecLayout L;
+    L.tab = 0;
+    L.lv = align16(sizeof(double) * table_layout(Q, T::B, T::D).total);
+    L.total = align16(L.lv + sizeof(R) * CH * T::B * W);
+    return L;
+}
+
+template <typename R, int ET, int SRC, int W>
+__global__ void __launch_bounds__(kThreads) k_vector(const tm_vector_args a) {
+    using T = Traits<ET>;
+    constexpr int D = T::D, B = T::B;
+    const tm_chunk_plan& P = a.plan;
+    const int CH = P.chunk_elems, Q = a.tables.n_quad;
+    const VecLayout L = vec_layout<R, ET, W>(CH, Q);
+    const TableLayout TL = table_layout(Q, B, D);
+    extern __shared__ __align__(16) unsigned char sm[];
+    double* tab = reinterpret_cast<double*>(sm + L.tab);
+    R* LV = reinterpret_cast<R*>(sm + L.lv);
+    for (int k = threadIdx.x; k < TL.total; k += blockDim.x) tab[k] = a.tables.packed[k];
+    __syncthreads();
+
+    const int64_t i0 = (int64_t)blockIdx.x * CH;
+    const int ne = (int)min((int64_t)CH, P.n_elements - i0);
+    const R* pts = static_cast<const R*>(a.points);
+    const R* val = static_cast<const R*>(a.values);
+    for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+        const int64_t i = i0 + el;
+        const int64_t e = P.elem_perm[i];
+        int32_t c[B];
+        R X[B][D];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            c[b] = P.conn[i * B + b];
+#pragma unroll
+            for (int d = 0; d < D; ++d) X[b][d] = ldg(pts + (int64_t)c[b] * D + d);
+        }
+        R acc[B][W];
+#pragma unroll
+        for (int p = 0; p < B; ++p)
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[p][w] = 0;
+        if constexpr (T::P1 != 0) {
+            R Xs[D + 1][D], C[D + 1][D];
+#pragma unroll
+            for (int b = 0; b <= D; ++b)
+#pragma unroll
+                for (int d = 0; d < D; ++d) Xs[b][d] = X[b][d];
+            const R adet = rabs(p1_gradients<R, D>(Xs, C));
+#pragma unroll
+            for (int p = 0; p < B; ++p)
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    R s = 0;
+                    if constexpr (SRC == TM_SOURCE_NODAL) {
+#pragma unroll
+                        for (int b = 0; b < B; ++b) s += (R)tab[TL.mhat + p * B + b] * ldg(val + (int64_t)c[b] * W + w);
+                    } else if constexpr (SRC == TM_SOURCE_CONST) {
+                        s = (R)tab[TL.lhat + p] * (R)a.constant[w];
+                    } else {
+                        for (int q = 0; q < Q; ++q)
+                            s += (R)tab[TL.w + q] * (R)tab[TL.phi + q * B + p] * ldg(val + (e * Q + q) * W + w);
+                    }
+                    acc[p][w] = adet * s;
+                }
+        } else {
+            for (int q = 0; q < Q; ++q) {
+                const double* dphi = tab + TL.dphi + q * D * B;
+                const double* phi = tab + TL.phi + q * B;
+                R J[D][D];
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int cc = 0; cc < D; ++cc) {
+                        R s = 0;
+#pragma unroll
+                        for (int b = 0; b < B; ++b) s += (R)dphi[r * B + b] * X[b][cc];
+                        J[r][cc] = s;
+                    }
+                R cof[D][D];
+                const R jxw = (R)tab[TL.w + q] * rabs(cofactors<R>(J, cof));
+                R fq[W];
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    if constexpr (SRC == TM_SOURCE_NODAL) {
+                        R s = 0;
+#pragma unroll
+                        for (int b = 0; b < B; ++b) s += ldg(val + (int64_t)c[b] * W + w) * (R)phi[b];
+                        fq[w] = s;
+                    } else if constexpr (SRC == TM_SOURCE_CONST) {
+                        fq[w] = (R)a.constant[w];
+                    } else {
+                        fq[w] = ldg(val + (e * Q + q) * W + w);
+                    }
+                }
+#pragma unroll
+                for (int p = 0; p < B; ++p)
+#pragma unroll
+                    for (int w = 0; w < W; ++w) acc[p][w] += jxw * (R)phi[p] * fq[w];
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < B; ++p)
+#pragma unroll
+            for (int w = 0; w < W; ++w) LV[(el * B + p) * W + w] = acc[p][w];
+    }
+    __syncthreads();
+    const int32_t s0 = P.chunk_begin[blockIdx.x], s1 = P.chunk_begin[blockIdx.x + 1];
+    R* out = static_cast<R*>(a.out);
+    R* part = static_cast<R*>(a.workspace);
+    for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+        const int p0 = P.slot_ptr[s], p1 = P.slot_ptr[s + 1];
+        R acc[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] = 0;
+        for (int p = p0; p < p1; ++p) {
+            const int idx = P.contrib[p] >> 1;
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[w] += LV[idx * W + w];
+        }
+        const int32_t tgt = P.slot_target[s];
+        if (tgt >= 0) {
+#pragma unroll
+            for (int w = 0; w < W; ++w) out[(int64_t)tgt * W + w] = acc[w];
+        } else {
+            const int64_t pi = -(int64_t)tgt - 1;
+#pragma unroll
+            for (int w = 0; w < W; ++w) part[pi * W + w] = acc[w];
+        }
+    }
+}
+
+template <typename R, int W>
+__global__ void __launch_bounds__(kThreads) k_vector_finalize(const tm_vector_args a) {
+    const tm_chunk_plan& P = a.plan;
+    const R* part = static_cast<const R*>(a.workspace);
+    R* out = static_cast<R*>(a.out);
+    for (int64_t sh = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sh < P.n_shared;
+         sh += (int64_t)gridDim.x * blockDim.x) {
+        const int p0 = P.shared_ptr[sh], p1 = P.shared_ptr[sh + 1];
+        const int64_t tgt = P.shared_target[sh];
+        R acc[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] = 0;
+        for (int p = p0; p < p1; ++p)
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[w] += part[(int64_t)p * W + w];
+#pragma unroll
+        for (int w = 0; w < W; ++w) out[tgt * W + w] = acc[w];
+    }
+}
+
+// ----------------------------------------------------- geometry, x at q
+template <int ET>
+__global__ void __launch_bounds__(kThreads) k_shape_grad_jxw(int64_t E, const int32_t* conn, const double* pts,
+                                                            tm_element_tables tb, double* grad, double* jxw) {
+    using T = Traits<ET>;
+    constexpr int D = T::D, B = T::B;
+    const int Q = tb.n_quad;
+    const TableLayout TL = table_layout(Q, B, D);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < E * Q;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = k / Q;
+        const int q = (int)(k - e * Q);
+        const double* dphi = tb.packed + TL.dphi + q * D * B;
+        double X[B][D];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const int64_t node = conn[e * B + b];
+#pragma unroll
+            for (int d = 0; d < D; ++d) X[b][d] = ldg(pts + node * D + d);
+        }
+        double J[D][D];
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                double s = 0;
+#pragma unroll
+                for (int b = 0; b < B; ++b) s += ldg(dphi + r * B + b) * X[b][c];
+                J[r][c] = s;
+            }
+        double cof[D][D];
+        const double det = cofactors<double>(J, cof);
+        const double inv = 1.0 / det;
+#pragma unroll
+        for (int b = 0; b < B; ++b)
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                double s = 0;
+#pragma unroll
+                for (int r = 0; r < D; ++r) s += ldg(dphi + r * B + b) * cof[r][c];
+                grad[(k * B + b) * D + c] = s * inv;
+            }
+        jxw[k] = ldg(tb.packed + TL.w + q) * fabs(det);
+    }
+}
+
+template <typename R, int ET>
+__global__ void __launch_bounds__(kThreads) k_quadrature_points(int64_t E, const int32_t* conn, const R* pts,
+                                                               tm_element_tables tb, R* xq) {
+    using T = Traits<ET>;
+    constexpr int D = T::D, B = T::B;
+    const int Q = tb.n_quad;
+    const TableLayout TL = table_layout(Q, B, D);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < E * Q;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = k / Q;
+        const int q = (int)(k - e * Q);
+        R x[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) x[d] = 0;
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const int64_t node = conn[e * B + b];
+            const R ph = (R)ldg(tb.packed + TL.phi + q * B + b);
+#pragma unroll
+            for (int d = 0; d < D; ++d) x[d] += ph * ldg(pts + node * D + d);
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) xq[k * D + d] = x[d];
+    }
+}
+
+// ------------------------------------------------------------- projector
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_project(int64_t n_to, int64_t width, const int64_t* seg,
+                                                     const int64_t* src, const R* x, R* out) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_to * width;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = k / width, w = k - t * width;
+        R s = 0;
+        for (int64_t p = seg[t]; p < seg[t + 1]; ++p) s += x[src[p] * width + w];
+        out[k] = s;
+    }
+}
+
+inline int grid_for(int64_t work, int per_block = kThreads) {
+    int64_t g = (work + per_block - 1) / per_block;
+    if (g < 1) g = 1;
+    if (g > 152 * 64) g = 152 * 64;
+    return (int)g;
+}
+
+inline int launch_status(const char* what) {
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        char buf[256];
+        snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(err));
+        return tm_set_error(TM_ERR_CUDA, buf);
+    }
+    return TM_OK;
+}
+
+template <typename K>
+inline int set_smem(K kernel, size_t bytes) {
+    if (bytes > 48 * 1024) {
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+            return launch_status("cudaFuncSetAttribute");
+    }
+    return TM_OK;
+}
+
+template <typename R, int ET, int FORMS>
+int run_matrix(const tm_matrix_args& a, cudaStream_t st) {
+    using T = Traits<ET>;
+    const MatLayout L = mat_layout<R, ET, FORMS>(a.plan.chunk_elems, a.tables.n_quad);
+    if (L.total > 227 * 1024) return tm_set_error(TM_ERR_TOO_LARGE, "tm_assemble_matrix: chunk needs more than 227 KB of shared memory");
+    if (a.plan.n_chunks > 0) {
+        int s = set_smem(k_matrix<R, ET, FORMS>, L.total);
+        if (s) return s;
+        if (a.event_begin && cudaEventRecord(static_cast<cudaEvent_t>(a.event_begin), st) != cudaSuccess)
+            return launch_status("cudaEventRecord");
+        k_matrix<R, ET, FORMS><<<a.plan.n_chunks, kThreads, L.total, st>>>(a);
+        if ((s = launch_status("k_matrix"))) return s;
+        if (a.event_end && cudaEventRecord(static_cast<cudaEvent_t>(a.event_end), st) != cudaSuccess)
+            return launch_status("cudaEventRecord");
+    }
+    if (a.plan.n_shared > 0) {
+        k_matrix_finalize<R, FORMS, T::D><<<grid_for(a.plan.n_shared), kThreads, 0, st>>>(a);
+        return launch_status("k_matrix_finalize");
+    }
+    return TM_OK;
+}
+
+template <typename R, int ET>
+int dispatch_forms(const tm_matrix_args& a, cudaStream_t st) {
+    switch (a.forms) {
+        case TM_FORM_DIFFUSION: return run_matrix<R, ET, TM_FORM_DIFFUSION>(a, st);
+        case TM_FORM_MASS: return run_matrix<R, ET, TM_FORM_MASS>(a, st);
+        case TM_FORM_DIFFUSION | TM_FORM_MASS: return run_matrix<R, ET, TM_FORM_DIFFUSION | TM_FORM_MASS>(a, st);
+        case TM_FORM_ELASTICITY: return run_matrix<R, ET, TM_FORM_ELASTICITY>(a, st);
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_matrix: unsupported form combination");
+    }
+}
+
+template <typename R>
+int dispatch_matrix(const tm_matrix_args& a, cudaStream_t st) {
+    switch (a.tables.element_type) {
+        case TM_TRI3: return dispatch_forms<R, TM_TRI3>(a, st);
+        case TM_TET4: return dispatch_forms<R, TM_TET4>(a, st);
+        case TM_TRI6: return dispatch_forms<R, TM_TRI6>(a, st);
+        case TM_TET10: return dispatch_forms<R, TM_TET10>(a, st);
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_matrix: unknown element type");
+    }
+}
+
+template <typename R, int ET, int SRC, int W>
+int run_vector(const tm_vector_args& a, cudaStream_t st) {
+    const VecLayout L = vec_layout<R, ET, W>(a.plan.chunk_elems, a.tables.n_quad);
+    if (L.total > 227 * 1024) return tm_set_error(TM_ERR_TOO_LARGE, "tm_assemble_vector: chunk needs more than 227 KB of shared memory");
+    if (cudaMemsetAsync(a.out, 0, sizeof(R) * a.n_points * W, st) != cudaSuccess)
+        return launch_status("cudaMemsetAsync");
+    if (a.plan.n_chunks > 0) {
+        int s = set_smem(k_vector<R, ET, SRC, W>, L.total);
+        if (s) return s;
+        k_vector<R, ET, SRC, W><<<a.plan.n_chunks, kThreads, L.total, st>>>(a);
+        if ((s = launch_status("k_vector"))) return s;
+    }
+    if (a.plan.n_shared > 0) {
+        k_vector_finalize<R, W><<<grid_for(a.plan.n_shared), kThreads, 0, st>>>(a);
+        return launch_status("k_vector_finalize");
+    }
+    return TM_OK;
+}
+
+template <typename R, int ET, int SRC>
+int dispatch_width(const tm_vector_args& a, cudaStream_t st) {
+    switch (a.width) {
+        case 1: return run_vector<R, ET, SRC, 1>(a, st);
+        case 2: return run_vector<R, ET, SRC, 2>(a, st);
+        case 3: return run_vector<R, ET, SRC, 3>(a, st);
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_vector: width must be 1..3");
+    }
+}
+
+template <typename R, int ET>
+int dispatch_source(const tm_vector_args& a, cudaStream_t st) {
+    switch (a.source) {
+        case TM_SOURCE_NODAL: return dispatch_width<R, ET, TM_SOURCE_NODAL>(a, st);
+        case TM_SOURCE_CONST: return dispatch_width<R, ET, TM_SOURCE_CONST>(a, st);
+        case TM_SOURCE_QUAD: return dispatch_width<R, ET, TM_SOURCE_QUAD>(a, st);
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_vector: unknown source kind");
+    }
+}
+
+template <typename R>
+int dispatch_vector(const tm_vector_args& a, cudaStream_t st) {
+    switch (a.tables.element_type) {
+        case TM_TRI3: return dispatch_source<R, TM_TRI3>(a, st);
+        case TM_TET4: return dispatch_source<R, TM_TET4>(a, st);
+        case TM_TRI6: return dispatch_source<R, TM_TRI6>(a, st);
+        case TM_TET10: return dispatch_source<R, TM_TET10>(a, st);
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_vector: unknown element type");
+    }
+}
+
+inline int basis_of(int et) {
+    switch (et) {
+        case TM_TRI3: return 3;
+        case TM_TET4: return 4;
+        case TM_TRI6: return 6;
+        case TM_TET10: return 10;
+        default: return -1;
+    }
+}
+
+int check_plan(const tm_chunk_plan& P, int B, int n_local, const char* who) {
+    char buf[256];
+    if (P.n_basis != B || P.n_local != n_local) {
+        snprintf(buf, sizeof(buf), "%s: plan has %d basis / %d local entries, expected %d / %d", who,
+                 P.n_basis, P.n_local, B, n_local);
+        return tm_set_error(TM_ERR_INVALID_ARG, buf);
+    }
+    if (P.n_elements > 0 && (!P.elem_perm || !P.conn || !P.chunk_begin || !P.slot_ptr || !P.contrib ||
+                             !P.slot_target || !P.slot_mirror))
+        return tm_set_error(TM_ERR_INVALID_ARG, "plan arrays must not be null");
+    if (P.n_shared > 0 && (!P.shared_ptr || !P.shared_target || !P.shared_mirror))
+        return tm_set_error(TM_ERR_INVALID_ARG, "plan shared arrays must not be null");
+    if (P.chunk_elems < 1 || (int64_t)P.chunk_elems * P.n_local * 2 > 65536)
+        return tm_set_error(TM_ERR_INVALID_ARG, "plan chunk size out of range");
+    return TM_OK;
+}
+
+}  // namespace tmk
+
+using namespace tmk;
+
+extern "C" size_t tm_matrix_workspace_bytes(const tm_matrix_args* a) {
+    if (!a) return 0;
+    const size_t rs = a->dtype == TM_F32 ? 4 : 8;
+    int per = 0;
+    if (a->forms & TM_FORM_ELASTICITY) {
+        const int D = (a->tables.element_type == TM_TRI3 || a->tables.element_type == TM_TRI6) ? 2 : 3;
+        per = D * D;
+    } else {
+        per = ((a->forms & TM_FORM_DIFFUSION) ? 1 : 0) + ((a->forms & TM_FORM_MASS) ? 1 : 0);
+    }
+    return rs * (size_t)a->plan.n_partials * per;
+}
+
+extern "C" int tm_assemble_matrix(const tm_matrix_args* a, tm_stream_t stream) {
+    if (!a) return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: null args");
+    const int B = basis_of(a->tables.element_type);
+    if (B < 0) return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_matrix: unknown element type");
+    int s = check_plan(a->plan, B, B * (B + 1) / 2, "tm_assemble_matrix");
+    if (s) return s;
+    if ((a->forms & TM_FORM_ELASTICITY) && (a->forms & ~TM_FORM_ELASTICITY))
+        return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_matrix: elasticity cannot be fused with other forms");
+    if (!a->tables.packed || a->tables.n_quad < 1)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: missing element tables");
+    if (a->plan.n_elements > 0 && !a->points)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: points is null");
+    if (((a->forms & TM_FORM_DIFFUSION) && !a->out_diffusion) || ((a->forms & TM_FORM_MASS) && !a->out_mass) ||
+        ((a->forms & TM_FORM_ELASTICITY) && !a->out_elasticity))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: output pointer is null");
+    if (a->plan.n_partials > 0 && !a->workspace)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: workspace is null");
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (a->dtype == TM_F64) return dispatch_matrix<double>(*a, st);
+    if (a->dtype == TM_F32) return dispatch_matrix<float>(*a, st);
+    return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: dtype must be TM_F64 or TM_F32");
+}
+
+extern "C" size_t tm_vector_workspace_bytes(const tm_vector_args* a) {
+    if (!a) return 0;
+    return (a->dtype == TM_F32 ? 4 : 8) * (size_t)a->plan.n_partials * (size_t)a->width;
+}
+
+extern "C" int tm_assemble_vector(const tm_vector_args* a, tm_stream_t stream) {
+    if (!a) return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_vector: null args");
+    const int B = basis_of(a->tables.element_type);
+    if (B < 0) return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_vector: unknown element type");
+    int s = check_plan(a->plan, B, B, "tm_assemble_vector");
+    if (s) return s;
+    if (!a->tables.packed || a->tables.n_quad < 1)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_vector: missing element tables");
+    if (!a->out || (a->plan.n_elements > 0 && !a->points) ||
+        (a->source != TM_SOURCE_CONST && a->plan.n_elements > 0 && !a->values))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_vector: null pointer");
+    if (a->plan.n_partials > 0 && !a->workspace)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_vector: workspace is null");
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (a->dtype == TM_F64) return dispatch_vector<double>(*a, st);
+    if (a->dtype == TM_F32) return dispatch_vector<float>(*a, st);
+    return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_vector: dtype must be TM_F64 or TM_F32");
+}
+
+extern "C" int tm_shape_grad_jxw(int64_t E, const int32_t* conn, const double* points, tm_element_tables tb,
+                                 double* grad, double* jxw, tm_stream_t stream) {
+    if (E < 0 || (E > 0 && (!conn || !points || !grad || !jxw || !tb.packed)))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_shape_grad_jxw: bad arguments");
+    if (E == 0) return TM_OK;
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int g = grid_for(E * tb.n_quad);
+    switch (tb.element_type) {
+        case TM_TRI3: k_shape_grad_jxw<TM_TRI3><<<g, kThreads, 0, st>>>(E, conn, points, tb, grad, jxw); break;
+        case TM_TET4: k_shape_grad_jxw<TM_TET4><<<g, kThreads, 0, st>>>(E, conn, points, tb, grad, jxw); break;
+        case TM_TRI6: k_shape_grad_jxw<TM_TRI6><<<g, kThreads, 0, st>>>(E, conn, points, tb, grad, jxw); break;
+        case TM_TET10: k_shape_grad_jxw<TM_TET10><<<g, kThreads, 0, st>>>(E, conn, points, tb, grad, jxw); break;
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_shape_grad_jxw: unknown element type");
+    }
+    return launch_status("k_shape_grad_jxw");
+}
+
+template <typename R>
+static int run_xq(int64_t E, const int32_t* conn, const void* pts, tm_element_tables tb, void* xq, cudaStream_t st) {
+    const int g = grid_for(E * tb.n_quad);
+    const R* p = static_cast<const R*>(pts);
+    R* o = static_cast<R*>(xq);
+    switch (tb.element_type) {
+        case TM_TRI3: k_quadrature_points<R, TM_TRI3><<<g, kThreads, 0, st>>>(E, conn, p, tb, o); break;
+        case TM_TET4: k_quadrature_points<R, TM_TET4><<<g, kThreads, 0, st>>>(E, conn, p, tb, o); break;
+        case TM_TRI6: k_quadrature_points<R, TM_TRI6><<<g, kThreads, 0, st>>>(E, conn, p, tb, o); break;
+        case TM_TET10: k_quadrature_points<R, TM_TET10><<<g, kThreads, 0, st>>>(E, conn, p, tb, o); break;
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_quadrature_points: unknown element type");
+    }
+    return launch_status("k_quadrature_points");
+}
+
+extern "C" int tm_quadrature_points(int32_t dtype, int64_t E, const int32_t* conn, const void* points,
+                                    tm_element_tables tb, void* xq, tm_stream_t stream) {
+    if (E < 0 || (E > 0 && (!conn || !points || !xq || !tb.packed)))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_quadrature_points: bad arguments");
+    if (E == 0) return TM_OK;
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (dtype == TM_F64) return run_xq<double>(E, conn, points, tb, xq, st);
+    if (dtype == TM_F32) return run_xq<float>(E, conn, points, tb, xq, st);
+    return tm_set_error(TM_ERR_INVALID_ARG, "tm_quadrature_points: bad dtype");
+}
+
+extern "C" int tm_project_reduce(int32_t dtype, int64_t n_to, int64_t width, const int64_t* seg_ptr,
+                                 const int64_t* src, const void* x, void* out, tm_stream_t stream) {
+    if (n_to < 0 || width < 1 || (n_to > 0 && (!seg_ptr || !out)))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_project_reduce: bad arguments");
+    if (n_to == 0) return TM_OK;
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int g = grid_for(n_to * width);
+    if (dtype == TM_F64)
+        k_project<double><<<g, kThreads, 0, st>>>(n_to, width, seg_ptr, src, static_cast<const double*>(x),
+                                                  static_cast<double*>(out));
+    else if (dtype == TM_F32)
+        k_project<float><<<g, kThreads, 0, st>>>(n_to, width, seg_ptr, src, static_cast<const float*>(x),
+                                                 static_cast<float*>(out));
+    else
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_project_reduce: bad dtype");
+    return launch_status("k_project");
+}

@@ -1,0 +1,303 @@
+// Host-side construction of the CSR pattern, the element->CSR slot map and
+// the element-chunk reduction plan (see tm_chunk_plan in the public header).
+//
+// Pattern and slot map reproduce ElementAssembler.from_mesh
+// (assemble/element_assembler.py:811-830): every local pair (i, j) of every
+// element contributes (conn[e,i], conn[e,j]); the pattern is the set of
+// distinct pairs sorted row-major, stored as int32 rows/cols, and the slot
+// map gives, element-major then i then j, the position of each pair in that
+// list.  Here it is built by a counting sort on rows and a per-row sort, in
+// O(E*B^2 log(deg)) time, instead of SciPy's COO->CSR conversion.
+#include "../../include/tensormesh_gb300.h"
+#include "tm_status.h"
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+struct tm_host_plan {
+    int32_t kind = 0, n_basis = 0, n_local = 0, chunk_elems = 0, n_chunks = 0;
+    int64_t n_elements = 0, n_points = 0, nnz = 0, n_partials = 0;
+    std::vector<int32_t> edge_row, edge_col;
+    std::vector<int64_t> slot;
+    std::vector<int32_t> chunk_begin, slot_ptr, slot_target, slot_mirror;
+    std::vector<uint16_t> contrib;
+    std::vector<int32_t> shared_ptr, shared_target, shared_mirror;
+    std::vector<int32_t> conn, perm;
+};
+
+namespace {
+
+struct Contribution {
+    int32_t target;
+    int32_t mirror;
+    uint16_t code;
+};
+
+void build_pattern(tm_host_plan& p, const int64_t* conn) {
+    const int64_t E = p.n_elements, N = p.n_points;
+    const int B = p.n_basis;
+    // counting sort of all E*B*B (row, col) pairs by row
+    std::vector<int64_t> row_ptr(N + 1, 0);
+    for (int64_t e = 0; e < E; ++e)
+        for (int a = 0; a < B; ++a) row_ptr[conn[e * B + a] + 1] += B;
+    for (int64_t r = 0; r < N; ++r) row_ptr[r + 1] += row_ptr[r];
+    std::vector<int32_t> cols(row_ptr[N]);
+    std::vector<int64_t> fill(row_ptr.begin(), row_ptr.end() - 1);
+    for (int64_t e = 0; e < E; ++e)
+        for (int a = 0; a < B; ++a) {
+            const int64_t r = conn[e * B + a];
+            for (int b = 0; b < B; ++b) cols[fill[r]++] = (int32_t)conn[e * B + b];
+        }
+    // sort + unique per row
+    std::vector<int64_t> urow_ptr(N + 1, 0);
+    int64_t nnz = 0;
+    for (int64_t r = 0; r < N; ++r) {
+        int32_t* s = cols.data() + row_ptr[r];
+        int32_t* t = cols.data() + row_ptr[r + 1];
+        std::sort(s, t);
+        int32_t* u = std::unique(s, t);
+        const int64_t cnt = u - s;
+        std::memmove(cols.data() + nnz, s, cnt * sizeof(int32_t));
+        nnz += cnt;
+        urow_ptr[r + 1] = nnz;
+    }
+    p.nnz = nnz;
+    p.edge_row.resize(nnz);
+    p.edge_col.assign(cols.begin(), cols.begin() + nnz);
+    for (int64_t r = 0; r < N; ++r)
+        for (int64_t k = urow_ptr[r]; k < urow_ptr[r + 1]; ++k) p.edge_row[k] = (int32_t)r;
+    // slot map, element-major, i-major, j-minor
+    p.slot.resize((size_t)E * B * B);
+    const int32_t* ucol = p.edge_col.data();
+    for (int64_t e = 0; e < E; ++e)
+        for (int a = 0; a < B; ++a) {
+            const int64_t r = conn[e * B + a];
+            const int32_t* s = ucol + urow_ptr[r];
+            const int32_t* t = ucol + urow_ptr[r + 1];
+            for (int b = 0; b < B; ++b) {
+                const int32_t c = (int32_t)conn[e * B + b];
+                p.slot[(e * B + a) * B + b] = (int64_t)(std::lower_bound(s, t, c) - ucol);
+            }
+        }
+}
+
+int build_chunks(tm_host_plan& p) {
+    const int64_t E = p.n_elements;
+    const int B = p.n_basis, NL = p.n_local, CH = p.chunk_elems;
+    const bool matrix = p.kind == TM_PLAN_KIND_MATRIX;
+    const int64_t n_targets = matrix ? p.nnz : p.n_points;
+    if ((int64_t)CH * NL * 2 > 65536) return TM_ERR_TOO_LARGE;
+    p.n_chunks = (int32_t)((E + CH - 1) / CH);
+    p.chunk_begin.assign(p.n_chunks + 1, 0);
+    p.slot_ptr.clear();
+    p.slot_ptr.push_back(0);
+    std::vector<Contribution> buf;
+    std::vector<int32_t> order;
+    std::vector<int32_t> chunks_per_target(n_targets, 0);
+    std::vector<int32_t> mirror_of(matrix ? n_targets : 0, -1);
+    for (int32_t k = 0; k < p.n_chunks; ++k) {
+        const int64_t i0 = (int64_t)k * CH, i1 = std::min<int64_t>(E, i0 + CH);
+        buf.clear();
+        for (int64_t i = i0; i < i1; ++i) {
+            const int el = (int)(i - i0);
+            const int64_t e = p.perm[i];
+            const int32_t* c = p.conn.data() + i * B;
+            if (matrix) {
+                int l = 0;
+                for (int a = 0; a < B; ++a)
+                    for (int b = a; b < B; ++b, ++l) {
+                        const int64_t pab = p.slot[(e * B + a) * B + b];
+                        const int64_t pba = p.slot[(e * B + b) * B + a];
+                        const uint16_t code = (uint16_t)((el * NL + l) << 1);
+                        if (c[a] < c[b]) {
+                            buf.push_back({(int32_t)pab, (int32_t)pba, code});
+                        } else if (c[a] > c[b]) {
+                            buf.push_back({(int32_t)pba, (int32_t)pab, (uint16_t)(code | 1)});
+                        } else {
+                            buf.push_back({(int32_t)pab, (int32_t)pab, code});
+                            if (a != b) buf.push_back({(int32_t)pab, (int32_t)pab, (uint16_t)(code | 1)});
+                        }
+                    }
+            } else {
+                for (int a = 0; a < B; ++a)
+                    buf.push_back({c[a], -1, (uint16_t)((el * NL + a) << 1)});
+            }
+        }
+        order.resize(buf.size());
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int32_t x, int32_t y) { return buf[x].target < buf[y].target; });
+        for (size_t q = 0; q < order.size(); ++q) {
+            const Contribution& cb = buf[order[q]];
+            if (q == 0 || buf[order[q - 1]].target != cb.target) {
+                if (q != 0) p.slot_ptr.push_back((int32_t)p.contrib.size());
+                p.slot_target.push_back(cb.target);
+                p.slot_mirror.push_back(cb.mirror);
+                chunks_per_target[cb.target] += 1;
+                if (matrix) mirror_of[cb.target] = cb.mirror;
+            }
+            p.contrib.push_back(cb.code);
+        }
+        if (!order.empty()) p.slot_ptr.push_back((int32_t)p.contrib.size());
+        p.chunk_begin[k + 1] = (int32_t)p.slot_target.size();
+    }
+    // shared targets, numbered in increasing target order; their partials are
+    // contiguous per target and ordered by chunk
+    std::vector<int32_t> shared_index(n_targets, -1);
+    p.shared_ptr.assign(1, 0);
+    for (int64_t t = 0; t < n_targets; ++t)
+        if (chunks_per_target[t] > 1) {
+            shared_index[t] = (int32_t)p.shared_target.size();
+            p.shared_target.push_back((int32_t)t);
+            p.shared_mirror.push_back(matrix ? mirror_of[t] : -1);
+            p.shared_ptr.push_back(p.shared_ptr.back() + chunks_per_target[t]);
+        }
+    p.n_partials = p.shared_ptr.back();
+    std::vector<int32_t> used(p.shared_target.size(), 0);
+    for (size_t s = 0; s < p.slot_target.size(); ++s) {
+        const int32_t t = p.slot_target[s];
+        const int32_t sh = shared_index[t];
+        if (sh >= 0) {
+            const int32_t part = p.shared_ptr[sh] + used[sh]++;
+            p.slot_target[s] = -(part + 1);
+        }
+    }
+    return TM_OK;
+}
+
+}  // namespace
+
+extern "C" int tm_plan_build(const int64_t* conn, int64_t n_elements, int32_t n_basis,
+                             int64_t n_points, int32_t kind, int32_t chunk_elems,
+                             const int32_t* perm, const int64_t* slot_map, tm_host_plan** out) {
+    if (!out) return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_build: out is null");
+    *out = nullptr;
+    if (n_elements < 0 || n_basis < 1 || n_basis > 10 || n_points < 0 || chunk_elems < 1 ||
+        (kind != TM_PLAN_KIND_MATRIX && kind != TM_PLAN_KIND_NODE) || (n_elements > 0 && !conn))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_build: bad arguments");
+    if (n_points > INT32_MAX || n_elements > INT32_MAX)
+        return tm_set_error(TM_ERR_TOO_LARGE, "tm_plan_build: more than 2^31 nodes or elements");
+    tm_host_plan* p = new (std::nothrow) tm_host_plan();
+    if (!p) return tm_set_error(TM_ERR_PLAN, "tm_plan_build: out of host memory");
+    try {
+        p->kind = kind;
+        p->n_elements = n_elements;
+        p->n_basis = n_basis;
+        p->n_points = n_points;
+        p->chunk_elems = chunk_elems;
+        p->n_local = kind == TM_PLAN_KIND_MATRIX ? n_basis * (n_basis + 1) / 2 : n_basis;
+        for (int64_t k = 0; k < n_elements * n_basis; ++k)
+            if (conn[k] < 0 || conn[k] >= n_points) {
+                delete p;
+                return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_build: connectivity index out of range");
+            }
+        p->perm.resize(n_elements);
+        if (perm) {
+            std::vector<char> seen(n_elements, 0);
+            for (int64_t i = 0; i < n_elements; ++i) {
+                if (perm[i] < 0 || perm[i] >= n_elements || seen[perm[i]]) {
+                    delete p;
+                    return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_build: perm is not a permutation");
+                }
+                seen[perm[i]] = 1;
+                p->perm[i] = perm[i];
+            }
+        } else {
+            std::iota(p->perm.begin(), p->perm.end(), 0);
+        }
+        p->conn.resize((size_t)n_elements * n_basis);
+        for (int64_t i = 0; i < n_elements; ++i)
+            for (int a = 0; a < n_basis; ++a)
+                p->conn[i * n_basis + a] = (int32_t)conn[(int64_t)p->perm[i] * n_basis + a];
+        if (kind == TM_PLAN_KIND_MATRIX) {
+            if (slot_map) {
+                p->slot.assign(slot_map, slot_map + (size_t)n_elements * n_basis * n_basis);
+                int64_t mx = -1;
+                for (int64_t v : p->slot) mx = std::max(mx, v);
+                p->nnz = mx + 1;
+            } else {
+                build_pattern(*p, conn);
+            }
+            if (p->nnz > INT32_MAX) {
+                delete p;
+                return tm_set_error(TM_ERR_TOO_LARGE, "tm_plan_build: more than 2^31 CSR entries");
+            }
+        }
+        const int st = build_chunks(*p);
+        if (st != TM_OK) {
+            delete p;
+            return tm_set_error(st, "tm_plan_build: chunk_elems * n_local * 2 exceeds 65536");
+        }
+    } catch (const std::bad_alloc&) {
+        delete p;
+        return tm_set_error(TM_ERR_PLAN, "tm_plan_build: out of host memory");
+    }
+    *out = p;
+    return TM_OK;
+}
+
+extern "C" int64_t tm_plan_array_size(const tm_host_plan* p, int32_t id) {
+    if (!p) return -1;
+    switch (id) {
+        case TM_PLAN_EDGE_ROW: return (int64_t)p->edge_row.size();
+        case TM_PLAN_EDGE_COL: return (int64_t)p->edge_col.size();
+        case TM_PLAN_SLOT: return (int64_t)p->slot.size();
+        case TM_PLAN_CHUNK_BEGIN: return (int64_t)p->chunk_begin.size();
+        case TM_PLAN_SLOT_PTR: return (int64_t)p->slot_ptr.size();
+        case TM_PLAN_CONTRIB: return (int64_t)p->contrib.size();
+        case TM_PLAN_SLOT_TARGET: return (int64_t)p->slot_target.size();
+        case TM_PLAN_SLOT_MIRROR: return (int64_t)p->slot_mirror.size();
+        case TM_PLAN_SHARED_PTR: return (int64_t)p->shared_ptr.size();
+        case TM_PLAN_SHARED_TARGET: return (int64_t)p->shared_target.size();
+        case TM_PLAN_SHARED_MIRROR: return (int64_t)p->shared_mirror.size();
+        case TM_PLAN_CONN: return (int64_t)p->conn.size();
+        case TM_PLAN_PERM: return (int64_t)p->perm.size();
+        default: return -1;
+    }
+}
+
+template <typename T>
+static int copy_vec(const std::vector<T>& v, void* dst) {
+    if (!v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(T));
+    return TM_OK;
+}
+
+extern "C" int tm_plan_copy_array(const tm_host_plan* p, int32_t id, void* dst) {
+    if (!p || (!dst && tm_plan_array_size(p, id) > 0))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_copy_array: null argument");
+    switch (id) {
+        case TM_PLAN_EDGE_ROW: return copy_vec(p->edge_row, dst);
+        case TM_PLAN_EDGE_COL: return copy_vec(p->edge_col, dst);
+        case TM_PLAN_SLOT: return copy_vec(p->slot, dst);
+        case TM_PLAN_CHUNK_BEGIN: return copy_vec(p->chunk_begin, dst);
+        case TM_PLAN_SLOT_PTR: return copy_vec(p->slot_ptr, dst);
+        case TM_PLAN_CONTRIB: return copy_vec(p->contrib, dst);
+        case TM_PLAN_SLOT_TARGET: return copy_vec(p->slot_target, dst);
+        case TM_PLAN_SLOT_MIRROR: return copy_vec(p->slot_mirror, dst);
+        case TM_PLAN_SHARED_PTR: return copy_vec(p->shared_ptr, dst);
+        case TM_PLAN_SHARED_TARGET: return copy_vec(p->shared_target, dst);
+        case TM_PLAN_SHARED_MIRROR: return copy_vec(p->shared_mirror, dst);
+        case TM_PLAN_CONN: return copy_vec(p->conn, dst);
+        case TM_PLAN_PERM: return copy_vec(p->perm, dst);
+        default: return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_copy_array: unknown array id");
+    }
+}
+
+extern "C" int64_t tm_plan_scalar(const tm_host_plan* p, int32_t which) {
+    if (!p) return -1;
+    switch (which) {
+        case 0: return p->nnz;
+        case 1: return p->n_chunks;
+        case 2: return (int64_t)p->slot_target.size();
+        case 3: return (int64_t)p->contrib.size();
+        case 4: return (int64_t)p->shared_target.size();
+        case 5: return p->n_partials;
+        case 6: return p->n_local;
+        default: return -1;
+    }
+}
+
+extern "C" void tm_plan_free(tm_host_plan* p) { delete p; }

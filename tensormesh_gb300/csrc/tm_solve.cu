@@ -1,0 +1,373 @@
+// Jacobi-preconditioned conjugate gradients on the GPU.
+//
+// Replaces the solve behind SparseMatrix.solve for SPD systems (the
+// reference's in-tree Krylov solvers are sparse/solve/torch_solve.py:70-248:
+// CG without preconditioner and Jacobi-BiCGSTAB, both a Python loop of torch
+// SpMVs).  Every scalar of the iteration (rz, pq, alpha, beta, residual
+// norms) stays on the device; one tm_pcg_iterate call runs n_iter
+// iterations as 4 kernel launches each with no host synchronisation, so the
+// host only reads the residual between batches of iterations.  Dot products
+// are reduced in a fixed order (per-block partials, then one block), so the
+// iteration is bitwise reproducible.  Dots are accumulated in float64 for
+// both float64 and float32 vectors.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <cstdio>
+#include <type_traits>
+
+#include "../../include/tensormesh_gb300.h"
+#include "tm_status.h"
+
+namespace tmk {
+
+constexpr int kSolveThreads = 256;
+constexpr int kDotBlocks = 608;   // 4 x 152 SMs
+
+// scalar slots
+enum { S_RZ = 0, S_PQ = 1, S_RZ_NEW = 2, S_RR = 3, S_BB = 4, S_ITER = 5, S_FLAG = 6 };
+
+template <typename R>
+__device__ __forceinline__ R ld(const R* p) { return __ldg(p); }
+
+// lane-partial of row `row` of A x for scalar CSR (H == 1) or block CSR rows:
+// lane l of the 8-lane group sums entries l, l+8, ... of the (block) row
+template <typename R, int H>
+__device__ __forceinline__ double row_partial(const tm_linear_operator& A, const R* x, int64_t row, int lane) {
+    const int64_t br = row / H;
+    const int a = (int)(row - br * H);
+    const R* val = static_cast<const R*>(A.values);
+    double s = 0;
+    for (int64_t p = A.row_ptr[br] + lane; p < A.row_ptr[br + 1]; p += 8) {
+        const int64_t c = A.col[p];
+        if (H == 1) {
+            s += (double)ld(val + p) * (double)ld(x + c);
+        } else {
+#pragma unroll
+            for (int b = 0; b < H; ++b) s += (double)ld(val + p * H * H + a * H + b) * (double)ld(x + c * H + b);
+        }
+    }
+    return s;
+}
+
+// butterfly sum over the 8 lanes of a group; every lane of the warp must call it
+__device__ __forceinline__ double group_sum(double s) {
+    s += __shfl_xor_sync(0xffffffffu, s, 4, 8);
+    s += __shfl_xor_sync(0xffffffffu, s, 2, 8);
+    s += __shfl_xor_sync(0xffffffffu, s, 1, 8);
+    return s;
+}
+
+// q = A p ; partial[blk] = sum p.q over this block's rows (in row order)
+template <typename R, int H>
+__global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A, const R* p, R* q,
+                                                            double* partial, const double* scal) {
+    __shared__ double red[kSolveThreads / 8];
+    const int64_t n = A.n_rows * H;
+    const int lane = threadIdx.x & 7, grp = threadIdx.x >> 3;
+    const bool stop = scal && scal[S_FLAG] != 0.0;
+    double acc = 0;
+    if (!stop) {
+        const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
+        for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
+            const int64_t r = base + grp;
+            // all 8 lanes of a group share r; the loop bound is uniform per block
+            const double s = group_sum(r < n ? row_partial<R, H>(A, p, r, lane) : 0.0);
+            if (r < n && lane == 0) {
+                q[r] = (R)s;
+                acc += s * (double)p[r];
+            }
+        }
+    }
+    if (lane == 0) red[grp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int g = 0; g < kSolveThreads / 8; ++g) t += red[g];
+        if (partial) partial[blockIdx.x] = t;
+    }
+}
+
+// fixed-order sum of per-block partials into scal[slot] (one block)
+__global__ void k_reduce_partials(const double* partial, int n, double* scal, int slot, int n_vec, int slot2) {
+    __shared__ double red[kSolveThreads];
+    for (int v = 0; v < n_vec; ++v) {
+        double s = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[v * n + i];
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) scal[v == 0 ? slot : slot2] = red[0];
+        __syncthreads();
+    }
+}
+
+// x += alpha p ; r -= alpha q ; z = dinv r ; partials: r.z and r.r
+template <typename R>
+__global__ void __launch_bounds__(kSolveThreads) k_update_xr(int64_t n, R* x, R* r, const R* p, const R* q, R* z,
+                                                             const R* dinv, double* partial, double* scal) {
+    __shared__ double red[2][kSolveThreads];
+    const double pq = scal[S_PQ];
+    bool stop = scal[S_FLAG] != 0.0;
+    if (!(pq > 0.0)) stop = true;   // breakdown (p^T A p <= 0 or NaN): freeze
+    const double alpha = stop ? 0.0 : scal[S_RZ] / pq;
+    double rz = 0, rr = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double ri = (double)r[i];
+        if (!stop) {
+            x[i] = (R)((double)x[i] + alpha * (double)p[i]);
+            ri = ri - alpha * (double)q[i];
+            r[i] = (R)ri;
+        }
+        const double zi = ri * (double)dinv[i];
+        z[i] = (R)zi;
+        rz += ri * zi;
+        rr += ri * ri;
+    }
+    red[0][threadIdx.x] = rz;
+    red[1][threadIdx.x] = rr;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + w];
+            red[1][threadIdx.x] += red[1][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = red[0][0];
+        partial[gridDim.x + blockIdx.x] = red[1][0];
+        if (blockIdx.x == 0 && !(pq > 0.0) && scal[S_FLAG] == 0.0) scal[S_FLAG] = 2.0;
+    }
+}
+
+// p = z + beta p ; rz <- rz_new ; iteration counter
+template <typename R>
+__global__ void __launch_bounds__(kSolveThreads) k_update_p(int64_t n, const R* z, R* p, double* scal) {
+    const bool stop = scal[S_FLAG] != 0.0;
+    const double rz_old = scal[S_RZ], rz_new = scal[S_RZ_NEW];
+    const double beta = rz_old != 0.0 ? rz_new / rz_old : 0.0;
+    if (!stop)
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+            p[i] = (R)((double)z[i] + beta * (double)p[i]);
+    // rz is replaced by rz_new in k_commit_rz, after every block has read it
+}
+
+__global__ void k_commit_rz(double* scal) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        if (scal[S_FLAG] == 0.0) {
+            scal[S_RZ] = scal[S_RZ_NEW];
+            scal[S_ITER] += 1.0;
+        }
+    }
+}
+
+// dinv = 1 / diag(A); r = b - A x ; z = dinv r ; p = z ; partials r.z, r.r, b.b
+template <typename R, int H>
+__global__ void __launch_bounds__(kSolveThreads) k_pcg_start(tm_linear_operator A, const R* b, const R* x,
+                                                             R* dinv, R* r, R* z, R* p, double* partial) {
+    __shared__ double red[3][kSolveThreads / 8];
+    const int64_t n = A.n_rows * H;
+    const R* val = static_cast<const R*>(A.values);
+    const int lane = threadIdx.x & 7, grp = threadIdx.x >> 3;
+    double rz = 0, rr = 0, bb = 0;
+    const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
+    for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
+        const int64_t i = base + grp;
+        const double ax = group_sum(i < n ? row_partial<R, H>(A, x, i, lane) : 0.0);
+        if (i < n && lane == 0) {
+            // diagonal entry of row i
+            const int64_t br = i / H;
+            const int a = (int)(i - br * H);
+            double d = 0;
+            for (int64_t q = A.row_ptr[br]; q < A.row_ptr[br + 1]; ++q)
+                if (A.col[q] == br) d += (double)val[q * H * H + a * H + a];
+            const double di = d != 0.0 ? 1.0 / d : 0.0;
+            dinv[i] = (R)di;
+            const double ri = (double)b[i] - ax;
+            r[i] = (R)ri;
+            const double zi = ri * di;
+            z[i] = (R)zi;
+            p[i] = (R)zi;
+            rz += ri * zi;
+            rr += ri * ri;
+            bb += (double)b[i] * (double)b[i];
+        }
+    }
+    if (lane == 0) {
+        red[0][grp] = rz;
+        red[1][grp] = rr;
+        red[2][grp] = bb;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t0 = 0, t1 = 0, t2 = 0;
+        for (int g = 0; g < kSolveThreads / 8; ++g) {
+            t0 += red[0][g];
+            t1 += red[1][g];
+            t2 += red[2][g];
+        }
+        partial[blockIdx.x] = t0;
+        partial[gridDim.x + blockIdx.x] = t1;
+        partial[2 * gridDim.x + blockIdx.x] = t2;
+    }
+}
+
+__global__ void k_reduce_start(const double* partial, int n, double* scal) {
+    __shared__ double red[kSolveThreads];
+    const int slots[3] = {S_RZ, S_RR, S_BB};
+    for (int v = 0; v < 3; ++v) {
+        double s = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[v * n + i];
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) scal[slots[v]] = red[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        scal[S_ITER] = 0.0;
+        scal[S_FLAG] = 0.0;
+        scal[S_PQ] = 0.0;
+        scal[S_RZ_NEW] = scal[S_RZ];
+    }
+}
+
+inline int status(const char* what) {
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        char buf[256];
+        snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(err));
+        return tm_set_error(TM_ERR_CUDA, buf);
+    }
+    return TM_OK;
+}
+
+inline int grid_rows(int64_t n) {
+    int64_t g = (n + kSolveThreads / 8 - 1) / (kSolveThreads / 8);
+    return (int)(g < 1 ? 1 : (g > kDotBlocks ? kDotBlocks : g));
+}
+inline int grid_vec(int64_t n) {
+    int64_t g = (n + kSolveThreads - 1) / kSolveThreads;
+    return (int)(g < 1 ? 1 : (g > kDotBlocks ? kDotBlocks : g));
+}
+
+template <typename R, int H>
+int pcg_start(const tm_pcg_args& a, cudaStream_t st) {
+    const int64_t n = a.A.n_rows * H;
+    const int g = grid_rows(n);
+    k_pcg_start<R, H><<<g, kSolveThreads, 0, st>>>(a.A, static_cast<const R*>(a.b), static_cast<const R*>(a.x),
+                                                     static_cast<R*>(a.dinv), static_cast<R*>(a.r),
+                                                     static_cast<R*>(a.z), static_cast<R*>(a.p), a.partials);
+    k_reduce_start<<<1, kSolveThreads, 0, st>>>(a.partials, g, a.scalars);
+    return status("tm_pcg_start");
+}
+
+template <typename R, int H>
+int pcg_iterate(const tm_pcg_args& a, int n_iter, cudaStream_t st) {
+    const int64_t n = a.A.n_rows * H;
+    const int gr = grid_rows(n), gv = grid_vec(n);
+    for (int it = 0; it < n_iter; ++it) {
+        k_spmv_dot<R, H><<<gr, kSolveThreads, 0, st>>>(a.A, static_cast<const R*>(a.p), static_cast<R*>(a.q),
+                                                         a.partials, a.scalars);
+        k_reduce_partials<<<1, kSolveThreads, 0, st>>>(a.partials, gr, a.scalars, S_PQ, 1, 0);
+        k_update_xr<R><<<gv, kSolveThreads, 0, st>>>(n, static_cast<R*>(a.x), static_cast<R*>(a.r),
+                                                     static_cast<const R*>(a.p), static_cast<const R*>(a.q),
+                                                     static_cast<R*>(a.z), static_cast<const R*>(a.dinv),
+                                                     a.partials, a.scalars);
+        k_reduce_partials<<<1, kSolveThreads, 0, st>>>(a.partials, gv, a.scalars, S_RZ_NEW, 2, S_RR);
+        k_update_p<R><<<gv, kSolveThreads, 0, st>>>(n, static_cast<const R*>(a.z), static_cast<R*>(a.p), a.scalars);
+        k_commit_rz<<<1, 32, 0, st>>>(a.scalars);
+    }
+    return status("tm_pcg_iterate");
+}
+
+template <typename R, int H>
+__global__ void __launch_bounds__(kSolveThreads) k_spmv_op(tm_linear_operator A, const R* x, R* y, double alpha,
+                                                           double beta) {
+    const int64_t n = A.n_rows * H;
+    const int lane = threadIdx.x & 7, grp = threadIdx.x >> 3;
+    const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
+    for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
+        const int64_t r = base + grp;
+        const double s = group_sum(r < n ? row_partial<R, H>(A, x, r, lane) : 0.0);
+        if (r < n && lane == 0) y[r] = (R)(beta == 0.0 ? alpha * s : alpha * s + beta * (double)y[r]);
+    }
+}
+
+template <typename R, int H>
+int spmv_op(const tm_linear_operator& A, const void* x, void* y, double alpha, double beta, cudaStream_t st) {
+    const int64_t n = A.n_rows * H;
+    int64_t g = (n + kSolveThreads / 8 - 1) / (kSolveThreads / 8);
+    if (g > 152 * 64) g = 152 * 64;
+    if (g < 1) g = 1;
+    k_spmv_op<R, H><<<(int)g, kSolveThreads, 0, st>>>(A, static_cast<const R*>(x), static_cast<R*>(y), alpha, beta);
+    return status("tm_spmv");
+}
+
+template <typename F>
+int dispatch_op(const tm_linear_operator& A, F&& f) {
+    if (A.dtype == TM_F64) {
+        switch (A.block) {
+            case 1: return f(double(), std::integral_constant<int, 1>());
+            case 2: return f(double(), std::integral_constant<int, 2>());
+            case 3: return f(double(), std::integral_constant<int, 3>());
+        }
+    } else if (A.dtype == TM_F32) {
+        switch (A.block) {
+            case 1: return f(float(), std::integral_constant<int, 1>());
+            case 2: return f(float(), std::integral_constant<int, 2>());
+            case 3: return f(float(), std::integral_constant<int, 3>());
+        }
+    }
+    return tm_set_error(TM_ERR_UNSUPPORTED, "linear operator: dtype must be F64/F32 and block 1..3");
+}
+
+int check_op(const tm_linear_operator& A) {
+    if (A.n_rows < 0 || (A.n_rows > 0 && (!A.row_ptr || !A.values || !A.col)))
+        return tm_set_error(TM_ERR_INVALID_ARG, "linear operator: null arrays");
+    return TM_OK;
+}
+
+}  // namespace tmk
+
+using namespace tmk;
+
+extern "C" int tm_spmv(const tm_linear_operator* A, const void* x, void* y, double alpha, double beta,
+                       tm_stream_t stream) {
+    if (!A || !x || !y) return tm_set_error(TM_ERR_INVALID_ARG, "tm_spmv: null argument");
+    int s = check_op(*A);
+    if (s) return s;
+    if (A->n_rows == 0) return TM_OK;
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    return dispatch_op(*A, [&](auto r, auto h) {
+        return spmv_op<decltype(r), decltype(h)::value>(*A, x, y, alpha, beta, st);
+    });
+}
+
+extern "C" size_t tm_pcg_partials_bytes(void) { return sizeof(double) * 3 * kDotBlocks; }
+
+extern "C" int tm_pcg_start(const tm_pcg_args* a, tm_stream_t stream) {
+    if (!a || !a->b || !a->x || !a->r || !a->z || !a->p || !a->q || !a->dinv || !a->scalars || !a->partials)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_pcg_start: null argument");
+    int s = check_op(a->A);
+    if (s) return s;
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    return dispatch_op(a->A, [&](auto r, auto h) { return pcg_start<decltype(r), decltype(h)::value>(*a, st); });
+}
+
+extern "C" int tm_pcg_iterate(const tm_pcg_args* a, int32_t n_iter, tm_stream_t stream) {
+    if (!a || n_iter < 0) return tm_set_error(TM_ERR_INVALID_ARG, "tm_pcg_iterate: bad argument");
+    int s = check_op(a->A);
+    if (s) return s;
+    if (a->A.n_rows == 0 || n_iter == 0) return TM_OK;
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    return dispatch_op(a->A, [&](auto r, auto h) {
+        return pcg_iterate<decltype(r), decltype(h)::value>(*a, n_iter, st);
+    });
+}

@@ -1,0 +1,249 @@
+"""Mesh topology: CSR pattern, element->CSR slot map and the element-chunk
+reduction plans, built once per mesh by the native plan builder
+(``tm_plan_build``) and kept on the device.
+
+``ElementAssembler.from_mesh`` (assemble/element_assembler.py:769-878)
+computes the pattern and slot map on the host with SciPy on every mesh; here
+the same arrays come from ``tm_plan_build`` together with the chunk plan the
+fused kernels reduce with.  Elements are processed in Morton (Z-curve) order
+of their centroids so that a chunk of consecutive elements is spatially
+compact and most CSR targets are reduced inside one chunk.
+"""
+import ctypes as C
+from typing import Dict, Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from .element import element_info, element_tables, packed_tables
+
+
+def _part_bits(x: np.ndarray, dims: int) -> np.ndarray:
+    """Spread the bits of x (uint64) so that consecutive bits are ``dims`` apart."""
+    x = x.astype(np.uint64)
+    if dims == 2:
+        x &= np.uint64(0xFFFFFFFF)
+        x = (x | (x << np.uint64(16))) & np.uint64(0x0000FFFF0000FFFF)
+        x = (x | (x << np.uint64(8))) & np.uint64(0x00FF00FF00FF00FF)
+        x = (x | (x << np.uint64(4))) & np.uint64(0x0F0F0F0F0F0F0F0F)
+        x = (x | (x << np.uint64(2))) & np.uint64(0x3333333333333333)
+        x = (x | (x << np.uint64(1))) & np.uint64(0x5555555555555555)
+        return x
+    x &= np.uint64(0x1FFFFF)
+    x = (x | (x << np.uint64(32))) & np.uint64(0x1F00000000FFFF)
+    x = (x | (x << np.uint64(16))) & np.uint64(0x1F0000FF0000FF)
+    x = (x | (x << np.uint64(8))) & np.uint64(0x100F00F00F00F00F)
+    x = (x | (x << np.uint64(4))) & np.uint64(0x10C30C30C30C30C3)
+    x = (x | (x << np.uint64(2))) & np.uint64(0x1249249249249249)
+    return x
+
+
+def morton_order(points: np.ndarray, conn: np.ndarray) -> np.ndarray:
+    """Processing order of the elements: increasing Morton code of the
+    centroid of their vertices (ties keep the original order)."""
+    E = conn.shape[0]
+    if E == 0:
+        return np.zeros(0, dtype=np.int32)
+    D = points.shape[1]
+    cent = points[conn[:, :D + 1]].mean(axis=1)
+    lo, hi = cent.min(0), cent.max(0)
+    span = np.where(hi > lo, hi - lo, 1.0)
+    bits = 31 if D == 2 else 21
+    q = np.floor((cent - lo) / span * ((1 << bits) - 1)).astype(np.uint64)
+    key = np.zeros(E, dtype=np.uint64)
+    for d in range(D):
+        key |= _part_bits(q[:, d], D) << np.uint64(d)
+    return np.argsort(key, kind="stable").astype(np.int32)
+
+
+class HostPlan:
+    """Arrays of one ``tm_plan_build`` call, as numpy arrays."""
+
+    _DTYPES = {
+        _lib.PLAN_EDGE_ROW: np.int32, _lib.PLAN_EDGE_COL: np.int32, _lib.PLAN_SLOT: np.int64,
+        _lib.PLAN_CHUNK_BEGIN: np.int32, _lib.PLAN_SLOT_PTR: np.int32, _lib.PLAN_CONTRIB: np.uint16,
+        _lib.PLAN_SLOT_TARGET: np.int32, _lib.PLAN_SLOT_MIRROR: np.int32,
+        _lib.PLAN_SHARED_PTR: np.int32, _lib.PLAN_SHARED_TARGET: np.int32,
+        _lib.PLAN_SHARED_MIRROR: np.int32, _lib.PLAN_CONN: np.int32, _lib.PLAN_PERM: np.int32,
+    }
+    _NAMES = {
+        _lib.PLAN_EDGE_ROW: "edge_row", _lib.PLAN_EDGE_COL: "edge_col", _lib.PLAN_SLOT: "slot",
+        _lib.PLAN_CHUNK_BEGIN: "chunk_begin", _lib.PLAN_SLOT_PTR: "slot_ptr",
+        _lib.PLAN_CONTRIB: "contrib", _lib.PLAN_SLOT_TARGET: "slot_target",
+        _lib.PLAN_SLOT_MIRROR: "slot_mirror", _lib.PLAN_SHARED_PTR: "shared_ptr",
+        _lib.PLAN_SHARED_TARGET: "shared_target", _lib.PLAN_SHARED_MIRROR: "shared_mirror",
+        _lib.PLAN_CONN: "conn", _lib.PLAN_PERM: "perm",
+    }
+
+    def __init__(self, conn: np.ndarray, n_points: int, kind: int, chunk_elems: int,
+                 perm: Optional[np.ndarray] = None, slot_map: Optional[np.ndarray] = None):
+        lib = _lib.load()
+        conn = np.ascontiguousarray(conn, dtype=np.int64)
+        E, B = conn.shape
+        perm_c = None if perm is None else np.ascontiguousarray(perm, dtype=np.int32)
+        slot_c = None if slot_map is None else np.ascontiguousarray(slot_map, dtype=np.int64)
+        handle = C.c_void_p()
+        st = lib.tm_plan_build(conn.ctypes.data if E else None, E, B, n_points, kind, chunk_elems,
+                               None if perm_c is None else perm_c.ctypes.data,
+                               None if slot_c is None else slot_c.ctypes.data, C.byref(handle))
+        _lib.check(st, "tm_plan_build")
+        try:
+            self.arrays: Dict[str, np.ndarray] = {}
+            for aid, dt in self._DTYPES.items():
+                n = lib.tm_plan_array_size(handle, aid)
+                arr = np.empty(n, dtype=dt)
+                if n:
+                    _lib.check(lib.tm_plan_copy_array(handle, aid, arr.ctypes.data), "tm_plan_copy_array")
+                self.arrays[self._NAMES[aid]] = arr
+            self.nnz = lib.tm_plan_scalar(handle, 0)
+            self.n_chunks = lib.tm_plan_scalar(handle, 1)
+            self.n_chunk_slots = lib.tm_plan_scalar(handle, 2)
+            self.n_contrib = lib.tm_plan_scalar(handle, 3)
+            self.n_shared = lib.tm_plan_scalar(handle, 4)
+            self.n_partials = lib.tm_plan_scalar(handle, 5)
+            self.n_local = lib.tm_plan_scalar(handle, 6)
+        finally:
+            lib.tm_plan_free(handle)
+        self.kind, self.n_elements, self.n_basis, self.n_points = kind, E, B, n_points
+        self.chunk_elems = chunk_elems
+
+
+class DevicePlan:
+    """A chunk plan on the device plus its ``tm_chunk_plan`` view."""
+
+    def __init__(self, host: HostPlan, device: torch.device):
+        a = host.arrays
+        t = lambda x: torch.from_numpy(x).to(device)
+        self.elem_perm = t(a["perm"])
+        self.conn = t(a["conn"])
+        self.chunk_begin = t(a["chunk_begin"])
+        self.slot_ptr = t(a["slot_ptr"])
+        self.contrib = t(a["contrib"].view(np.int16))   # uint16 bits
+        self.slot_target = t(a["slot_target"])
+        self.slot_mirror = t(a["slot_mirror"])
+        self.shared_ptr = t(a["shared_ptr"])
+        self.shared_target = t(a["shared_target"])
+        self.shared_mirror = t(a["shared_mirror"])
+        self.n_elements, self.n_basis, self.n_local = host.n_elements, host.n_basis, host.n_local
+        self.chunk_elems, self.n_chunks = host.chunk_elems, host.n_chunks
+        self.n_targets = host.nnz if host.kind == _lib.TM_PLAN_KIND_MATRIX else host.n_points
+        self.n_shared, self.n_partials = host.n_shared, host.n_partials
+        self.n_chunk_slots, self.n_contrib = host.n_chunk_slots, host.n_contrib
+        self.device = device
+
+    def struct(self) -> _lib.ChunkPlan:
+        p = _lib.ChunkPlan()
+        p.n_elements, p.n_basis, p.n_local = self.n_elements, self.n_basis, self.n_local
+        p.chunk_elems, p.n_chunks, p.n_targets = self.chunk_elems, self.n_chunks, self.n_targets
+        p.n_shared, p.n_partials = self.n_shared, self.n_partials
+        for name in ("elem_perm", "conn", "chunk_begin", "slot_ptr", "contrib", "slot_target",
+                     "slot_mirror", "shared_ptr", "shared_target", "shared_mirror"):
+            setattr(p, name, _lib.ptr(getattr(self, name)))
+        return p
+
+    def nbytes(self) -> int:
+        return sum(getattr(self, n).numel() * getattr(self, n).element_size()
+                   for n in ("elem_perm", "conn", "chunk_begin", "slot_ptr", "contrib", "slot_target",
+                             "slot_mirror", "shared_ptr", "shared_target", "shared_mirror"))
+
+
+# chunk sizes (elements per CTA) by element type and whether the form is a
+# DxD block form; chosen so that the locals of a chunk fit in shared memory
+CHUNK_ELEMS = {
+    ("triangle", False): 256, ("triangle", True): 256,
+    ("tetra", False): 256, ("tetra", True): 128,
+    ("triangle6", False): 64, ("triangle6", True): 64,
+    ("tetra10", False): 32, ("tetra10", True): 32,
+}
+NODE_CHUNK_ELEMS = {"triangle": 256, "tetra": 256, "triangle6": 128, "tetra10": 128}
+
+
+class Topology:
+    """Everything about one mesh (one element type) that does not change
+    between calls: connectivity, pattern, slot map, tables, chunk plans."""
+
+    def __init__(self, points: torch.Tensor, conn: torch.Tensor, etype: str, quadrature_order: int,
+                 matrix: bool = True):
+        info = element_info(etype)
+        self.etype, self.info, self.quadrature_order = etype, info, quadrature_order
+        self.n_points = int(points.shape[0])
+        self.n_elements = int(conn.shape[0])
+        conn_np = conn.detach().cpu().numpy().astype(np.int64)
+        pts_np = points.detach().cpu().to(torch.float64).numpy()
+        self.perm = morton_order(pts_np, conn_np)
+        self._conn_np = conn_np
+        self._plans: Dict[tuple, DevicePlan] = {}
+        self._host_node: Optional[HostPlan] = None
+        self._tables: Dict[torch.device, torch.Tensor] = {}
+        self._conn32: Dict[torch.device, torch.Tensor] = {}
+        self.edges = None
+        self.slot = None
+        self._layout_hash = None
+        self._row_ptr: Dict[torch.device, torch.Tensor] = {}
+        if matrix:
+            ch = CHUNK_ELEMS[(etype, False)]
+            host = HostPlan(conn_np, self.n_points, _lib.TM_PLAN_KIND_MATRIX, ch, self.perm)
+            self.edges = torch.from_numpy(np.stack([host.arrays["edge_row"], host.arrays["edge_col"]]))
+            self.slot = torch.from_numpy(host.arrays["slot"])
+            self.nnz = int(host.nnz)
+            self._pending = {("matrix", ch): host}
+        else:
+            self.nnz = 0
+            self._pending = {}
+
+    # -- device objects -------------------------------------------------------
+    def tables(self, device: torch.device) -> torch.Tensor:
+        if device not in self._tables:
+            self._tables[device] = torch.from_numpy(packed_tables(self.etype, self.quadrature_order)).to(device)
+        return self._tables[device]
+
+    def table_struct(self, device: torch.device) -> _lib.ElementTables:
+        t = _lib.ElementTables()
+        t.element_type = self.info.code
+        t.n_quad = len(element_tables(self.etype, self.quadrature_order)["w"])
+        t.packed = _lib.ptr(self.tables(device))
+        return t
+
+    def conn32(self, device: torch.device) -> torch.Tensor:
+        if device not in self._conn32:
+            self._conn32[device] = torch.from_numpy(self._conn_np.astype(np.int32)).to(device)
+        return self._conn32[device]
+
+    def matrix_plan(self, device: torch.device, block: bool = False) -> DevicePlan:
+        ch = CHUNK_ELEMS[(self.etype, block)]
+        key = ("matrix", ch, device)
+        if key not in self._plans:
+            host = self._pending.pop(("matrix", ch), None)
+            if host is None:
+                host = HostPlan(self._conn_np, self.n_points, _lib.TM_PLAN_KIND_MATRIX, ch, self.perm,
+                                slot_map=self.slot.numpy())
+            self._plans[key] = DevicePlan(host, device)
+        return self._plans[key]
+
+    def node_plan(self, device: torch.device) -> DevicePlan:
+        ch = NODE_CHUNK_ELEMS[self.etype]
+        key = ("node", ch, device)
+        if key not in self._plans:
+            host = HostPlan(self._conn_np, self.n_points, _lib.TM_PLAN_KIND_NODE, ch, self.perm)
+            self._plans[key] = DevicePlan(host, device)
+        return self._plans[key]
+
+    def row_ptr(self, device: torch.device) -> torch.Tensor:
+        """CSR row pointer of the (row-major sorted) pattern."""
+        if device not in self._row_ptr:
+            counts = np.bincount(self.edges[0].numpy(), minlength=self.n_points)
+            rp = np.zeros(self.n_points + 1, dtype=np.int64)
+            np.cumsum(counts, out=rp[1:])
+            self._row_ptr[device] = torch.from_numpy(rp).to(device)
+        return self._row_ptr[device]
+
+    @property
+    def layout_hash(self) -> str:
+        """SHA-256 of the int32 row bytes followed by the int32 column bytes,
+        the value ``SparseMatrix.__init__`` computes (sparse/matrix.py:82-86)."""
+        if self._layout_hash is None:
+            import hashlib
+            self._layout_hash = hashlib.sha256(self.edges[0].numpy().tobytes()
+                                               + self.edges[1].numpy().tobytes()).hexdigest()
+        return self._layout_hash

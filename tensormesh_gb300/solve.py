@@ -1,0 +1,104 @@
+"""SpMV and Jacobi-preconditioned CG over ``SparseMatrix`` (GPU kernels of
+``csrc/tm_solve.cu``).
+
+``pcg_solve`` replaces ``SparseMatrix.solve`` for the symmetric positive
+definite systems of the assembly path.  The reference inherits ``solve``
+from torch-sla (direct solvers, or CG for large systems,
+docs/source/user_guide/batched_workflows.rst:124-131); its in-tree Krylov
+templates are ``cg_py`` / ``bicgstab_py`` (sparse/solve/torch_solve.py:70-248).
+"""
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional
+
+import torch
+
+from . import _lib
+
+
+def _register():
+    return _lib.load()
+
+
+LinearOperator = _lib.LinearOperator
+PcgArgs = _lib.PcgArgs
+
+
+def operator_of(A) -> tuple:
+    """(LinearOperator struct, tensors to keep alive) for a SparseMatrix."""
+    rp, col, perm, H = A._csr_structure()
+    vals = A.values.detach()
+    if perm is not None:
+        vals = vals.reshape(-1, H * H)[perm].reshape(-1)
+    vals = vals.contiguous()
+    op = LinearOperator()
+    op.dtype = _lib.dtype_code(vals.dtype)
+    op.block = H
+    op.n_rows = rp.numel() - 1
+    op.row_ptr, op.col, op.values = _lib.ptr(rp), _lib.ptr(col), _lib.ptr(vals)
+    return op, (rp, col, vals)
+
+
+def spmv(A, x: torch.Tensor, out: Optional[torch.Tensor] = None, alpha: float = 1.0,
+         beta: float = 0.0) -> torch.Tensor:
+    lib = _register()
+    _lib.require_cuda(A.values, "SparseMatrix values")
+    x = x.to(device=A.values.device, dtype=A.values.dtype).contiguous()
+    if out is None:
+        out = torch.empty(A.shape[0], dtype=A.values.dtype, device=A.values.device)
+        beta = 0.0
+    op, keep = operator_of(A)
+    _lib.check(lib.tm_spmv(C.byref(op), _lib.ptr(x), _lib.ptr(out), alpha, beta,
+                           _lib.stream_handle(x.device)), "tm_spmv")
+    return out
+
+
+@dataclass
+class SolveInfo:
+    iterations: int
+    relative_residual: float
+    converged: bool
+    breakdown: bool
+
+
+def pcg_solve(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, rtol: float = 1e-10,
+              max_iter: Optional[int] = None, check_every: int = 25, return_info: bool = False):
+    """Solve A x = b with Jacobi-preconditioned CG to ||b - A x|| <= rtol ||b||.
+
+    The iteration runs in batches of ``check_every`` iterations with all
+    scalars on the device; the host reads the residual between batches."""
+    lib = _register()
+    _lib.require_cuda(A.values, "SparseMatrix values")
+    dev, dt = A.values.device, A.values.dtype
+    b = b.to(device=dev, dtype=dt).contiguous()
+    n = A.shape[0]
+    if max_iter is None:
+        max_iter = max(1000, 10 * n)
+    x = torch.zeros(n, dtype=dt, device=dev) if x0 is None else x0.to(device=dev, dtype=dt).clone()
+    work = torch.empty(5, n, dtype=dt, device=dev)
+    scal = torch.zeros(8, dtype=torch.float64, device=dev)
+    partials = torch.empty(lib.tm_pcg_partials_bytes() // 8, dtype=torch.float64, device=dev)
+    op, keep = operator_of(A)
+    args = PcgArgs()
+    args.A = op
+    args.b, args.x = _lib.ptr(b), _lib.ptr(x)
+    args.r, args.z, args.p, args.q, args.dinv = (_lib.ptr(work[i]) for i in range(5))
+    args.scalars, args.partials = _lib.ptr(scal), _lib.ptr(partials)
+    stream = _lib.stream_handle(dev)
+    _lib.check(lib.tm_pcg_start(C.byref(args), stream), "tm_pcg_start")
+    host = torch.empty(8, dtype=torch.float64, pin_memory=True)
+    done = 0
+    while True:
+        host.copy_(scal, non_blocking=True)
+        torch.cuda.current_stream(dev).synchronize()
+        rr, bb, flag = float(host[3]), float(host[4]), float(host[6])
+        rel = (rr / bb) ** 0.5 if bb > 0 else rr ** 0.5
+        if rel <= rtol or flag != 0.0 or done >= max_iter or bb == 0.0:
+            break
+        k = min(check_every, max_iter - done)
+        _lib.check(lib.tm_pcg_iterate(C.byref(args), k, stream), "tm_pcg_iterate")
+        done += k
+    info = SolveInfo(int(host[5]), rel, rel <= rtol, flag == 2.0 and rel > rtol)
+    if return_info:
+        return x, info
+    return x

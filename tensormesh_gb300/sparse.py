@@ -1,0 +1,195 @@
+"""``SparseMatrix``: the COO container the assemblers return.
+
+Mirrors ``tensormesh.sparse.SparseMatrix`` (sparse/matrix.py:26-381): the
+constructor ``SparseMatrix(edata, row, col, shape)``, the attributes
+``values``/``edata``, ``row_indices``/``row`` (int64), ``col_indices``/``col``,
+``shape``, ``nnz``, ``edges``, ``layout_hash`` and ``has_same_layout``,
+``to_dense``, ``@`` and ``solve``, and ``from_block_coo``.
+
+Differences that do not change results:
+
+* The reference hashes the (row, col) bytes on the host on every
+  construction (sparse/matrix.py:82-86).  Here the SHA-256 of the same bytes
+  is computed on first access and, for matrices produced by an assembler,
+  once per mesh.
+* Block matrices (``from_block_coo``) keep their [n_block, H, H] values and
+  expand the scalar row/col indices only when asked.
+* ``@`` runs the library's CSR / block-CSR SpMV kernels; ``solve`` runs the
+  Jacobi-preconditioned CG of ``tensormesh_gb300.solve`` (the reference
+  delegates to torch-sla, which picks a direct or iterative backend).
+"""
+import hashlib
+from typing import Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+class SparseMatrix:
+    def __init__(self, edata: torch.Tensor, row: torch.Tensor, col: torch.Tensor,
+                 shape: Tuple[int, int], *, _topology=None, _block: int = 1,
+                 _block_row: Optional[torch.Tensor] = None, _block_col: Optional[torch.Tensor] = None,
+                 _sorted: Optional[bool] = None):
+        self.values = edata
+        self._row_src = row
+        self._col_src = col
+        self.shape = (int(shape[0]), int(shape[1]))
+        self._topology = _topology
+        self._block = int(_block)
+        self._block_row = _block_row
+        self._block_col = _block_col
+        self._row64 = None
+        self._col64 = None
+        self._hash = None
+        self._sorted = _sorted
+        self._csr = None
+
+    # ------------------------------------------------------------ attributes
+    @property
+    def edata(self) -> torch.Tensor:
+        return self.values
+
+    @property
+    def row_indices(self) -> torch.Tensor:
+        if self._row64 is None:
+            if self._block > 1:
+                self._row64, self._col64 = self._expand_block()
+            else:
+                self._row64 = self._row_src.long()
+        return self._row64
+
+    @property
+    def col_indices(self) -> torch.Tensor:
+        if self._col64 is None:
+            if self._block > 1:
+                self._row64, self._col64 = self._expand_block()
+            else:
+                self._col64 = self._col_src.long()
+        return self._col64
+
+    row = row_indices
+    col = col_indices
+
+    @property
+    def edges(self) -> torch.Tensor:
+        return torch.stack([self.row_indices, self.col_indices], 0)
+
+    @property
+    def nnz(self) -> int:
+        return int(self.values.numel())
+
+    @property
+    def device(self) -> torch.device:
+        return self.values.device
+
+    @property
+    def dtype(self) -> torch.dtype:
+        return self.values.dtype
+
+    @property
+    def layout_hash(self) -> str:
+        """SHA-256 of the row bytes followed by the column bytes as passed to
+        the constructor (sparse/matrix.py:82-86)."""
+        if self._hash is None:
+            if self._topology is not None and self._block == 1:
+                self._hash = self._topology.layout_hash
+            else:
+                r = self._row_src if self._block == 1 else self.row_indices
+                c = self._col_src if self._block == 1 else self.col_indices
+                self._hash = hashlib.sha256(r.detach().cpu().numpy().tobytes()
+                                            + c.detach().cpu().numpy().tobytes()).hexdigest()
+        return self._hash
+
+    def has_same_layout(self, other) -> bool:
+        h = other if isinstance(other, str) else other.layout_hash
+        return self.layout_hash == h
+
+    # ---------------------------------------------------------- conversions
+    def _expand_block(self):
+        """row*H + a, col*H + b in [block, a, b] order (sparse/matrix.py:370-376)."""
+        H = self._block
+        br = self._block_row.to(self.values.device).long()
+        bc = self._block_col.to(self.values.device).long()
+        a = torch.arange(H, device=br.device).repeat_interleave(H)
+        b = torch.arange(H, device=br.device).repeat(H)
+        return ((br[:, None] * H + a).reshape(-1), (bc[:, None] * H + b).reshape(-1))
+
+    @staticmethod
+    def from_block_coo(edata: torch.Tensor, row: torch.Tensor, col: torch.Tensor,
+                       shape: Tuple[int, int], *, _topology=None) -> "SparseMatrix":
+        """Expand [n_block, H, H] block storage into an (N*H, N*H) matrix whose
+        scalar entries are ordered [block, a, b] (sparse/matrix.py:332-381)."""
+        H = int(edata.shape[1])
+        assert edata.shape[2] == H, f"from_block_coo expects square blocks, got {tuple(edata.shape)}"
+        return SparseMatrix(edata.reshape(-1), row, col, (shape[0] * H, shape[1] * H),
+                            _topology=_topology, _block=H, _block_row=row, _block_col=col)
+
+    def to_dense(self) -> torch.Tensor:
+        out = torch.zeros(self.shape, dtype=self.values.dtype, device=self.values.device)
+        out.index_put_((self.row_indices, self.col_indices), self.values, accumulate=True)
+        return out
+
+    def to_scipy_coo(self):
+        import scipy.sparse
+        return scipy.sparse.coo_matrix(
+            (self.values.detach().cpu().numpy(),
+             (self.row_indices.cpu().numpy(), self.col_indices.cpu().numpy())), shape=self.shape)
+
+    def with_values(self, values: torch.Tensor) -> "SparseMatrix":
+        """Same layout, new values (no re-hash, shared CSR structures)."""
+        m = SparseMatrix(values, self._row_src, self._col_src, self.shape, _topology=self._topology,
+                         _block=self._block, _block_row=self._block_row, _block_col=self._block_col,
+                         _sorted=self._sorted)
+        m._hash, m._row64, m._col64, m._csr = self._hash, self._row64, self._col64, self._csr
+        return m
+
+    # ------------------------------------------------------------ CSR view
+    def _csr_structure(self):
+        """(row_ptr int64, col int32, perm or None, block) on the values' device.
+
+        Matrices whose (block) rows are sorted -- every assembler output and
+        every condensed matrix -- need no permutation."""
+        if self._csr is not None:
+            return self._csr
+        dev = self.values.device
+        H = self._block
+        if H > 1:
+            br, bc = self._block_row.to(dev).long(), self._block_col.to(dev).long()
+            n = self.shape[0] // H
+        else:
+            br, bc = self._row_src.to(dev).long(), self._col_src.to(dev).long()
+            n = self.shape[0]
+        key = br * self.shape[1] + bc
+        perm = None
+        if self._sorted is not True:
+            if key.numel() > 1 and not bool((key[1:] >= key[:-1]).all()):
+                perm = torch.argsort(key, stable=True)
+                br, bc = br[perm], bc[perm]
+        if self._topology is not None and H == 1 and perm is None:
+            rp = self._topology.row_ptr(dev)
+        else:
+            counts = torch.bincount(br, minlength=n)
+            rp = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+            torch.cumsum(counts, 0, out=rp[1:])
+        self._csr = (rp, bc.to(torch.int32).contiguous(), perm, H)
+        return self._csr
+
+    def matvec(self, x: torch.Tensor, out: Optional[torch.Tensor] = None, alpha: float = 1.0,
+               beta: float = 0.0) -> torch.Tensor:
+        from .solve import spmv
+        return spmv(self, x, out=out, alpha=alpha, beta=beta)
+
+    def __matmul__(self, x: torch.Tensor) -> torch.Tensor:
+        if x.dim() == 1:
+            return self.matvec(x)
+        return torch.stack([self.matvec(x[:, j].contiguous()) for j in range(x.shape[1])], 1)
+
+    def solve(self, b: torch.Tensor, **kwargs) -> torch.Tensor:
+        from .solve import pcg_solve
+        return pcg_solve(self, b, **kwargs)
+
+    def __repr__(self):
+        return (f"SparseMatrix(shape={self.shape}, nnz={self.nnz}, dtype={self.dtype}, "
+                f"device={self.device}{', block=%d' % self._block if self._block > 1 else ''})")

@@ -1,0 +1,137 @@
+"""Native plan builder (tm_plan_build): CSR pattern and slot map bit-exact
+with the oracle, and the chunk plan's fixed-order reduction (emulated here in
+numpy on oracle element locals) equal to the oracle's index_add_ scatter."""
+import numpy as np
+import pytest
+import torch
+
+from tensormesh_gb300 import _lib
+from tensormesh_gb300.mesh import gen_unit_cube, gen_unit_square
+from tensormesh_gb300.plan import HostPlan, morton_order
+from oracle import fem_oracle as O
+
+
+def emulate_matrix(h, loc):
+    """Phase 2 + finalisation of k_matrix on [E,B,B,H,H] locals (element order)."""
+    a = h.arrays
+    B = h.n_basis
+    H = loc.shape[-1]
+    iu = [(p, q) for p in range(B) for q in range(p, B)]
+    L = np.stack([loc[a["perm"]][:, p, q] for p, q in iu], 1)
+    out = np.full((h.nnz, H, H), np.nan)
+    part = np.full((h.n_partials, H, H), np.nan)
+    CH = h.chunk_elems
+    for k in range(h.n_chunks):
+        Lc = L[k * CH:(k + 1) * CH].reshape(-1, H, H)
+        for s in range(a["chunk_begin"][k], a["chunk_begin"][k + 1]):
+            acc = np.zeros((H, H))
+            for p in range(a["slot_ptr"][s], a["slot_ptr"][s + 1]):
+                code = int(a["contrib"][p])
+                acc += Lc[code >> 1].T if code & 1 else Lc[code >> 1]
+            t = a["slot_target"][s]
+            if t >= 0:
+                out[t] = acc
+                if a["slot_mirror"][s] != t:
+                    out[a["slot_mirror"][s]] = acc.T
+            else:
+                part[-t - 1] = acc
+    for sh in range(h.n_shared):
+        acc = part[a["shared_ptr"][sh]:a["shared_ptr"][sh + 1]].sum(0)
+        t, m = a["shared_target"][sh], a["shared_mirror"][sh]
+        out[t] = acc
+        if m != t:
+            out[m] = acc.T
+    return out
+
+
+def emulate_vector(h, loc, n_points):
+    a = h.arrays
+    L = loc[a["perm"]]
+    out = np.zeros((n_points,) + loc.shape[2:])
+    part = np.full((h.n_partials,) + loc.shape[2:], np.nan)
+    CH = h.chunk_elems
+    for k in range(h.n_chunks):
+        Lc = L[k * CH:(k + 1) * CH].reshape(-1, *loc.shape[2:])
+        for s in range(a["chunk_begin"][k], a["chunk_begin"][k + 1]):
+            acc = sum(Lc[int(a["contrib"][p]) >> 1] for p in range(a["slot_ptr"][s], a["slot_ptr"][s + 1]))
+            t = a["slot_target"][s]
+            if t >= 0:
+                out[t] = acc
+            else:
+                part[-t - 1] = acc
+    for sh in range(h.n_shared):
+        out[a["shared_target"][sh]] = part[a["shared_ptr"][sh]:a["shared_ptr"][sh + 1]].sum(0)
+    return out
+
+
+MESHES = [
+    ("tetra", lambda: gen_unit_cube(3, jitter=0.2, seed=1)),
+    ("triangle", lambda: gen_unit_square(5, jitter=0.2, seed=2)),
+    ("tetra10", lambda: gen_unit_cube(2, order=2, jitter=0.1, seed=3)),
+    ("triangle6", lambda: gen_unit_square(3, order=2, jitter=0.1, seed=4)),
+]
+
+
+@pytest.mark.parametrize("et,make", MESHES)
+@pytest.mark.parametrize("chunk", [1, 5, 16, 500])
+def test_pattern_and_reduction(et, make, chunk):
+    m = make()
+    conn = m.elements().numpy()
+    perm = morton_order(m.points.numpy(), conn)
+    h = HostPlan(conn, m.n_points, _lib.TM_PLAN_KIND_MATRIX, chunk, perm)
+    edges, slot = O.element_pattern(m.elements(), m.n_points)
+    assert np.array_equal(h.arrays["edge_row"], edges[0].numpy())
+    assert np.array_equal(h.arrays["edge_col"], edges[1].numpy())
+    assert np.array_equal(h.arrays["slot"], slot.numpy())
+    E = torch.rand(conn.shape[0], dtype=torch.float64, generator=torch.Generator().manual_seed(0)) + 0.5
+    loc = O.element_locals_elasticity(m.points, m.elements(), et, E, 0.3, 2).numpy()
+    out = emulate_matrix(h, loc)
+    _, _, ref = O.assemble_matrix(m.points, m.elements(), m.n_points,
+                                  lambda p, c, E: O.element_locals_elasticity(p, c, et, E, 0.3, 2), E=E)
+    assert not np.isnan(out).any()
+    np.testing.assert_allclose(out, ref.numpy(), rtol=0, atol=1e-13 * np.abs(ref.numpy()).max())
+    # node plan: load vector
+    hn = HostPlan(conn, m.n_points, _lib.TM_PLAN_KIND_NODE, chunk, perm)
+    locv = np.random.default_rng(0).standard_normal((conn.shape[0], conn.shape[1], 2))
+    outv = emulate_vector(hn, locv, m.n_points)
+    refv = O.reduce_project(torch.from_numpy(conn.reshape(-1)), torch.from_numpy(locv.reshape(-1, 2)), m.n_points)
+    np.testing.assert_allclose(outv, refv.numpy(), atol=1e-13)
+
+
+def test_slot_map_reuse_and_identity_perm():
+    m = gen_unit_cube(2, jitter=0.1, seed=9)
+    conn = m.elements().numpy()
+    h1 = HostPlan(conn, m.n_points, _lib.TM_PLAN_KIND_MATRIX, 7)
+    h2 = HostPlan(conn, m.n_points, _lib.TM_PLAN_KIND_MATRIX, 3, slot_map=h1.arrays["slot"])
+    assert h2.nnz == h1.nnz
+    assert np.array_equal(h1.arrays["perm"], np.arange(conn.shape[0]))
+    loc = O.element_locals_diffusion(m.points, m.elements(), "tetra", None, 2).numpy()[..., None, None]
+    np.testing.assert_allclose(emulate_matrix(h2, loc)[:, 0, 0], emulate_matrix(h1, loc)[:, 0, 0], atol=1e-14)
+
+
+def test_degenerate_repeated_node():
+    """An element listing a node twice maps two local pairs onto one diagonal
+    slot (both the pair and its transpose are added)."""
+    pts = torch.tensor([[0., 0.], [1., 0.], [0., 1.], [1., 1.]], dtype=torch.float64)
+    conn = np.array([[0, 1, 2], [1, 3, 2], [1, 1, 2]])
+    h = HostPlan(conn, 4, _lib.TM_PLAN_KIND_MATRIX, 2)
+    rng = np.random.default_rng(1)
+    loc = rng.standard_normal((3, 3, 3, 2, 2))
+    loc = loc + loc.transpose(0, 2, 1, 4, 3)                 # symmetric element matrices
+    edges, slot = O.element_pattern(torch.from_numpy(conn), 4)
+    ref = O.reduce_project(slot, torch.from_numpy(loc.reshape(-1, 2, 2)), edges.shape[1]).numpy()
+    np.testing.assert_allclose(emulate_matrix(h, loc), ref, atol=1e-13)
+
+
+def test_empty_mesh():
+    h = HostPlan(np.zeros((0, 4), dtype=np.int64), 5, _lib.TM_PLAN_KIND_MATRIX, 16)
+    assert h.nnz == 0 and h.n_chunks == 0 and h.n_partials == 0
+
+
+def test_rejects_bad_input():
+    with pytest.raises(_lib.TmError):
+        HostPlan(np.array([[0, 1, 7]]), 3, _lib.TM_PLAN_KIND_MATRIX, 4)          # index out of range
+    with pytest.raises(_lib.TmError):
+        HostPlan(np.array([[0, 1, 2], [0, 2, 1]]), 3, _lib.TM_PLAN_KIND_MATRIX, 4, perm=np.array([1, 1]))
+    with pytest.raises(_lib.TmError):
+        HostPlan(np.zeros((10, 10), dtype=np.int64), 10, _lib.TM_PLAN_KIND_MATRIX, 1000)  # u16 overflow
