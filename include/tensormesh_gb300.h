@@ -175,6 +175,21 @@ size_t tm_matrix_workspace_bytes(const tm_matrix_args* args);
 int tm_assemble_matrix(const tm_matrix_args* args, tm_stream_t stream);
 
 /*
+ * Allocation-free variant of tm_assemble_matrix.  It has no counterpart in
+ * the reference.  For callers that cannot allocate GPU memory (an FFI host
+ * that only holds device pointers given to it by another framework, a
+ * process confined to a fixed device pool): same arguments and results, but
+ * args->workspace is ignored and the partial sums live in a static device
+ * array of TM_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps
+ * until exit.  Plans needing more (tm_matrix_workspace_bytes) are rejected
+ * with TM_ERR_TOO_LARGE.  The first call on a device looks the array up
+ * (with that device current): make it before any stream capture.  Calls
+ * share the array: calls whose kernels overlap on the GPU race.
+ */
+#define TM_NOALLOC_SCRATCH_BYTES (64u << 20)
+int tm_assemble_matrix_noalloc(const tm_matrix_args* args, tm_stream_t stream);
+
+/*
  * Linear-form assembly into a nodal vector (NodeAssembler.__call__,
  * assemble/node_assembler.py:242-409, with const_node_assembler /
  * func_node_assembler, assemble/builtin.py:730-813).

@@ -847,3 +847,92 @@ extern "C" int tm_project_reduce(int32_t dtype, int64_t n_to, int64_t width, con
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_project_reduce: bad dtype");
     return launch_status("k_project");
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of tm_assemble_matrix.
+//
+// Some callers cannot allocate GPU memory: a host runtime that binds this
+// library through a foreign-function interface and only holds device
+// pointers handed to it by another framework, or a process whose device
+// memory is owned by a fixed pool it may not grow.  They still pass the
+// points, coefficients and output arrays, but cannot provide the partial-sum
+// workspace.  This entry point runs the same kernels with that workspace
+// taken from a file-scope device array of TM_NOALLOC_SCRATCH_BYTES, which
+// every GPU that loads the library holds until the process exits.
+//
+// The array's address is looked up once per device, with that device
+// current, by the first call on that device (cudaGetSymbolAddress); make
+// that first call before any stream capture.  Nothing in the array has to
+// start at zero: each call writes every partial it later reads.  All calls
+// share the one array, so calls whose kernels overlap on the GPU (on
+// different streams, or from different host threads) race on it; order them
+// on one stream or serialise them.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace tmk {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[TM_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+static void* g_noalloc_ptr[kMaxDevices] = {};
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch(void** out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return launch_status("cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices)
+        return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_matrix_noalloc: device index above 63");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (err != cudaSuccess || !p) {
+            char buf[256];
+            snprintf(buf, sizeof(buf), "tm_assemble_matrix_noalloc: cudaGetSymbolAddress failed: %s",
+                     cudaGetErrorString(err));
+            cudaGetLastError();
+            return tm_set_error(TM_ERR_CUDA, buf);
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return TM_OK;
+}
+
+}  // namespace tmk
+
+extern "C" int tm_assemble_matrix_noalloc(const tm_matrix_args* a, tm_stream_t stream) {
+    if (!a) return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: null args");
+    const int B = basis_of(a->tables.element_type);
+    if (B < 0) return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_matrix_noalloc: unknown element type");
+    int s = check_plan(a->plan, B, B * (B + 1) / 2, "tm_assemble_matrix_noalloc");
+    if (s) return s;
+    if ((a->forms & TM_FORM_ELASTICITY) && (a->forms & ~TM_FORM_ELASTICITY))
+        return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_matrix_noalloc: elasticity cannot be fused with other forms");
+    if (!a->tables.packed || a->tables.n_quad < 1)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: missing element tables");
+    if (a->plan.n_elements > 0 && !a->points)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: points is null");
+    if (((a->forms & TM_FORM_DIFFUSION) && !a->out_diffusion) || ((a->forms & TM_FORM_MASS) && !a->out_mass) ||
+        ((a->forms & TM_FORM_ELASTICITY) && !a->out_elasticity))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: output pointer is null");
+    if (a->dtype != TM_F64 && a->dtype != TM_F32)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: dtype must be TM_F64 or TM_F32");
+    const size_t need = tm_matrix_workspace_bytes(a);
+    if (need > (size_t)TM_NOALLOC_SCRATCH_BYTES) {
+        char buf[256];
+        snprintf(buf, sizeof(buf),
+                 "tm_assemble_matrix_noalloc: this plan needs %zu bytes of partial sums, above the %zu-byte "
+                 "static scratch; use tm_assemble_matrix with a caller-provided workspace",
+                 need, (size_t)TM_NOALLOC_SCRATCH_BYTES);
+        return tm_set_error(TM_ERR_TOO_LARGE, buf);
+    }
+    void* scratch = nullptr;
+    if ((s = noalloc_scratch(&scratch))) return s;
+    tm_matrix_args b = *a;
+    b.workspace = scratch;
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (b.dtype == TM_F64) return dispatch_matrix<double>(b, st);
+    return dispatch_matrix<float>(b, st);
+}
