@@ -142,6 +142,13 @@ int64_t tm_plan_scalar(const tm_host_plan* plan, int32_t which);
 void tm_plan_free(tm_host_plan* plan);
 
 /*
+ * Float64 P1 diffusion / mass locals and their reduction are computed in
+ * double-float arithmetic (hi + lo pairs of floats, ~48 bits, relative
+ * error ~1e-14) on the FP32 pipes; chunks whose data fall outside the
+ * range where that is exact enough (an element whose largest edge component
+ * is outside [2^-20, 2^20], a coefficient outside [2^-30, 2^30], |det J|
+ * below 2^-100, a local above 2^100) are recomputed in FP64 arithmetic.
+ *
  * Bilinear-form assembly into CSR values (ElementAssembler.__call__,
  * assemble/element_assembler.py:231-445, with Transformation.batch_shape_grad_jxw,
  * element/transformation.py:1219-1276, Element.eval_shape_grad,
@@ -170,6 +177,8 @@ typedef struct tm_matrix_args {
     tm_chunk_plan plan;
     void* event_begin;         /* optional cudaEvent_t recorded before the element-chunk kernel */
     void* event_end;           /* optional cudaEvent_t recorded after it (before finalisation) */
+    int32_t* stats;            /* optional device int32 [1]: += chunks whose float64 P1 locals left the
+                                  double-float range and were recomputed in FP64 arithmetic */
 } tm_matrix_args;
 size_t tm_matrix_workspace_bytes(const tm_matrix_args* args);
 int tm_assemble_matrix(const tm_matrix_args* args, tm_stream_t stream);

@@ -54,7 +54,7 @@ class MatrixArgs(C.Structure):
         ("poisson", C.c_double), ("out_diffusion", C.c_void_p), ("out_mass", C.c_void_p),
         ("out_elasticity", C.c_void_p), ("workspace", C.c_void_p),
         ("tables", ElementTables), ("plan", ChunkPlan),
-        ("event_begin", C.c_void_p), ("event_end", C.c_void_p),
+        ("event_begin", C.c_void_p), ("event_end", C.c_void_p), ("stats", C.c_void_p),
     ]
 
 

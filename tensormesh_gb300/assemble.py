@@ -263,14 +263,15 @@ def _coef(value, dtype, device, E, name):
 
 
 def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_data=None,
-                   scalar_data=None, _events=None):
+                   scalar_data=None, _events=None, _stats: Optional[torch.Tensor] = None):
     """Assemble several built-in forms over one mesh in one fused launch when
     they can share it (diffusion and mass do), else one launch per form.
 
     Returns the value tensors ([nnz] per scalar form, [nnz, D, D] for
     elasticity) in the order of ``assemblers``.  ``_events`` (two recorded
     ``torch.cuda.Event``) are recorded around the element-chunk kernel of
-    the first launch, for timing."""
+    the first launch, for timing; ``_stats`` (a device int32 [1]) counts the
+    chunks whose float64 P1 locals were recomputed in FP64 arithmetic."""
     first = assemblers[0]
     for a in assemblers[1:]:
         if a._topology is not first._topology:
@@ -343,6 +344,8 @@ def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_da
         if _events is not None:
             args.event_begin, args.event_end = _events[0].cuda_event, _events[1].cuda_event
             _events = None
+        if _stats is not None:
+            args.stats = _lib.ptr(_stats)
         _lib.check(lib.tm_assemble_matrix(C_byref(args), _lib.stream_handle(dev)), "tm_assemble_matrix")
     return out
 

@@ -17,8 +17,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <cstdio>
+#include <type_traits>
 
 #include "../../include/tensormesh_gb300.h"
+#include "tm_df64.cuh"
 #include "tm_element.cuh"
 #include "tm_status.h"
 
@@ -44,7 +46,7 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q) {
     L.tab = o;
     o = align16(o + sizeof(double) * table_layout(Q, B, D).total);
     L.mhl = o;
-    o = align16(o + sizeof(double) * NL);
+    o = align16(o + sizeof(double) * NL * 2);   // mass template: doubles, then double-float pairs
     L.x = L.g = L.jw = o;
     if (!T::P1) {
         L.x = o;
@@ -88,11 +90,15 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
 
     for (int k = threadIdx.x; k < TL.total; k += blockDim.x) tab[k] = a.tables.packed[k];
     __syncthreads();
+    // float64 P1 diffusion/mass: double-float arithmetic on the FP32 pipes
+    constexpr bool DF64 = std::is_same<R, double>::value && T::P1 != 0 && !ELAST;
+    f2* mh2 = reinterpret_cast<f2*>(mhl + NL);
     if (MASS && T::P1)
         for (int l = threadIdx.x; l < NL; l += blockDim.x) {
             int pa, pb;
             upper_pair<B>(l, pa, pb);
             mhl[l] = tab[TL.mhat + pa * B + pb];
+            if (DF64) mh2[l] = split_double(mhl[l]);
         }
 
     const int64_t i0 = (int64_t)blockIdx.x * CH;
@@ -105,41 +111,140 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
     const R clam = nu / ((R(1) + nu) * (R(1) - R(2) * nu));
     const R cmu = R(1) / (R(2) * (R(1) + nu));
 
+    bool use_df = false;
     if constexpr (T::P1 != 0) {
         const R wsum = (R)tab[TL.wsum];
-        for (int el = threadIdx.x; el < ne; el += blockDim.x) {
-            const int64_t i = i0 + el;
-            const int e = P.elem_perm[i];
-            R X[B][D];
+        auto native_p1 = [&]() {
+            for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+                const int64_t i = i0 + el;
+                const int e = P.elem_perm[i];
+                R X[B][D];
 #pragma unroll
-            for (int b = 0; b < B; ++b) {
-                const int64_t node = P.conn[i * B + b];
+                for (int b = 0; b < B; ++b) {
+                    const int64_t node = P.conn[i * B + b];
 #pragma unroll
-                for (int d = 0; d < D; ++d) X[b][d] = ldg(pts + node * D + d);
+                    for (int d = 0; d < D; ++d) X[b][d] = ldg(pts + node * D + d);
+                }
+                R C[B][D];
+                const R det = p1_gradients<R, D>(X, C);
+                const R adet = rabs(det);
+                if constexpr (DIFF) {
+                    const R kv = (kap ? ldg(kap + e) : R(1)) * kscale;
+                    const R s = kv * wsum / adet;
+                    int l = 0;
+#pragma unroll
+                    for (int p = 0; p < B; ++p)
+#pragma unroll
+                        for (int q = p; q < B; ++q, ++l) LD[el * NL + l] = s * dot<R, D>(C[p], C[q]);
+                }
+                if constexpr (MASS) LM[el] = adet * mscale;
+                if constexpr (ELAST) {
+                    const R Ey = (yng ? ldg(yng + e) : R(1)) * yscale;
+                    const R s = wsum / adet;
+                    int l = 0;
+#pragma unroll
+                    for (int p = 0; p < B; ++p)
+#pragma unroll
+                        for (int q = p; q < B; ++q, ++l)
+                            elastic_block<R, D>(C[p], C[q], Ey * clam, Ey * cmu, s, LE + (el * NL + l) * HH, false);
+                }
             }
-            R C[B][D];
-            const R det = p1_gradients<R, D>(X, C);
-            const R adet = rabs(det);
-            if constexpr (DIFF) {
-                const R kv = (kap ? ldg(kap + e) : R(1)) * kscale;
-                const R s = kv * wsum / adet;
-                int l = 0;
+        };
+        if constexpr (DF64) {
+            f2* LD2 = reinterpret_cast<f2*>(LD);
+            f2* LM2 = reinterpret_cast<f2*>(LM);
+            bool bad = !exponent_in_band(a.kappa_scale, 30) || !exponent_in_band(a.mass_scale, 30) ||
+                       !exponent_in_band(tab[TL.wsum], 30);
+            if (MASS && threadIdx.x == 0)
+                for (int k = 0; k < B * B; ++k) bad |= !exponent_in_band(tab[TL.mhat + k], 30);
+            const f2 ks = split_double(a.kappa_scale), ms = split_double(a.mass_scale);
+            const f2 ws = split_double(tab[TL.wsum]);
+            for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+                const int64_t i = i0 + el;
+                const int e = P.elem_perm[i];
+                double X[B][D];
 #pragma unroll
-                for (int p = 0; p < B; ++p)
+                for (int b = 0; b < B; ++b) {
+                    const int64_t node = P.conn[i * B + b];
 #pragma unroll
-                    for (int q = p; q < B; ++q, ++l) LD[el * NL + l] = s * dot<R, D>(C[p], C[q]);
+                    for (int d = 0; d < D; ++d) X[b][d] = ldg(static_cast<const double*>(a.points) + node * D + d);
+                }
+                // J[i][j] = x_{i+1,j} - x_{0,j}: the one FP64 step, then split.
+                // The element's scale (its largest edge component) must lie in
+                // [2^-20, 2^20]; smaller components are fine at that scale.
+                f2 J[D][D];
+                int emax = 0;
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int c = 0; c < D; ++c) {
+                        const double dd = X[r + 1][c] - X[0][c];
+                        emax = max(emax, biased_exponent(dd));
+                        J[r][c] = split_double(dd);
+                    }
+                bad |= emax < 1023 - 20 || emax >= 1023 + 20;
+                f2 cof[D][D];
+                f2 det;
+                if constexpr (D == 3) {
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        const int r1 = (r + 1) % 3, r2 = (r + 2) % 3;
+                        cof[r][0] = f2_diff_of_products(J[r1][1], J[r2][2], J[r1][2], J[r2][1]);
+                        cof[r][1] = f2_diff_of_products(J[r1][2], J[r2][0], J[r1][0], J[r2][2]);
+                        cof[r][2] = f2_diff_of_products(J[r1][0], J[r2][1], J[r1][1], J[r2][0]);
+                    }
+                    det = f2_dot3(J[0], cof[0]);
+                } else {
+                    cof[0][0] = J[1][1];
+                    cof[0][1] = f2_neg(J[1][0]);
+                    cof[1][0] = f2_neg(J[0][1]);
+                    cof[1][1] = J[0][0];
+                    det = f2_diff_of_products(J[0][0], J[1][1], J[0][1], J[1][0]);
+                }
+                f2 C[B][D];
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    f2 acc = cof[0][c];
+#pragma unroll
+                    for (int r = 1; r < D; ++r) acc = f2_add(acc, cof[r][c]);
+                    C[0][c] = f2_neg(acc);
+#pragma unroll
+                    for (int r = 0; r < D; ++r) C[r + 1][c] = cof[r][c];
+                }
+                const f2 adet = f2_abs(det);
+                bad |= !(adet.hi > 0.0f) || !f2_in_band(adet, -100, 100);
+                if constexpr (DIFF) {
+                    const double kd = kap ? ldg(static_cast<const double*>(a.kappa) + e) : 1.0;
+                    bad |= !exponent_in_band(kd, 30);
+                    const f2 sc = f2_mul(f2_mul(split_double(kd), ks), f2_mul(ws, f2_recip(adet)));
+                    f2 Dv[B][D];
+#pragma unroll
+                    for (int p = 0; p < B; ++p)
+#pragma unroll
+                        for (int c = 0; c < D; ++c) Dv[p][c] = f2_mul(sc, C[p][c]);
+                    int l = 0;
+#pragma unroll
+                    for (int p = 0; p < B; ++p)
+#pragma unroll
+                        for (int q = p; q < B; ++q, ++l) {
+                            const f2 v = D == 3 ? f2_dot3(Dv[p], C[q]) : f2_dot2(Dv[p], C[q]);
+                            bad |= !f2_in_band(v, -127, 100);   // finite, no overflow
+                            LD2[el * NL + l] = v;
+                        }
+                }
+                if constexpr (MASS) {
+                    const f2 v = f2_mul(adet, ms);
+                    bad |= !f2_in_band(v, -127, 100);
+                    LM2[el] = v;
+                }
             }
-            if constexpr (MASS) LM[el] = adet * mscale;
-            if constexpr (ELAST) {
-                const R Ey = (yng ? ldg(yng + e) : R(1)) * yscale;
-                const R s = wsum / adet;
-                int l = 0;
-#pragma unroll
-                for (int p = 0; p < B; ++p)
-#pragma unroll
-                    for (int q = p; q < B; ++q, ++l)
-                        elastic_block<R, D>(C[p], C[q], Ey * clam, Ey * cmu, s, LE + (el * NL + l) * HH, false);
+            use_df = !__syncthreads_or(bad);
+            if (!use_df) {
+                if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats, 1);
+                native_p1();
             }
+        } else {
+            native_p1();
         }
     } else {
         R* X = reinterpret_cast<R*>(sm + L.x);
@@ -213,6 +318,18 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
 
     // phase 2: fixed-order reduction of the chunk's targets
     const int32_t s0 = P.chunk_begin[blockIdx.x], s1 = P.chunk_begin[blockIdx.x + 1];
+    // bit l set when local entry l is a diagonal (a, a); mass_sym when the
+    // mass template has one diagonal and one off-diagonal value (every
+    // symmetric quadrature rule), so that the mass of a target is
+    // m_diag * sum |det| + m_off * sum |det| over its contributions
+    uint64_t diag_mask = 0;
+    bool mass_sym = false;
+    if constexpr (DF64 && MASS) {
+        for (int pa = 0; pa < B; ++pa) diag_mask |= 1ull << (pa * B - pa * (pa - 1) / 2);
+        mass_sym = true;
+        for (int l = 0; l < NL; ++l)
+            mass_sym &= mhl[l] == (((diag_mask >> l) & 1u) ? mhl[0] : mhl[1]);
+    }
     R* oD = static_cast<R*>(a.out_diffusion);
     R* oM = static_cast<R*>(a.out_mass);
     R* oE = static_cast<R*>(a.out_elasticity);
@@ -224,6 +341,48 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
         R ae[HH];
 #pragma unroll
         for (int k = 0; k < HH; ++k) ae[k] = 0;
+        if (DF64 && use_df) {
+            // compensated sums: TwoSum on the high parts, the error terms and
+            // the low parts summed in plain float (|error| ~ 2^-48 of the terms)
+            const f2* LD2 = reinterpret_cast<const f2*>(LD);
+            const f2* LM2 = reinterpret_cast<const f2*>(LM);
+            float kh = 0.0f, ke = 0.0f;                   // diffusion
+            float dh = 0.0f, de = 0.0f, oh = 0.0f, oe = 0.0f;   // |det| on diagonal / off-diagonal template entries
+            f2 sm2 = {0.0f, 0.0f};                        // mass, general template
+            for (int p = p0; p < p1; ++p) {
+                const int idx = P.contrib[p] >> 1;
+                if constexpr (DIFF) {
+                    const f2 v = LD2[idx];
+                    const f2 t = two_sum(kh, v.hi);
+                    kh = t.hi;
+                    ke = __fadd_rn(ke, __fadd_rn(t.lo, v.lo));
+                }
+                if constexpr (MASS) {
+                    const int el = idx / NL;
+                    const int l = idx - el * NL;
+                    const f2 v = LM2[el];
+                    if (mass_sym) {
+                        if ((diag_mask >> l) & 1u) {
+                            const f2 t = two_sum(dh, v.hi);
+                            dh = t.hi;
+                            de = __fadd_rn(de, __fadd_rn(t.lo, v.lo));
+                        } else {
+                            const f2 t = two_sum(oh, v.hi);
+                            oh = t.hi;
+                            oe = __fadd_rn(oe, __fadd_rn(t.lo, v.lo));
+                        }
+                    } else {
+                        sm2 = f2_add(sm2, f2_mul(v, mh2[l]));
+                    }
+                }
+            }
+            if constexpr (DIFF) ad = (R)f2_to_double(two_sum(kh, ke));
+            if constexpr (MASS) {
+                if (mass_sym)
+                    sm2 = f2_add(f2_mul(two_sum(dh, de), mh2[0]), f2_mul(two_sum(oh, oe), mh2[1]));
+                am = (R)f2_to_double(sm2);
+            }
+        } else
         for (int p = p0; p < p1; ++p) {
             const int code = P.contrib[p];
             const int idx = code >> 1;

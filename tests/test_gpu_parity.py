@@ -160,3 +160,37 @@ def test_spmv_and_pcg(cuda):
     assert info.converged
     ref = torch.linalg.solve(Ki.to_dense(), bi)
     assert rel_fro(ui, ref) <= 1e-11
+
+
+@pytest.mark.parametrize("etype", ["tetra", "triangle"])
+def test_double_float_path_and_fp64_fallback(etype, cuda):
+    """Float64 P1 diffusion/mass runs in double-float arithmetic; chunks whose
+    data leave its range are recomputed in FP64.  Both must match the oracle
+    to 1e-12, and the stats counter tells which path ran."""
+    make = (lambda: tg.gen_unit_cube(6, jitter=0.2, seed=31)) if etype == "tetra" else \
+        (lambda: tg.gen_unit_square(40, jitter=0.2, seed=32))
+    base = make()
+    E = base.n_elements
+    rng = np.random.default_rng(33)
+    cases = {
+        "plain": (1.0, 0.0, rng.lognormal(0.0, 1.0, E), False),
+        "translated": (1.0, 1.0e4, rng.lognormal(0.0, 1.0, E), False),
+        "tiny": (1.0e-9, 0.0, rng.lognormal(0.0, 1.0, E), True),
+        "huge_kappa": (1.0, 0.0, rng.lognormal(0.0, 1.0, E) * 1e12, True),
+    }
+    for name, (scale, shift, kap, expect_fallback) in cases.items():
+        pts = base.points * scale + shift
+        conn = base.elements()
+        kappa = torch.from_numpy(kap)
+        mesh = tg.Mesh(pts, {etype: conn}).to(cuda)
+        K_asm = tg.LaplaceElementAssembler.from_mesh(mesh)
+        M_asm = tg.MassElementAssembler.from_assembler(K_asm)
+        stats = torch.zeros(1, dtype=torch.int32, device=cuda)
+        K, M = tg.assemble_forms([K_asm, M_asm], mesh.points, {"kappa": kappa.to(cuda)}, _stats=stats)
+        _, _, Ko = O.assemble_matrix(pts, conn, base.n_points,
+                                     lambda p, c, kappa: O.element_locals_diffusion(p, c, etype, kappa, 2), kappa=kappa)
+        _, _, Mo = O.assemble_matrix(pts, conn, base.n_points, lambda p, c: O.element_locals_mass(p, c, etype, 2))
+        assert rel_fro(K, Ko) <= TOL, name
+        assert rel_fro(M, Mo) <= TOL, name
+        fell_back = int(stats.item())
+        assert (fell_back > 0) == expect_fallback, (name, fell_back)
