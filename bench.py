@@ -34,6 +34,12 @@ METRIC = "P1-tet elements assembled/s vs ref torch-GPU (FP64, <=1e-12 rel); batc
 WORKLOAD = "diffusion_mass_tet_64: P1 tet K(kappa)+M, 64^3 cubes x 6 Kuhn, 1,572,864 elements, 274,625 nodes, FP64"
 
 
+def _workload_name(n):
+    if n == 64:
+        return WORKLOAD
+    return f"diffusion_mass_tet_{n}: P1 tet K(kappa)+M, {n}^3 cubes x 6 Kuhn, {6 * n ** 3} elements, FP64"
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -163,7 +169,7 @@ def run_ours(args, ws, rank, local):
     from tensormesh_gb300 import _lib, workloads as W
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    wl = W.diffusion_mass_tet(64)
+    wl = W.diffusion_mass_tet(args.cubes)
     mesh = wl.mesh.to(dev)
     kappa = wl.data["kappa"].to(dev)
     K_asm = tg.LaplaceElementAssembler.from_mesh(mesh)
@@ -251,7 +257,7 @@ def run_ours(args, ws, rank, local):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded jittered Kuhn-split cube, lognormal kappa)",
-        "config": {"workload": WORKLOAD, "elements": E, "nodes": N, "nnz": nnz, "forms": ["diffusion", "mass"],
+        "config": {"workload": _workload_name(args.cubes), "elements": E, "nodes": N, "nnz": nnz, "forms": ["diffusion", "mass"],
                    "quadrature_order": 2, "l2": "flushed between steps (512 MB write)",
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": E * ws / (e2e_ms * 1e-3), "unit": "elements/s", "ms_per_step": e2e_ms,
@@ -278,7 +284,7 @@ def run_reference(args, ws, rank, local):
     from tensormesh_gb300 import workloads as W
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
-    wl = W.diffusion_mass_tet(64)
+    wl = W.diffusion_mass_tet(args.cubes)
     pts, conn, kappa = wl.mesh.points, wl.mesh.elements(), wl.data["kappa"]
     edges, slot = O.element_pattern(conn, wl.mesh.n_points)
     E = conn.shape[0]
@@ -295,7 +301,7 @@ def run_reference(args, ws, rank, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded jittered Kuhn-split cube, lognormal kappa)",
-            "config": {"workload": WORKLOAD, "elements": E, "parallelism": "host cores"},
+            "config": {"workload": _workload_name(args.cubes), "elements": E, "parallelism": "host cores"},
             "cpu_baseline": {"value": E / s, "unit": "elements/s", "cores": threads, "kind": "port",
                              "sample": f"full workload per step, reference op sequence restated in torch "
                                        f"(CPU, {threads} threads), incl. per-call SparseMatrix hashing"},
@@ -330,6 +336,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-gpu-reference", action="store_true")
+    ap.add_argument("--cubes", type=int, default=64, help="cubes per side of the Kuhn-split cube (64: 1,572,864 elements)")
     args = ap.parse_args()
     ws, rank, local = _dist()
     if args.impl == "reference":

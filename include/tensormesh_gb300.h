@@ -77,8 +77,10 @@ typedef struct tm_element_tables {
  * contributions its elements make to a target (a CSR position for matrix
  * plans, a node for node plans) in shared memory, in a fixed order, and
  * writes either the final value (the target is touched by this chunk only)
- * or a partial that tm finalisation sums in chunk order.  No atomics: the
- * result is bitwise reproducible.
+ * or a partial.  The last chunk to deliver a partial of a shared target
+ * (found with one counter per shared target) sums that target's partials in
+ * chunk order.  No floating-point atomics and no waiting: the result is
+ * bitwise reproducible.
  */
 typedef struct tm_chunk_plan {
     int64_t n_elements;
@@ -95,7 +97,8 @@ typedef struct tm_chunk_plan {
     const int32_t* slot_ptr;       /* [n_chunk_slots+1] */
     const uint16_t* contrib;       /* [n_contrib] ((e_local*n_local + l) << 1) | transpose */
     const int32_t* slot_target;    /* [n_chunk_slots] >= 0 target; < 0: -(partial+1) */
-    const int32_t* slot_mirror;    /* [n_chunk_slots] transposed CSR position or -1 */
+    const int32_t* slot_mirror;    /* [n_chunk_slots] target < 0: its shared index; else the
+                                      transposed CSR position (matrix plans) or -1 */
     const int32_t* shared_ptr;     /* [n_shared+1] partial ranges, chunk order */
     const int32_t* shared_target;  /* [n_shared] */
     const int32_t* shared_mirror;  /* [n_shared] */
@@ -156,7 +159,9 @@ void tm_plan_free(tm_host_plan* plan);
  * assemble/projector.py:95-123, fused in one pass).
  * Outputs: out_* [nnz] (diffusion, mass) and [nnz*D*D] (elasticity, blocks
  * in [edge, a, b] order as SparseMatrix.from_block_coo expects,
- * sparse/matrix.py:332-381).  workspace: device, >= tm_matrix_workspace_bytes().
+ * sparse/matrix.py:332-381).  workspace: device, >= tm_matrix_workspace_bytes():
+ * the partials plus one int32 counter per shared target, which the call
+ * clears (cudaMemsetAsync on the stream) before its kernel.
  */
 typedef struct tm_matrix_args {
     int32_t dtype;             /* TM_F64 / TM_F32: points, coefficients and outputs */
@@ -246,6 +251,50 @@ int tm_project_reduce(int32_t dtype, int64_t n_to, int64_t width, const int64_t*
 int tm_quadrature_points(int32_t dtype, int64_t n_elements, const int32_t* conn, const void* points,
                          tm_element_tables tables, void* xq, tm_stream_t stream);
 
+/*
+ * Adjoint of P1 diffusion / load assembly (float64): gradients with respect
+ * to the per-element coefficient and the node coordinates, recomputing the
+ * geometry per element.  Replaces autograd through the reference's assembly
+ * graph (assemble/element_assembler.py:390-445 -> element/element.py:960-966
+ * -> element/transformation.py:1267-1273) and, for a loss through a linear
+ * solve, the adjoint of sparse/solve/torch_sla_solve.py:90-137 combined with
+ * it: with k_mode TM_ADJ_K_OUTER the weights dL/dK_ab = -lambda_a u_b are
+ * formed per element from the solution u and the adjoint lambda.
+ *   k_mode TM_ADJ_K_CSR:   weights[nnz] = dL/dvalues, slot_map [E*B*B] int64
+ *   load_source:           adds the term of b = |det J| beta weighted by lam
+ * Outputs (either may be NULL): grad_kappa [E] (dL/dkappa, element order),
+ * grad_points [N*D] (dL/dx, reduced with the node plan).
+ */
+#define TM_ADJ_K_NONE   0
+#define TM_ADJ_K_CSR    1
+#define TM_ADJ_K_OUTER  2
+#define TM_ADJ_LOAD_NONE  0
+#define TM_ADJ_LOAD_CONST 1
+#define TM_ADJ_LOAD_NODAL 2
+typedef struct tm_adjoint_args {
+    int32_t dtype;             /* TM_F64 */
+    int32_t k_mode;
+    int32_t load_source;
+    int32_t reserved;
+    int64_t n_points;
+    const void* points;        /* [N*D] */
+    const void* kappa;         /* [E] or NULL */
+    double kappa_scale;
+    const void* weights;       /* TM_ADJ_K_CSR: [nnz] */
+    const int64_t* slot_map;   /* TM_ADJ_K_CSR: [E*B*B] */
+    const void* u;             /* TM_ADJ_K_OUTER: [N] */
+    const void* lam;           /* TM_ADJ_K_OUTER and load term: [N] */
+    double load_const;         /* TM_ADJ_LOAD_CONST */
+    const void* load_values;   /* TM_ADJ_LOAD_NODAL: [N] */
+    void* grad_kappa;          /* [E] or NULL */
+    void* grad_points;         /* [N*D] or NULL */
+    void* workspace;           /* >= tm_adjoint_workspace_bytes() */
+    tm_element_tables tables;
+    tm_chunk_plan plan;        /* node plan of the mesh */
+} tm_adjoint_args;
+size_t tm_adjoint_workspace_bytes(const tm_adjoint_args* args);
+int tm_adjoint_p1(const tm_adjoint_args* args, tm_stream_t stream);
+
 /* ---- sparse linear algebra (SparseMatrix @ and solve) ------------------- */
 /*
  * CSR (block == 1) or block-CSR (block == H, HxH row-major blocks) operator.
@@ -288,6 +337,40 @@ typedef struct tm_pcg_args {
 size_t tm_pcg_partials_bytes(void);
 int tm_pcg_start(const tm_pcg_args* args, tm_stream_t stream);
 int tm_pcg_iterate(const tm_pcg_args* args, int32_t n_iter, tm_stream_t stream);
+
+/*
+ * Batched Jacobi-PCG over the diagonal blocks [system_offset[s],
+ * system_offset[s+1]) of one block-diagonal CSR matrix (offset-concatenated
+ * meshes), all systems in one launch; no counterpart in the reference, which
+ * solves varying meshes one at a time (batched_workflows.rst:247-249).
+ * Rows with dirichlet[i] != 0 keep x[i] as given and are excluded from the
+ * iteration (solving K_ii x_i = b_i - K_io x_o).  x holds the initial guess
+ * on entry.  work: device [5 * n_rows] of the matrix type.  queue: device
+ * int32 [1] (cleared by the call).  status: device [n_systems] or NULL.
+ * Convergence: ||r|| <= rtol ||b|| over the free rows of the system.
+ */
+#define TM_PCG_CONVERGED 1
+#define TM_PCG_MAX_ITER  2
+#define TM_PCG_BREAKDOWN 3
+typedef struct tm_pcg_status {
+    int32_t iterations;
+    int32_t flag;              /* TM_PCG_* */
+    double relative_residual;
+} tm_pcg_status;
+typedef struct tm_batched_pcg_args {
+    int32_t n_systems;
+    int32_t max_iter;
+    double rtol;
+    const int64_t* system_offset;   /* device [n_systems+1] */
+    tm_linear_operator A;           /* block == 1 */
+    const uint8_t* dirichlet;       /* device [n_rows] or NULL */
+    const void* b;
+    void* x;
+    void* work;
+    int32_t* queue;
+    tm_pcg_status* status;
+} tm_batched_pcg_args;
+int tm_batched_pcg(const tm_batched_pcg_args* args, tm_stream_t stream);
 
 #ifdef __cplusplus
 }

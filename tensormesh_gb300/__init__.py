@@ -15,6 +15,7 @@ from .builtin import (LaplaceElementAssembler, DiffusionElementAssembler, MassEl
                       LoadNodeAssembler)
 from .solve import pcg_solve
 from .condense import Condenser
+from .adjoint import solve_diffusion
 
 __version__ = "0.1.0"
 
@@ -23,5 +24,5 @@ __all__ = [
     "SparseMatrix", "ElementAssembler", "NodeAssembler", "assemble_forms", "LaplaceElementAssembler",
     "DiffusionElementAssembler", "MassElementAssembler", "LinearElasticityElementAssembler",
     "const_node_assembler", "func_node_assembler", "LoadNodeAssembler", "pcg_solve",
-    "element_type2dimension", "element_type2order", "Condenser",
+    "element_type2dimension", "element_type2order", "Condenser", "solve_diffusion",
 ]

@@ -67,6 +67,21 @@ class VectorArgs(C.Structure):
     ]
 
 
+class AdjointArgs(C.Structure):
+    _fields_ = [
+        ("dtype", C.c_int32), ("k_mode", C.c_int32), ("load_source", C.c_int32), ("reserved", C.c_int32),
+        ("n_points", C.c_int64), ("points", C.c_void_p), ("kappa", C.c_void_p), ("kappa_scale", C.c_double),
+        ("weights", C.c_void_p), ("slot_map", C.c_void_p), ("u", C.c_void_p), ("lam", C.c_void_p),
+        ("load_const", C.c_double), ("load_values", C.c_void_p), ("grad_kappa", C.c_void_p),
+        ("grad_points", C.c_void_p), ("workspace", C.c_void_p),
+        ("tables", ElementTables), ("plan", ChunkPlan),
+    ]
+
+
+TM_ADJ_K_NONE, TM_ADJ_K_CSR, TM_ADJ_K_OUTER = 0, 1, 2
+TM_ADJ_LOAD_NONE, TM_ADJ_LOAD_CONST, TM_ADJ_LOAD_NODAL = 0, 1, 2
+
+
 class LinearOperator(C.Structure):
     _fields_ = [("dtype", C.c_int32), ("block", C.c_int32), ("n_rows", C.c_int64),
                 ("row_ptr", C.c_void_p), ("col", C.c_void_p), ("values", C.c_void_p)]
@@ -76,6 +91,20 @@ class PcgArgs(C.Structure):
     _fields_ = [("A", LinearOperator), ("b", C.c_void_p), ("x", C.c_void_p), ("r", C.c_void_p),
                 ("z", C.c_void_p), ("p", C.c_void_p), ("q", C.c_void_p), ("dinv", C.c_void_p),
                 ("scalars", C.c_void_p), ("partials", C.c_void_p)]
+
+
+class PcgStatus(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("flag", C.c_int32), ("relative_residual", C.c_double)]
+
+
+class BatchedPcgArgs(C.Structure):
+    _fields_ = [("n_systems", C.c_int32), ("max_iter", C.c_int32), ("rtol", C.c_double),
+                ("system_offset", C.c_void_p), ("A", LinearOperator), ("dirichlet", C.c_void_p),
+                ("b", C.c_void_p), ("x", C.c_void_p), ("work", C.c_void_p), ("queue", C.c_void_p),
+                ("status", C.c_void_p)]
+
+
+TM_PCG_CONVERGED, TM_PCG_MAX_ITER, TM_PCG_BREAKDOWN = 1, 2, 3
 
 
 _SIGNATURES = {
@@ -100,6 +129,9 @@ _SIGNATURES = {
                                     C.c_void_p, C.c_void_p, C.c_void_p]),
     "tm_spmv": (C.c_int, [C.POINTER(LinearOperator), C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                           C.c_void_p]),
+    "tm_adjoint_workspace_bytes": (C.c_size_t, [C.POINTER(AdjointArgs)]),
+    "tm_adjoint_p1": (C.c_int, [C.POINTER(AdjointArgs), C.c_void_p]),
+    "tm_batched_pcg": (C.c_int, [C.POINTER(BatchedPcgArgs), C.c_void_p]),
     "tm_pcg_partials_bytes": (C.c_size_t, []),
     "tm_pcg_start": (C.c_int, [C.POINTER(PcgArgs), C.c_void_p]),
     "tm_pcg_iterate": (C.c_int, [C.POINTER(PcgArgs), C.c_int32, C.c_void_p]),

@@ -1,0 +1,196 @@
+"""Differentiation of the assembly path with hand-written adjoint kernels.
+
+The reference differentiates by running torch autograd through its
+assembly graph and a solver adjoint (sparse/solve/torch_sla_solve.py:90-137,
+docs/source/user_guide/differentiability.rst:34-56).  Here:
+
+* ``DiffusionAssembly`` -- the values of a P1 diffusion matrix as a function
+  of node coordinates and per-element kappa; its backward runs the
+  ``tm_adjoint_p1`` kernel on dL/dvalues (CSR weights through the slot map).
+* ``LoadAssembly`` -- a P1 load vector as a function of node coordinates.
+* ``SparseSolve`` -- x = A^-1 b with Jacobi-PCG; backward solves A^T lambda =
+  dL/dx (A symmetric) and returns dL/dvalues = -lambda_row x_col, dL/db = lambda.
+* ``solve_diffusion`` -- the fused form for losses through a Dirichlet
+  diffusion solve: forward assembles, condenses and solves; backward solves
+  the adjoint system once and runs ``tm_adjoint_p1`` with the weights
+  -lambda_a u_b formed per element, so dL/dK is never materialised and the
+  geometry is recomputed instead of stored.
+"""
+import ctypes as C
+from typing import Optional
+
+import torch
+
+from . import _lib
+from .element import element_tables
+
+
+def _adjoint_call(topo, points, kappa, kappa_scale, k_mode, weights=None, slot=None, u=None, lam=None,
+                  load_source=_lib.TM_ADJ_LOAD_NONE, load_const=0.0, load_values=None,
+                  want_kappa=True, want_points=True):
+    lib = _lib.load()
+    dev = points.device
+    pts = points.detach().to(torch.float64).contiguous()
+    E = topo.n_elements
+    plan = topo.node_plan(dev)
+    a = _lib.AdjointArgs()
+    a.dtype = _lib.TM_F64
+    a.k_mode = k_mode
+    a.load_source = load_source
+    a.n_points = topo.n_points
+    a.points = _lib.ptr(pts)
+    kap = None if kappa is None else kappa.detach().to(torch.float64).contiguous()
+    a.kappa = _lib.ptr(kap)
+    a.kappa_scale = float(kappa_scale)
+    wts = None if weights is None else weights.detach().to(torch.float64).contiguous()
+    a.weights = _lib.ptr(wts)
+    a.slot_map = _lib.ptr(slot)
+    uu = None if u is None else u.detach().to(torch.float64).contiguous()
+    ll = None if lam is None else lam.detach().to(torch.float64).contiguous()
+    a.u, a.lam = _lib.ptr(uu), _lib.ptr(ll)
+    a.load_const = float(load_const)
+    lv = None if load_values is None else load_values.detach().to(torch.float64).contiguous()
+    a.load_values = _lib.ptr(lv)
+    gk = torch.empty(E, dtype=torch.float64, device=dev) if want_kappa else None
+    gp = torch.empty(topo.n_points, topo.info.dim, dtype=torch.float64, device=dev) if want_points else None
+    a.grad_kappa, a.grad_points = _lib.ptr(gk), _lib.ptr(gp)
+    a.plan = plan.struct()
+    a.tables = topo.table_struct(dev)
+    ws = torch.empty(max(1, lib.tm_adjoint_workspace_bytes(C.byref(a))), dtype=torch.uint8, device=dev)
+    a.workspace = _lib.ptr(ws)
+    _lib.check(lib.tm_adjoint_p1(C.byref(a), _lib.stream_handle(dev)), "tm_adjoint_p1")
+    return gk, gp
+
+
+def _require_p1(topo):
+    if topo.etype not in ("triangle", "tetra"):
+        raise NotImplementedError("gradients are implemented for P1 triangles and tetrahedra")
+
+
+class DiffusionAssembly(torch.autograd.Function):
+    """values = K(points, kappa) of a LaplaceElementAssembler (float64, P1)."""
+
+    @staticmethod
+    def forward(ctx, points, kappa, asm, kappa_scale):
+        from .assemble import assemble_forms
+        ed = {} if kappa is None else {"kappa": kappa.detach()}
+        sd = {} if kappa is not None else {"kappa": kappa_scale}
+        (values,) = assemble_forms([asm], points.detach(), ed, sd)
+        ctx.asm = asm
+        ctx.kappa_scale = kappa_scale if kappa is not None else kappa_scale
+        ctx.save_for_backward(points, kappa if kappa is not None else torch.empty(0))
+        ctx.has_kappa = kappa is not None
+        return values
+
+    @staticmethod
+    def backward(ctx, gvals):
+        points, kappa = ctx.saved_tensors
+        asm = ctx.asm
+        topo = asm._topology
+        _require_p1(topo)
+        et = asm.element_types[0]
+        slot = asm.projector[et].indices.to(points.device)
+        kap = kappa if ctx.has_kappa else None
+        gk, gp = _adjoint_call(topo, points, kap, ctx.kappa_scale if ctx.has_kappa else ctx.kappa_scale,
+                               _lib.TM_ADJ_K_CSR, weights=gvals, slot=slot,
+                               want_kappa=ctx.has_kappa and ctx.needs_input_grad[1],
+                               want_points=ctx.needs_input_grad[0])
+        return (gp.to(points.dtype) if gp is not None else None,
+                gk.to(kappa.dtype) if gk is not None else None, None, None)
+
+
+class LoadAssembly(torch.autograd.Function):
+    """b(points) for a constant or nodal source (float64, P1)."""
+
+    @staticmethod
+    def forward(ctx, points, topo, source, const, values, run):
+        ctx.topo, ctx.source, ctx.const = topo, source, const
+        ctx.save_for_backward(points, values if values is not None else torch.empty(0))
+        ctx.has_values = values is not None
+        return run()
+
+    @staticmethod
+    def backward(ctx, gb):
+        points, values = ctx.saved_tensors
+        _require_p1(ctx.topo)
+        load = _lib.TM_ADJ_LOAD_CONST if ctx.source == _lib.TM_SOURCE_CONST else _lib.TM_ADJ_LOAD_NODAL
+        _, gp = _adjoint_call(ctx.topo, points, None, 1.0, _lib.TM_ADJ_K_NONE, lam=gb.reshape(-1),
+                              load_source=load, load_const=ctx.const,
+                              load_values=values if ctx.has_values else None, want_kappa=False)
+        return gp.to(points.dtype), None, None, None, None, None
+
+
+class SparseSolve(torch.autograd.Function):
+    """x = A^-1 b for a symmetric positive definite SparseMatrix A."""
+
+    @staticmethod
+    def forward(ctx, values, b, A, kwargs):
+        from .solve import pcg_solve
+        x = pcg_solve(A.with_values(values.detach()), b.detach(), **kwargs)
+        ctx.A, ctx.kwargs = A, kwargs
+        ctx.save_for_backward(values, x)
+        return x
+
+    @staticmethod
+    def backward(ctx, gx):
+        from .solve import pcg_solve
+        values, x = ctx.saved_tensors
+        A = ctx.A.with_values(values.detach())
+        lam = pcg_solve(A, gx.detach(), **ctx.kwargs)
+        gvals = None
+        if ctx.needs_input_grad[0]:
+            gvals = -lam[A.row_indices] * x[A.col_indices]
+        return gvals, lam, None, None
+
+
+class _DiffusionSolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, points, kappa, asm, load, condenser, f, rtol):
+        from .assemble import assemble_forms
+        from .solve import pcg_solve
+        topo = asm._topology
+        ed = {"kappa": kappa.detach()}
+        (values,) = assemble_forms([asm], points.detach(), ed)
+        K = asm._build_output(values)
+        if f is None:
+            b = load(points.detach())
+        else:
+            b = load(points.detach(), point_data={"f": f})
+        Ki, bi = condenser(K, b)
+        ui = pcg_solve(Ki, bi, rtol=rtol)
+        u = condenser.recover(ui)
+        ctx.asm, ctx.load, ctx.cond, ctx.Ki, ctx.rtol = asm, load, condenser, Ki, rtol
+        ctx.save_for_backward(points, kappa, u, f if f is not None else torch.empty(0))
+        ctx.has_f = f is not None
+        return u
+
+    @staticmethod
+    def backward(ctx, gu):
+        from .solve import pcg_solve
+        points, kappa, u, f = ctx.saved_tensors
+        topo = ctx.asm._topology
+        _require_p1(topo)
+        cond = ctx.cond
+        lam_i = pcg_solve(ctx.Ki, cond.restrict(gu.detach().to(torch.float64)), rtol=ctx.rtol)
+        lam = cond.prolong(lam_i)
+        source = getattr(ctx.load, "_tm_source", None)
+        if ctx.has_f:
+            load, lconst, lvals = _lib.TM_ADJ_LOAD_NODAL, 0.0, f
+        elif source is not None and source[0] == "const":
+            load, lconst, lvals = _lib.TM_ADJ_LOAD_CONST, float(torch.as_tensor(source[1])), None
+        else:
+            raise NotImplementedError("solve_diffusion: the load must be a constant or a nodal source")
+        gk, gp = _adjoint_call(topo, points, kappa, 1.0, _lib.TM_ADJ_K_OUTER, u=u, lam=lam, load_source=load,
+                               load_const=lconst, load_values=lvals,
+                               want_kappa=ctx.needs_input_grad[1], want_points=ctx.needs_input_grad[0])
+        return (gp.to(points.dtype) if gp is not None else None, gk.to(kappa.dtype) if gk is not None else None,
+                None, None, None, None, None)
+
+
+def solve_diffusion(asm, load, condenser, points: torch.Tensor, kappa: torch.Tensor,
+                    f: Optional[torch.Tensor] = None, rtol: float = 1e-12) -> torch.Tensor:
+    """u(points, kappa) solving K(kappa, points) u = b(points) with the
+    Dirichlet data of ``condenser``; differentiable in ``points`` and
+    ``kappa`` through the fused adjoint (one adjoint PCG solve and one
+    element pass per backward)."""
+    return _DiffusionSolve.apply(points, kappa, asm, load, condenser, f, rtol)

@@ -217,6 +217,17 @@ class ElementAssembler(_AssemblerBase):
                 f"built-in families (LaplaceElementAssembler / DiffusionElementAssembler, "
                 f"MassElementAssembler, LinearElasticityElementAssembler)")
         et, points, ed, sd = self._prepare(points, point_data, element_data, scalar_data)
+        if torch.is_grad_enabled() and (points.requires_grad or any(
+                torch.is_tensor(v) and v.requires_grad for v in list(ed.values()) + list(sd.values()))):
+            if form != "diffusion":
+                raise NotImplementedError(f"gradients of the {form} form are not implemented")
+            from .adjoint import DiffusionAssembly
+            kap = self._tm_coefficients(ed, sd, self.elements[et].shape[0]).get("kappa")
+            if torch.is_tensor(kap) and kap.dim() > 0:
+                values = DiffusionAssembly.apply(points, kap, self, 1.0)
+            else:
+                values = DiffusionAssembly.apply(points, None, self, 1.0 if kap is None else float(kap))
+            return self._build_output(values)
         (values,) = assemble_forms([self], points, ed, sd)
         return self._build_output(values)
 
@@ -473,13 +484,30 @@ def assemble_linear_form(asm: NodeAssembler, fn: Callable, points: torch.Tensor,
     source = getattr(asm, "_tm_source", None) if fn == asm.forward else None
     Q = len(element_tables(topo.etype, topo.quadrature_order)["w"])
     E = topo.n_elements
+    needs_grad = torch.is_grad_enabled() and (points.requires_grad or any(
+        torch.is_tensor(v) and v.requires_grad for v in list(point_data.values()) + list(scalar_data.values())))
     if source is not None and source[0] == "const":
         c = torch.as_tensor(source[1], dtype=torch.float64).reshape(-1)
-        return _run_vector(topo, pts, _lib.TM_SOURCE_CONST, None, c.tolist(), int(c.numel()))
+        run = lambda: _run_vector(topo, pts, _lib.TM_SOURCE_CONST, None, c.tolist(), int(c.numel()))
+        if needs_grad:
+            if c.numel() != 1 or not points.requires_grad:
+                raise NotImplementedError("gradients of vector-valued loads are not implemented")
+            from .adjoint import LoadAssembly
+            return LoadAssembly.apply(points, topo, _lib.TM_SOURCE_CONST, float(c[0]), None, run)
+        return run()
     if source is not None and source[0] == "nodal" and source[1] in point_data:
         f = point_data[source[1]].to(device=dev, dtype=dt)
         width = 1 if f.dim() == 1 else int(np.prod(f.shape[1:]))
-        return _run_vector(topo, pts, _lib.TM_SOURCE_NODAL, f.reshape(f.shape[0], width).contiguous(), None, width)
+        fv = f.detach().reshape(f.shape[0], width).contiguous()
+        run = lambda: _run_vector(topo, pts, _lib.TM_SOURCE_NODAL, fv, None, width)
+        if needs_grad:
+            if width != 1 or f.requires_grad:
+                raise NotImplementedError("gradients with respect to the nodal source are not implemented")
+            from .adjoint import LoadAssembly
+            return LoadAssembly.apply(points, topo, _lib.TM_SOURCE_NODAL, 0.0, fv.reshape(-1), run)
+        return run()
+    if needs_grad:
+        raise NotImplementedError("gradients of general linear forms are not implemented")
     # general source g(x, data) * v: evaluate g at the quadrature points
     args = {}
     need_x = "x" in params

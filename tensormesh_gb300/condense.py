@@ -23,6 +23,7 @@ class Condenser(nn.Module):
         self.register_buffer("dirichlet_mask", dirichlet_mask)
         self.register_buffer("dirichlet_value", self._normalize_value(dirichlet_value))
         self.inner_row = None
+        self._blocks = None
         self.layout_hash = None
         self.K_ou2in = None
         self.n_dof = None
@@ -41,7 +42,51 @@ class Condenser(nn.Module):
             f"dirichlet_value must have length n_dof ({mask.shape[0]}) or n_outer_dof ({n_outer}), got {value.shape[0]}"
         return value
 
+    def _compute_block_layout(self, matrix: SparseMatrix) -> bool:
+        """Node-aligned masks on block matrices: condense whole HxH blocks.
+
+        The kept scalar entries are exactly the entries of the kept blocks,
+        in the same [block, a, b] order, so the values, rows and columns equal
+        those of the scalar condensation while the result stays a block
+        matrix (block-CSR SpMV, no index expansion)."""
+        H = matrix._block
+        dev = matrix.device
+        mask = self.dirichlet_mask.to(dev)
+        if H == 1 or mask.numel() % H:
+            return False
+        node_mask = mask.view(-1, H)
+        if not bool((node_mask == node_mask[:, :1]).all()):
+            return False
+        nmask = node_mask[:, 0]
+        br = matrix._block_row.to(dev).long()
+        bc = matrix._block_col.to(dev).long()
+        inner_n = ~nmask
+        ib = inner_n[br] & inner_n[bc]
+        ob = inner_n[br] & nmask[bc]
+        ni_n, no_n = int(inner_n.sum()), int(nmask.sum())
+        local = torch.full((nmask.numel(),), -1, dtype=torch.long, device=dev)
+        local[inner_n] = torch.arange(ni_n, device=dev)
+        local[nmask] = torch.arange(no_n, device=dev)
+        blk_in = torch.nonzero(ib).reshape(-1)
+        blk_out = torch.nonzero(ob).reshape(-1)
+        k = torch.arange(H * H, device=dev)
+        self.inner_idx = (blk_in[:, None] * (H * H) + k).reshape(-1)
+        self.ou2in_idx = (blk_out[:, None] * (H * H) + k).reshape(-1)
+        self._blocks = (H, local[br[blk_in]], local[bc[blk_in]], local[br[blk_out]], local[bc[blk_out]], ni_n, no_n)
+        self.inner_row = None
+        self.is_inner_dof, self.is_outer_dof = ~mask, mask
+        self.inner_shape, self.ou2in_shape = (ni_n * H, ni_n * H), (ni_n * H, no_n * H)
+        self.n_inner_dof, self.n_outer_dof, self.n_dof = ni_n * H, no_n * H, matrix.shape[0]
+        self.layout_hash = matrix.layout_hash
+        self._sorted = bool(matrix._sorted)
+        self._K_template = None
+        self._Kio_template = None
+        return True
+
     def _compute_layout(self, matrix: SparseMatrix):
+        self._blocks = None
+        if self._compute_block_layout(matrix):
+            return
         dev = matrix.device
         mask = self.dirichlet_mask.to(dev)
         edge_u, edge_v = matrix.row_indices, matrix.col_indices
@@ -73,7 +118,7 @@ class Condenser(nn.Module):
     def __call__(self, matrix: SparseMatrix, rhs: Optional[torch.Tensor] = None) -> Tuple[SparseMatrix, torch.Tensor]:
         if rhs is None:
             rhs = torch.zeros(matrix.shape[0], dtype=matrix.dtype, device=matrix.device)
-        if self.inner_row is None:
+        if self.n_dof is None:
             self._compute_layout(matrix)
         assert matrix.shape[0] == self.n_dof and matrix.shape[1] == self.n_dof, \
             f"the shape of matrix must be [{self.n_dof}, {self.n_dof}], but got {matrix.shape}"
@@ -81,7 +126,15 @@ class Condenser(nn.Module):
             "the layout of the matrix is changed, please recompute the condensed matrix"
         assert rhs.shape[0] == self.n_dof, f"the shape of rhs must be [{self.n_dof}, ...], but got {rhs.shape}"
         vals = matrix.values
-        if self._K_template is None:
+        if self._K_template is None and self._blocks is not None:
+            H, ir, ic, orow, ocol, ni_n, no_n = self._blocks
+            self._K_template = SparseMatrix.from_block_coo(vals[self.inner_idx].view(-1, H, H), ir, ic, (ni_n, ni_n))
+            self._K_template._sorted = self._sorted or None
+            self._Kio_template = SparseMatrix.from_block_coo(vals[self.ou2in_idx].view(-1, H, H), orow, ocol,
+                                                             (ni_n, no_n))
+            self._Kio_template._sorted = self._sorted or None
+            K_inner, K_ou2in = self._K_template, self._Kio_template
+        elif self._K_template is None:
             self._K_template = SparseMatrix(vals[self.inner_idx], self.inner_row, self.inner_col, self.inner_shape,
                                             _sorted=self._sorted or None)
             self._Kio_template = SparseMatrix(vals[self.ou2in_idx], self.ou2in_row, self.ou2in_col, self.ou2in_shape,

@@ -11,9 +11,11 @@
 // (element, then local entry), replacing ReduceProjector's index_add_
 // (assemble/projector.py:95-123).  Targets touched by one chunk only are
 // written directly -- for symmetric forms the value is also written to the
-// transposed CSR position -- the others go to a partial that a second
-// kernel sums in chunk order.  There are no atomics: results are bitwise
-// reproducible run to run.
+// transposed CSR position.  For the others each chunk publishes a partial;
+// the last chunk to publish one (one integer counter per shared target)
+// sums the target's partials in chunk order and writes it.  Nothing waits
+// and no floating-point value is accumulated atomically: results are
+// bitwise reproducible run to run.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <cstdio>
@@ -22,16 +24,30 @@
 #include "../../include/tensormesh_gb300.h"
 #include "tm_df64.cuh"
 #include "tm_element.cuh"
+#include "tm_reduce.cuh"
 #include "tm_status.h"
 
 namespace tmk {
 
 constexpr int kThreads = 256;
 
-__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+// bytes of partial sums per partial: the scalar forms each keep one value,
+// elasticity a DxD block
+template <typename R, int ET, int FORMS>
+__host__ __device__ inline size_t partial_bytes_per(void) {
+    constexpr int D = Traits<ET>::D;
+    if (FORMS & TM_FORM_ELASTICITY) return sizeof(R) * D * D;
+    return sizeof(R) * (((FORMS & TM_FORM_DIFFUSION) ? 1 : 0) + ((FORMS & TM_FORM_MASS) ? 1 : 0));
+}
+
+// the float64 P1 diffusion / mass kernels run in double-float arithmetic
+template <typename R, int ET, int FORMS>
+__host__ __device__ constexpr bool use_df64() {
+    return std::is_same<R, double>::value && Traits<ET>::P1 != 0 && (FORMS & TM_FORM_ELASTICITY) == 0;
+}
 
 struct MatLayout {
-    size_t tab, mhl, x, g, jw, ld, lm, le, total;
+    size_t tab, mhl, x, g, jw, ld, ls, lm, le, total;
 };
 
 template <typename R, int ET, int FORMS>
@@ -41,6 +57,7 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q) {
     constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
     constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
     constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
+    constexpr bool DF64 = use_df64<R, ET, FORMS>();
     MatLayout L;
     size_t o = 0;
     L.tab = o;
@@ -58,6 +75,8 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q) {
     }
     L.ld = o;
     if (DIFF) o = align16(o + sizeof(R) * CH * NL);
+    L.ls = o;
+    if (DIFF && DF64) o = align16(o + sizeof(R) * CH);
     L.lm = o;
     if (MASS) o = align16(o + sizeof(R) * CH * (T::P1 ? 1 : NL));
     L.le = o;
@@ -69,6 +88,9 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q) {
 template <typename R>
 __device__ __forceinline__ R rabs(R x) { return x < R(0) ? -x : x; }
 
+template <typename R>
+__device__ __forceinline__ R ld_cg(const R* p) { return __ldcg(p); }
+
 template <typename R, int ET, int FORMS>
 __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
     using T = Traits<ET>;
@@ -76,6 +98,7 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
     constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
     constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
     constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
+    constexpr bool DF64 = use_df64<R, ET, FORMS>();
     constexpr int HH = ELAST ? D * D : 1;
     const tm_chunk_plan& P = a.plan;
     const int CH = P.chunk_elems, Q = a.tables.n_quad;
@@ -84,15 +107,14 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
     extern __shared__ __align__(16) unsigned char sm[];
     double* tab = reinterpret_cast<double*>(sm + L.tab);
     double* mhl = reinterpret_cast<double*>(sm + L.mhl);
+    f2* mh2 = reinterpret_cast<f2*>(mhl + NL);
     R* LD = reinterpret_cast<R*>(sm + L.ld);
+    R* LS = reinterpret_cast<R*>(sm + L.ls);
     R* LM = reinterpret_cast<R*>(sm + L.lm);
     R* LE = reinterpret_cast<R*>(sm + L.le);
 
     for (int k = threadIdx.x; k < TL.total; k += blockDim.x) tab[k] = a.tables.packed[k];
     __syncthreads();
-    // float64 P1 diffusion/mass: double-float arithmetic on the FP32 pipes
-    constexpr bool DF64 = std::is_same<R, double>::value && T::P1 != 0 && !ELAST;
-    f2* mh2 = reinterpret_cast<f2*>(mhl + NL);
     if (MASS && T::P1)
         for (int l = threadIdx.x; l < NL; l += blockDim.x) {
             int pa, pb;
@@ -114,6 +136,7 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
     bool use_df = false;
     if constexpr (T::P1 != 0) {
         const R wsum = (R)tab[TL.wsum];
+        // P1 simplices in the arithmetic of R: unscaled gradients C_b (g_b = C_b / det)
         auto native_p1 = [&]() {
             for (int el = threadIdx.x; el < ne; el += blockDim.x) {
                 const int64_t i = i0 + el;
@@ -151,7 +174,11 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
             }
         };
         if constexpr (DF64) {
-            f2* LD2 = reinterpret_cast<f2*>(LD);
+            // Double-float locals: for diffusion the unscaled Gram entries
+            // G_ab = C_a . C_b (LD) and the per-element scale kappa W / |det|
+            // (LS), multiplied during the reduction; for mass |det| rho (LM).
+            f2* LG2 = reinterpret_cast<f2*>(LD);
+            f2* LS2 = reinterpret_cast<f2*>(LS);
             f2* LM2 = reinterpret_cast<f2*>(LM);
             bool bad = !exponent_in_band(a.kappa_scale, 30) || !exponent_in_band(a.mass_scale, 30) ||
                        !exponent_in_band(tab[TL.wsum], 30);
@@ -201,36 +228,48 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
                     cof[1][1] = J[0][0];
                     det = f2_diff_of_products(J[0][0], J[1][1], J[0][1], J[1][0]);
                 }
-                f2 C[B][D];
-#pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    f2 acc = cof[0][c];
-#pragma unroll
-                    for (int r = 1; r < D; ++r) acc = f2_add(acc, cof[r][c]);
-                    C[0][c] = f2_neg(acc);
-#pragma unroll
-                    for (int r = 0; r < D; ++r) C[r + 1][c] = cof[r][c];
-                }
                 const f2 adet = f2_abs(det);
                 bad |= !(adet.hi > 0.0f) || !f2_in_band(adet, -100, 100);
                 if constexpr (DIFF) {
+                    // Gram matrix of the cofactor rows; vertex 0 has C_0 = -sum_i cof_i,
+                    // so C_0.C_0 = sum_ij G_ij and C_0.C_{j+1} = -sum_i G_ij
+                    f2 G[D][D];
+#pragma unroll
+                    for (int r = 0; r < D; ++r)
+#pragma unroll
+                        for (int c = r; c < D; ++c) {
+                            G[r][c] = D == 3 ? f2_dot3(cof[r], cof[c]) : f2_dot2(cof[r], cof[c]);
+                            G[c][r] = G[r][c];
+                        }
+                    f2 rs[D];
+                    int gmax = 0;
+#pragma unroll
+                    for (int c = 0; c < D; ++c) {
+                        f2 acc = G[0][c];
+#pragma unroll
+                        for (int r = 1; r < D; ++r) acc = f2_add(acc, G[r][c]);
+                        rs[c] = acc;
+                        gmax = max(gmax, (int)((__float_as_uint(G[c][c].hi) >> 23) & 0xFF));
+                    }
+                    f2 tot = rs[0];
+#pragma unroll
+                    for (int c = 1; c < D; ++c) tot = f2_add(tot, rs[c]);
+                    gmax = max(gmax, (int)((__float_as_uint(tot.hi) >> 23) & 0xFF));
                     const double kd = kap ? ldg(static_cast<const double*>(a.kappa) + e) : 1.0;
                     bad |= !exponent_in_band(kd, 30);
                     const f2 sc = f2_mul(f2_mul(split_double(kd), ks), f2_mul(ws, f2_recip(adet)));
-                    f2 Dv[B][D];
-#pragma unroll
-                    for (int p = 0; p < B; ++p)
-#pragma unroll
-                        for (int c = 0; c < D; ++c) Dv[p][c] = f2_mul(sc, C[p][c]);
+                    const int sexp = (int)((__float_as_uint(sc.hi) >> 23) & 0xFF);
+                    bad |= !f2_finite(sc) || (gmax - 127) + (sexp - 127) >= 100;
+                    LS2[el] = sc;
+                    f2* g = LG2 + el * NL;
                     int l = 0;
+                    g[l++] = tot;
 #pragma unroll
-                    for (int p = 0; p < B; ++p)
+                    for (int q = 0; q < D; ++q) g[l++] = f2_neg(rs[q]);
 #pragma unroll
-                        for (int q = p; q < B; ++q, ++l) {
-                            const f2 v = D == 3 ? f2_dot3(Dv[p], C[q]) : f2_dot2(Dv[p], C[q]);
-                            bad |= !f2_in_band(v, -127, 100);   // finite, no overflow
-                            LD2[el * NL + l] = v;
-                        }
+                    for (int p = 0; p < D; ++p)
+#pragma unroll
+                        for (int q = p; q < D; ++q) g[l++] = G[p][q];
                 }
                 if constexpr (MASS) {
                     const f2 v = f2_mul(adet, ms);
@@ -327,14 +366,36 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
     if constexpr (DF64 && MASS) {
         for (int pa = 0; pa < B; ++pa) diag_mask |= 1ull << (pa * B - pa * (pa - 1) / 2);
         mass_sym = true;
-        for (int l = 0; l < NL; ++l)
-            mass_sym &= mhl[l] == (((diag_mask >> l) & 1u) ? mhl[0] : mhl[1]);
+        for (int l = 0; l < NL; ++l) mass_sym &= mhl[l] == (((diag_mask >> l) & 1u) ? mhl[0] : mhl[1]);
     }
     R* oD = static_cast<R*>(a.out_diffusion);
     R* oM = static_cast<R*>(a.out_mass);
     R* oE = static_cast<R*>(a.out_elasticity);
     R* part = static_cast<R*>(a.workspace);
     const int64_t np = P.n_partials;
+    int32_t* counters = reinterpret_cast<int32_t*>(static_cast<unsigned char*>(a.workspace) +
+                                                   align16(partial_bytes_per<R, ET, FORMS>() * (size_t)np));
+    // a target's value at its CSR position and, for symmetric forms, the
+    // transpose at the mirrored position
+    auto write_out = [&](int64_t tgt, int64_t mir, R ad, R am, const R* ae) {
+        if constexpr (DIFF) {
+            oD[tgt] = ad;
+            if (mir != tgt) oD[mir] = ad;
+        }
+        if constexpr (MASS) {
+            oM[tgt] = am;
+            if (mir != tgt) oM[mir] = am;
+        }
+        if constexpr (ELAST) {
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    oE[tgt * HH + r * D + c] = ae[r * D + c];
+                    if (mir != tgt) oE[mir * HH + c * D + r] = ae[r * D + c];
+                }
+        }
+    };
     for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
         const int p0 = P.slot_ptr[s], p1 = P.slot_ptr[s + 1];
         R ad = 0, am = 0;
@@ -344,21 +405,26 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
         if (DF64 && use_df) {
             // compensated sums: TwoSum on the high parts, the error terms and
             // the low parts summed in plain float (|error| ~ 2^-48 of the terms)
-            const f2* LD2 = reinterpret_cast<const f2*>(LD);
+            const f2* LG2 = reinterpret_cast<const f2*>(LD);
+            const f2* LS2 = reinterpret_cast<const f2*>(LS);
             const f2* LM2 = reinterpret_cast<const f2*>(LM);
-            float kh = 0.0f, ke = 0.0f;                   // diffusion
-            float dh = 0.0f, de = 0.0f, oh = 0.0f, oe = 0.0f;   // |det| on diagonal / off-diagonal template entries
-            f2 sm2 = {0.0f, 0.0f};                        // mass, general template
+            float kh = 0.0f, ke = 0.0f;                             // diffusion
+            float dh = 0.0f, de = 0.0f, oh = 0.0f, oe = 0.0f;       // |det| on diagonal / off-diagonal entries
+            f2 sm2 = {0.0f, 0.0f};                                  // mass, general template
             for (int p = p0; p < p1; ++p) {
                 const int idx = P.contrib[p] >> 1;
+                const int el = idx / NL;
                 if constexpr (DIFF) {
-                    const f2 v = LD2[idx];
-                    const f2 t = two_sum(kh, v.hi);
+                    const f2 sc = LS2[el], g = LG2[idx];
+                    const float pr = __fmul_rn(sc.hi, g.hi);
+                    float er = __fmaf_rn(sc.hi, g.hi, -pr);
+                    er = __fmaf_rn(sc.hi, g.lo, er);
+                    er = __fmaf_rn(sc.lo, g.hi, er);
+                    const f2 t = two_sum(kh, pr);
                     kh = t.hi;
-                    ke = __fadd_rn(ke, __fadd_rn(t.lo, v.lo));
+                    ke = __fadd_rn(ke, __fadd_rn(t.lo, er));
                 }
                 if constexpr (MASS) {
-                    const int el = idx / NL;
                     const int l = idx - el * NL;
                     const f2 v = LM2[el];
                     if (mass_sym) {
@@ -378,58 +444,41 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
             }
             if constexpr (DIFF) ad = (R)f2_to_double(two_sum(kh, ke));
             if constexpr (MASS) {
-                if (mass_sym)
-                    sm2 = f2_add(f2_mul(two_sum(dh, de), mh2[0]), f2_mul(two_sum(oh, oe), mh2[1]));
+                if (mass_sym) sm2 = f2_add(f2_mul(two_sum(dh, de), mh2[0]), f2_mul(two_sum(oh, oe), mh2[1]));
                 am = (R)f2_to_double(sm2);
             }
-        } else
-        for (int p = p0; p < p1; ++p) {
-            const int code = P.contrib[p];
-            const int idx = code >> 1;
-            if constexpr (DIFF) ad += LD[idx];
-            if constexpr (MASS) {
-                if constexpr (T::P1 != 0) {
-                    const int el = idx / NL;
-                    am += LM[el] * (R)mhl[idx - el * NL];
-                } else {
-                    am += LM[idx];
+        } else {
+            for (int p = p0; p < p1; ++p) {
+                const int code = P.contrib[p];
+                const int idx = code >> 1;
+                if constexpr (DIFF) ad += LD[idx];
+                if constexpr (MASS) {
+                    if constexpr (T::P1 != 0) {
+                        const int el = idx / NL;
+                        am += LM[el] * (R)mhl[idx - el * NL];
+                    } else {
+                        am += LM[idx];
+                    }
                 }
-            }
-            if constexpr (ELAST) {
-                const R* blk = LE + (size_t)idx * HH;
-                if (code & 1) {
+                if constexpr (ELAST) {
+                    const R* blk = LE + (size_t)idx * HH;
+                    if (code & 1) {
 #pragma unroll
-                    for (int r = 0; r < D; ++r)
+                        for (int r = 0; r < D; ++r)
 #pragma unroll
-                        for (int c = 0; c < D; ++c) ae[r * D + c] += blk[c * D + r];
-                } else {
+                            for (int c = 0; c < D; ++c) ae[r * D + c] += blk[c * D + r];
+                    } else {
 #pragma unroll
-                    for (int k = 0; k < HH; ++k) ae[k] += blk[k];
+                        for (int k = 0; k < HH; ++k) ae[k] += blk[k];
+                    }
                 }
             }
         }
-        const int32_t tgt = P.slot_target[s];
-        if (tgt >= 0) {
-            const int32_t mir = P.slot_mirror[s];
-            if constexpr (DIFF) {
-                oD[tgt] = ad;
-                if (mir != tgt) oD[mir] = ad;
-            }
-            if constexpr (MASS) {
-                oM[tgt] = am;
-                if (mir != tgt) oM[mir] = am;
-            }
-            if constexpr (ELAST) {
-#pragma unroll
-                for (int r = 0; r < D; ++r)
-#pragma unroll
-                    for (int c = 0; c < D; ++c) {
-                        oE[(int64_t)tgt * HH + r * D + c] = ae[r * D + c];
-                        if (mir != tgt) oE[(int64_t)mir * HH + c * D + r] = ae[r * D + c];
-                    }
-            }
-        } else {
-            const int64_t pi = -(int64_t)tgt - 1;
+        const int64_t tgt = P.slot_target[s];
+        if (tgt < 0) {
+            // shared target: publish this chunk's partial (summed below by
+            // the last chunk to publish one)
+            const int64_t pi = -tgt - 1;
             if constexpr (ELAST) {
 #pragma unroll
                 for (int k = 0; k < HH; ++k) part[pi * HH + k] = ae[k];
@@ -438,56 +487,36 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
                 if constexpr (DIFF) part[(f++) * np + pi] = ad;
                 if constexpr (MASS) part[(f++) * np + pi] = am;
             }
+            continue;
         }
+        write_out(tgt, P.slot_mirror[s], ad, am, ae);
     }
-}
-
-// sum the partials of targets shared by several chunks, in chunk order
-template <typename R, int FORMS, int D>
-__global__ void __launch_bounds__(kThreads) k_matrix_finalize(const tm_matrix_args a) {
-    constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
-    constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
-    constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
-    constexpr int HH = ELAST ? D * D : 1;
-    const tm_chunk_plan& P = a.plan;
-    const R* part = static_cast<const R*>(a.workspace);
-    const int64_t np = P.n_partials;
-    R* oD = static_cast<R*>(a.out_diffusion);
-    R* oM = static_cast<R*>(a.out_mass);
-    R* oE = static_cast<R*>(a.out_elasticity);
-    for (int64_t sh = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sh < P.n_shared;
-         sh += (int64_t)gridDim.x * blockDim.x) {
-        const int p0 = P.shared_ptr[sh], p1 = P.shared_ptr[sh + 1];
-        const int64_t tgt = P.shared_target[sh], mir = P.shared_mirror[sh];
-        if constexpr (ELAST) {
-            R acc[HH];
+    if (np > 0) {
+        // one fence per thread publishes all of its partials; then count, and
+        // the last chunk of each shared target sums its partials in chunk order
+        __threadfence();
+        for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+            const int32_t tgt = P.slot_target[s];
+            if (tgt >= 0) continue;
+            const int32_t sh = P.slot_mirror[s];
+            const int32_t q0 = P.shared_ptr[sh], q1 = P.shared_ptr[sh + 1];
+            if (atomicAdd(counters + sh, 1) != q1 - q0 - 1) continue;
+            __threadfence();
+            R ad = 0, am = 0;
+            R ae[HH];
 #pragma unroll
-            for (int k = 0; k < HH; ++k) acc[k] = 0;
-            for (int p = p0; p < p1; ++p)
+            for (int k = 0; k < HH; ++k) ae[k] = 0;
+            for (int q = q0; q < q1; ++q) {
+                if constexpr (ELAST) {
 #pragma unroll
-                for (int k = 0; k < HH; ++k) acc[k] += part[(int64_t)p * HH + k];
-#pragma unroll
-            for (int r = 0; r < D; ++r)
-#pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    oE[tgt * HH + r * D + c] = acc[r * D + c];
-                    if (mir != tgt) oE[mir * HH + c * D + r] = acc[r * D + c];
+                    for (int k = 0; k < HH; ++k) ae[k] += ld_cg(part + (int64_t)q * HH + k);
+                } else {
+                    int f = 0;
+                    if constexpr (DIFF) ad += ld_cg(part + (f++) * np + q);
+                    if constexpr (MASS) am += ld_cg(part + (f++) * np + q);
                 }
-        } else {
-            int f = 0;
-            if constexpr (DIFF) {
-                R acc = 0;
-                for (int p = p0; p < p1; ++p) acc += part[f * np + p];
-                oD[tgt] = acc;
-                if (mir != tgt) oD[mir] = acc;
-                ++f;
             }
-            if constexpr (MASS) {
-                R acc = 0;
-                for (int p = p0; p < p1; ++p) acc += part[f * np + p];
-                oM[tgt] = acc;
-                if (mir != tgt) oM[mir] = acc;
-            }
+            write_out(P.shared_target[sh], P.shared_mirror[sh], ad, am, ae);
         }
     }
 }
@@ -605,49 +634,7 @@ __global__ void __launch_bounds__(kThreads) k_vector(const tm_vector_args a) {
             for (int w = 0; w < W; ++w) LV[(el * B + p) * W + w] = acc[p][w];
     }
     __syncthreads();
-    const int32_t s0 = P.chunk_begin[blockIdx.x], s1 = P.chunk_begin[blockIdx.x + 1];
-    R* out = static_cast<R*>(a.out);
-    R* part = static_cast<R*>(a.workspace);
-    for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-        const int p0 = P.slot_ptr[s], p1 = P.slot_ptr[s + 1];
-        R acc[W];
-#pragma unroll
-        for (int w = 0; w < W; ++w) acc[w] = 0;
-        for (int p = p0; p < p1; ++p) {
-            const int idx = P.contrib[p] >> 1;
-#pragma unroll
-            for (int w = 0; w < W; ++w) acc[w] += LV[idx * W + w];
-        }
-        const int32_t tgt = P.slot_target[s];
-        if (tgt >= 0) {
-#pragma unroll
-            for (int w = 0; w < W; ++w) out[(int64_t)tgt * W + w] = acc[w];
-        } else {
-            const int64_t pi = -(int64_t)tgt - 1;
-#pragma unroll
-            for (int w = 0; w < W; ++w) part[pi * W + w] = acc[w];
-        }
-    }
-}
-
-template <typename R, int W>
-__global__ void __launch_bounds__(kThreads) k_vector_finalize(const tm_vector_args a) {
-    const tm_chunk_plan& P = a.plan;
-    const R* part = static_cast<const R*>(a.workspace);
-    R* out = static_cast<R*>(a.out);
-    for (int64_t sh = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sh < P.n_shared;
-         sh += (int64_t)gridDim.x * blockDim.x) {
-        const int p0 = P.shared_ptr[sh], p1 = P.shared_ptr[sh + 1];
-        const int64_t tgt = P.shared_target[sh];
-        R acc[W];
-#pragma unroll
-        for (int w = 0; w < W; ++w) acc[w] = 0;
-        for (int p = p0; p < p1; ++p)
-#pragma unroll
-            for (int w = 0; w < W; ++w) acc[w] += part[(int64_t)p * W + w];
-#pragma unroll
-        for (int w = 0; w < W; ++w) out[tgt * W + w] = acc[w];
-    }
+    node_reduce<R, W>(P, LV, static_cast<R*>(a.out), a.workspace);
 }
 
 // ----------------------------------------------------- geometry, x at q
@@ -763,23 +750,23 @@ inline int set_smem(K kernel, size_t bytes) {
 
 template <typename R, int ET, int FORMS>
 int run_matrix(const tm_matrix_args& a, cudaStream_t st) {
-    using T = Traits<ET>;
     const MatLayout L = mat_layout<R, ET, FORMS>(a.plan.chunk_elems, a.tables.n_quad);
     if (L.total > 227 * 1024) return tm_set_error(TM_ERR_TOO_LARGE, "tm_assemble_matrix: chunk needs more than 227 KB of shared memory");
-    if (a.plan.n_chunks > 0) {
-        int s = set_smem(k_matrix<R, ET, FORMS>, L.total);
-        if (s) return s;
-        if (a.event_begin && cudaEventRecord(static_cast<cudaEvent_t>(a.event_begin), st) != cudaSuccess)
-            return launch_status("cudaEventRecord");
-        k_matrix<R, ET, FORMS><<<a.plan.n_chunks, kThreads, L.total, st>>>(a);
-        if ((s = launch_status("k_matrix"))) return s;
-        if (a.event_end && cudaEventRecord(static_cast<cudaEvent_t>(a.event_end), st) != cudaSuccess)
-            return launch_status("cudaEventRecord");
-    }
+    if (a.plan.n_chunks == 0) return TM_OK;
     if (a.plan.n_shared > 0) {
-        k_matrix_finalize<R, FORMS, T::D><<<grid_for(a.plan.n_shared), kThreads, 0, st>>>(a);
-        return launch_status("k_matrix_finalize");
+        void* counters = static_cast<unsigned char*>(a.workspace) +
+                         align16(partial_bytes_per<R, ET, FORMS>() * (size_t)a.plan.n_partials);
+        if (cudaMemsetAsync(counters, 0, sizeof(int32_t) * (size_t)a.plan.n_shared, st) != cudaSuccess)
+            return launch_status("cudaMemsetAsync");
     }
+    int s = set_smem(k_matrix<R, ET, FORMS>, L.total);
+    if (s) return s;
+    if (a.event_begin && cudaEventRecord(static_cast<cudaEvent_t>(a.event_begin), st) != cudaSuccess)
+        return launch_status("cudaEventRecord");
+    k_matrix<R, ET, FORMS><<<a.plan.n_chunks, kThreads, L.total, st>>>(a);
+    if ((s = launch_status("k_matrix"))) return s;
+    if (a.event_end && cudaEventRecord(static_cast<cudaEvent_t>(a.event_end), st) != cudaSuccess)
+        return launch_status("cudaEventRecord");
     return TM_OK;
 }
 
@@ -811,17 +798,16 @@ int run_vector(const tm_vector_args& a, cudaStream_t st) {
     if (L.total > 227 * 1024) return tm_set_error(TM_ERR_TOO_LARGE, "tm_assemble_vector: chunk needs more than 227 KB of shared memory");
     if (cudaMemsetAsync(a.out, 0, sizeof(R) * a.n_points * W, st) != cudaSuccess)
         return launch_status("cudaMemsetAsync");
-    if (a.plan.n_chunks > 0) {
-        int s = set_smem(k_vector<R, ET, SRC, W>, L.total);
-        if (s) return s;
-        k_vector<R, ET, SRC, W><<<a.plan.n_chunks, kThreads, L.total, st>>>(a);
-        if ((s = launch_status("k_vector"))) return s;
-    }
+    if (a.plan.n_chunks == 0) return TM_OK;
     if (a.plan.n_shared > 0) {
-        k_vector_finalize<R, W><<<grid_for(a.plan.n_shared), kThreads, 0, st>>>(a);
-        return launch_status("k_vector_finalize");
+        void* counters = static_cast<unsigned char*>(a.workspace) + align16(sizeof(R) * W * (size_t)a.plan.n_partials);
+        if (cudaMemsetAsync(counters, 0, sizeof(int32_t) * (size_t)a.plan.n_shared, st) != cudaSuccess)
+            return launch_status("cudaMemsetAsync");
     }
-    return TM_OK;
+    int s = set_smem(k_vector<R, ET, SRC, W>, L.total);
+    if (s) return s;
+    k_vector<R, ET, SRC, W><<<a.plan.n_chunks, kThreads, L.total, st>>>(a);
+    return launch_status("k_vector");
 }
 
 template <typename R, int ET, int SRC>
@@ -896,7 +882,8 @@ extern "C" size_t tm_matrix_workspace_bytes(const tm_matrix_args* a) {
     } else {
         per = ((a->forms & TM_FORM_DIFFUSION) ? 1 : 0) + ((a->forms & TM_FORM_MASS) ? 1 : 0);
     }
-    return rs * (size_t)a->plan.n_partials * per;
+    // partials, then one int32 counter per shared target
+    return align16(rs * (size_t)a->plan.n_partials * per) + sizeof(int32_t) * (size_t)a->plan.n_shared;
 }
 
 extern "C" int tm_assemble_matrix(const tm_matrix_args* a, tm_stream_t stream) {
@@ -924,7 +911,8 @@ extern "C" int tm_assemble_matrix(const tm_matrix_args* a, tm_stream_t stream) {
 
 extern "C" size_t tm_vector_workspace_bytes(const tm_vector_args* a) {
     if (!a) return 0;
-    return (a->dtype == TM_F32 ? 4 : 8) * (size_t)a->plan.n_partials * (size_t)a->width;
+    return align16((a->dtype == TM_F32 ? 4 : 8) * (size_t)a->plan.n_partials * (size_t)a->width) +
+           sizeof(int32_t) * (size_t)a->plan.n_shared;
 }
 
 extern "C" int tm_assemble_vector(const tm_vector_args* a, tm_stream_t stream) {

@@ -1,0 +1,194 @@
+// Batched Jacobi-PCG over the diagonal blocks of one block-diagonal CSR
+// matrix: many independent SPD systems of uneven sizes (offset-concatenated
+// meshes) solved in one launch.
+//
+// The reference has no batched varying-mesh solve: it builds, assembles,
+// condenses and solves one mesh after another
+// (docs/source/user_guide/batched_workflows.rst:247-249), with Jacobi-
+// preconditioned Krylov loops of torch SpMVs as its in-tree templates
+// (sparse/solve/torch_solve.py:70-248).
+//
+// Persistent CTAs take systems from a queue (one integer counter) and run
+// the whole PCG of a system with __syncthreads only: no grid-wide barrier,
+// no waiting on other CTAs.  Every loop is bounded by max_iter.  Reductions
+// are per thread in row order and then a fixed tree in shared memory, so the
+// result of a system does not depend on which CTA solved it.  Dirichlet rows
+// (dirichlet[i] != 0) keep x_i as given on input and are excluded from the
+// iteration (p_i = r_i = 0), which solves the condensed system
+// K_ii x_i = b_i - K_io x_o without extracting K_ii.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <cstdio>
+#include <type_traits>
+
+#include "../../include/tensormesh_gb300.h"
+#include "tm_status.h"
+
+namespace tmk {
+
+constexpr int kBatchThreads = 512;
+
+template <int N>
+__device__ __forceinline__ void block_sum(double (&v)[N], double* red) {
+    // red: [N][kBatchThreads] scratch; fixed-order tree
+#pragma unroll
+    for (int k = 0; k < N; ++k) red[k * kBatchThreads + threadIdx.x] = v[k];
+    __syncthreads();
+    for (int w = kBatchThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+#pragma unroll
+            for (int k = 0; k < N; ++k) red[k * kBatchThreads + threadIdx.x] += red[k * kBatchThreads + threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = red[k * kBatchThreads];
+    __syncthreads();
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBatchThreads) k_batched_pcg(const tm_batched_pcg_args a) {
+    __shared__ double red[3 * kBatchThreads];
+    __shared__ int sys_s;
+    const int64_t* rp = a.A.row_ptr;
+    const int32_t* col = a.A.col;
+    const R* val = static_cast<const R*>(a.A.values);
+    const R* b = static_cast<const R*>(a.b);
+    R* x = static_cast<R*>(a.x);
+    const int64_t n_all = a.A.n_rows;
+    R* r = static_cast<R*>(a.work);
+    R* z = r + n_all;
+    R* p = z + n_all;
+    R* q = p + n_all;
+    R* dinv = q + n_all;
+    const uint8_t* fixed = a.dirichlet;
+    const double tol2 = a.rtol * a.rtol;
+    for (;;) {
+        if (threadIdx.x == 0) sys_s = atomicAdd(a.queue, 1);
+        __syncthreads();
+        const int sys = sys_s;
+        __syncthreads();
+        if (sys >= a.n_systems) return;
+        const int64_t r0 = a.system_offset[sys], r1 = a.system_offset[sys + 1];
+        // start: r = b - A x on free rows, z = r / diag, p = z
+        double v3[3] = {0.0, 0.0, 0.0};   // rz, rr, bb
+        for (int64_t i = r0 + threadIdx.x; i < r1; i += kBatchThreads) {
+            if (fixed && fixed[i]) {
+                r[i] = z[i] = p[i] = q[i] = dinv[i] = R(0);
+                continue;
+            }
+            double ax = 0.0, d = 0.0;
+            for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
+                const int64_t c = col[k];
+                const double v = (double)val[k];
+                ax += v * (double)x[c];
+                if (c == i) d += v;
+            }
+            const double ri = (double)b[i] - ax;
+            const double di = d != 0.0 ? 1.0 / d : 0.0;
+            const double zi = ri * di;
+            dinv[i] = (R)di;
+            r[i] = (R)ri;
+            z[i] = (R)zi;
+            p[i] = (R)zi;
+            v3[0] += ri * zi;
+            v3[1] += ri * ri;
+            v3[2] += (double)b[i] * (double)b[i];
+        }
+        block_sum<3>(v3, red);
+        double rz = v3[0], rr = v3[1];
+        const double bb = v3[2];
+        int it = 0, flag = 0;
+        while (true) {
+            if (rr <= tol2 * bb || bb == 0.0) {
+                flag = TM_PCG_CONVERGED;
+                break;
+            }
+            if (it >= a.max_iter) {
+                flag = TM_PCG_MAX_ITER;
+                break;
+            }
+            // q = A p, pq
+            double v1[1] = {0.0};
+            for (int64_t i = r0 + threadIdx.x; i < r1; i += kBatchThreads) {
+                if (fixed && fixed[i]) continue;
+                double s = 0.0;
+                for (int64_t k = rp[i]; k < rp[i + 1]; ++k) s += (double)val[k] * (double)p[col[k]];
+                q[i] = (R)s;
+                v1[0] += (double)p[i] * s;
+            }
+            block_sum<1>(v1, red);
+            const double pq = v1[0];
+            if (!(pq > 0.0)) {
+                flag = TM_PCG_BREAKDOWN;
+                break;
+            }
+            const double alpha = rz / pq;
+            double v2[2] = {0.0, 0.0};
+            for (int64_t i = r0 + threadIdx.x; i < r1; i += kBatchThreads) {
+                if (fixed && fixed[i]) continue;
+                x[i] = (R)((double)x[i] + alpha * (double)p[i]);
+                const double ri = (double)r[i] - alpha * (double)q[i];
+                r[i] = (R)ri;
+                const double zi = ri * (double)dinv[i];
+                z[i] = (R)zi;
+                v2[0] += ri * zi;
+                v2[1] += ri * ri;
+            }
+            block_sum<2>(v2, red);
+            const double beta = rz != 0.0 ? v2[0] / rz : 0.0;
+            rz = v2[0];
+            rr = v2[1];
+            for (int64_t i = r0 + threadIdx.x; i < r1; i += kBatchThreads) {
+                if (fixed && fixed[i]) continue;
+                p[i] = (R)((double)z[i] + beta * (double)p[i]);
+            }
+            __syncthreads();
+            ++it;
+        }
+        if (threadIdx.x == 0 && a.status) {
+            a.status[sys].iterations = it;
+            a.status[sys].flag = flag;
+            a.status[sys].relative_residual = bb > 0.0 ? sqrt(rr / bb) : sqrt(rr);
+        }
+        __syncthreads();
+    }
+}
+
+inline int bstatus(const char* what) {
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        char buf[256];
+        snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(err));
+        return tm_set_error(TM_ERR_CUDA, buf);
+    }
+    return TM_OK;
+}
+
+}  // namespace tmk
+
+using namespace tmk;
+
+extern "C" int tm_batched_pcg(const tm_batched_pcg_args* a, tm_stream_t stream) {
+    if (!a) return tm_set_error(TM_ERR_INVALID_ARG, "tm_batched_pcg: null args");
+    if (a->n_systems < 0 || a->max_iter < 0 || a->A.block != 1 || a->A.n_rows < 0)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_batched_pcg: bad sizes (scalar CSR only)");
+    if (a->n_systems == 0) return TM_OK;
+    if (!a->system_offset || !a->A.row_ptr || !a->A.col || !a->A.values || !a->b || !a->x || !a->work ||
+        !a->queue)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_batched_pcg: null pointer");
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(a->queue, 0, sizeof(int32_t), st) != cudaSuccess) return bstatus("cudaMemsetAsync");
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int grid = 2 * (sms > 0 ? sms : 152);
+    if (grid > a->n_systems) grid = a->n_systems;
+    if (a->A.dtype == TM_F64)
+        k_batched_pcg<double><<<grid, kBatchThreads, 0, st>>>(*a);
+    else if (a->A.dtype == TM_F32)
+        k_batched_pcg<float><<<grid, kBatchThreads, 0, st>>>(*a);
+    else
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_batched_pcg: dtype must be TM_F64 or TM_F32");
+    return bstatus("k_batched_pcg");
+}

@@ -163,6 +163,7 @@ int build_chunks(tm_host_plan& p) {
         if (sh >= 0) {
             const int32_t part = p.shared_ptr[sh] + used[sh]++;
             p.slot_target[s] = -(part + 1);
+            p.slot_mirror[s] = sh;
         }
     }
     return TM_OK;

@@ -187,6 +187,11 @@ class SparseMatrix:
         return torch.stack([self.matvec(x[:, j].contiguous()) for j in range(x.shape[1])], 1)
 
     def solve(self, b: torch.Tensor, **kwargs) -> torch.Tensor:
+        """x = A^-1 b (A symmetric positive definite) by Jacobi-PCG;
+        differentiable in the values and in b."""
+        if torch.is_grad_enabled() and (self.values.requires_grad or b.requires_grad):
+            from .adjoint import SparseSolve
+            return SparseSolve.apply(self.values, b, self, kwargs)
         from .solve import pcg_solve
         return pcg_solve(self, b, **kwargs)
 
