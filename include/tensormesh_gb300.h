@@ -77,10 +77,10 @@ typedef struct tm_element_tables {
  * contributions its elements make to a target (a CSR position for matrix
  * plans, a node for node plans) in shared memory, in a fixed order, and
  * writes either the final value (the target is touched by this chunk only)
- * or a partial.  The last chunk to deliver a partial of a shared target
- * (found with one counter per shared target) sums that target's partials in
- * chunk order.  No floating-point atomics and no waiting: the result is
- * bitwise reproducible.
+ * or a partial.  Matrix plans sum the partials of each shared target in
+ * chunk order in a second kernel; node plans let the last chunk to deliver a
+ * partial of a shared node (one counter per shared node) do that sum.  No
+ * floating-point atomics and no waiting: the result is bitwise reproducible.
  */
 typedef struct tm_chunk_plan {
     int64_t n_elements;
@@ -159,9 +159,8 @@ void tm_plan_free(tm_host_plan* plan);
  * assemble/projector.py:95-123, fused in one pass).
  * Outputs: out_* [nnz] (diffusion, mass) and [nnz*D*D] (elasticity, blocks
  * in [edge, a, b] order as SparseMatrix.from_block_coo expects,
- * sparse/matrix.py:332-381).  workspace: device, >= tm_matrix_workspace_bytes():
- * the partials plus one int32 counter per shared target, which the call
- * clears (cudaMemsetAsync on the stream) before its kernel.
+ * sparse/matrix.py:332-381).  workspace: device, >= tm_matrix_workspace_bytes()
+ * (the partial sums of shared targets).
  */
 typedef struct tm_matrix_args {
     int32_t dtype;             /* TM_F64 / TM_F32: points, coefficients and outputs */

@@ -11,11 +11,11 @@
 // (element, then local entry), replacing ReduceProjector's index_add_
 // (assemble/projector.py:95-123).  Targets touched by one chunk only are
 // written directly -- for symmetric forms the value is also written to the
-// transposed CSR position.  For the others each chunk publishes a partial;
-// the last chunk to publish one (one integer counter per shared target)
-// sums the target's partials in chunk order and writes it.  Nothing waits
-// and no floating-point value is accumulated atomically: results are
-// bitwise reproducible run to run.
+// transposed CSR position.  For the others each chunk writes a partial, and
+// k_matrix_finalize sums each shared target's partials in chunk order (the
+// node-plan kernels instead let the last chunk to deliver a partial do that
+// sum, see tm_reduce.cuh).  No floating-point value is accumulated
+// atomically: results are bitwise reproducible run to run.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <cstdio>
@@ -31,19 +31,17 @@ namespace tmk {
 
 constexpr int kThreads = 256;
 
-// bytes of partial sums per partial: the scalar forms each keep one value,
-// elasticity a DxD block
-template <typename R, int ET, int FORMS>
-__host__ __device__ inline size_t partial_bytes_per(void) {
-    constexpr int D = Traits<ET>::D;
-    if (FORMS & TM_FORM_ELASTICITY) return sizeof(R) * D * D;
-    return sizeof(R) * (((FORMS & TM_FORM_DIFFUSION) ? 1 : 0) + ((FORMS & TM_FORM_MASS) ? 1 : 0));
-}
-
 // the float64 P1 diffusion / mass kernels run in double-float arithmetic
 template <typename R, int ET, int FORMS>
 __host__ __device__ constexpr bool use_df64() {
     return std::is_same<R, double>::value && Traits<ET>::P1 != 0 && (FORMS & TM_FORM_ELASTICITY) == 0;
+}
+
+// resident CTAs per SM the compiler must allow: the double-float kernel fits
+// five 256-thread CTAs in 48 registers without spilling
+template <typename R, int ET, int FORMS>
+constexpr int matrix_min_blocks() {
+    return use_df64<R, ET, FORMS>() ? 5 : 1;
 }
 
 struct MatLayout {
@@ -92,7 +90,7 @@ template <typename R>
 __device__ __forceinline__ R ld_cg(const R* p) { return __ldcg(p); }
 
 template <typename R, int ET, int FORMS>
-__global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
+__global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>())) k_matrix(const tm_matrix_args a) {
     using T = Traits<ET>;
     constexpr int D = T::D, B = T::B, NL = B * (B + 1) / 2;
     constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
@@ -372,9 +370,6 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
     R* oM = static_cast<R*>(a.out_mass);
     R* oE = static_cast<R*>(a.out_elasticity);
     R* part = static_cast<R*>(a.workspace);
-    const int64_t np = P.n_partials;
-    int32_t* counters = reinterpret_cast<int32_t*>(static_cast<unsigned char*>(a.workspace) +
-                                                   align16(partial_bytes_per<R, ET, FORMS>() * (size_t)np));
     // a target's value at its CSR position and, for symmetric forms, the
     // transpose at the mirrored position
     auto write_out = [&](int64_t tgt, int64_t mir, R ad, R am, const R* ae) {
@@ -476,47 +471,64 @@ __global__ void __launch_bounds__(kThreads) k_matrix(const tm_matrix_args a) {
         }
         const int64_t tgt = P.slot_target[s];
         if (tgt < 0) {
-            // shared target: publish this chunk's partial (summed below by
-            // the last chunk to publish one)
+            // shared target: this chunk's partial, summed in chunk order by
+            // k_matrix_finalize (partials interleaved per target)
             const int64_t pi = -tgt - 1;
             if constexpr (ELAST) {
 #pragma unroll
                 for (int k = 0; k < HH; ++k) part[pi * HH + k] = ae[k];
+            } else if constexpr (DIFF && MASS) {
+                part[2 * pi] = ad;
+                part[2 * pi + 1] = am;
             } else {
-                int f = 0;
-                if constexpr (DIFF) part[(f++) * np + pi] = ad;
-                if constexpr (MASS) part[(f++) * np + pi] = am;
+                part[pi] = DIFF ? ad : am;
             }
             continue;
         }
         write_out(tgt, P.slot_mirror[s], ad, am, ae);
     }
-    if (np > 0) {
-        // one fence per thread publishes all of its partials; then count, and
-        // the last chunk of each shared target sums its partials in chunk order
-        __threadfence();
-        for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-            const int32_t tgt = P.slot_target[s];
-            if (tgt >= 0) continue;
-            const int32_t sh = P.slot_mirror[s];
-            const int32_t q0 = P.shared_ptr[sh], q1 = P.shared_ptr[sh + 1];
-            if (atomicAdd(counters + sh, 1) != q1 - q0 - 1) continue;
-            __threadfence();
-            R ad = 0, am = 0;
-            R ae[HH];
+}
+
+// sum the partials of the targets shared by several chunks, in chunk order
+template <typename R, int ET, int FORMS>
+__global__ void __launch_bounds__(kThreads) k_matrix_finalize(const tm_matrix_args a) {
+    constexpr int D = Traits<ET>::D;
+    constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
+    constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
+    constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
+    constexpr int W = ELAST ? D * D : ((DIFF ? 1 : 0) + (MASS ? 1 : 0));
+    const tm_chunk_plan& P = a.plan;
+    const R* part = static_cast<const R*>(a.workspace);
+    R* oD = static_cast<R*>(a.out_diffusion);
+    R* oM = static_cast<R*>(a.out_mass);
+    R* oE = static_cast<R*>(a.out_elasticity);
+    for (int64_t sh = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sh < P.n_shared;
+         sh += (int64_t)gridDim.x * blockDim.x) {
+        const int q0 = P.shared_ptr[sh], q1 = P.shared_ptr[sh + 1];
+        const int64_t tgt = P.shared_target[sh], mir = P.shared_mirror[sh];
+        R acc[W];
 #pragma unroll
-            for (int k = 0; k < HH; ++k) ae[k] = 0;
-            for (int q = q0; q < q1; ++q) {
-                if constexpr (ELAST) {
+        for (int k = 0; k < W; ++k) acc[k] = 0;
+        for (int q = q0; q < q1; ++q)
 #pragma unroll
-                    for (int k = 0; k < HH; ++k) ae[k] += ld_cg(part + (int64_t)q * HH + k);
-                } else {
-                    int f = 0;
-                    if constexpr (DIFF) ad += ld_cg(part + (f++) * np + q);
-                    if constexpr (MASS) am += ld_cg(part + (f++) * np + q);
+            for (int k = 0; k < W; ++k) acc[k] += part[(int64_t)q * W + k];
+        if constexpr (ELAST) {
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    oE[tgt * W + r * D + c] = acc[r * D + c];
+                    if (mir != tgt) oE[mir * W + c * D + r] = acc[r * D + c];
                 }
+        } else {
+            if constexpr (DIFF) {
+                oD[tgt] = acc[0];
+                if (mir != tgt) oD[mir] = acc[0];
             }
-            write_out(P.shared_target[sh], P.shared_mirror[sh], ad, am, ae);
+            if constexpr (MASS) {
+                oM[tgt] = acc[W - 1];
+                if (mir != tgt) oM[mir] = acc[W - 1];
+            }
         }
     }
 }
@@ -753,12 +765,6 @@ int run_matrix(const tm_matrix_args& a, cudaStream_t st) {
     const MatLayout L = mat_layout<R, ET, FORMS>(a.plan.chunk_elems, a.tables.n_quad);
     if (L.total > 227 * 1024) return tm_set_error(TM_ERR_TOO_LARGE, "tm_assemble_matrix: chunk needs more than 227 KB of shared memory");
     if (a.plan.n_chunks == 0) return TM_OK;
-    if (a.plan.n_shared > 0) {
-        void* counters = static_cast<unsigned char*>(a.workspace) +
-                         align16(partial_bytes_per<R, ET, FORMS>() * (size_t)a.plan.n_partials);
-        if (cudaMemsetAsync(counters, 0, sizeof(int32_t) * (size_t)a.plan.n_shared, st) != cudaSuccess)
-            return launch_status("cudaMemsetAsync");
-    }
     int s = set_smem(k_matrix<R, ET, FORMS>, L.total);
     if (s) return s;
     if (a.event_begin && cudaEventRecord(static_cast<cudaEvent_t>(a.event_begin), st) != cudaSuccess)
@@ -767,6 +773,10 @@ int run_matrix(const tm_matrix_args& a, cudaStream_t st) {
     if ((s = launch_status("k_matrix"))) return s;
     if (a.event_end && cudaEventRecord(static_cast<cudaEvent_t>(a.event_end), st) != cudaSuccess)
         return launch_status("cudaEventRecord");
+    if (a.plan.n_shared > 0) {
+        k_matrix_finalize<R, ET, FORMS><<<grid_for(a.plan.n_shared), kThreads, 0, st>>>(a);
+        return launch_status("k_matrix_finalize");
+    }
     return TM_OK;
 }
 
@@ -882,8 +892,7 @@ extern "C" size_t tm_matrix_workspace_bytes(const tm_matrix_args* a) {
     } else {
         per = ((a->forms & TM_FORM_DIFFUSION) ? 1 : 0) + ((a->forms & TM_FORM_MASS) ? 1 : 0);
     }
-    // partials, then one int32 counter per shared target
-    return align16(rs * (size_t)a->plan.n_partials * per) + sizeof(int32_t) * (size_t)a->plan.n_shared;
+    return rs * (size_t)a->plan.n_partials * per;
 }
 
 extern "C" int tm_assemble_matrix(const tm_matrix_args* a, tm_stream_t stream) {

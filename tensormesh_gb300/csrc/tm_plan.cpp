@@ -15,6 +15,7 @@
 #include <cstring>
 #include <new>
 #include <numeric>
+#include <utility>
 #include <vector>
 
 struct tm_host_plan {
@@ -96,6 +97,7 @@ int build_chunks(tm_host_plan& p) {
     p.slot_ptr.push_back(0);
     std::vector<Contribution> buf;
     std::vector<int32_t> order;
+    std::vector<std::pair<int32_t, int32_t>> groups;   // (first position in order, count)
     std::vector<int32_t> chunks_per_target(n_targets, 0);
     std::vector<int32_t> mirror_of(matrix ? n_targets : 0, -1);
     for (int32_t k = 0; k < p.n_chunks; ++k) {
@@ -130,18 +132,27 @@ int build_chunks(tm_host_plan& p) {
         std::iota(order.begin(), order.end(), 0);
         std::stable_sort(order.begin(), order.end(),
                          [&](int32_t x, int32_t y) { return buf[x].target < buf[y].target; });
-        for (size_t q = 0; q < order.size(); ++q) {
-            const Contribution& cb = buf[order[q]];
-            if (q == 0 || buf[order[q - 1]].target != cb.target) {
-                if (q != 0) p.slot_ptr.push_back((int32_t)p.contrib.size());
-                p.slot_target.push_back(cb.target);
-                p.slot_mirror.push_back(cb.mirror);
-                chunks_per_target[cb.target] += 1;
-                if (matrix) mirror_of[cb.target] = cb.mirror;
-            }
-            p.contrib.push_back(cb.code);
+        // runs of one target, then emitted by decreasing contribution count so
+        // that the threads of a warp (one target each) loop equally long; a
+        // target's own contributions keep their (element, entry) order
+        groups.clear();
+        for (size_t q = 0; q < order.size(); ++q)
+            if (q == 0 || buf[order[q - 1]].target != buf[order[q]].target) groups.push_back({(int32_t)q, 0});
+        for (size_t g = 0; g < groups.size(); ++g)
+            groups[g].second = (g + 1 < groups.size() ? groups[g + 1].first : (int32_t)order.size()) - groups[g].first;
+        std::stable_sort(groups.begin(), groups.end(),
+                         [](const std::pair<int32_t, int32_t>& x, const std::pair<int32_t, int32_t>& y) {
+                             return x.second > y.second;
+                         });
+        for (const auto& g : groups) {
+            const Contribution& head = buf[order[g.first]];
+            p.slot_target.push_back(head.target);
+            p.slot_mirror.push_back(head.mirror);
+            chunks_per_target[head.target] += 1;
+            if (matrix) mirror_of[head.target] = head.mirror;
+            for (int32_t q = g.first; q < g.first + g.second; ++q) p.contrib.push_back(buf[order[q]].code);
+            p.slot_ptr.push_back((int32_t)p.contrib.size());
         }
-        if (!order.empty()) p.slot_ptr.push_back((int32_t)p.contrib.size());
         p.chunk_begin[k + 1] = (int32_t)p.slot_target.size();
     }
     // shared targets, numbered in increasing target order; their partials are

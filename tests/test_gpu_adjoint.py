@@ -5,7 +5,8 @@ of the bilinear functional -lambda^T K(kappa, x) u + lambda^T b(x).
 
 Tolerances: 1e-9 relative to the reference's autograd gradient (the solves
 are PCG to 1e-14 here, direct there); 1e-8 relative to central differences
-(eps = 1e-6, losses from exact dense solves); 1e-10 against the oracle."""
+(eps = 1e-6, losses from extended-precision dense solves); 1e-10 against
+the oracle."""
 import numpy as np
 import pytest
 import torch
@@ -62,21 +63,47 @@ def test_fused_adjoint_matches_reference_autograd(cuda):
     assert rel_fro(pts.grad, g["grad_points"]) <= 1e-9
 
 
-def _dense_loss(mesh, pts, kappa, u_t):
-    """Loss with the kernels' K and b and an exact dense solve (for FD)."""
-    asm = tg.LaplaceElementAssembler.from_mesh(tg.Mesh(pts, mesh.cells, mesh.point_data))
-    src = tg.const_node_assembler(1.0).from_mesh(tg.Mesh(pts, mesh.cells, mesh.point_data))
+def _solve_spd_extended(A, b):
+    """Gaussian elimination without pivoting (A is SPD) in numpy longdouble."""
+    A = A.copy()
+    b = b.copy()
+    n = A.shape[0]
+    for k in range(n - 1):
+        f = A[k + 1:, k] / A[k, k]
+        A[k + 1:, k:] -= f[:, None] * A[k, k:][None, :]
+        b[k + 1:] -= f * b[k]
+    x = np.zeros(n, dtype=A.dtype)
+    for k in range(n - 1, -1, -1):
+        x[k] = (b[k] - A[k, k + 1:] @ x[k + 1:]) / A[k, k]
+    return x
+
+
+def _fd_loss(mesh, pts, kappa, u_t):
+    """Loss with the kernels' float64 K and b, the condensed system solved in
+    extended precision: the finite differences then measure the model, not
+    the rounding noise of a float64 solve (which, divided by 2 eps times one
+    element's share of the loss, would be ~1e-6 relative)."""
+    m = tg.Mesh(pts, mesh.cells, mesh.point_data)
+    asm = tg.LaplaceElementAssembler.from_mesh(m)
+    src = tg.const_node_assembler(1.0).from_mesh(m)
     with torch.no_grad():
         K = asm(pts, element_data={"kappa": kappa})
         b = src(pts)
-        mask = mesh.boundary_mask
-        Kd = K.to_dense()[~mask][:, ~mask]
-        u = torch.linalg.solve(Kd, b[~mask])
-        return float(((u - u_t[~mask]) ** 2).sum())
+    free = (~mesh.boundary_mask).cpu().numpy()
+    Kd = K.to_dense().cpu().numpy()[free][:, free].astype(np.longdouble)
+    u = _solve_spd_extended(Kd, b.cpu().numpy()[free].astype(np.longdouble))
+    d = u - u_t.cpu().numpy()[free].astype(np.longdouble)
+    return (d * d).sum()
 
 
 def test_adjoint_against_central_differences(cuda):
-    mesh = tg.gen_unit_cube(6, jitter=0.15, seed=41).to(cuda)
+    """dL/dkappa and dL/dx at 32 seeded elements and 32 seeded node
+    coordinates against central differences (eps = 1e-6) of the same
+    discrete model, within 1e-8 relative (1e-11 of the largest gradient
+    entry for entries near zero)."""
+    extended = np.finfo(np.longdouble).eps < 1e-25          # IEEE quad (aarch64)
+    tol = 1e-8 if extended else 1e-6
+    mesh = tg.gen_unit_cube(5, jitter=0.15, seed=41).to(cuda)
     rng = np.random.default_rng(42)
     kappa0 = torch.from_numpy(rng.lognormal(0.0, 0.5, mesh.n_elements)).to(cuda)
     u_t = torch.from_numpy(rng.uniform(0.0, 0.05, mesh.n_points)).to(cuda)
@@ -85,29 +112,27 @@ def test_adjoint_against_central_differences(cuda):
     cond = tg.Condenser(mesh.boundary_mask)
     pts = mesh.points.clone().requires_grad_(True)
     kappa = kappa0.clone().requires_grad_(True)
-    u = tg.solve_diffusion(asm, src, cond, pts, kappa, rtol=1e-14)
+    u = tg.solve_diffusion(asm, src, cond, pts, kappa, rtol=1e-15)
     loss = ((u - u_t) ** 2)[~mesh.boundary_mask].sum()
     loss.backward()
     eps = 1e-6
-    gk = kappa.grad
-    gx = pts.grad
-    els = rng.choice(mesh.n_elements, 32, replace=False)
-    for e in els:
+    gk = kappa.grad.cpu().numpy()
+    gx = pts.grad.cpu().numpy()
+    for e in rng.choice(mesh.n_elements, 32, replace=False):
         kp, km = kappa0.clone(), kappa0.clone()
         kp[e] *= 1 + eps
         km[e] *= 1 - eps
-        fd = (_dense_loss(mesh, mesh.points, kp, u_t) - _dense_loss(mesh, mesh.points, km, u_t)) / (2 * eps * kappa0[e])
-        assert abs(fd - float(gk[e])) <= 1e-8 * float(gk.abs().max()) + 1e-6 * abs(float(gk[e])), (e, fd, float(gk[e]))
+        fd = float((_fd_loss(mesh, mesh.points, kp, u_t) - _fd_loss(mesh, mesh.points, km, u_t))
+                   / (2 * eps * float(kappa0[e])))
+        assert abs(fd - gk[e]) <= tol * abs(fd) + 1e-11 * np.abs(gk).max(), (e, fd, gk[e])
     interior = torch.nonzero(~mesh.boundary_mask).reshape(-1).cpu().numpy()
-    nodes = rng.choice(interior, 32, replace=False)
-    for n in nodes:
+    for n in rng.choice(interior, 32, replace=False):
         d = int(rng.integers(0, 3))
         pp, pm = mesh.points.clone(), mesh.points.clone()
         pp[n, d] += eps
         pm[n, d] -= eps
-        fd = (_dense_loss(mesh, pp, kappa0, u_t) - _dense_loss(mesh, pm, kappa0, u_t)) / (2 * eps)
-        assert abs(fd - float(gx[n, d])) <= 1e-8 * float(gx.abs().max()) + 1e-6 * abs(float(gx[n, d])), \
-            (n, d, fd, float(gx[n, d]))
+        fd = float((_fd_loss(mesh, pp, kappa0, u_t) - _fd_loss(mesh, pm, kappa0, u_t)) / (2 * eps))
+        assert abs(fd - gx[n, d]) <= tol * abs(fd) + 1e-11 * np.abs(gx).max(), (n, d, fd, gx[n, d])
 
 
 def test_adjoint_kernel_full_size_inverse_diffusion_48(cuda):
