@@ -78,20 +78,40 @@ def _solve_spd_extended(A, b):
     return x
 
 
+def _p1_tet_system_extended(pts, conn, kappa, n):
+    """Dense K(kappa) and load b (f = 1) of P1 tets in numpy longdouble, with
+    the same quadrature nodes and weights (order 2) as the float64 path:
+    K_e = kappa_e sum_q w_q |det A| G G^T, b_a = sum_q w_q |det A| phi_a(xi_q),
+    G the barycentric gradients (columns of A^-1, A the edge matrix)."""
+    L = np.longdouble
+    w, xi = (t.numpy().astype(L) for t in O.quadrature("tetra", 2))
+    phi = np.concatenate([1 - xi.sum(1, keepdims=True), xi], 1)          # [Q, 4]
+    X = pts.astype(L)[conn]                                              # [E, 4, 3]
+    A = X[:, 1:] - X[:, :1]                                              # rows x_i - x_0
+    c0 = np.cross(A[:, 1], A[:, 2])
+    c1 = np.cross(A[:, 2], A[:, 0])
+    c2 = np.cross(A[:, 0], A[:, 1])
+    det = (A[:, 0] * c0).sum(1)
+    g = np.stack([c0, c1, c2], 1) / det[:, None, None]                   # grad lambda_{1..3}
+    G = np.concatenate([-g.sum(1, keepdims=True), g], 1)                 # [E, 4, 3]
+    vol = np.abs(det)
+    Ke = (kappa.astype(L) * vol * w.sum())[:, None, None] * np.einsum("eai,ebi->eab", G, G)
+    K = np.zeros((n, n), dtype=L)
+    np.add.at(K, (conn[:, :, None], conn[:, None, :]), Ke)
+    b = np.zeros(n, dtype=L)
+    np.add.at(b, conn, vol[:, None] * (w[:, None] * phi).sum(0)[None, :])
+    return K, b
+
+
 def _fd_loss(mesh, pts, kappa, u_t):
-    """Loss with the kernels' float64 K and b, the condensed system solved in
-    extended precision: the finite differences then measure the model, not
-    the rounding noise of a float64 solve (which, divided by 2 eps times one
-    element's share of the loss, would be ~1e-6 relative)."""
-    m = tg.Mesh(pts, mesh.cells, mesh.point_data)
-    asm = tg.LaplaceElementAssembler.from_mesh(m)
-    src = tg.const_node_assembler(1.0).from_mesh(m)
-    with torch.no_grad():
-        K = asm(pts, element_data={"kappa": kappa})
-        b = src(pts)
+    """Loss of the same discrete model evaluated entirely in extended
+    precision (assembly and solve): with eps = 1e-6 the float64 rounding of K
+    alone (one ulp of a node's sum over ~24 elements, divided by eps times
+    one element's share) would put ~1e-8 of noise into the differences."""
     free = (~mesh.boundary_mask).cpu().numpy()
-    Kd = K.to_dense().cpu().numpy()[free][:, free].astype(np.longdouble)
-    u = _solve_spd_extended(Kd, b.cpu().numpy()[free].astype(np.longdouble))
+    K, b = _p1_tet_system_extended(pts.cpu().numpy(), mesh.elements().cpu().numpy(),
+                                   kappa.cpu().numpy(), mesh.n_points)
+    u = _solve_spd_extended(K[free][:, free], b[free])
     d = u - u_t.cpu().numpy()[free].astype(np.longdouble)
     return (d * d).sum()
 
