@@ -94,12 +94,13 @@ typedef struct tm_chunk_plan {
     const int32_t* elem_perm;      /* [E] processing position -> element id */
     const int32_t* conn;           /* [E*B] connectivity in processing order */
     const int32_t* chunk_begin;    /* [n_chunks+1] */
-    const int32_t* slot_ptr;       /* [n_chunk_slots+1] */
+    const int32_t* slot_ptr;       /* [n_chunk_slots+1]; a chunk's slots by decreasing count */
     const uint16_t* contrib;       /* [n_contrib] ((e_local*n_local + l) << 1) | transpose */
     const int32_t* slot_target;    /* [n_chunk_slots] >= 0 target; < 0: -(partial+1) */
     const int32_t* slot_mirror;    /* [n_chunk_slots] target < 0: its shared index; else the
                                       transposed CSR position (matrix plans) or -1 */
-    const int32_t* shared_ptr;     /* [n_shared+1] partial ranges, chunk order */
+    const int32_t* shared_ptr;     /* [n_shared+1] partial ranges, chunk order; shared
+                                      targets by decreasing partial count, then target */
     const int32_t* shared_target;  /* [n_shared] */
     const int32_t* shared_mirror;  /* [n_shared] */
 } tm_chunk_plan;

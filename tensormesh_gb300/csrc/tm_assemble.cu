@@ -403,9 +403,13 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
             const f2* LG2 = reinterpret_cast<const f2*>(LD);
             const f2* LS2 = reinterpret_cast<const f2*>(LS);
             const f2* LM2 = reinterpret_cast<const f2*>(LM);
+            // a CSR position receives only diagonal local entries (a, a) or
+            // only off-diagonal ones, so with mass_sym one sum of |det| per
+            // target is scaled by the template value of its class
             float kh = 0.0f, ke = 0.0f;                             // diffusion
-            float dh = 0.0f, de = 0.0f, oh = 0.0f, oe = 0.0f;       // |det| on diagonal / off-diagonal entries
+            float vh = 0.0f, ve = 0.0f;                             // mass: sum of |det|
             f2 sm2 = {0.0f, 0.0f};                                  // mass, general template
+            int l_first = 0;
             for (int p = p0; p < p1; ++p) {
                 const int idx = P.contrib[p] >> 1;
                 const int el = idx / NL;
@@ -420,26 +424,20 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
                     ke = __fadd_rn(ke, __fadd_rn(t.lo, er));
                 }
                 if constexpr (MASS) {
-                    const int l = idx - el * NL;
                     const f2 v = LM2[el];
                     if (mass_sym) {
-                        if ((diag_mask >> l) & 1u) {
-                            const f2 t = two_sum(dh, v.hi);
-                            dh = t.hi;
-                            de = __fadd_rn(de, __fadd_rn(t.lo, v.lo));
-                        } else {
-                            const f2 t = two_sum(oh, v.hi);
-                            oh = t.hi;
-                            oe = __fadd_rn(oe, __fadd_rn(t.lo, v.lo));
-                        }
+                        const f2 t = two_sum(vh, v.hi);
+                        vh = t.hi;
+                        ve = __fadd_rn(ve, __fadd_rn(t.lo, v.lo));
+                        if (p == p0) l_first = idx - el * NL;
                     } else {
-                        sm2 = f2_add(sm2, f2_mul(v, mh2[l]));
+                        sm2 = f2_add(sm2, f2_mul(v, mh2[idx - el * NL]));
                     }
                 }
             }
             if constexpr (DIFF) ad = (R)f2_to_double(two_sum(kh, ke));
             if constexpr (MASS) {
-                if (mass_sym) sm2 = f2_add(f2_mul(two_sum(dh, de), mh2[0]), f2_mul(two_sum(oh, oe), mh2[1]));
+                if (mass_sym) sm2 = f2_mul(two_sum(vh, ve), mh2[((diag_mask >> l_first) & 1u) ? 0 : 1]);
                 am = (R)f2_to_double(sm2);
             }
         } else {

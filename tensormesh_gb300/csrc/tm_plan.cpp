@@ -155,17 +155,23 @@ int build_chunks(tm_host_plan& p) {
         }
         p.chunk_begin[k + 1] = (int32_t)p.slot_target.size();
     }
-    // shared targets, numbered in increasing target order; their partials are
-    // contiguous per target and ordered by chunk
+    // shared targets, numbered by decreasing partial count and then by
+    // target (neighbouring threads of the finalizing kernel loop equally
+    // long); their partials are contiguous per target and ordered by chunk
     std::vector<int32_t> shared_index(n_targets, -1);
-    p.shared_ptr.assign(1, 0);
+    std::vector<int32_t> by_count;
     for (int64_t t = 0; t < n_targets; ++t)
-        if (chunks_per_target[t] > 1) {
-            shared_index[t] = (int32_t)p.shared_target.size();
-            p.shared_target.push_back((int32_t)t);
-            p.shared_mirror.push_back(matrix ? mirror_of[t] : -1);
-            p.shared_ptr.push_back(p.shared_ptr.back() + chunks_per_target[t]);
-        }
+        if (chunks_per_target[t] > 1) by_count.push_back((int32_t)t);
+    std::stable_sort(by_count.begin(), by_count.end(), [&](int32_t x, int32_t y) {
+        return chunks_per_target[x] > chunks_per_target[y];
+    });
+    p.shared_ptr.assign(1, 0);
+    for (const int32_t t : by_count) {
+        shared_index[t] = (int32_t)p.shared_target.size();
+        p.shared_target.push_back(t);
+        p.shared_mirror.push_back(matrix ? mirror_of[t] : -1);
+        p.shared_ptr.push_back(p.shared_ptr.back() + chunks_per_target[t]);
+    }
     p.n_partials = p.shared_ptr.back();
     std::vector<int32_t> used(p.shared_target.size(), 0);
     for (size_t s = 0; s < p.slot_target.size(); ++s) {

@@ -135,3 +135,31 @@ def test_rejects_bad_input():
         HostPlan(np.array([[0, 1, 2], [0, 2, 1]]), 3, _lib.TM_PLAN_KIND_MATRIX, 4, perm=np.array([1, 1]))
     with pytest.raises(_lib.TmError):
         HostPlan(np.zeros((10, 10), dtype=np.int64), 10, _lib.TM_PLAN_KIND_MATRIX, 1000)  # u16 overflow
+
+
+@pytest.mark.parametrize("kind", [_lib.TM_PLAN_KIND_MATRIX, _lib.TM_PLAN_KIND_NODE])
+def test_plan_orderings(kind):
+    """Slots of a chunk by decreasing contribution count, each target's
+    contributions in (element, entry) order; shared targets by decreasing
+    partial count, then target; partials of a target in chunk order."""
+    m = gen_unit_cube(4, jitter=0.2, seed=5)
+    conn = m.elements().numpy()
+    h = HostPlan(conn, m.n_points, kind, 32, morton_order(m.points.numpy(), conn))
+    a = h.arrays
+    cnt = np.diff(a["slot_ptr"])
+    for k in range(h.n_chunks):
+        c = cnt[a["chunk_begin"][k]:a["chunk_begin"][k + 1]]
+        assert (np.diff(c) <= 0).all()
+        for s in range(a["chunk_begin"][k], a["chunk_begin"][k + 1]):
+            codes = a["contrib"][a["slot_ptr"][s]:a["slot_ptr"][s + 1]] >> 1
+            assert (np.diff(codes.astype(np.int64)) > 0).all()
+    pc = np.diff(a["shared_ptr"])
+    assert (pc >= 2).all() and (np.diff(pc) <= 0).all()
+    key = -pc.astype(np.int64) * (1 << 32) + a["shared_target"]
+    assert (np.diff(key) > 0).all()
+    chunk_of_slot = np.repeat(np.arange(h.n_chunks), np.diff(a["chunk_begin"]))
+    part_chunk = np.full(h.n_partials, -1)
+    shared = a["slot_target"] < 0
+    part_chunk[-a["slot_target"][shared] - 1] = chunk_of_slot[shared]
+    for sh in range(h.n_shared):
+        assert (np.diff(part_chunk[a["shared_ptr"][sh]:a["shared_ptr"][sh + 1]]) > 0).all()
