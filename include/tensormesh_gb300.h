@@ -32,6 +32,7 @@ typedef struct CUstream_st* tm_stream_t;   /* == cudaStream_t */
 #define TM_ERR_CUDA           3   /* kernel launch or runtime error */
 #define TM_ERR_PLAN           4   /* plan construction failed (host) */
 #define TM_ERR_TOO_LARGE      5   /* size above a documented limit */
+#define TM_ERR_DEVICE_WAIT    6   /* a kernel's bounded wait on an asynchronous copy ran out */
 
 /* ---- element types (element/element_type.py:57-87) --------------------- */
 #define TM_TRI3   0   /* "triangle"  */
@@ -56,6 +57,12 @@ typedef struct CUstream_st* tm_stream_t;   /* == cudaStream_t */
 const char* tm_error_string(int status);
 const char* tm_last_error_message(void);
 int tm_version(void);
+/* Device-side fault word of the current device: kernels whose bounded wait
+ * on an asynchronous copy ran out set it and skip their remaining work
+ * instead of hanging.  Synchronises the device, returns TM_ERR_DEVICE_WAIT
+ * when the word was set (and clears it), TM_OK otherwise.  No counterpart
+ * in the reference. */
+int tm_device_fault(void);
 
 /*
  * Reference-element tables of one (element type, quadrature order): a flat
@@ -103,7 +110,15 @@ typedef struct tm_chunk_plan {
                                       targets by decreasing partial count, then target */
     const int32_t* shared_target;  /* [n_shared] */
     const int32_t* shared_mirror;  /* [n_shared] */
+    const int32_t* chunk_contrib;  /* [n_chunks+1] slot_ptr[chunk_begin[k]] */
+    int32_t max_chunk_slots;       /* largest chunk_begin[k+1] - chunk_begin[k] */
+    int32_t max_chunk_contrib;     /* largest chunk_contrib[k+1] - chunk_contrib[k] */
 } tm_chunk_plan;
+/* tm_assemble_matrix copies each chunk's part of slot_ptr, slot_target,
+ * slot_mirror and contrib into shared memory with bulk asynchronous copies
+ * (TMA): these four arrays must start on a 16-byte boundary and stay readable
+ * up to the next multiple of 16 bytes past their last element (allocate 16
+ * bytes more); the call checks the alignment. */
 
 /*
  * Host-side plan construction (replaces ElementAssembler.from_mesh,
@@ -139,9 +154,11 @@ int tm_plan_build(const int64_t* conn, int64_t n_elements, int32_t n_basis, int6
 #define TM_PLAN_SHARED_MIRROR 10  /* int32               */
 #define TM_PLAN_CONN          11  /* int32  [E*B]        */
 #define TM_PLAN_PERM          12  /* int32  [E]          */
+#define TM_PLAN_CHUNK_CONTRIB 13  /* int32  [n_chunks+1] */
 int64_t tm_plan_array_size(const tm_host_plan* plan, int32_t array_id);   /* elements */
 int tm_plan_copy_array(const tm_host_plan* plan, int32_t array_id, void* host_dst);
-/* scalars: 0 nnz, 1 n_chunks, 2 n_chunk_slots, 3 n_contrib, 4 n_shared, 5 n_partials, 6 n_local */
+/* scalars: 0 nnz, 1 n_chunks, 2 n_chunk_slots, 3 n_contrib, 4 n_shared, 5 n_partials, 6 n_local,
+ *          7 max_chunk_slots, 8 max_chunk_contrib */
 int64_t tm_plan_scalar(const tm_host_plan* plan, int32_t which);
 void tm_plan_free(tm_host_plan* plan);
 
@@ -184,6 +201,7 @@ typedef struct tm_matrix_args {
     void* event_end;           /* optional cudaEvent_t recorded after it (before finalisation) */
     int32_t* stats;            /* optional device int32 [1]: += chunks whose float64 P1 locals left the
                                   double-float range and were recomputed in FP64 arithmetic */
+    void* event_done;          /* optional cudaEvent_t recorded after the call's last launch */
 } tm_matrix_args;
 size_t tm_matrix_workspace_bytes(const tm_matrix_args* args);
 int tm_assemble_matrix(const tm_matrix_args* args, tm_stream_t stream);

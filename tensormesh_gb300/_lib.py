@@ -23,7 +23,7 @@ TM_SOURCE_NODAL, TM_SOURCE_CONST, TM_SOURCE_QUAD = 0, 1, 2
 TM_PLAN_KIND_MATRIX, TM_PLAN_KIND_NODE = 0, 1
 (PLAN_EDGE_ROW, PLAN_EDGE_COL, PLAN_SLOT, PLAN_CHUNK_BEGIN, PLAN_SLOT_PTR, PLAN_CONTRIB,
  PLAN_SLOT_TARGET, PLAN_SLOT_MIRROR, PLAN_SHARED_PTR, PLAN_SHARED_TARGET, PLAN_SHARED_MIRROR,
- PLAN_CONN, PLAN_PERM) = range(13)
+ PLAN_CONN, PLAN_PERM, PLAN_CHUNK_CONTRIB) = range(14)
 
 
 class TmError(RuntimeError):
@@ -42,7 +42,8 @@ class ChunkPlan(C.Structure):
         ("elem_perm", C.c_void_p), ("conn", C.c_void_p), ("chunk_begin", C.c_void_p),
         ("slot_ptr", C.c_void_p), ("contrib", C.c_void_p), ("slot_target", C.c_void_p),
         ("slot_mirror", C.c_void_p), ("shared_ptr", C.c_void_p), ("shared_target", C.c_void_p),
-        ("shared_mirror", C.c_void_p),
+        ("shared_mirror", C.c_void_p), ("chunk_contrib", C.c_void_p), ("max_chunk_slots", C.c_int32),
+        ("max_chunk_contrib", C.c_int32),
     ]
 
 
@@ -55,6 +56,7 @@ class MatrixArgs(C.Structure):
         ("out_elasticity", C.c_void_p), ("workspace", C.c_void_p),
         ("tables", ElementTables), ("plan", ChunkPlan),
         ("event_begin", C.c_void_p), ("event_end", C.c_void_p), ("stats", C.c_void_p),
+        ("event_done", C.c_void_p),
     ]
 
 
@@ -111,6 +113,7 @@ _SIGNATURES = {
     "tm_error_string": (C.c_char_p, [C.c_int]),
     "tm_last_error_message": (C.c_char_p, []),
     "tm_version": (C.c_int, []),
+    "tm_device_fault": (C.c_int, []),
     "tm_plan_build": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32,
                                 C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "tm_plan_array_size": (C.c_int64, [C.c_void_p, C.c_int32]),

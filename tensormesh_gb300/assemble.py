@@ -279,10 +279,11 @@ def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_da
     they can share it (diffusion and mass do), else one launch per form.
 
     Returns the value tensors ([nnz] per scalar form, [nnz, D, D] for
-    elasticity) in the order of ``assemblers``.  ``_events`` (two recorded
-    ``torch.cuda.Event``) are recorded around the element-chunk kernel of
-    the first launch, for timing; ``_stats`` (a device int32 [1]) counts the
-    chunks whose float64 P1 locals were recomputed in FP64 arithmetic."""
+    elasticity) in the order of ``assemblers``.  ``_events`` (two or three
+    ``torch.cuda.Event``) are recorded before and after the element-chunk
+    kernel of the first launch and, the third, after that launch's last
+    kernel, for timing; ``_stats`` (a device int32 [1]) counts the chunks
+    whose float64 P1 locals were recomputed in FP64 arithmetic."""
     first = assemblers[0]
     for a in assemblers[1:]:
         if a._topology is not first._topology:
@@ -354,6 +355,8 @@ def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_da
         args.workspace = _lib.ptr(ws)
         if _events is not None:
             args.event_begin, args.event_end = _events[0].cuda_event, _events[1].cuda_event
+            if len(_events) > 2:
+                args.event_done = _events[2].cuda_event
             _events = None
         if _stats is not None:
             args.stats = _lib.ptr(_stats)

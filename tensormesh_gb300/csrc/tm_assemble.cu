@@ -26,10 +26,15 @@
 #include "tm_element.cuh"
 #include "tm_reduce.cuh"
 #include "tm_status.h"
+#include "tm_tma.cuh"
 
 namespace tmk {
 
 constexpr int kThreads = 256;
+
+// set by a kernel whose bounded wait on a staged copy ran out (read and
+// cleared by tm_device_fault)
+__device__ int g_device_fault = 0;
 
 // the float64 P1 diffusion / mass kernels run in double-float arithmetic
 template <typename R, int ET, int FORMS>
@@ -45,11 +50,12 @@ constexpr int matrix_min_blocks() {
 }
 
 struct MatLayout {
-    size_t tab, mhl, x, g, jw, ld, ls, lm, le, total;
+    size_t tab, mhl, x, g, jw, ld, ls, lm, le, bar, sp, st, sm, ct, total;
 };
 
+// MS / MC: the plan's largest chunk in slots / contributions (staged copies)
 template <typename R, int ET, int FORMS>
-__host__ __device__ inline MatLayout mat_layout(int CH, int Q) {
+__host__ __device__ inline MatLayout mat_layout(int CH, int Q, int MS, int MC) {
     using T = Traits<ET>;
     constexpr int D = T::D, B = T::B, NL = B * (B + 1) / 2;
     constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
@@ -73,15 +79,30 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q) {
     }
     L.ld = o;
     if (DIFF) o = align16(o + sizeof(R) * CH * NL);
-    L.ls = o;
-    if (DIFF && DF64) o = align16(o + sizeof(R) * CH);
+    L.ls = o;   // double-float path: per element {scale, |det| rho} as four floats
+    if (DF64) o = align16(o + 16 * (size_t)CH);
     L.lm = o;
     if (MASS) o = align16(o + sizeof(R) * CH * (T::P1 ? 1 : NL));
     L.le = o;
     if (ELAST) o = align16(o + sizeof(R) * CH * NL * D * D);
+    // the chunk's plan: an mbarrier, then 16-byte windows of slot_ptr,
+    // slot_target, slot_mirror and contrib
+    L.bar = o;
+    o += 16;
+    L.sp = o;
+    o += stage_capacity((int64_t)MS + 1, 4);
+    L.st = o;
+    o += stage_capacity(MS, 4);
+    L.sm = o;
+    o += stage_capacity(MS, 4);
+    L.ct = o;
+    o += stage_capacity(MC, 2);
     L.total = o;
     return L;
 }
+
+// tries of the bounded wait for a chunk's staged plan (seconds at most)
+constexpr uint32_t kStageTries = 1u << 22;
 
 template <typename R>
 __device__ __forceinline__ R rabs(R x) { return x < R(0) ? -x : x; }
@@ -100,9 +121,33 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
     constexpr int HH = ELAST ? D * D : 1;
     const tm_chunk_plan& P = a.plan;
     const int CH = P.chunk_elems, Q = a.tables.n_quad;
-    const MatLayout L = mat_layout<R, ET, FORMS>(CH, Q);
+    const MatLayout L = mat_layout<R, ET, FORMS>(CH, Q, P.max_chunk_slots, P.max_chunk_contrib);
     const TableLayout TL = table_layout(Q, B, D);
     extern __shared__ __align__(16) unsigned char sm[];
+
+    // stage this chunk's slots and contributions (bulk copies that land
+    // while phase 1 runs)
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L.bar);
+    const int32_t s0 = P.chunk_begin[blockIdx.x], s1 = P.chunk_begin[blockIdx.x + 1];
+    const int32_t c0 = P.chunk_contrib[blockIdx.x], c1 = P.chunk_contrib[blockIdx.x + 1];
+    const StageRange w_sp = stage_range(s0, (int64_t)s1 + 1, 4), w_st = stage_range(s0, s1, 4);
+    const StageRange w_ct = stage_range(c0, c1, 2);
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        mbar_arrive_expect_tx(bar, w_sp.bytes + 2 * w_st.bytes + w_ct.bytes);
+        const unsigned char* g_sp = reinterpret_cast<const unsigned char*>(P.slot_ptr);
+        const unsigned char* g_st = reinterpret_cast<const unsigned char*>(P.slot_target);
+        const unsigned char* g_sm = reinterpret_cast<const unsigned char*>(P.slot_mirror);
+        const unsigned char* g_ct = reinterpret_cast<const unsigned char*>(P.contrib);
+        bulk_copy_g2s(sm + L.sp, g_sp + w_sp.begin, w_sp.bytes, bar);
+        bulk_copy_g2s(sm + L.st, g_st + w_st.begin, w_st.bytes, bar);
+        bulk_copy_g2s(sm + L.sm, g_sm + w_st.begin, w_st.bytes, bar);
+        if (w_ct.bytes) bulk_copy_g2s(sm + L.ct, g_ct + w_ct.begin, w_ct.bytes, bar);
+    }
+    const int32_t* SP = reinterpret_cast<const int32_t*>(sm + L.sp) + w_sp.skip;   // slot_ptr[s0 + j]
+    const int32_t* ST = reinterpret_cast<const int32_t*>(sm + L.st) + w_st.skip;   // slot_target[s0 + j]
+    const int32_t* SM = reinterpret_cast<const int32_t*>(sm + L.sm) + w_st.skip;   // slot_mirror[s0 + j]
+    const uint16_t* CT = reinterpret_cast<const uint16_t*>(sm + L.ct) + w_ct.skip;  // contrib[c0 + q]
     double* tab = reinterpret_cast<double*>(sm + L.tab);
     double* mhl = reinterpret_cast<double*>(sm + L.mhl);
     f2* mh2 = reinterpret_cast<f2*>(mhl + NL);
@@ -176,8 +221,7 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
             // G_ab = C_a . C_b (LD) and the per-element scale kappa W / |det|
             // (LS), multiplied during the reduction; for mass |det| rho (LM).
             f2* LG2 = reinterpret_cast<f2*>(LD);
-            f2* LS2 = reinterpret_cast<f2*>(LS);
-            f2* LM2 = reinterpret_cast<f2*>(LM);
+            float4* LR = reinterpret_cast<float4*>(LS);
             bool bad = !exponent_in_band(a.kappa_scale, 30) || !exponent_in_band(a.mass_scale, 30) ||
                        !exponent_in_band(tab[TL.wsum], 30);
             if (MASS && threadIdx.x == 0)
@@ -228,6 +272,7 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
                 }
                 const f2 adet = f2_abs(det);
                 bad |= !(adet.hi > 0.0f) || !f2_in_band(adet, -100, 100);
+                float4 rec = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 if constexpr (DIFF) {
                     // Gram matrix of the cofactor rows; vertex 0 has C_0 = -sum_i cof_i,
                     // so C_0.C_0 = sum_ij G_ij and C_0.C_{j+1} = -sum_i G_ij
@@ -258,7 +303,8 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
                     const f2 sc = f2_mul(f2_mul(split_double(kd), ks), f2_mul(ws, f2_recip(adet)));
                     const int sexp = (int)((__float_as_uint(sc.hi) >> 23) & 0xFF);
                     bad |= !f2_finite(sc) || (gmax - 127) + (sexp - 127) >= 100;
-                    LS2[el] = sc;
+                    rec.x = sc.hi;
+                    rec.y = sc.lo;
                     f2* g = LG2 + el * NL;
                     int l = 0;
                     g[l++] = tot;
@@ -272,8 +318,10 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
                 if constexpr (MASS) {
                     const f2 v = f2_mul(adet, ms);
                     bad |= !f2_in_band(v, -127, 100);
-                    LM2[el] = v;
+                    rec.z = v.hi;
+                    rec.w = v.lo;
                 }
+                LR[el] = rec;
             }
             use_df = !__syncthreads_or(bad);
             if (!use_df) {
@@ -351,10 +399,15 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
             }
         }
     }
-    __syncthreads();
+    // the staged plan must have landed; a wait that runs out flags the
+    // device and leaves the chunk unwritten
+    if (!__syncthreads_and(mbar_wait_bounded(bar, 0, kStageTries))) {
+        if (threadIdx.x == 0) atomicExch(&g_device_fault, 1);
+        mbar_wait_bounded(bar, 0, kStageTries);      // copies in flight end before the CTA does
+        return;
+    }
 
     // phase 2: fixed-order reduction of the chunk's targets
-    const int32_t s0 = P.chunk_begin[blockIdx.x], s1 = P.chunk_begin[blockIdx.x + 1];
     // bit l set when local entry l is a diagonal (a, a); mass_sym when the
     // mass template has one diagonal and one off-diagonal value (every
     // symmetric quadrature rule), so that the mass of a target is
@@ -391,86 +444,12 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
                 }
         }
     };
-    for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-        const int p0 = P.slot_ptr[s], p1 = P.slot_ptr[s + 1];
-        R ad = 0, am = 0;
-        R ae[HH];
-#pragma unroll
-        for (int k = 0; k < HH; ++k) ae[k] = 0;
-        if (DF64 && use_df) {
-            // compensated sums: TwoSum on the high parts, the error terms and
-            // the low parts summed in plain float (|error| ~ 2^-48 of the terms)
-            const f2* LG2 = reinterpret_cast<const f2*>(LD);
-            const f2* LS2 = reinterpret_cast<const f2*>(LS);
-            const f2* LM2 = reinterpret_cast<const f2*>(LM);
-            // a CSR position receives only diagonal local entries (a, a) or
-            // only off-diagonal ones, so with mass_sym one sum of |det| per
-            // target is scaled by the template value of its class
-            float kh = 0.0f, ke = 0.0f;                             // diffusion
-            float vh = 0.0f, ve = 0.0f;                             // mass: sum of |det|
-            f2 sm2 = {0.0f, 0.0f};                                  // mass, general template
-            int l_first = 0;
-            for (int p = p0; p < p1; ++p) {
-                const int idx = P.contrib[p] >> 1;
-                const int el = idx / NL;
-                if constexpr (DIFF) {
-                    const f2 sc = LS2[el], g = LG2[idx];
-                    const float pr = __fmul_rn(sc.hi, g.hi);
-                    float er = __fmaf_rn(sc.hi, g.hi, -pr);
-                    er = __fmaf_rn(sc.hi, g.lo, er);
-                    er = __fmaf_rn(sc.lo, g.hi, er);
-                    const f2 t = two_sum(kh, pr);
-                    kh = t.hi;
-                    ke = __fadd_rn(ke, __fadd_rn(t.lo, er));
-                }
-                if constexpr (MASS) {
-                    const f2 v = LM2[el];
-                    if (mass_sym) {
-                        const f2 t = two_sum(vh, v.hi);
-                        vh = t.hi;
-                        ve = __fadd_rn(ve, __fadd_rn(t.lo, v.lo));
-                        if (p == p0) l_first = idx - el * NL;
-                    } else {
-                        sm2 = f2_add(sm2, f2_mul(v, mh2[idx - el * NL]));
-                    }
-                }
-            }
-            if constexpr (DIFF) ad = (R)f2_to_double(two_sum(kh, ke));
-            if constexpr (MASS) {
-                if (mass_sym) sm2 = f2_mul(two_sum(vh, ve), mh2[((diag_mask >> l_first) & 1u) ? 0 : 1]);
-                am = (R)f2_to_double(sm2);
-            }
-        } else {
-            for (int p = p0; p < p1; ++p) {
-                const int code = P.contrib[p];
-                const int idx = code >> 1;
-                if constexpr (DIFF) ad += LD[idx];
-                if constexpr (MASS) {
-                    if constexpr (T::P1 != 0) {
-                        const int el = idx / NL;
-                        am += LM[el] * (R)mhl[idx - el * NL];
-                    } else {
-                        am += LM[idx];
-                    }
-                }
-                if constexpr (ELAST) {
-                    const R* blk = LE + (size_t)idx * HH;
-                    if (code & 1) {
-#pragma unroll
-                        for (int r = 0; r < D; ++r)
-#pragma unroll
-                            for (int c = 0; c < D; ++c) ae[r * D + c] += blk[c * D + r];
-                    } else {
-#pragma unroll
-                        for (int k = 0; k < HH; ++k) ae[k] += blk[k];
-                    }
-                }
-            }
-        }
-        const int64_t tgt = P.slot_target[s];
+    // a slot's result: its CSR position(s), or this chunk's partial of a
+    // shared target (summed in chunk order by k_matrix_finalize; partials
+    // interleaved per target)
+    auto emit = [&](int j, R ad, R am, const R* ae) {
+        const int64_t tgt = ST[j];
         if (tgt < 0) {
-            // shared target: this chunk's partial, summed in chunk order by
-            // k_matrix_finalize (partials interleaved per target)
             const int64_t pi = -tgt - 1;
             if constexpr (ELAST) {
 #pragma unroll
@@ -481,9 +460,111 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
             } else {
                 part[pi] = DIFF ? ad : am;
             }
-            continue;
+            return;
         }
-        write_out(tgt, P.slot_mirror[s], ad, am, ae);
+        write_out(tgt, SM[j], ad, am, ae);
+    };
+    const int ns = s1 - s0;
+
+    if constexpr (DF64) {
+        if (use_df) {
+            // compensated sums: TwoSum on the high parts, the error terms and
+            // the low parts summed in plain float (|error| ~ 2^-48 of the
+            // terms).  A CSR position receives only diagonal local entries
+            // (a, a) or only off-diagonal ones, so with mass_sym one sum of
+            // |det| per target is scaled by the template value of its class.
+            const f2* LG2 = reinterpret_cast<const f2*>(LD);
+            const float4* LR = reinterpret_cast<const float4*>(LS);
+            auto reduce = [&](auto msym_tag) {
+                [[maybe_unused]] constexpr bool MSYM = decltype(msym_tag)::value;
+                for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+                    const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
+                    [[maybe_unused]] float kh = 0.0f, ke = 0.0f;   // diffusion
+                    [[maybe_unused]] float vh = 0.0f, ve = 0.0f;   // mass: sum of |det| (mass_sym)
+                    [[maybe_unused]] f2 sm2 = {0.0f, 0.0f};        // mass, general template
+                    for (int p = p0; p < p1; ++p) {
+                        const unsigned idx = (unsigned)CT[p] >> 1;
+                        const unsigned el = idx / (unsigned)NL;
+                        float4 r;
+                        if constexpr (MASS) {
+                            r = LR[el];
+                        } else {
+                            const float2 h = reinterpret_cast<const float2*>(LR)[2 * el];
+                            r = make_float4(h.x, h.y, 0.0f, 0.0f);
+                        }
+                        if constexpr (DIFF) {
+                            const f2 g = LG2[idx];
+                            const float pr = __fmul_rn(r.x, g.hi);
+                            float er = __fmaf_rn(r.x, g.hi, -pr);
+                            er = __fmaf_rn(r.x, g.lo, er);
+                            er = __fmaf_rn(r.y, g.hi, er);
+                            const f2 t = two_sum(kh, pr);
+                            kh = t.hi;
+                            ke = __fadd_rn(ke, __fadd_rn(t.lo, er));
+                        }
+                        if constexpr (MASS) {
+                            if constexpr (MSYM) {
+                                const f2 t = two_sum(vh, r.z);
+                                vh = t.hi;
+                                ve = __fadd_rn(ve, __fadd_rn(t.lo, r.w));
+                            } else {
+                                sm2 = f2_add(sm2, f2_mul(f2_make(r.z, r.w), mh2[idx - el * (unsigned)NL]));
+                            }
+                        }
+                    }
+                    R ad = 0, am = 0;
+                    if constexpr (DIFF) ad = (R)f2_to_double(two_sum(kh, ke));
+                    if constexpr (MASS) {
+                        if constexpr (MSYM) {
+                            const unsigned idx = (unsigned)CT[p0] >> 1;
+                            const unsigned l = idx - (idx / (unsigned)NL) * (unsigned)NL;
+                            sm2 = f2_mul(two_sum(vh, ve), mh2[((diag_mask >> l) & 1u) ? 0 : 1]);
+                        }
+                        am = (R)f2_to_double(sm2);
+                    }
+                    emit(j, ad, am, nullptr);
+                }
+            };
+            if (mass_sym)
+                reduce(std::true_type{});
+            else
+                reduce(std::false_type{});
+            return;
+        }
+    }
+
+    for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+        const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
+        R ad = 0, am = 0;
+        R ae[HH];
+#pragma unroll
+        for (int k = 0; k < HH; ++k) ae[k] = 0;
+        for (int p = p0; p < p1; ++p) {
+            const int code = CT[p];
+            const int idx = code >> 1;
+            if constexpr (DIFF) ad += LD[idx];
+            if constexpr (MASS) {
+                if constexpr (T::P1 != 0) {
+                    const int el = idx / NL;
+                    am += LM[el] * (R)mhl[idx - el * NL];
+                } else {
+                    am += LM[idx];
+                }
+            }
+            if constexpr (ELAST) {
+                const R* blk = LE + (size_t)idx * HH;
+                if (code & 1) {
+#pragma unroll
+                    for (int r = 0; r < D; ++r)
+#pragma unroll
+                        for (int c = 0; c < D; ++c) ae[r * D + c] += blk[c * D + r];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < HH; ++k) ae[k] += blk[k];
+                }
+            }
+        }
+        emit(j, ad, am, ae);
     }
 }
 
@@ -760,7 +841,8 @@ inline int set_smem(K kernel, size_t bytes) {
 
 template <typename R, int ET, int FORMS>
 int run_matrix(const tm_matrix_args& a, cudaStream_t st) {
-    const MatLayout L = mat_layout<R, ET, FORMS>(a.plan.chunk_elems, a.tables.n_quad);
+    const MatLayout L = mat_layout<R, ET, FORMS>(a.plan.chunk_elems, a.tables.n_quad, a.plan.max_chunk_slots,
+                                                 a.plan.max_chunk_contrib);
     if (L.total > 227 * 1024) return tm_set_error(TM_ERR_TOO_LARGE, "tm_assemble_matrix: chunk needs more than 227 KB of shared memory");
     if (a.plan.n_chunks == 0) return TM_OK;
     int s = set_smem(k_matrix<R, ET, FORMS>, L.total);
@@ -773,8 +855,10 @@ int run_matrix(const tm_matrix_args& a, cudaStream_t st) {
         return launch_status("cudaEventRecord");
     if (a.plan.n_shared > 0) {
         k_matrix_finalize<R, ET, FORMS><<<grid_for(a.plan.n_shared), kThreads, 0, st>>>(a);
-        return launch_status("k_matrix_finalize");
+        if ((s = launch_status("k_matrix_finalize"))) return s;
     }
+    if (a.event_done && cudaEventRecord(static_cast<cudaEvent_t>(a.event_done), st) != cudaSuccess)
+        return launch_status("cudaEventRecord");
     return TM_OK;
 }
 
@@ -871,14 +955,43 @@ int check_plan(const tm_chunk_plan& P, int B, int n_local, const char* who) {
         return tm_set_error(TM_ERR_INVALID_ARG, "plan arrays must not be null");
     if (P.n_shared > 0 && (!P.shared_ptr || !P.shared_target || !P.shared_mirror))
         return tm_set_error(TM_ERR_INVALID_ARG, "plan shared arrays must not be null");
+    if (P.n_elements > 0 && !P.chunk_contrib)
+        return tm_set_error(TM_ERR_INVALID_ARG, "plan chunk_contrib must not be null");
     if (P.chunk_elems < 1 || (int64_t)P.chunk_elems * P.n_local * 2 > 65536)
         return tm_set_error(TM_ERR_INVALID_ARG, "plan chunk size out of range");
+    return TM_OK;
+}
+
+// the arrays k_matrix stages with bulk copies start on 16-byte boundaries,
+// and the plan's chunk sizes are consistent with its arrays' lengths
+int check_staged(const tm_chunk_plan& P, const char* who) {
+    char buf[256];
+    const uintptr_t mis = reinterpret_cast<uintptr_t>(P.slot_ptr) | reinterpret_cast<uintptr_t>(P.slot_target) |
+                          reinterpret_cast<uintptr_t>(P.slot_mirror) | reinterpret_cast<uintptr_t>(P.contrib);
+    if (P.n_elements > 0 && (mis & 15u)) {
+        snprintf(buf, sizeof(buf), "%s: slot_ptr, slot_target, slot_mirror and contrib must be 16-byte aligned", who);
+        return tm_set_error(TM_ERR_INVALID_ARG, buf);
+    }
+    if (P.n_elements > 0 && (P.max_chunk_slots < 1 || P.max_chunk_contrib < 1)) {
+        snprintf(buf, sizeof(buf), "%s: plan max_chunk_slots / max_chunk_contrib not set", who);
+        return tm_set_error(TM_ERR_INVALID_ARG, buf);
+    }
     return TM_OK;
 }
 
 }  // namespace tmk
 
 using namespace tmk;
+
+extern "C" int tm_device_fault(void) {
+    if (cudaDeviceSynchronize() != cudaSuccess) return launch_status("tm_device_fault");
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_device_fault, sizeof(int)) != cudaSuccess) return launch_status("tm_device_fault");
+    if (!v) return TM_OK;
+    const int zero = 0;
+    if (cudaMemcpyToSymbol(g_device_fault, &zero, sizeof(int)) != cudaSuccess) return launch_status("tm_device_fault");
+    return tm_set_error(TM_ERR_DEVICE_WAIT, "a kernel's bounded wait on a staged copy ran out");
+}
 
 extern "C" size_t tm_matrix_workspace_bytes(const tm_matrix_args* a) {
     if (!a) return 0;
@@ -910,6 +1023,7 @@ extern "C" int tm_assemble_matrix(const tm_matrix_args* a, tm_stream_t stream) {
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: output pointer is null");
     if (a->plan.n_partials > 0 && !a->workspace)
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: workspace is null");
+    if ((s = check_staged(a->plan, "tm_assemble_matrix"))) return s;
     const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (a->dtype == TM_F64) return dispatch_matrix<double>(*a, st);
     if (a->dtype == TM_F32) return dispatch_matrix<float>(*a, st);
@@ -1073,6 +1187,7 @@ extern "C" int tm_assemble_matrix_noalloc(const tm_matrix_args* a, tm_stream_t s
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: output pointer is null");
     if (a->dtype != TM_F64 && a->dtype != TM_F32)
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: dtype must be TM_F64 or TM_F32");
+    if ((s = check_staged(a->plan, "tm_assemble_matrix_noalloc"))) return s;
     const size_t need = tm_matrix_workspace_bytes(a);
     if (need > (size_t)TM_NOALLOC_SCRATCH_BYTES) {
         char buf[256];

@@ -23,7 +23,8 @@ struct tm_host_plan {
     int64_t n_elements = 0, n_points = 0, nnz = 0, n_partials = 0;
     std::vector<int32_t> edge_row, edge_col;
     std::vector<int64_t> slot;
-    std::vector<int32_t> chunk_begin, slot_ptr, slot_target, slot_mirror;
+    std::vector<int32_t> chunk_begin, chunk_contrib, slot_ptr, slot_target, slot_mirror;
+    int32_t max_chunk_slots = 0, max_chunk_contrib = 0;
     std::vector<uint16_t> contrib;
     std::vector<int32_t> shared_ptr, shared_target, shared_mirror;
     std::vector<int32_t> conn, perm;
@@ -155,6 +156,14 @@ int build_chunks(tm_host_plan& p) {
         }
         p.chunk_begin[k + 1] = (int32_t)p.slot_target.size();
     }
+    // first contribution of every chunk, and the largest chunk, for kernels
+    // that stage a chunk's slots and contributions in shared memory
+    p.chunk_contrib.resize(p.chunk_begin.size());
+    for (size_t k = 0; k < p.chunk_begin.size(); ++k) p.chunk_contrib[k] = p.slot_ptr[p.chunk_begin[k]];
+    for (size_t k = 0; k + 1 < p.chunk_begin.size(); ++k) {
+        p.max_chunk_slots = std::max(p.max_chunk_slots, p.chunk_begin[k + 1] - p.chunk_begin[k]);
+        p.max_chunk_contrib = std::max(p.max_chunk_contrib, p.chunk_contrib[k + 1] - p.chunk_contrib[k]);
+    }
     // shared targets, numbered by decreasing partial count and then by
     // target (neighbouring threads of the finalizing kernel loop equally
     // long); their partials are contiguous per target and ordered by chunk
@@ -273,6 +282,7 @@ extern "C" int64_t tm_plan_array_size(const tm_host_plan* p, int32_t id) {
         case TM_PLAN_SHARED_MIRROR: return (int64_t)p->shared_mirror.size();
         case TM_PLAN_CONN: return (int64_t)p->conn.size();
         case TM_PLAN_PERM: return (int64_t)p->perm.size();
+        case TM_PLAN_CHUNK_CONTRIB: return (int64_t)p->chunk_contrib.size();
         default: return -1;
     }
 }
@@ -300,6 +310,7 @@ extern "C" int tm_plan_copy_array(const tm_host_plan* p, int32_t id, void* dst) 
         case TM_PLAN_SHARED_MIRROR: return copy_vec(p->shared_mirror, dst);
         case TM_PLAN_CONN: return copy_vec(p->conn, dst);
         case TM_PLAN_PERM: return copy_vec(p->perm, dst);
+        case TM_PLAN_CHUNK_CONTRIB: return copy_vec(p->chunk_contrib, dst);
         default: return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_copy_array: unknown array id");
     }
 }
@@ -314,6 +325,8 @@ extern "C" int64_t tm_plan_scalar(const tm_host_plan* p, int32_t which) {
         case 4: return (int64_t)p->shared_target.size();
         case 5: return p->n_partials;
         case 6: return p->n_local;
+        case 7: return p->max_chunk_slots;
+        case 8: return p->max_chunk_contrib;
         default: return -1;
     }
 }

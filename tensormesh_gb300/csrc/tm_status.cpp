@@ -23,8 +23,9 @@ extern "C" const char* tm_error_string(int status) {
         case TM_ERR_CUDA: return "CUDA error";
         case TM_ERR_PLAN: return "plan construction failed";
         case TM_ERR_TOO_LARGE: return "size above a supported limit";
+        case TM_ERR_DEVICE_WAIT: return "a device-side wait ran out";
         default: return "unknown status";
     }
 }
 
-extern "C" int tm_version(void) { return 1; }
+extern "C" int tm_version(void) { return 2; }

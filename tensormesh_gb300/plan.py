@@ -66,6 +66,7 @@ class HostPlan:
         _lib.PLAN_SLOT_TARGET: np.int32, _lib.PLAN_SLOT_MIRROR: np.int32,
         _lib.PLAN_SHARED_PTR: np.int32, _lib.PLAN_SHARED_TARGET: np.int32,
         _lib.PLAN_SHARED_MIRROR: np.int32, _lib.PLAN_CONN: np.int32, _lib.PLAN_PERM: np.int32,
+        _lib.PLAN_CHUNK_CONTRIB: np.int32,
     }
     _NAMES = {
         _lib.PLAN_EDGE_ROW: "edge_row", _lib.PLAN_EDGE_COL: "edge_col", _lib.PLAN_SLOT: "slot",
@@ -73,7 +74,7 @@ class HostPlan:
         _lib.PLAN_CONTRIB: "contrib", _lib.PLAN_SLOT_TARGET: "slot_target",
         _lib.PLAN_SLOT_MIRROR: "slot_mirror", _lib.PLAN_SHARED_PTR: "shared_ptr",
         _lib.PLAN_SHARED_TARGET: "shared_target", _lib.PLAN_SHARED_MIRROR: "shared_mirror",
-        _lib.PLAN_CONN: "conn", _lib.PLAN_PERM: "perm",
+        _lib.PLAN_CONN: "conn", _lib.PLAN_PERM: "perm", _lib.PLAN_CHUNK_CONTRIB: "chunk_contrib",
     }
 
     def __init__(self, conn: np.ndarray, n_points: int, kind: int, chunk_elems: int,
@@ -103,6 +104,8 @@ class HostPlan:
             self.n_shared = lib.tm_plan_scalar(handle, 4)
             self.n_partials = lib.tm_plan_scalar(handle, 5)
             self.n_local = lib.tm_plan_scalar(handle, 6)
+            self.max_chunk_slots = lib.tm_plan_scalar(handle, 7)
+            self.max_chunk_contrib = lib.tm_plan_scalar(handle, 8)
         finally:
             lib.tm_plan_free(handle)
         self.kind, self.n_elements, self.n_basis, self.n_points = kind, E, B, n_points
@@ -112,16 +115,23 @@ class HostPlan:
 class DevicePlan:
     """A chunk plan on the device plus its ``tm_chunk_plan`` view."""
 
+    _ARRAYS = ("elem_perm", "conn", "chunk_begin", "slot_ptr", "contrib", "slot_target", "slot_mirror",
+               "shared_ptr", "shared_target", "shared_mirror", "chunk_contrib")
+
     def __init__(self, host: HostPlan, device: torch.device):
         a = host.arrays
         t = lambda x: torch.from_numpy(x).to(device)
+        # arrays the assembly kernel stages with bulk copies: 16 bytes of
+        # zeros past the end keep every 16-byte window readable
+        tp = lambda x: torch.from_numpy(np.concatenate([x, np.zeros(16 // x.itemsize, x.dtype)])).to(device)
         self.elem_perm = t(a["perm"])
         self.conn = t(a["conn"])
         self.chunk_begin = t(a["chunk_begin"])
-        self.slot_ptr = t(a["slot_ptr"])
-        self.contrib = t(a["contrib"].view(np.int16))   # uint16 bits
-        self.slot_target = t(a["slot_target"])
-        self.slot_mirror = t(a["slot_mirror"])
+        self.chunk_contrib = t(a["chunk_contrib"])
+        self.slot_ptr = tp(a["slot_ptr"])
+        self.contrib = tp(a["contrib"].view(np.int16))   # uint16 bits
+        self.slot_target = tp(a["slot_target"])
+        self.slot_mirror = tp(a["slot_mirror"])
         self.shared_ptr = t(a["shared_ptr"])
         self.shared_target = t(a["shared_target"])
         self.shared_mirror = t(a["shared_mirror"])
@@ -130,22 +140,24 @@ class DevicePlan:
         self.n_targets = host.nnz if host.kind == _lib.TM_PLAN_KIND_MATRIX else host.n_points
         self.n_shared, self.n_partials = host.n_shared, host.n_partials
         self.n_chunk_slots, self.n_contrib = host.n_chunk_slots, host.n_contrib
+        self.max_chunk_slots, self.max_chunk_contrib = host.max_chunk_slots, host.max_chunk_contrib
         self.device = device
 
     def struct(self) -> _lib.ChunkPlan:
+        if getattr(self, "_struct", None) is not None:
+            return self._struct
         p = _lib.ChunkPlan()
         p.n_elements, p.n_basis, p.n_local = self.n_elements, self.n_basis, self.n_local
         p.chunk_elems, p.n_chunks, p.n_targets = self.chunk_elems, self.n_chunks, self.n_targets
         p.n_shared, p.n_partials = self.n_shared, self.n_partials
-        for name in ("elem_perm", "conn", "chunk_begin", "slot_ptr", "contrib", "slot_target",
-                     "slot_mirror", "shared_ptr", "shared_target", "shared_mirror"):
+        p.max_chunk_slots, p.max_chunk_contrib = self.max_chunk_slots, self.max_chunk_contrib
+        for name in self._ARRAYS:
             setattr(p, name, _lib.ptr(getattr(self, name)))
+        self._struct = p
         return p
 
     def nbytes(self) -> int:
-        return sum(getattr(self, n).numel() * getattr(self, n).element_size()
-                   for n in ("elem_perm", "conn", "chunk_begin", "slot_ptr", "contrib", "slot_target",
-                             "slot_mirror", "shared_ptr", "shared_target", "shared_mirror"))
+        return sum(getattr(self, n).numel() * getattr(self, n).element_size() for n in self._ARRAYS)
 
 
 # chunk sizes (elements per CTA) by element type and whether the form is a
@@ -199,11 +211,14 @@ class Topology:
         return self._tables[device]
 
     def table_struct(self, device: torch.device) -> _lib.ElementTables:
-        t = _lib.ElementTables()
-        t.element_type = self.info.code
-        t.n_quad = len(element_tables(self.etype, self.quadrature_order)["w"])
-        t.packed = _lib.ptr(self.tables(device))
-        return t
+        cache = self.__dict__.setdefault("_table_structs", {})
+        if device not in cache:
+            t = _lib.ElementTables()
+            t.element_type = self.info.code
+            t.n_quad = len(element_tables(self.etype, self.quadrature_order)["w"])
+            t.packed = _lib.ptr(self.tables(device))
+            cache[device] = t
+        return cache[device]
 
     def conn32(self, device: torch.device) -> torch.Tensor:
         if device not in self._conn32:
