@@ -114,11 +114,11 @@ typedef struct tm_chunk_plan {
     int32_t max_chunk_slots;       /* largest chunk_begin[k+1] - chunk_begin[k] */
     int32_t max_chunk_contrib;     /* largest chunk_contrib[k+1] - chunk_contrib[k] */
 } tm_chunk_plan;
-/* tm_assemble_matrix copies each chunk's part of slot_ptr, slot_target,
- * slot_mirror and contrib into shared memory with bulk asynchronous copies
- * (TMA): these four arrays must start on a 16-byte boundary and stay readable
- * up to the next multiple of 16 bytes past their last element (allocate 16
- * bytes more); the call checks the alignment. */
+/* tm_assemble_matrix copies each chunk's part of slot_ptr and contrib into
+ * shared memory with bulk asynchronous copies (TMA): these two arrays must
+ * start on a 16-byte boundary and stay readable up to the next multiple of 16
+ * bytes past their last element (allocate 16 bytes more); the call checks the
+ * alignment. */
 
 /*
  * Host-side plan construction (replaces ElementAssembler.from_mesh,

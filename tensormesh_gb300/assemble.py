@@ -282,8 +282,10 @@ def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_da
     elasticity) in the order of ``assemblers``.  ``_events`` (two or three
     ``torch.cuda.Event``) are recorded before and after the element-chunk
     kernel of the first launch and, the third, after that launch's last
-    kernel, for timing; ``_stats`` (a device int32 [1]) counts the chunks
-    whose float64 P1 locals were recomputed in FP64 arithmetic."""
+    kernel, for timing (any may be None; an event between the two kernels
+    makes them run back to back instead of overlapping the second's
+    launch); ``_stats`` (a device int32 [1]) counts the chunks whose float64
+    P1 locals were recomputed in FP64 arithmetic."""
     first = assemblers[0]
     for a in assemblers[1:]:
         if a._topology is not first._topology:
@@ -354,9 +356,10 @@ def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_da
         ws = torch.empty(max(1, ws_bytes), dtype=torch.uint8, device=dev)
         args.workspace = _lib.ptr(ws)
         if _events is not None:
-            args.event_begin, args.event_end = _events[0].cuda_event, _events[1].cuda_event
+            ev = lambda e: 0 if e is None else e.cuda_event
+            args.event_begin, args.event_end = ev(_events[0]), ev(_events[1])
             if len(_events) > 2:
-                args.event_done = _events[2].cuda_event
+                args.event_done = ev(_events[2])
             _events = None
         if _stats is not None:
             args.stats = _lib.ptr(_stats)

@@ -42,15 +42,23 @@ __host__ __device__ constexpr bool use_df64() {
     return std::is_same<R, double>::value && Traits<ET>::P1 != 0 && (FORMS & TM_FORM_ELASTICITY) == 0;
 }
 
-// resident CTAs per SM the compiler must allow: the double-float kernel fits
-// five 256-thread CTAs in 48 registers without spilling
+// threads of a k_matrix CTA: one per element of a 384-tet chunk (a 4x4x4
+// octant of cubes in Morton order) for the double-float tet kernel
+template <typename R, int ET, int FORMS>
+constexpr int matrix_threads() {
+    return use_df64<R, ET, FORMS>() && ET == TM_TET4 ? 384 : kThreads;
+}
+
+// resident CTAs per SM the compiler must allow: four 384-thread CTAs of the
+// double-float tet kernel (40 registers), five 256-thread CTAs of the
+// double-float triangle kernel (48 registers)
 template <typename R, int ET, int FORMS>
 constexpr int matrix_min_blocks() {
-    return use_df64<R, ET, FORMS>() ? 5 : 1;
+    return use_df64<R, ET, FORMS>() ? (ET == TM_TET4 ? 4 : 5) : 1;
 }
 
 struct MatLayout {
-    size_t tab, mhl, x, g, jw, ld, ls, lm, le, bar, sp, st, sm, ct, total;
+    size_t tab, mhl, x, g, jw, ld, ls, lm, le, bar, sp, ct, total;
 };
 
 // MS / MC: the plan's largest chunk in slots / contributions (staged copies)
@@ -81,20 +89,19 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q, int MS, int MC) {
     if (DIFF) o = align16(o + sizeof(R) * CH * NL);
     L.ls = o;   // double-float path: per element {scale, |det| rho} as four floats
     if (DF64) o = align16(o + 16 * (size_t)CH);
-    L.lm = o;
-    if (MASS) o = align16(o + sizeof(R) * CH * (T::P1 ? 1 : NL));
+    L.lm = o;   // the double-float path's FP64 fallback keeps its masses in the records' space
+    if (DF64)
+        L.lm = L.ls;
+    else if (MASS)
+        o = align16(o + sizeof(R) * CH * (T::P1 ? 1 : NL));
     L.le = o;
     if (ELAST) o = align16(o + sizeof(R) * CH * NL * D * D);
-    // the chunk's plan: an mbarrier, then 16-byte windows of slot_ptr,
-    // slot_target, slot_mirror and contrib
+    // the chunk's plan: an mbarrier, then 16-byte windows of slot_ptr and
+    // contrib
     L.bar = o;
     o += 16;
     L.sp = o;
     o += stage_capacity((int64_t)MS + 1, 4);
-    L.st = o;
-    o += stage_capacity(MS, 4);
-    L.sm = o;
-    o += stage_capacity(MS, 4);
     L.ct = o;
     o += stage_capacity(MC, 2);
     L.total = o;
@@ -111,7 +118,8 @@ template <typename R>
 __device__ __forceinline__ R ld_cg(const R* p) { return __ldcg(p); }
 
 template <typename R, int ET, int FORMS>
-__global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>())) k_matrix(const tm_matrix_args a) {
+__global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_blocks<R, ET, FORMS>()))
+    k_matrix(const tm_matrix_args a) {
     using T = Traits<ET>;
     constexpr int D = T::D, B = T::B, NL = B * (B + 1) / 2;
     constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
@@ -125,28 +133,25 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
     const TableLayout TL = table_layout(Q, B, D);
     extern __shared__ __align__(16) unsigned char sm[];
 
+    // the finalising grid may be scheduled once every chunk has started
+    asm volatile("griddepcontrol.launch_dependents;");
+
     // stage this chunk's slots and contributions (bulk copies that land
     // while phase 1 runs)
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L.bar);
     const int32_t s0 = P.chunk_begin[blockIdx.x], s1 = P.chunk_begin[blockIdx.x + 1];
     const int32_t c0 = P.chunk_contrib[blockIdx.x], c1 = P.chunk_contrib[blockIdx.x + 1];
-    const StageRange w_sp = stage_range(s0, (int64_t)s1 + 1, 4), w_st = stage_range(s0, s1, 4);
+    const StageRange w_sp = stage_range(s0, (int64_t)s1 + 1, 4);
     const StageRange w_ct = stage_range(c0, c1, 2);
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
-        mbar_arrive_expect_tx(bar, w_sp.bytes + 2 * w_st.bytes + w_ct.bytes);
+        mbar_arrive_expect_tx(bar, w_sp.bytes + w_ct.bytes);
         const unsigned char* g_sp = reinterpret_cast<const unsigned char*>(P.slot_ptr);
-        const unsigned char* g_st = reinterpret_cast<const unsigned char*>(P.slot_target);
-        const unsigned char* g_sm = reinterpret_cast<const unsigned char*>(P.slot_mirror);
         const unsigned char* g_ct = reinterpret_cast<const unsigned char*>(P.contrib);
         bulk_copy_g2s(sm + L.sp, g_sp + w_sp.begin, w_sp.bytes, bar);
-        bulk_copy_g2s(sm + L.st, g_st + w_st.begin, w_st.bytes, bar);
-        bulk_copy_g2s(sm + L.sm, g_sm + w_st.begin, w_st.bytes, bar);
         if (w_ct.bytes) bulk_copy_g2s(sm + L.ct, g_ct + w_ct.begin, w_ct.bytes, bar);
     }
     const int32_t* SP = reinterpret_cast<const int32_t*>(sm + L.sp) + w_sp.skip;   // slot_ptr[s0 + j]
-    const int32_t* ST = reinterpret_cast<const int32_t*>(sm + L.st) + w_st.skip;   // slot_target[s0 + j]
-    const int32_t* SM = reinterpret_cast<const int32_t*>(sm + L.sm) + w_st.skip;   // slot_mirror[s0 + j]
     const uint16_t* CT = reinterpret_cast<const uint16_t*>(sm + L.ct) + w_ct.skip;  // contrib[c0 + q]
     double* tab = reinterpret_cast<double*>(sm + L.tab);
     double* mhl = reinterpret_cast<double*>(sm + L.mhl);
@@ -447,8 +452,7 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
     // a slot's result: its CSR position(s), or this chunk's partial of a
     // shared target (summed in chunk order by k_matrix_finalize; partials
     // interleaved per target)
-    auto emit = [&](int j, R ad, R am, const R* ae) {
-        const int64_t tgt = ST[j];
+    auto emit = [&](int64_t tgt, int64_t mir, R ad, R am, const R* ae) {
         if (tgt < 0) {
             const int64_t pi = -tgt - 1;
             if constexpr (ELAST) {
@@ -462,7 +466,7 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
             }
             return;
         }
-        write_out(tgt, SM[j], ad, am, ae);
+        write_out(tgt, mir, ad, am, ae);
     };
     const int ns = s1 - s0;
 
@@ -479,6 +483,7 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
                 [[maybe_unused]] constexpr bool MSYM = decltype(msym_tag)::value;
                 for (int j = threadIdx.x; j < ns; j += blockDim.x) {
                     const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
+                    const int32_t tgt = __ldcs(P.slot_target + s0 + j), mir = __ldcs(P.slot_mirror + s0 + j);
                     [[maybe_unused]] float kh = 0.0f, ke = 0.0f;   // diffusion
                     [[maybe_unused]] float vh = 0.0f, ve = 0.0f;   // mass: sum of |det| (mass_sym)
                     [[maybe_unused]] f2 sm2 = {0.0f, 0.0f};        // mass, general template
@@ -522,7 +527,7 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
                         }
                         am = (R)f2_to_double(sm2);
                     }
-                    emit(j, ad, am, nullptr);
+                    emit(tgt, mir, ad, am, nullptr);
                 }
             };
             if (mass_sym)
@@ -535,6 +540,7 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
 
     for (int j = threadIdx.x; j < ns; j += blockDim.x) {
         const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
+        const int32_t tgt = __ldcs(P.slot_target + s0 + j), mir = __ldcs(P.slot_mirror + s0 + j);
         R ad = 0, am = 0;
         R ae[HH];
 #pragma unroll
@@ -564,7 +570,7 @@ __global__ void __launch_bounds__(kThreads, (matrix_min_blocks<R, ET, FORMS>()))
                 }
             }
         }
-        emit(j, ad, am, ae);
+        emit(tgt, mir, ad, am, ae);
     }
 }
 
@@ -576,21 +582,49 @@ __global__ void __launch_bounds__(kThreads) k_matrix_finalize(const tm_matrix_ar
     constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
     constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
     constexpr int W = ELAST ? D * D : ((DIFF ? 1 : 0) + (MASS ? 1 : 0));
+    // float64 scalar partials are summed in double-float arithmetic (FP32
+    // pipes) and rounded once; a target with a partial outside the range in
+    // which the split keeps 48 bits is summed in FP64
+    constexpr bool DFSUM = std::is_same<R, double>::value && !ELAST;
     const tm_chunk_plan& P = a.plan;
     const R* part = static_cast<const R*>(a.workspace);
     R* oD = static_cast<R*>(a.out_diffusion);
     R* oM = static_cast<R*>(a.out_mass);
     R* oE = static_cast<R*>(a.out_elasticity);
+    // launched as a programmatic dependent of k_matrix: wait for its results
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     for (int64_t sh = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sh < P.n_shared;
          sh += (int64_t)gridDim.x * blockDim.x) {
         const int q0 = P.shared_ptr[sh], q1 = P.shared_ptr[sh + 1];
         const int64_t tgt = P.shared_target[sh], mir = P.shared_mirror[sh];
         R acc[W];
+        bool done = false;
+        if constexpr (DFSUM) {
+            f2 acc2[W];
+            bool ok = true;
 #pragma unroll
-        for (int k = 0; k < W; ++k) acc[k] = 0;
-        for (int q = q0; q < q1; ++q)
+            for (int k = 0; k < W; ++k) acc2[k] = f2_make(0.0f, 0.0f);
+            for (int q = q0; q < q1; ++q)
 #pragma unroll
-            for (int k = 0; k < W; ++k) acc[k] += part[(int64_t)q * W + k];
+                for (int k = 0; k < W; ++k) {
+                    const double x = __ldcg(reinterpret_cast<const double*>(part) + (int64_t)q * W + k);
+                    const int e = biased_exponent(x);
+                    ok &= x == 0.0 || (e >= 1023 - 78 && e < 1023 + 120);
+                    acc2[k] = f2_add(acc2[k], split_double(x));
+                }
+            if (ok) {
+#pragma unroll
+                for (int k = 0; k < W; ++k) acc[k] = (R)f2_to_double(acc2[k]);
+                done = true;
+            }
+        }
+        if (!done) {
+#pragma unroll
+            for (int k = 0; k < W; ++k) acc[k] = 0;
+            for (int q = q0; q < q1; ++q)
+#pragma unroll
+                for (int k = 0; k < W; ++k) acc[k] += part[(int64_t)q * W + k];
+        }
         if constexpr (ELAST) {
 #pragma unroll
             for (int r = 0; r < D; ++r)
@@ -849,12 +883,26 @@ int run_matrix(const tm_matrix_args& a, cudaStream_t st) {
     if (s) return s;
     if (a.event_begin && cudaEventRecord(static_cast<cudaEvent_t>(a.event_begin), st) != cudaSuccess)
         return launch_status("cudaEventRecord");
-    k_matrix<R, ET, FORMS><<<a.plan.n_chunks, kThreads, L.total, st>>>(a);
+    k_matrix<R, ET, FORMS><<<a.plan.n_chunks, matrix_threads<R, ET, FORMS>(), L.total, st>>>(a);
     if ((s = launch_status("k_matrix"))) return s;
     if (a.event_end && cudaEventRecord(static_cast<cudaEvent_t>(a.event_end), st) != cudaSuccess)
         return launch_status("cudaEventRecord");
     if (a.plan.n_shared > 0) {
-        k_matrix_finalize<R, ET, FORMS><<<grid_for(a.plan.n_shared), kThreads, 0, st>>>(a);
+        // programmatic dependent launch: the finalising grid is scheduled
+        // while k_matrix drains and waits (griddepcontrol.wait) for its
+        // results; not when an event separates the two launches
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid_for(a.plan.n_shared));
+        cfg.blockDim = dim3(kThreads);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = a.event_end ? 0 : 1;
+        if (cudaLaunchKernelEx(&cfg, k_matrix_finalize<R, ET, FORMS>, a) != cudaSuccess)
+            return launch_status("k_matrix_finalize");
         if ((s = launch_status("k_matrix_finalize"))) return s;
     }
     if (a.event_done && cudaEventRecord(static_cast<cudaEvent_t>(a.event_done), st) != cudaSuccess)
@@ -966,10 +1014,9 @@ int check_plan(const tm_chunk_plan& P, int B, int n_local, const char* who) {
 // and the plan's chunk sizes are consistent with its arrays' lengths
 int check_staged(const tm_chunk_plan& P, const char* who) {
     char buf[256];
-    const uintptr_t mis = reinterpret_cast<uintptr_t>(P.slot_ptr) | reinterpret_cast<uintptr_t>(P.slot_target) |
-                          reinterpret_cast<uintptr_t>(P.slot_mirror) | reinterpret_cast<uintptr_t>(P.contrib);
+    const uintptr_t mis = reinterpret_cast<uintptr_t>(P.slot_ptr) | reinterpret_cast<uintptr_t>(P.contrib);
     if (P.n_elements > 0 && (mis & 15u)) {
-        snprintf(buf, sizeof(buf), "%s: slot_ptr, slot_target, slot_mirror and contrib must be 16-byte aligned", who);
+        snprintf(buf, sizeof(buf), "%s: slot_ptr and contrib must be 16-byte aligned", who);
         return tm_set_error(TM_ERR_INVALID_ARG, buf);
     }
     if (P.n_elements > 0 && (P.max_chunk_slots < 1 || P.max_chunk_contrib < 1)) {

@@ -130,8 +130,8 @@ class DevicePlan:
         self.chunk_contrib = t(a["chunk_contrib"])
         self.slot_ptr = tp(a["slot_ptr"])
         self.contrib = tp(a["contrib"].view(np.int16))   # uint16 bits
-        self.slot_target = tp(a["slot_target"])
-        self.slot_mirror = tp(a["slot_mirror"])
+        self.slot_target = t(a["slot_target"])
+        self.slot_mirror = t(a["slot_mirror"])
         self.shared_ptr = t(a["shared_ptr"])
         self.shared_target = t(a["shared_target"])
         self.shared_mirror = t(a["shared_mirror"])
@@ -164,7 +164,7 @@ class DevicePlan:
 # DxD block form; chosen so that the locals of a chunk fit in shared memory
 CHUNK_ELEMS = {
     ("triangle", False): 256, ("triangle", True): 256,
-    ("tetra", False): 256, ("tetra", True): 128,
+    ("tetra", False): 384, ("tetra", True): 128,
     ("triangle6", False): 64, ("triangle6", True): 64,
     ("tetra10", False): 32, ("tetra10", True): 32,
 }
