@@ -161,6 +161,37 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
     R* LM = reinterpret_cast<R*>(sm + L.lm);
     R* LE = reinterpret_cast<R*>(sm + L.le);
 
+    // per-CTA constants of the double-float path, computed once by thread 0:
+    // the range check of the scales and of the mass template, and the
+    // template's class structure (bit l of diag_mask set when local entry l
+    // is a diagonal (a, a); mass_sym when the template has one diagonal and
+    // one off-diagonal value, as every symmetric quadrature rule gives, so
+    // that the mass of a target is its class value times the sum of |det| rho
+    // of its contributions)
+    __shared__ struct {
+        unsigned diag_mask;
+        int mass_sym, bad;
+    } cta;
+    if constexpr (DF64) {
+        if (threadIdx.x == 0) {
+            const double* pk = a.tables.packed;
+            int bad = !exponent_in_band(a.kappa_scale, 30) || !exponent_in_band(a.mass_scale, 30) ||
+                      !exponent_in_band(pk[TL.wsum], 30);
+            unsigned dm = 0;
+            int msym = 0;
+            if constexpr (MASS) {
+                for (int k = 0; k < B * B; ++k) bad |= !exponent_in_band(pk[TL.mhat + k], 30);
+                for (int pa = 0; pa < B; ++pa) dm |= 1u << (pa * B - pa * (pa - 1) / 2);
+                const double m_diag = pk[TL.mhat], m_off = pk[TL.mhat + 1];
+                msym = 1;
+                for (int pa = 0; pa < B; ++pa)
+                    for (int pb = pa; pb < B; ++pb) msym &= pk[TL.mhat + pa * B + pb] == (pa == pb ? m_diag : m_off);
+            }
+            cta.diag_mask = dm;
+            cta.mass_sym = msym;
+            cta.bad = bad;
+        }
+    }
     for (int k = threadIdx.x; k < TL.total; k += blockDim.x) tab[k] = a.tables.packed[k];
     __syncthreads();
     if (MASS && T::P1)
@@ -227,10 +258,7 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
             // (LS), multiplied during the reduction; for mass |det| rho (LM).
             f2* LG2 = reinterpret_cast<f2*>(LD);
             float4* LR = reinterpret_cast<float4*>(LS);
-            bool bad = !exponent_in_band(a.kappa_scale, 30) || !exponent_in_band(a.mass_scale, 30) ||
-                       !exponent_in_band(tab[TL.wsum], 30);
-            if (MASS && threadIdx.x == 0)
-                for (int k = 0; k < B * B; ++k) bad |= !exponent_in_band(tab[TL.mhat + k], 30);
+            bool bad = cta.bad != 0;
             const f2 ks = split_double(a.kappa_scale), ms = split_double(a.mass_scale);
             const f2 ws = split_double(tab[TL.wsum]);
             for (int el = threadIdx.x; el < ne; el += blockDim.x) {
@@ -413,16 +441,11 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
     }
 
     // phase 2: fixed-order reduction of the chunk's targets
-    // bit l set when local entry l is a diagonal (a, a); mass_sym when the
-    // mass template has one diagonal and one off-diagonal value (every
-    // symmetric quadrature rule), so that the mass of a target is
-    // m_diag * sum |det| + m_off * sum |det| over its contributions
-    uint64_t diag_mask = 0;
+    uint32_t diag_mask = 0;
     bool mass_sym = false;
     if constexpr (DF64 && MASS) {
-        for (int pa = 0; pa < B; ++pa) diag_mask |= 1ull << (pa * B - pa * (pa - 1) / 2);
-        mass_sym = true;
-        for (int l = 0; l < NL; ++l) mass_sym &= mhl[l] == (((diag_mask >> l) & 1u) ? mhl[0] : mhl[1]);
+        diag_mask = cta.diag_mask;
+        mass_sym = cta.mass_sym != 0;
     }
     R* oD = static_cast<R*>(a.out_diffusion);
     R* oM = static_cast<R*>(a.out_mass);
