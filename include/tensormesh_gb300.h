@@ -262,6 +262,40 @@ int tm_project_reduce(int32_t dtype, int64_t n_to, int64_t width, const int64_t*
                       const int64_t* src, const void* x, void* out, tm_stream_t stream);
 
 /*
+ * Dirichlet static condensation in one launch (Condenser.__call__ and
+ * condense_rhs, operator/condense.py:238-337): from the values of the full
+ * matrix,
+ *   out_kept[k] = values[kept_src[k]]               (the values of K_ii)
+ *   out_io[j]   = values[io_src[j]]                 (the values of K_io)
+ *   out_rhs[r, w] = rhs[inner_dof[r], w] - sum over q in [row_ptr[r], row_ptr[r+1])
+ *                   of values[row_src[q]] * outer_value[row_col[q]]
+ * (the same K_io u_o for every trailing column w, as the reference
+ * broadcasts it), each row's sum in q order.  The index arrays are the
+ * caller's cached layout; no host synchronisation.  Any part may be empty.
+ */
+typedef struct tm_condense_args {
+    int32_t dtype;
+    int32_t width;                 /* columns of rhs / out_rhs (trailing dims flattened) */
+    const void* values;            /* [nnz] scalar entries of the full matrix */
+    int64_t n_kept;
+    const int64_t* kept_src;       /* [n_kept] */
+    void* out_kept;                /* [n_kept] */
+    int64_t n_io;
+    const int64_t* io_src;         /* [n_io] */
+    void* out_io;                  /* [n_io] */
+    int64_t n_inner;
+    const int64_t* inner_dof;      /* [n_inner] full index of each inner dof */
+    const int64_t* row_ptr;        /* [n_inner+1] K_io entries of each inner row */
+    int64_t n_row_entries;         /* row_ptr[n_inner] */
+    const int64_t* row_src;        /* [n_row_entries] positions in values */
+    const int64_t* row_col;        /* [n_row_entries] outer dof (local index) */
+    const void* outer_value;       /* [n_outer] prescribed values u_o */
+    const void* rhs;               /* [n_dof, width] */
+    void* out_rhs;                 /* [n_inner, width] */
+} tm_condense_args;
+int tm_condense(const tm_condense_args* args, tm_stream_t stream);
+
+/*
  * Physical coordinates of the quadrature points, x_q = sum_b phi_b(q) X_b
  * (the "x" argument of NodeAssembler forms, node_assembler.py:302-303),
  * xq [E*Q*D], element order.  Used to evaluate func_node_assembler sources.

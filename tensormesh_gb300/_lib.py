@@ -84,6 +84,17 @@ TM_ADJ_K_NONE, TM_ADJ_K_CSR, TM_ADJ_K_OUTER = 0, 1, 2
 TM_ADJ_LOAD_NONE, TM_ADJ_LOAD_CONST, TM_ADJ_LOAD_NODAL = 0, 1, 2
 
 
+class CondenseArgs(C.Structure):
+    _fields_ = [
+        ("dtype", C.c_int32), ("width", C.c_int32), ("values", C.c_void_p),
+        ("n_kept", C.c_int64), ("kept_src", C.c_void_p), ("out_kept", C.c_void_p),
+        ("n_io", C.c_int64), ("io_src", C.c_void_p), ("out_io", C.c_void_p),
+        ("n_inner", C.c_int64), ("inner_dof", C.c_void_p), ("row_ptr", C.c_void_p),
+        ("n_row_entries", C.c_int64), ("row_src", C.c_void_p), ("row_col", C.c_void_p),
+        ("outer_value", C.c_void_p), ("rhs", C.c_void_p), ("out_rhs", C.c_void_p),
+    ]
+
+
 class LinearOperator(C.Structure):
     _fields_ = [("dtype", C.c_int32), ("block", C.c_int32), ("n_rows", C.c_int64),
                 ("row_ptr", C.c_void_p), ("col", C.c_void_p), ("values", C.c_void_p)]
@@ -128,6 +139,7 @@ _SIGNATURES = {
                                     C.c_void_p, C.c_void_p]),
     "tm_quadrature_points": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, ElementTables,
                                        C.c_void_p, C.c_void_p]),
+    "tm_condense": (C.c_int, [C.POINTER(CondenseArgs), C.c_void_p]),
     "tm_project_reduce": (C.c_int, [C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p]),
     "tm_spmv": (C.c_int, [C.POINTER(LinearOperator), C.c_void_p, C.c_void_p, C.c_double, C.c_double,

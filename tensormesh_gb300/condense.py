@@ -4,15 +4,64 @@
 ``prolong``, ``update_dirichlet``.
 
 The edge masks and local numbering are computed once per sparsity layout and
-cached; the condensed matrices reuse the cached index arrays and their CSR
-structure, so a repeated call does no host work and no host hashing.
+cached; every call after that is one ``tm_condense`` launch (the K_ii and K_io
+value gathers and rhs_i - K_io u_o together) on the cached index arrays, with
+no host synchronisation and no host hashing.  The condensed matrices reuse
+the cached index arrays and their CSR structure.
 """
+import ctypes
 from typing import Optional, Tuple
 
 import torch
 import torch.nn as nn
 
+from . import _lib
 from .sparse import SparseMatrix
+
+
+class _CondenseFn(torch.autograd.Function):
+    """tm_condense with gradients: d/d values is a copy of the output
+    gradients to their (distinct) source positions plus -u_o times the row
+    gradient at the K_io positions; d/d rhs is the output gradient at the
+    inner dofs; d/d u_o is -K_io^T times the row gradients."""
+
+    @staticmethod
+    def forward(ctx, cond, values, rhs, uo, row_src, with_mats):
+        kept, io_vals, f_inner = cond._launch(values, rhs, with_mats, with_mats, row_src, uo)
+        ctx.cond, ctx.row_src, ctx.with_mats = cond, row_src, with_mats
+        ctx.shapes = (values.shape, rhs.shape)
+        ctx.save_for_backward(values, uo)
+        return kept, io_vals, f_inner
+
+    @staticmethod
+    def backward(ctx, g_kept, g_io, g_f):
+        cond, row_src = ctx.cond, ctx.row_src
+        values, uo = ctx.saved_tensors
+        vshape, rshape = ctx.shapes
+        n_inner = cond._k_inner_dof.numel()
+        gf = g_f.reshape(n_inner, -1) if g_f is not None else None
+        gsum = gf.sum(1) if gf is not None else None
+        g_vals = g_rhs = g_uo = None
+        if ctx.needs_input_grad[1]:
+            g_vals = torch.zeros(vshape, dtype=values.dtype, device=values.device).reshape(-1)
+            if ctx.with_mats and g_kept is not None:
+                g_vals[cond._k_kept] = g_kept.reshape(-1)
+            if ctx.with_mats and g_io is not None:
+                g_vals[cond._k_io] = g_io.reshape(-1)
+            if gsum is not None and row_src.numel():
+                row_of = torch.repeat_interleave(torch.arange(n_inner, device=values.device),
+                                                 cond._k_row_ptr[1:] - cond._k_row_ptr[:-1])
+                g_vals[row_src] += -uo[cond._k_row_col] * gsum[row_of]
+            g_vals = g_vals.reshape(vshape)
+        if ctx.needs_input_grad[2] and gf is not None:
+            g_rhs = torch.zeros(rshape[0], gf.shape[1], dtype=gf.dtype, device=gf.device)
+            g_rhs[cond._k_inner_dof] = gf
+            g_rhs = g_rhs.reshape(rshape)
+        if ctx.needs_input_grad[3] and gsum is not None and row_src.numel():
+            row_of = torch.repeat_interleave(torch.arange(n_inner, device=values.device),
+                                             cond._k_row_ptr[1:] - cond._k_row_ptr[:-1])
+            g_uo = torch.zeros_like(uo).index_add_(0, cond._k_row_col, -values.reshape(-1)[row_src] * gsum[row_of])
+        return None, g_vals, g_rhs, g_uo, None, None
 
 
 class Condenser(nn.Module):
@@ -73,6 +122,11 @@ class Condenser(nn.Module):
         self.inner_idx = (blk_in[:, None] * (H * H) + k).reshape(-1)
         self.ou2in_idx = (blk_out[:, None] * (H * H) + k).reshape(-1)
         self._blocks = (H, local[br[blk_in]], local[bc[blk_in]], local[br[blk_out]], local[bc[blk_out]], ni_n, no_n)
+        # scalar entries of the K_io blocks: row (inner node, a), column (outer node, b)
+        hh = torch.arange(H, device=dev)
+        srow = (local[br[blk_out]][:, None, None] * H + hh[None, :, None]).expand(-1, H, H).reshape(-1)
+        scol = (local[bc[blk_out]][:, None, None] * H + hh[None, None, :]).expand(-1, H, H).reshape(-1)
+        self._kernel_layout(torch.nonzero(~mask).reshape(-1), srow, scol, ni_n * H)
         self.inner_row = None
         self.is_inner_dof, self.is_outer_dof = ~mask, mask
         self.inner_shape, self.ou2in_shape = (ni_n * H, ni_n * H), (ni_n * H, no_n * H)
@@ -104,6 +158,7 @@ class Condenser(nn.Module):
         self.inner_col = local[edge_v[self.inner_idx]]
         self.ou2in_row = local[edge_u[self.ou2in_idx]]
         self.ou2in_col = local[edge_v[self.ou2in_idx]]
+        self._kernel_layout(torch.nonzero(inner).reshape(-1), self.ou2in_row, self.ou2in_col, ni)
         self.is_inner_dof, self.is_outer_dof = inner, mask
         self.inner_shape, self.ou2in_shape = (ni, ni), (ni, no)
         self.n_inner_dof, self.n_outer_dof, self.n_dof = ni, no, matrix.shape[0]
@@ -111,6 +166,53 @@ class Condenser(nn.Module):
         self._sorted = bool(matrix._sorted) and matrix._block == 1
         self._K_template = None
         self._Kio_template = None
+
+    def _kernel_layout(self, inner_dof, io_row, io_col, n_inner):
+        """Index arrays of tm_condense: the K_io entries (in K_io's own order,
+        io_row / io_col their inner row and outer column) re-listed by inner
+        row, stably, as positions in the full values (row_src) and in the
+        K_io values (row_src_io)."""
+        order = torch.sort(io_row, stable=True).indices
+        counts = torch.bincount(io_row, minlength=n_inner) if io_row.numel() else \
+            torch.zeros(n_inner, dtype=torch.long, device=io_row.device)
+        self._k_inner_dof = inner_dof.long().contiguous()
+        self._k_row_ptr = torch.cat([counts.new_zeros(1), torch.cumsum(counts, 0)]).long().contiguous()
+        self._k_row_src_io = order.long().contiguous()
+        self._k_row_src = self.ou2in_idx[order].long().contiguous()
+        self._k_row_col = io_col[order].long().contiguous()
+        self._k_kept = self.inner_idx.long().contiguous()
+        self._k_io = self.ou2in_idx.long().contiguous()
+
+    def _condense(self, values, rhs, row_src, with_mats):
+        uo = self.dirichlet_value
+        if torch.is_grad_enabled() and (values.requires_grad or rhs.requires_grad or uo.requires_grad):
+            return _CondenseFn.apply(self, values, rhs, uo, row_src, with_mats)
+        return self._launch(values, rhs, with_mats, with_mats, row_src, uo)
+
+    def _launch(self, values, rhs, kept, io, row_src, uo):
+        """One tm_condense call; returns (K_ii values, K_io values, f_i)."""
+        dev, dt = values.device, values.dtype
+        _lib.require_cuda(values, "matrix values")
+        n_inner = self._k_inner_dof.numel()
+        rhs2 = rhs.reshape(rhs.shape[0], -1).contiguous()
+        W = rhs2.shape[1]
+        out_kept = torch.empty(self._k_kept.numel() if kept else 0, dtype=dt, device=dev)
+        out_io = torch.empty(self._k_io.numel() if io else 0, dtype=dt, device=dev)
+        out_rhs = torch.empty(n_inner, W, dtype=dt, device=dev)
+        uo = uo.detach().contiguous()
+        values = values.detach().contiguous()
+        rhs2 = rhs2.detach()
+        a = _lib.CondenseArgs()
+        a.dtype, a.width, a.values = _lib.dtype_code(dt), max(1, W), _lib.ptr(values)
+        a.n_kept, a.kept_src, a.out_kept = out_kept.numel(), _lib.ptr(self._k_kept), _lib.ptr(out_kept)
+        a.n_io, a.io_src, a.out_io = out_io.numel(), _lib.ptr(self._k_io), _lib.ptr(out_io)
+        a.n_inner = n_inner if W > 0 else 0
+        a.inner_dof, a.row_ptr = _lib.ptr(self._k_inner_dof), _lib.ptr(self._k_row_ptr)
+        a.n_row_entries, a.row_src = row_src.numel(), _lib.ptr(row_src)
+        a.row_col, a.outer_value = _lib.ptr(self._k_row_col), _lib.ptr(uo)
+        a.rhs, a.out_rhs = _lib.ptr(rhs2), _lib.ptr(out_rhs)
+        _lib.check(_lib.load().tm_condense(ctypes.byref(a), _lib.stream_handle(dev)), "tm_condense")
+        return out_kept, out_io, out_rhs.reshape(n_inner, *rhs.shape[1:])
 
     def update_dirichlet(self, dirichlet_value: torch.Tensor):
         self.dirichlet_value = self._normalize_value(dirichlet_value)
@@ -126,43 +228,37 @@ class Condenser(nn.Module):
             "the layout of the matrix is changed, please recompute the condensed matrix"
         assert rhs.shape[0] == self.n_dof, f"the shape of rhs must be [{self.n_dof}, ...], but got {rhs.shape}"
         vals = matrix.values
+        self.dirichlet_value = self.dirichlet_value.to(dtype=vals.dtype, device=vals.device)
+        rhs = rhs.to(dtype=vals.dtype, device=vals.device)
+        kept, io_vals, f_inner = self._condense(vals.reshape(-1), rhs, self._k_row_src, True)
         if self._K_template is None and self._blocks is not None:
             H, ir, ic, orow, ocol, ni_n, no_n = self._blocks
-            self._K_template = SparseMatrix.from_block_coo(vals[self.inner_idx].view(-1, H, H), ir, ic, (ni_n, ni_n))
+            self._K_template = SparseMatrix.from_block_coo(kept.view(-1, H, H), ir, ic, (ni_n, ni_n))
             self._K_template._sorted = self._sorted or None
-            self._Kio_template = SparseMatrix.from_block_coo(vals[self.ou2in_idx].view(-1, H, H), orow, ocol,
-                                                             (ni_n, no_n))
+            self._Kio_template = SparseMatrix.from_block_coo(io_vals.view(-1, H, H), orow, ocol, (ni_n, no_n))
             self._Kio_template._sorted = self._sorted or None
             K_inner, K_ou2in = self._K_template, self._Kio_template
         elif self._K_template is None:
-            self._K_template = SparseMatrix(vals[self.inner_idx], self.inner_row, self.inner_col, self.inner_shape,
+            self._K_template = SparseMatrix(kept, self.inner_row, self.inner_col, self.inner_shape,
                                             _sorted=self._sorted or None)
-            self._Kio_template = SparseMatrix(vals[self.ou2in_idx], self.ou2in_row, self.ou2in_col, self.ou2in_shape,
+            self._Kio_template = SparseMatrix(io_vals, self.ou2in_row, self.ou2in_col, self.ou2in_shape,
                                               _sorted=self._sorted or None)
             K_inner, K_ou2in = self._K_template, self._Kio_template
         else:
-            K_inner = self._K_template.with_values(vals[self.inner_idx])
-            K_ou2in = self._Kio_template.with_values(vals[self.ou2in_idx])
+            H = self._blocks[0] if self._blocks is not None else 1
+            K_inner = self._K_template.with_values(kept.view(-1, H, H) if H > 1 else kept)
+            K_ou2in = self._Kio_template.with_values(io_vals.view(-1, H, H) if H > 1 else io_vals)
         self.K_ou2in = K_ou2in
-        self.dirichlet_value = self.dirichlet_value.to(dtype=vals.dtype, device=vals.device)
-        rhs = rhs.to(dtype=vals.dtype, device=vals.device)
-        return K_inner, self._minus(rhs)
-
-    def _minus(self, rhs):
-        out = rhs[self.is_inner_dof]
-        if self.n_outer_dof and bool((self.dirichlet_value != 0).any()):
-            t = self.K_ou2in @ self.dirichlet_value
-            for _ in range(rhs.dim() - 1):
-                t = t.unsqueeze(-1)
-            out = out - t
-        return out
+        return K_inner, f_inner
 
     def condense_rhs(self, rhs: torch.Tensor) -> torch.Tensor:
         assert self.K_ou2in is not None, \
             "call the Condenser on a matrix first; condense_rhs reuses the cached K_io block"
-        rhs = rhs.to(dtype=self.K_ou2in.dtype, device=self.K_ou2in.device)
+        io_vals = self.K_ou2in.values
+        rhs = rhs.to(dtype=io_vals.dtype, device=io_vals.device)
         self.dirichlet_value = self.dirichlet_value.to(dtype=rhs.dtype, device=rhs.device)
-        return self._minus(rhs)
+        _, _, f_inner = self._condense(io_vals.reshape(-1), rhs, self._k_row_src_io, False)
+        return f_inner
 
     def recover(self, u: torch.Tensor) -> torch.Tensor:
         assert u.shape[0] == self.n_inner_dof, f"the shape of u must be [{self.n_inner_dof}, ...], but got {u.shape}"
