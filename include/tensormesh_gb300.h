@@ -135,6 +135,19 @@ typedef struct tm_chunk_plan {
  * position of every local pair in that pattern.
  */
 typedef struct tm_host_plan tm_host_plan;
+/*
+ * Processing order of the elements (host): increasing Morton code of the
+ * centroid of each element's first dim+1 nodes (its vertices), quantised to
+ * 31 (2-D) or 21 (3-D) bits per axis over the centroids' bounding box; ties
+ * keep element order.  points: host float64 [n_points*dim]; conn: host int64
+ * [n_elements*n_basis]; perm: host int32 [n_elements] out.  Chunks of
+ * consecutive elements in this order are compact regions of the mesh (a
+ * locality renumbering; no counterpart in the reference).
+ */
+int tm_morton_order(const double* points, int64_t n_points, int32_t dim, const int64_t* conn,
+                    int64_t n_elements, int32_t n_basis, int32_t* perm);
+/* Plan construction and tm_morton_order run on TM_HOST_THREADS host threads
+ * (default: all hardware threads); their results do not depend on it. */
 #define TM_PLAN_KIND_MATRIX 0
 #define TM_PLAN_KIND_NODE   1
 int tm_plan_build(const int64_t* conn, int64_t n_elements, int32_t n_basis, int64_t n_points,

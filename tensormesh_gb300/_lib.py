@@ -139,6 +139,7 @@ _SIGNATURES = {
                                     C.c_void_p, C.c_void_p]),
     "tm_quadrature_points": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, ElementTables,
                                        C.c_void_p, C.c_void_p]),
+    "tm_morton_order": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]),
     "tm_condense": (C.c_int, [C.POINTER(CondenseArgs), C.c_void_p]),
     "tm_project_reduce": (C.c_int, [C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -12,9 +12,13 @@
 #include "tm_status.h"
 
 #include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <numeric>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -38,52 +42,118 @@ struct Contribution {
     uint16_t code;
 };
 
+// host threads for plan construction: TM_HOST_THREADS if set, else all
+// hardware threads (at most 64)
+int host_threads() {
+    const char* env = std::getenv("TM_HOST_THREADS");
+    int n = env ? std::atoi(env) : 0;
+    if (n <= 0) n = (int)std::thread::hardware_concurrency();
+    return std::max(1, std::min(n, 64));
+}
+
+// f(begin, end) over T contiguous ranges of [0, n) on T threads (the calling
+// thread takes the first); an allocation failure on any thread is rethrown
+template <class F>
+void parallel_for(int64_t n, int T, F&& f) {
+    if (n <= 0) return;
+    T = (int)std::min<int64_t>(T, n);
+    if (T <= 1) {
+        f(int64_t(0), n);
+        return;
+    }
+    const int64_t step = (n + T - 1) / T;
+    std::atomic<bool> failed(false);
+    auto run = [&](int64_t b, int64_t e) {
+        try {
+            f(b, e);
+        } catch (...) {
+            failed = true;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; ++t) {
+        const int64_t b = t * step, e = std::min(n, b + step);
+        if (b < e) pool.emplace_back(run, b, e);
+    }
+    run(0, std::min(n, step));
+    for (auto& th : pool) th.join();
+    if (failed) throw std::bad_alloc();
+}
+
 void build_pattern(tm_host_plan& p, const int64_t* conn) {
     const int64_t E = p.n_elements, N = p.n_points;
     const int B = p.n_basis;
-    // counting sort of all E*B*B (row, col) pairs by row
+    // counting sort of all E*B*B (row, col) pairs by row: contiguous element
+    // ranges count their rows, then each range fills its rows after the
+    // earlier ranges' entries (the sequential order), on host threads
+    const int T = (int)std::max<int64_t>(1, std::min<int64_t>(host_threads(), E / 4096 + 1));
+    const int64_t estep = (E + T - 1) / T;
+    std::vector<std::vector<int32_t>> cnt(T, std::vector<int32_t>(N, 0));
+    parallel_for(T, T, [&](int64_t t0, int64_t t1) {
+        for (int64_t t = t0; t < t1; ++t)
+            for (int64_t e = t * estep; e < std::min(E, (t + 1) * estep); ++e)
+                for (int a = 0; a < B; ++a) cnt[t][conn[e * B + a]] += B;
+    });
     std::vector<int64_t> row_ptr(N + 1, 0);
-    for (int64_t e = 0; e < E; ++e)
-        for (int a = 0; a < B; ++a) row_ptr[conn[e * B + a] + 1] += B;
-    for (int64_t r = 0; r < N; ++r) row_ptr[r + 1] += row_ptr[r];
-    std::vector<int32_t> cols(row_ptr[N]);
-    std::vector<int64_t> fill(row_ptr.begin(), row_ptr.end() - 1);
-    for (int64_t e = 0; e < E; ++e)
-        for (int a = 0; a < B; ++a) {
-            const int64_t r = conn[e * B + a];
-            for (int b = 0; b < B; ++b) cols[fill[r]++] = (int32_t)conn[e * B + b];
-        }
-    // sort + unique per row
-    std::vector<int64_t> urow_ptr(N + 1, 0);
-    int64_t nnz = 0;
     for (int64_t r = 0; r < N; ++r) {
-        int32_t* s = cols.data() + row_ptr[r];
-        int32_t* t = cols.data() + row_ptr[r + 1];
-        std::sort(s, t);
-        int32_t* u = std::unique(s, t);
-        const int64_t cnt = u - s;
-        std::memmove(cols.data() + nnz, s, cnt * sizeof(int32_t));
-        nnz += cnt;
-        urow_ptr[r + 1] = nnz;
+        int64_t o = 0;
+        for (int t = 0; t < T; ++t) {
+            const int32_t c = cnt[t][r];
+            cnt[t][r] = (int32_t)o;   // offset of range t within row r
+            o += c;
+        }
+        row_ptr[r + 1] = row_ptr[r] + o;
     }
+    std::vector<int32_t> cols(row_ptr[N]);
+    parallel_for(T, T, [&](int64_t t0, int64_t t1) {
+        for (int64_t t = t0; t < t1; ++t)
+            for (int64_t e = t * estep; e < std::min(E, (t + 1) * estep); ++e)
+                for (int a = 0; a < B; ++a) {
+                    const int64_t r = conn[e * B + a];
+                    int32_t& f = cnt[t][r];
+                    for (int b = 0; b < B; ++b) cols[row_ptr[r] + f++] = (int32_t)conn[e * B + b];
+                }
+    });
+    cnt.clear();
+    cnt.shrink_to_fit();
+    // sort + unique per row, then compaction (rows on host threads)
+    const int TR = host_threads();
+    std::vector<int64_t> ucnt(N, 0);
+    parallel_for(N, TR, [&](int64_t r0, int64_t r1) {
+        for (int64_t r = r0; r < r1; ++r) {
+            int32_t* s = cols.data() + row_ptr[r];
+            int32_t* t = cols.data() + row_ptr[r + 1];
+            std::sort(s, t);
+            ucnt[r] = std::unique(s, t) - s;
+        }
+    });
+    std::vector<int64_t> urow_ptr(N + 1, 0);
+    for (int64_t r = 0; r < N; ++r) urow_ptr[r + 1] = urow_ptr[r] + ucnt[r];
+    const int64_t nnz = urow_ptr[N];
     p.nnz = nnz;
     p.edge_row.resize(nnz);
-    p.edge_col.assign(cols.begin(), cols.begin() + nnz);
-    for (int64_t r = 0; r < N; ++r)
-        for (int64_t k = urow_ptr[r]; k < urow_ptr[r + 1]; ++k) p.edge_row[k] = (int32_t)r;
+    p.edge_col.resize(nnz);
+    parallel_for(N, TR, [&](int64_t r0, int64_t r1) {
+        for (int64_t r = r0; r < r1; ++r) {
+            std::copy(cols.begin() + row_ptr[r], cols.begin() + row_ptr[r] + ucnt[r], p.edge_col.begin() + urow_ptr[r]);
+            std::fill(p.edge_row.begin() + urow_ptr[r], p.edge_row.begin() + urow_ptr[r + 1], (int32_t)r);
+        }
+    });
     // slot map, element-major, i-major, j-minor
     p.slot.resize((size_t)E * B * B);
     const int32_t* ucol = p.edge_col.data();
-    for (int64_t e = 0; e < E; ++e)
-        for (int a = 0; a < B; ++a) {
-            const int64_t r = conn[e * B + a];
-            const int32_t* s = ucol + urow_ptr[r];
-            const int32_t* t = ucol + urow_ptr[r + 1];
-            for (int b = 0; b < B; ++b) {
-                const int32_t c = (int32_t)conn[e * B + b];
-                p.slot[(e * B + a) * B + b] = (int64_t)(std::lower_bound(s, t, c) - ucol);
+    parallel_for(E, TR, [&](int64_t e0, int64_t e1) {
+        for (int64_t e = e0; e < e1; ++e)
+            for (int a = 0; a < B; ++a) {
+                const int64_t r = conn[e * B + a];
+                const int32_t* s = ucol + urow_ptr[r];
+                const int32_t* t = ucol + urow_ptr[r + 1];
+                for (int b = 0; b < B; ++b) {
+                    const int32_t c = (int32_t)conn[e * B + b];
+                    p.slot[(e * B + a) * B + b] = (int64_t)(std::lower_bound(s, t, c) - ucol);
+                }
             }
-        }
+    });
 }
 
 int build_chunks(tm_host_plan& p) {
@@ -93,68 +163,120 @@ int build_chunks(tm_host_plan& p) {
     const int64_t n_targets = matrix ? p.nnz : p.n_points;
     if ((int64_t)CH * NL * 2 > 65536) return TM_ERR_TOO_LARGE;
     p.n_chunks = (int32_t)((E + CH - 1) / CH);
-    p.chunk_begin.assign(p.n_chunks + 1, 0);
-    p.slot_ptr.clear();
-    p.slot_ptr.push_back(0);
-    std::vector<Contribution> buf;
-    std::vector<int32_t> order;
-    std::vector<std::pair<int32_t, int32_t>> groups;   // (first position in order, count)
-    std::vector<int32_t> chunks_per_target(n_targets, 0);
-    std::vector<int32_t> mirror_of(matrix ? n_targets : 0, -1);
-    for (int32_t k = 0; k < p.n_chunks; ++k) {
-        const int64_t i0 = (int64_t)k * CH, i1 = std::min<int64_t>(E, i0 + CH);
-        buf.clear();
-        for (int64_t i = i0; i < i1; ++i) {
-            const int el = (int)(i - i0);
-            const int64_t e = p.perm[i];
-            const int32_t* c = p.conn.data() + i * B;
-            if (matrix) {
-                int l = 0;
-                for (int a = 0; a < B; ++a)
-                    for (int b = a; b < B; ++b, ++l) {
-                        const int64_t pab = p.slot[(e * B + a) * B + b];
-                        const int64_t pba = p.slot[(e * B + b) * B + a];
-                        const uint16_t code = (uint16_t)((el * NL + l) << 1);
-                        if (c[a] < c[b]) {
-                            buf.push_back({(int32_t)pab, (int32_t)pba, code});
-                        } else if (c[a] > c[b]) {
-                            buf.push_back({(int32_t)pba, (int32_t)pab, (uint16_t)(code | 1)});
-                        } else {
-                            buf.push_back({(int32_t)pab, (int32_t)pab, code});
-                            if (a != b) buf.push_back({(int32_t)pab, (int32_t)pab, (uint16_t)(code | 1)});
-                        }
+    // Chunks are independent: ranges of chunks are built on host threads
+    // into per-range arrays, then concatenated in chunk order, so the plan
+    // does not depend on the number of threads.
+    struct Part {
+        std::vector<int32_t> slot_target, slot_mirror, slot_len, chunk_slots;
+        std::vector<uint16_t> contrib;
+    };
+    const int T = host_threads();
+    const int64_t per = std::max<int64_t>(1, (p.n_chunks + T - 1) / T);
+    const int n_parts = (int)((p.n_chunks + per - 1) / per);
+    std::vector<Part> parts(n_parts);
+    parallel_for(n_parts, T, [&](int64_t part_begin, int64_t part_end) {
+        std::vector<Contribution> buf;
+        std::vector<int32_t> order;
+        std::vector<std::pair<int32_t, int32_t>> groups;   // (first position in order, count)
+        for (int64_t pi = part_begin; pi < part_end; ++pi) {
+            Part& out = parts[pi];
+            const int64_t k0 = pi * per, k1 = std::min<int64_t>(p.n_chunks, k0 + per);
+            for (int64_t k = k0; k < k1; ++k) {
+                const int64_t i0 = k * CH, i1 = std::min<int64_t>(E, i0 + CH);
+                buf.clear();
+                for (int64_t i = i0; i < i1; ++i) {
+                    const int el = (int)(i - i0);
+                    const int64_t e = p.perm[i];
+                    const int32_t* c = p.conn.data() + i * B;
+                    if (matrix) {
+                        int l = 0;
+                        for (int a = 0; a < B; ++a)
+                            for (int b = a; b < B; ++b, ++l) {
+                                const int64_t pab = p.slot[(e * B + a) * B + b];
+                                const int64_t pba = p.slot[(e * B + b) * B + a];
+                                const uint16_t code = (uint16_t)((el * NL + l) << 1);
+                                if (c[a] < c[b]) {
+                                    buf.push_back({(int32_t)pab, (int32_t)pba, code});
+                                } else if (c[a] > c[b]) {
+                                    buf.push_back({(int32_t)pba, (int32_t)pab, (uint16_t)(code | 1)});
+                                } else {
+                                    buf.push_back({(int32_t)pab, (int32_t)pab, code});
+                                    if (a != b) buf.push_back({(int32_t)pab, (int32_t)pab, (uint16_t)(code | 1)});
+                                }
+                            }
+                    } else {
+                        for (int a = 0; a < B; ++a) buf.push_back({c[a], -1, (uint16_t)((el * NL + a) << 1)});
                     }
-            } else {
-                for (int a = 0; a < B; ++a)
-                    buf.push_back({c[a], -1, (uint16_t)((el * NL + a) << 1)});
+                }
+                order.resize(buf.size());
+                std::iota(order.begin(), order.end(), 0);
+                std::stable_sort(order.begin(), order.end(),
+                                 [&](int32_t x, int32_t y) { return buf[x].target < buf[y].target; });
+                // runs of one target, then emitted by decreasing contribution
+                // count so that the threads of a warp (one target each) loop
+                // equally long; a target's own contributions keep their
+                // (element, entry) order
+                groups.clear();
+                for (size_t q = 0; q < order.size(); ++q)
+                    if (q == 0 || buf[order[q - 1]].target != buf[order[q]].target) groups.push_back({(int32_t)q, 0});
+                for (size_t g = 0; g < groups.size(); ++g)
+                    groups[g].second =
+                        (g + 1 < groups.size() ? groups[g + 1].first : (int32_t)order.size()) - groups[g].first;
+                std::stable_sort(groups.begin(), groups.end(),
+                                 [](const std::pair<int32_t, int32_t>& x, const std::pair<int32_t, int32_t>& y) {
+                                     return x.second > y.second;
+                                 });
+                for (const auto& g : groups) {
+                    const Contribution& head = buf[order[g.first]];
+                    out.slot_target.push_back(head.target);
+                    out.slot_mirror.push_back(head.mirror);
+                    out.slot_len.push_back(g.second);
+                    for (int32_t q = g.first; q < g.first + g.second; ++q) out.contrib.push_back(buf[order[q]].code);
+                }
+                out.chunk_slots.push_back((int32_t)groups.size());
             }
         }
-        order.resize(buf.size());
-        std::iota(order.begin(), order.end(), 0);
-        std::stable_sort(order.begin(), order.end(),
-                         [&](int32_t x, int32_t y) { return buf[x].target < buf[y].target; });
-        // runs of one target, then emitted by decreasing contribution count so
-        // that the threads of a warp (one target each) loop equally long; a
-        // target's own contributions keep their (element, entry) order
-        groups.clear();
-        for (size_t q = 0; q < order.size(); ++q)
-            if (q == 0 || buf[order[q - 1]].target != buf[order[q]].target) groups.push_back({(int32_t)q, 0});
-        for (size_t g = 0; g < groups.size(); ++g)
-            groups[g].second = (g + 1 < groups.size() ? groups[g + 1].first : (int32_t)order.size()) - groups[g].first;
-        std::stable_sort(groups.begin(), groups.end(),
-                         [](const std::pair<int32_t, int32_t>& x, const std::pair<int32_t, int32_t>& y) {
-                             return x.second > y.second;
-                         });
-        for (const auto& g : groups) {
-            const Contribution& head = buf[order[g.first]];
-            p.slot_target.push_back(head.target);
-            p.slot_mirror.push_back(head.mirror);
-            chunks_per_target[head.target] += 1;
-            if (matrix) mirror_of[head.target] = head.mirror;
-            for (int32_t q = g.first; q < g.first + g.second; ++q) p.contrib.push_back(buf[order[q]].code);
-            p.slot_ptr.push_back((int32_t)p.contrib.size());
+    });
+    // concatenate in chunk order
+    std::vector<size_t> so(n_parts + 1, 0), co(n_parts + 1, 0);
+    for (int q = 0; q < n_parts; ++q) {
+        so[q + 1] = so[q] + parts[q].slot_target.size();
+        co[q + 1] = co[q] + parts[q].contrib.size();
+    }
+    const size_t n_slots = so[n_parts], n_contrib = co[n_parts];
+    if (n_slots > (size_t)INT32_MAX || n_contrib > (size_t)INT32_MAX) return TM_ERR_TOO_LARGE;
+    p.chunk_begin.assign(p.n_chunks + 1, 0);
+    p.slot_target.resize(n_slots);
+    p.slot_mirror.resize(n_slots);
+    p.slot_ptr.assign(n_slots + 1, 0);
+    p.contrib.resize(n_contrib);
+    parallel_for(n_parts, T, [&](int64_t q0, int64_t q1) {
+        for (int64_t q = q0; q < q1; ++q) {
+            const Part& pt = parts[q];
+            std::copy(pt.slot_target.begin(), pt.slot_target.end(), p.slot_target.begin() + so[q]);
+            std::copy(pt.slot_mirror.begin(), pt.slot_mirror.end(), p.slot_mirror.begin() + so[q]);
+            std::copy(pt.contrib.begin(), pt.contrib.end(), p.contrib.begin() + co[q]);
+            size_t c = co[q];
+            for (size_t j = 0; j < pt.slot_len.size(); ++j) {
+                c += pt.slot_len[j];
+                p.slot_ptr[so[q] + j + 1] = (int32_t)c;
+            }
         }
-        p.chunk_begin[k + 1] = (int32_t)p.slot_target.size();
+    });
+    {
+        int64_t k = 0;
+        for (const Part& pt : parts)
+            for (const int32_t ns : pt.chunk_slots) {
+                p.chunk_begin[k + 1] = p.chunk_begin[k] + ns;
+                ++k;
+            }
+    }
+    parts.clear();
+    std::vector<int32_t> chunks_per_target(n_targets, 0);
+    std::vector<int32_t> mirror_of(matrix ? n_targets : 0, -1);
+    for (size_t j = 0; j < n_slots; ++j) {
+        chunks_per_target[p.slot_target[j]] += 1;
+        if (matrix) mirror_of[p.slot_target[j]] = p.slot_mirror[j];
     }
     // first contribution of every chunk, and the largest chunk, for kernels
     // that stage a chunk's slots and contributions in shared memory
@@ -196,6 +318,94 @@ int build_chunks(tm_host_plan& p) {
 }
 
 }  // namespace
+
+namespace {
+
+uint64_t spread_bits(uint64_t x, int dims) {
+    if (dims == 2) {
+        x &= 0xFFFFFFFFull;
+        x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
+        x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
+        x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
+        x = (x | (x << 2)) & 0x3333333333333333ull;
+        x = (x | (x << 1)) & 0x5555555555555555ull;
+        return x;
+    }
+    x &= 0x1FFFFFull;
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+}  // namespace
+
+extern "C" int tm_morton_order(const double* points, int64_t n_points, int32_t dim, const int64_t* conn,
+                               int64_t n_elements, int32_t n_basis, int32_t* perm) {
+    if (n_elements < 0 || n_points < 0 || (dim != 2 && dim != 3) || n_basis < dim + 1 ||
+        (n_elements > 0 && (!points || !conn || !perm)))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_morton_order: bad arguments");
+    if (n_elements > INT32_MAX) return tm_set_error(TM_ERR_TOO_LARGE, "tm_morton_order: more than 2^31 elements");
+    if (n_elements == 0) return TM_OK;
+    const int D = dim, V = dim + 1;
+    for (int64_t k = 0; k < n_elements * n_basis; ++k)
+        if (conn[k] < 0 || conn[k] >= n_points)
+            return tm_set_error(TM_ERR_INVALID_ARG, "tm_morton_order: connectivity index out of range");
+    try {
+        const int T = host_threads();
+        // centroid of the vertices ((x0 + x1) + x2 ...) / (D + 1), and their box
+        std::vector<double> cent((size_t)n_elements * D);
+        parallel_for(n_elements, T, [&](int64_t e0, int64_t e1) {
+            for (int64_t e = e0; e < e1; ++e)
+                for (int d = 0; d < D; ++d) {
+                    double s = points[conn[e * n_basis] * D + d];
+                    for (int v = 1; v < V; ++v) s += points[conn[e * n_basis + v] * D + d];
+                    cent[e * D + d] = s / (double)V;
+                }
+        });
+        double lo[3], hi[3], span[3];
+        for (int d = 0; d < D; ++d) {
+            lo[d] = hi[d] = cent[d];
+            for (int64_t e = 1; e < n_elements; ++e) {
+                lo[d] = std::min(lo[d], cent[e * D + d]);
+                hi[d] = std::max(hi[d], cent[e * D + d]);
+            }
+            span[d] = hi[d] > lo[d] ? hi[d] - lo[d] : 1.0;
+        }
+        const int bits = D == 2 ? 31 : 21;
+        const double scale = (double)((1ll << bits) - 1);
+        std::vector<std::pair<uint64_t, int32_t>> key((size_t)n_elements);
+        parallel_for(n_elements, T, [&](int64_t e0, int64_t e1) {
+            for (int64_t e = e0; e < e1; ++e) {
+                uint64_t k = 0;
+                for (int d = 0; d < D; ++d) {
+                    const double q = std::floor((cent[e * D + d] - lo[d]) / span[d] * scale);
+                    k |= spread_bits((uint64_t)q, D) << d;
+                }
+                key[e] = {k, (int32_t)e};
+            }
+        });
+        // sort ranges on host threads, then merge; (key, index) pairs give
+        // the stable order
+        const int64_t step = (n_elements + T - 1) / T;
+        parallel_for(T, T, [&](int64_t t0, int64_t t1) {
+            for (int64_t t = t0; t < t1; ++t) {
+                const int64_t b = std::min(n_elements, t * step), e = std::min(n_elements, (t + 1) * step);
+                std::sort(key.begin() + b, key.begin() + e);
+            }
+        });
+        for (int64_t w = step; w < n_elements; w *= 2)
+            for (int64_t b = 0; b + w < n_elements; b += 2 * w)
+                std::inplace_merge(key.begin() + b, key.begin() + b + w,
+                                   key.begin() + std::min(n_elements, b + 2 * w));
+        for (int64_t e = 0; e < n_elements; ++e) perm[e] = key[e].second;
+    } catch (const std::bad_alloc&) {
+        return tm_set_error(TM_ERR_PLAN, "tm_morton_order: out of host memory");
+    }
+    return TM_OK;
+}
 
 extern "C" int tm_plan_build(const int64_t* conn, int64_t n_elements, int32_t n_basis,
                              int64_t n_points, int32_t kind, int32_t chunk_elems,

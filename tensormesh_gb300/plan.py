@@ -19,42 +19,19 @@ from . import _lib
 from .element import element_info, element_tables, packed_tables
 
 
-def _part_bits(x: np.ndarray, dims: int) -> np.ndarray:
-    """Spread the bits of x (uint64) so that consecutive bits are ``dims`` apart."""
-    x = x.astype(np.uint64)
-    if dims == 2:
-        x &= np.uint64(0xFFFFFFFF)
-        x = (x | (x << np.uint64(16))) & np.uint64(0x0000FFFF0000FFFF)
-        x = (x | (x << np.uint64(8))) & np.uint64(0x00FF00FF00FF00FF)
-        x = (x | (x << np.uint64(4))) & np.uint64(0x0F0F0F0F0F0F0F0F)
-        x = (x | (x << np.uint64(2))) & np.uint64(0x3333333333333333)
-        x = (x | (x << np.uint64(1))) & np.uint64(0x5555555555555555)
-        return x
-    x &= np.uint64(0x1FFFFF)
-    x = (x | (x << np.uint64(32))) & np.uint64(0x1F00000000FFFF)
-    x = (x | (x << np.uint64(16))) & np.uint64(0x1F0000FF0000FF)
-    x = (x | (x << np.uint64(8))) & np.uint64(0x100F00F00F00F00F)
-    x = (x | (x << np.uint64(4))) & np.uint64(0x10C30C30C30C30C3)
-    x = (x | (x << np.uint64(2))) & np.uint64(0x1249249249249249)
-    return x
-
-
 def morton_order(points: np.ndarray, conn: np.ndarray) -> np.ndarray:
     """Processing order of the elements: increasing Morton code of the
-    centroid of their vertices (ties keep the original order)."""
+    centroid of their vertices, ties in element order (``tm_morton_order``,
+    on host threads)."""
     E = conn.shape[0]
+    perm = np.zeros(E, dtype=np.int32)
     if E == 0:
-        return np.zeros(0, dtype=np.int32)
-    D = points.shape[1]
-    cent = points[conn[:, :D + 1]].mean(axis=1)
-    lo, hi = cent.min(0), cent.max(0)
-    span = np.where(hi > lo, hi - lo, 1.0)
-    bits = 31 if D == 2 else 21
-    q = np.floor((cent - lo) / span * ((1 << bits) - 1)).astype(np.uint64)
-    key = np.zeros(E, dtype=np.uint64)
-    for d in range(D):
-        key |= _part_bits(q[:, d], D) << np.uint64(d)
-    return np.argsort(key, kind="stable").astype(np.int32)
+        return perm
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    c64 = np.ascontiguousarray(conn, dtype=np.int64)
+    _lib.check(_lib.load().tm_morton_order(pts.ctypes.data, pts.shape[0], pts.shape[1], c64.ctypes.data, E,
+                                           c64.shape[1], perm.ctypes.data), "tm_morton_order")
+    return perm
 
 
 class HostPlan:

@@ -163,3 +163,63 @@ def test_plan_orderings(kind):
     part_chunk[-a["slot_target"][shared] - 1] = chunk_of_slot[shared]
     for sh in range(h.n_shared):
         assert (np.diff(part_chunk[a["shared_ptr"][sh]:a["shared_ptr"][sh + 1]]) > 0).all()
+
+
+@pytest.mark.parametrize("kind", [_lib.TM_PLAN_KIND_MATRIX, _lib.TM_PLAN_KIND_NODE])
+def test_plan_independent_of_host_threads(kind, monkeypatch):
+    """The plan is built on host threads (TM_HOST_THREADS, default all
+    cores); every array is the same whatever their number."""
+    m = gen_unit_cube(6, jitter=0.2, seed=7)
+    conn = m.elements().numpy()
+    perm = morton_order(m.points.numpy(), conn)
+    built = []
+    for threads in ("1", "3", "8"):
+        monkeypatch.setenv("TM_HOST_THREADS", threads)
+        built.append(HostPlan(conn, m.n_points, kind, 64, perm))
+    for h in built[1:]:
+        for name, arr in built[0].arrays.items():
+            assert np.array_equal(arr, h.arrays[name]), name
+
+
+def _spread(x, dims):
+    x = x.astype(np.uint64)
+    if dims == 2:
+        x &= np.uint64(0xFFFFFFFF)
+        for sh, mk in ((16, 0x0000FFFF0000FFFF), (8, 0x00FF00FF00FF00FF), (4, 0x0F0F0F0F0F0F0F0F),
+                       (2, 0x3333333333333333), (1, 0x5555555555555555)):
+            x = (x | (x << np.uint64(sh))) & np.uint64(mk)
+        return x
+    x &= np.uint64(0x1FFFFF)
+    for sh, mk in ((32, 0x1F00000000FFFF), (16, 0x1F0000FF0000FF), (8, 0x100F00F00F00F00F),
+                   (4, 0x10C30C30C30C30C3), (2, 0x1249249249249249)):
+        x = (x | (x << np.uint64(sh))) & np.uint64(mk)
+    return x
+
+
+def _morton_numpy(points, conn):
+    """The ordering restated in numpy: stable argsort of the interleaved
+    quantised centroid coordinates."""
+    D = points.shape[1]
+    cent = points[conn[:, :D + 1]].mean(axis=1)
+    lo, hi = cent.min(0), cent.max(0)
+    span = np.where(hi > lo, hi - lo, 1.0)
+    bits = 31 if D == 2 else 21
+    q = np.floor((cent - lo) / span * ((1 << bits) - 1)).astype(np.uint64)
+    key = np.zeros(conn.shape[0], dtype=np.uint64)
+    for d in range(D):
+        key |= _spread(q[:, d], D) << np.uint64(d)
+    return np.argsort(key, kind="stable").astype(np.int32)
+
+
+@pytest.mark.parametrize("make", [lambda: gen_unit_cube(7, jitter=0.25, seed=11),
+                                  lambda: gen_unit_square(40, jitter=0.25, seed=12),
+                                  lambda: gen_unit_cube(3, order=2, jitter=0.1, seed=13)])
+def test_morton_order_matches_numpy(make, monkeypatch):
+    m = make()
+    pts, conn = m.points.numpy(), m.elements().numpy()
+    ref = _morton_numpy(pts, conn)
+    for threads in ("1", "5"):
+        monkeypatch.setenv("TM_HOST_THREADS", threads)
+        assert np.array_equal(morton_order(pts, conn), ref)
+    with pytest.raises(_lib.TmError):
+        morton_order(pts, np.full_like(conn, pts.shape[0]))
