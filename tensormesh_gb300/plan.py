@@ -239,3 +239,12 @@ class Topology:
             self._layout_hash = hashlib.sha256(self.edges[0].numpy().tobytes()
                                                + self.edges[1].numpy().tobytes()).hexdigest()
         return self._layout_hash
+
+    def block_layout_hash(self, H: int) -> str:
+        """layout_hash of the (N*H, N*H) block matrix on this pattern (its
+        expanded int64 scalar rows and columns), computed once per H."""
+        cache = self.__dict__.setdefault("_block_hashes", {})
+        if H not in cache:
+            from .sparse import block_layout_hash
+            cache[H] = block_layout_hash(self.edges[0], self.edges[1], H)
+        return cache[H]

@@ -27,6 +27,22 @@ import torch
 from . import _lib
 
 
+def block_layout_hash(block_row: torch.Tensor, block_col: torch.Tensor, H: int, slice_blocks: int = 1 << 20) -> str:
+    """SHA-256 of the int64 scalar rows (block_row * H + a), then the scalar
+    columns (block_col * H + b), in [block, a, b] order -- the bytes of the
+    expanded matrix's row and column arrays -- hashed slice by slice."""
+    h = hashlib.sha256()
+    a = torch.arange(H, dtype=torch.long).repeat_interleave(H)
+    b = torch.arange(H, dtype=torch.long).repeat(H)
+    for src, off in ((block_row, a), (block_col, b)):
+        src = src.detach()
+        off = off.to(src.device)
+        for s0 in range(0, src.numel(), slice_blocks):
+            part = (src[s0:s0 + slice_blocks].long()[:, None] * H + off).reshape(-1)
+            h.update(part.cpu().numpy().tobytes())
+    return h.hexdigest()
+
+
 class SparseMatrix:
     def __init__(self, edata: torch.Tensor, row: torch.Tensor, col: torch.Tensor,
                  shape: Tuple[int, int], *, _topology=None, _block: int = 1,
@@ -91,15 +107,19 @@ class SparseMatrix:
     @property
     def layout_hash(self) -> str:
         """SHA-256 of the row bytes followed by the column bytes as passed to
-        the constructor (sparse/matrix.py:82-86)."""
+        the constructor (sparse/matrix.py:82-86); for block matrices, of the
+        expanded int64 scalar rows and columns, computed in slices without
+        materialising them and kept per block size on the mesh topology."""
         if self._hash is None:
             if self._topology is not None and self._block == 1:
                 self._hash = self._topology.layout_hash
+            elif self._block > 1 and self._topology is not None:
+                self._hash = self._topology.block_layout_hash(self._block)
+            elif self._block > 1:
+                self._hash = block_layout_hash(self._block_row, self._block_col, self._block)
             else:
-                r = self._row_src if self._block == 1 else self.row_indices
-                c = self._col_src if self._block == 1 else self.col_indices
-                self._hash = hashlib.sha256(r.detach().cpu().numpy().tobytes()
-                                            + c.detach().cpu().numpy().tobytes()).hexdigest()
+                self._hash = hashlib.sha256(self._row_src.detach().cpu().numpy().tobytes()
+                                            + self._col_src.detach().cpu().numpy().tobytes()).hexdigest()
         return self._hash
 
     def has_same_layout(self, other) -> bool:
