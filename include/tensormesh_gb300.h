@@ -384,7 +384,8 @@ int tm_spmv(const tm_linear_operator* A, const void* x, void* y, double alpha, d
  * tm_pcg_start computes diag(A)^-1, r = b - A x, z, p and the scalars;
  * tm_pcg_iterate runs n_iter iterations without host synchronisation.
  * scalars (device float64 [8]): 0 rz, 1 pAp, 2 rz_new, 3 r.r, 4 b.b,
- * 5 iterations done, 6 flag (0 running, 2 breakdown: pAp <= 0 or NaN).
+ * 5 iterations done, 6 flag (0 running, 1 converged (tm_pcg_iterate_until),
+ * 2 breakdown: pAp <= 0 or NaN).
  * A breakdown freezes x; convergence is decided by the caller from r.r/b.b.
  */
 typedef struct tm_pcg_args {
@@ -402,6 +403,16 @@ typedef struct tm_pcg_args {
 size_t tm_pcg_partials_bytes(void);
 int tm_pcg_start(const tm_pcg_args* args, tm_stream_t stream);
 int tm_pcg_iterate(const tm_pcg_args* args, int32_t n_iter, tm_stream_t stream);
+/*
+ * Up to max_iter iterations in one cooperative launch (every block resident,
+ * grid barriers between the SpMV, the x/r/z update and the p update of each
+ * iteration), stopping on the device once r.r <= rtol^2 b.b (flag 1) or on a
+ * breakdown (flag 2).  Same scalars as tm_pcg_iterate; dot products in a
+ * fixed order, so the result is bitwise reproducible for a given GPU.  A
+ * barrier wait that runs out (it cannot while all blocks are resident) ends
+ * the launch and sets the word read by tm_device_fault.
+ */
+int tm_pcg_iterate_until(const tm_pcg_args* args, int32_t max_iter, double rtol, tm_stream_t stream);
 
 /*
  * Batched Jacobi-PCG over the diagonal blocks [system_offset[s],

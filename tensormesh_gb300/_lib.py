@@ -16,7 +16,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LOCK = threading.Lock()
 _LIB = None
 
-TM_OK, TM_ERR_INVALID_ARG, TM_ERR_UNSUPPORTED, TM_ERR_CUDA, TM_ERR_PLAN, TM_ERR_TOO_LARGE = range(6)
+(TM_OK, TM_ERR_INVALID_ARG, TM_ERR_UNSUPPORTED, TM_ERR_CUDA, TM_ERR_PLAN, TM_ERR_TOO_LARGE,
+ TM_ERR_DEVICE_WAIT) = range(7)
 TM_F64, TM_F32 = 0, 1
 TM_FORM_DIFFUSION, TM_FORM_MASS, TM_FORM_ELASTICITY = 1, 2, 4
 TM_SOURCE_NODAL, TM_SOURCE_CONST, TM_SOURCE_QUAD = 0, 1, 2
@@ -151,6 +152,7 @@ _SIGNATURES = {
     "tm_pcg_partials_bytes": (C.c_size_t, []),
     "tm_pcg_start": (C.c_int, [C.POINTER(PcgArgs), C.c_void_p]),
     "tm_pcg_iterate": (C.c_int, [C.POINTER(PcgArgs), C.c_int32, C.c_void_p]),
+    "tm_pcg_iterate_until": (C.c_int, [C.POINTER(PcgArgs), C.c_int32, C.c_double, C.c_void_p]),
 }
 
 EXPORTED = tuple(_SIGNATURES)

@@ -1057,10 +1057,13 @@ extern "C" int tm_device_fault(void) {
     if (cudaDeviceSynchronize() != cudaSuccess) return launch_status("tm_device_fault");
     int v = 0;
     if (cudaMemcpyFromSymbol(&v, g_device_fault, sizeof(int)) != cudaSuccess) return launch_status("tm_device_fault");
+    const int solver = tmk_take_solve_fault();
+    if (solver < 0) return launch_status("tm_device_fault");
+    v |= solver;
     if (!v) return TM_OK;
     const int zero = 0;
     if (cudaMemcpyToSymbol(g_device_fault, &zero, sizeof(int)) != cudaSuccess) return launch_status("tm_device_fault");
-    return tm_set_error(TM_ERR_DEVICE_WAIT, "a kernel's bounded wait on a staged copy ran out");
+    return tm_set_error(TM_ERR_DEVICE_WAIT, "a kernel's bounded wait (staged copy or grid barrier) ran out");
 }
 
 extern "C" size_t tm_matrix_workspace_bytes(const tm_matrix_args* a) {

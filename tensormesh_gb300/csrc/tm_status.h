@@ -3,3 +3,6 @@
 #include "../../include/tensormesh_gb300.h"
 
 int tm_set_error(int status, const char* message);
+
+// read and clear the PCG kernels' device fault word (1 set, 0 clear, -1 error)
+int tmk_take_solve_fault();

@@ -65,8 +65,10 @@ def pcg_solve(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, rtol: float
               max_iter: Optional[int] = None, check_every: int = 25, return_info: bool = False):
     """Solve A x = b with Jacobi-preconditioned CG to ||b - A x|| <= rtol ||b||.
 
-    The iteration runs in batches of ``check_every`` iterations with all
-    scalars on the device; the host reads the residual between batches."""
+    Iterations run in one persistent cooperative kernel per batch
+    (``tm_pcg_iterate_until``: grid barriers between phases, stop on the
+    device at convergence); a batch is at most ``max(check_every, 2000)``
+    iterations, and the host reads the scalars between batches."""
     lib = _register()
     _lib.require_cuda(A.values, "SparseMatrix values")
     dev, dt = A.values.device, A.values.dtype
@@ -95,9 +97,10 @@ def pcg_solve(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, rtol: float
         rel = (rr / bb) ** 0.5 if bb > 0 else rr ** 0.5
         if rel <= rtol or flag != 0.0 or done >= max_iter or bb == 0.0:
             break
-        k = min(check_every, max_iter - done)
-        _lib.check(lib.tm_pcg_iterate(C.byref(args), k, stream), "tm_pcg_iterate")
+        k = min(max(check_every, 2000), max_iter - done)
+        _lib.check(lib.tm_pcg_iterate_until(C.byref(args), k, rtol, stream), "tm_pcg_iterate_until")
         done += k
+    _lib.check(lib.tm_device_fault(), "pcg_solve")
     info = SolveInfo(int(host[5]), rel, rel <= rtol, flag == 2.0 and rel > rtol)
     if return_info:
         return x, info

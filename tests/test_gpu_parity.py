@@ -215,3 +215,60 @@ def test_staged_plan_multichunk(etype, make, cuda):
                                  lambda p, c, kappa: O.element_locals_diffusion(p, c, etype, kappa, 2), kappa=kap)
     assert rel_fro(K.values, Ko) <= TOL
     assert _lib.load().tm_device_fault() == _lib.TM_OK
+
+
+@pytest.mark.parametrize("block", [False, True])
+def test_persistent_pcg_matches_launch_loop(block, cuda):
+    """tm_pcg_iterate_until (one cooperative launch, stop on the device)
+    reaches the same solution as tm_pcg_iterate (six launches per
+    iteration), sets the converged flag, and repeats bit for bit."""
+    import ctypes
+    from tensormesh_gb300 import _lib, solve as S
+    if block:
+        mesh = tg.gen_unit_cube(4, order=2, jitter=0.1, seed=91).to(cuda)
+        E = torch.from_numpy(np.random.default_rng(92).uniform(0.5, 2.0, mesh.n_elements)).to(cuda)
+        K = tg.LinearElasticityElementAssembler.from_mesh(mesh, nu=0.3)(mesh.points, element_data={"E": E})
+        mask = (mesh.points[:, 2] == 0.0).repeat_interleave(3)
+    else:
+        mesh = tg.gen_unit_cube(10, jitter=0.2, seed=93).to(cuda)
+        K = tg.LaplaceElementAssembler.from_mesh(mesh)(mesh.points)
+        mask = mesh.boundary_mask
+    b = torch.from_numpy(np.random.default_rng(94).standard_normal(K.shape[0])).to(cuda)
+    Kc, bc = tg.Condenser(mask)(K, b)
+    lib = _lib.load()
+
+    def solve(until):
+        n = bc.numel()
+        x = torch.zeros(n, dtype=torch.float64, device=cuda)
+        work = torch.empty(5, n, dtype=torch.float64, device=cuda)
+        scal = torch.zeros(8, dtype=torch.float64, device=cuda)
+        part = torch.empty(lib.tm_pcg_partials_bytes() // 8, dtype=torch.float64, device=cuda)
+        op, keep = S.operator_of(Kc)
+        a = S.PcgArgs()
+        a.A = op
+        a.b, a.x = _lib.ptr(bc), _lib.ptr(x)
+        a.r, a.z, a.p, a.q, a.dinv = (_lib.ptr(work[i]) for i in range(5))
+        a.scalars, a.partials = _lib.ptr(scal), _lib.ptr(part)
+        st = _lib.stream_handle(torch.device(cuda))
+        _lib.check(lib.tm_pcg_start(ctypes.byref(a), st), "start")
+        if until:
+            _lib.check(lib.tm_pcg_iterate_until(ctypes.byref(a), 20000, 1e-12, st), "until")
+        else:
+            done = 0
+            while done < 20000:
+                _lib.check(lib.tm_pcg_iterate(ctypes.byref(a), 50, st), "iterate")
+                done += 50
+                s = scal.cpu()
+                if s[3] <= 1e-24 * s[4]:
+                    break
+        torch.cuda.synchronize()
+        return x.clone(), scal.cpu().clone()
+
+    x1, s1 = solve(True)
+    x2, s2 = solve(True)
+    x0, s0 = solve(False)
+    assert torch.equal(x1, x2) and torch.equal(s1, s2)
+    assert s1[6] == 1.0 and s1[3] <= 1e-24 * s1[4]
+    assert s1[5] <= s0[5]
+    assert rel_fro(x1, x0) <= 1e-10
+    assert lib.tm_device_fault() == 0
