@@ -258,6 +258,45 @@ size_t tm_vector_workspace_bytes(const tm_vector_args* args);
 int tm_assemble_vector(const tm_vector_args* args, tm_stream_t stream);
 
 /*
+ * Boundary-facet load vectors (FacetAssembler.__call__ for the forms
+ * c v, f v with nodal f, and g(x) v, assemble/facet_assembler.py:123-277):
+ *   out[i, w] = sum over facet items of sum_q w_q |F_q| g_w(x_q) psi_i(t_q)
+ * where an item is one selected (element, facet) pair given by its facet's
+ * nodes (plan.conn, facet-local order: vertices, then P2 edge nodes for
+ * facet edges [[1,2],[0,2],[0,1]]), psi its own Lagrange basis at the facet
+ * quadrature points t_q, and |F| = sqrt(det(F^T F)) the measure of its map
+ * from the reference facet (Gauss-Legendre on [0, 1] for lines, the triangle
+ * rule for triangles).  The plan is a node plan (tm_plan_build kind 1) over
+ * the items' connectivity; the reduction is the deterministic node-plan
+ * reduction of tm_assemble_vector.  out [n_points*width] is overwritten.
+ */
+#define TM_FACET_LINE2  0   /* P1 edge of a triangle, in 2-D */
+#define TM_FACET_LINE3  1   /* P2 edge of a triangle6, in 2-D */
+#define TM_FACET_TRI3   2   /* P1 face of a tetra, in 3-D */
+#define TM_FACET_TRI6   3   /* P2 face of a tetra10, in 3-D */
+typedef struct tm_facet_tables {
+    int32_t facet_type;        /* TM_FACET_* */
+    int32_t n_quad;            /* Q */
+    const double* packed;      /* device [w(Q) | psi(Q*Bf) | dpsi(Q*(D-1)*Bf)] */
+} tm_facet_tables;
+typedef struct tm_facet_vector_args {
+    int32_t dtype;
+    int32_t source;            /* TM_SOURCE_CONST, TM_SOURCE_NODAL or TM_SOURCE_QUAD */
+    int32_t width;             /* 1..3 */
+    int32_t pad0;
+    int64_t n_points;
+    const void* points;        /* [n_points, D] */
+    const void* values;        /* NODAL: [n_points, width]; QUAD: [n_items, Q, width], item order */
+    double const_value[3];     /* CONST: one value per component */
+    void* out;                 /* [n_points, width] */
+    void* workspace;           /* tm_facet_vector_workspace_bytes */
+    tm_facet_tables tables;
+    tm_chunk_plan plan;
+} tm_facet_vector_args;
+size_t tm_facet_vector_workspace_bytes(const tm_facet_vector_args* args);
+int tm_assemble_facet_vector(const tm_facet_vector_args* args, tm_stream_t stream);
+
+/*
  * Physical shape gradients and |det J| w per element and quadrature point
  * (Transformation.batch_shape_grad_jxw, element/transformation.py:1219-1276).
  * grad [E*Q*B*D], jxw [E*Q], element order, float64.

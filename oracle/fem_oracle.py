@@ -302,6 +302,92 @@ def assemble_load(points, conn, etype, n_points, f_nodes=None, const=None, func=
 
 
 # ---------------------------------------------------------------------------
+# Boundary facets (assemble/facet_assembler.py:123-277, 367-515)
+# ---------------------------------------------------------------------------
+# Gauss-Legendre on [-1, 1] (element/quadrature.py:36-53), mapped to [0, 1]
+_GL_W = {1: [2.0], 2: [1.0, 1.0],
+         3: [0.55555555555555555556, 0.88888888888888888889, 0.55555555555555555556],
+         4: [0.34785484513745385737, 0.65214515486254614263, 0.65214515486254614263, 0.34785484513745385737]}
+_GL_P = {1: [0.0], 2: [-0.57735026918962576451, 0.57735026918962576451],
+         3: [-0.77459666924148337704, 0.0, 0.77459666924148337704],
+         4: [-0.8611363115940526, -0.3399810435848563, 0.3399810435848563, 0.8611363115940526]}
+_FACET_VERTS = {2: [[0, 1], [1, 2], [2, 0]], 3: [[0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]]}
+
+
+def _facet_rule(dim, qorder):
+    """Facet-local weights [Qf] and points [Qf, dim-1]: lines [0, 1]
+    (element/quadrature.py:13-66), triangles the element rule."""
+    if dim == 2:
+        w = torch.tensor(_GL_W[qorder], dtype=DT) / 2
+        return w, ((torch.tensor(_GL_P[qorder], dtype=DT) + 1) / 2)[:, None]
+    return quadrature("triangle", qorder)
+
+
+def facet_nodes(etype):
+    """Local nodes of each facet: its vertices, then (P2) the element's edge
+    nodes whose two ends are both facet vertices."""
+    dim, order, _ = ELEMENT[etype]
+    edges = _TRI_EDGE if dim == 2 else _TET_EDGE
+    out = []
+    for vs in _FACET_VERTS[dim]:
+        nodes = list(vs)
+        if order == 2:
+            nodes += [dim + 1 + k for k, (a, b) in enumerate(edges) if a in vs and b in vs]
+        out.append(nodes)
+    return out
+
+
+def assemble_facet_load(points, conn, etype, boundary, n_points, qorder=2, f_nodes=None, const=None, func=None):
+    """b_i = sum over the selected (element, facet) pairs of
+    sum_q w_q |F_q| g(x_q) phi_i(xi_q), in the element's frame as the
+    reference writes it (facet_assembler.py:123-277): a facet of an element
+    is selected when all its nodes are boundary nodes (:367-515); xi_q is the
+    facet quadrature point mapped into the element's reference coordinates,
+    phi the cell basis, |F| = sqrt(det(F^T F)) with F = J G, J the cell
+    Jacobian at xi_q and G the facet map's gradient (element.py:1295-1408),
+    and every cell node receives its value.  ``f_nodes`` nodal values
+    [N] or [N, W] interpolated with phi, ``const`` a scalar or a vector of
+    length W, ``func`` a function of x_q."""
+    dim, order, nb = ELEMENT[etype]
+    conn = conn.long()
+    verts = basis_nodes(etype)[:dim + 1]                 # reference vertex coordinates
+    exps = _monomials(dim, order)
+    coef = torch.linalg.inv(_eval_monomials(exps, basis_nodes(etype))).T
+    wf, tf = _facet_rule(dim, qorder)
+    width = 1
+    if f_nodes is not None and f_nodes.dim() == 2:
+        width = f_nodes.shape[1]
+    if const is not None and torch.as_tensor(const).dim() == 1:
+        width = torch.as_tensor(const).numel()
+    out = torch.zeros(n_points, width, dtype=DT)
+    for k, (vs, fnodes) in enumerate(zip(_FACET_VERTS[dim], facet_nodes(etype))):
+        sel = boundary[conn[:, fnodes]].all(1)
+        if not bool(sel.any()):
+            continue
+        c = conn[sel]
+        G = torch.stack([verts[vs[j]] - verts[vs[0]] for j in range(1, dim)], 1)   # [dim, dim-1]
+        xi = verts[vs[0]][None, :] + tf @ G.T                                        # [Qf, dim]
+        phi = _eval_monomials(exps, xi) @ coef.T                                     # [Qf, B]
+        dphi = torch.einsum("qdm,bm->qdb", _eval_monomial_grads(exps, xi), coef)    # [Qf, dim, B]
+        X = points[c]                                                                # [E, B, dim]
+        J = torch.einsum("qib,ebj->eqji", dphi, X)                                   # [E, Qf, dim(x), dim(xi)]
+        F = J @ G                                                                    # [E, Qf, dim, dim-1]
+        detF = torch.sqrt(torch.linalg.det(F.transpose(-1, -2) @ F))                # [E, Qf]
+        if f_nodes is not None:
+            fv = f_nodes.reshape(n_points, -1)[c]                                    # [E, B, W]
+            g = torch.einsum("ebw,qb->eqw", fv, phi)
+        elif func is not None:
+            g = func(torch.einsum("ebd,qb->eqd", X, phi)).reshape(c.shape[0], len(wf), -1)
+        else:
+            cv = torch.as_tensor(1.0 if const is None else const, dtype=DT).reshape(1, 1, -1)
+            g = cv.expand(c.shape[0], len(wf), width)
+        loc = torch.einsum("q,eq,eqw,qb->ebw", wf, detF, g, phi)
+        out.index_add_(0, c.reshape(-1), loc.reshape(-1, width))
+    return out[:, 0] if width == 1 and (f_nodes is None or f_nodes.dim() == 1) and \
+        (const is None or torch.as_tensor(const).dim() == 0) else out
+
+
+# ---------------------------------------------------------------------------
 # Dirichlet condensation (operator/condense.py:182-296) and a direct solve
 # ---------------------------------------------------------------------------
 def condense(values, row, col, n, mask, rhs, value=None):

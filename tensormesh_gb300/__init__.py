@@ -13,6 +13,7 @@ from .assemble import ElementAssembler, NodeAssembler, assemble_forms
 from .builtin import (LaplaceElementAssembler, DiffusionElementAssembler, MassElementAssembler,
                       LinearElasticityElementAssembler, const_node_assembler, func_node_assembler,
                       LoadNodeAssembler)
+from .facet import FacetAssembler, LoadFacetAssembler, const_facet_assembler, func_facet_assembler
 from .solve import pcg_solve
 from .condense import Condenser
 from .adjoint import solve_diffusion
@@ -25,4 +26,5 @@ __all__ = [
     "DiffusionElementAssembler", "MassElementAssembler", "LinearElasticityElementAssembler",
     "const_node_assembler", "func_node_assembler", "LoadNodeAssembler", "pcg_solve",
     "element_type2dimension", "element_type2order", "Condenser", "solve_diffusion",
+    "FacetAssembler", "LoadFacetAssembler", "const_facet_assembler", "func_facet_assembler",
 ]

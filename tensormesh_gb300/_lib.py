@@ -70,6 +70,19 @@ class VectorArgs(C.Structure):
     ]
 
 
+class FacetTables(C.Structure):
+    _fields_ = [("facet_type", C.c_int32), ("n_quad", C.c_int32), ("packed", C.c_void_p)]
+
+
+class FacetVectorArgs(C.Structure):
+    _fields_ = [
+        ("dtype", C.c_int32), ("source", C.c_int32), ("width", C.c_int32), ("pad0", C.c_int32),
+        ("n_points", C.c_int64), ("points", C.c_void_p), ("values", C.c_void_p),
+        ("const_value", C.c_double * 3), ("out", C.c_void_p), ("workspace", C.c_void_p),
+        ("tables", FacetTables), ("plan", ChunkPlan),
+    ]
+
+
 class AdjointArgs(C.Structure):
     _fields_ = [
         ("dtype", C.c_int32), ("k_mode", C.c_int32), ("load_source", C.c_int32), ("reserved", C.c_int32),
@@ -141,6 +154,8 @@ _SIGNATURES = {
     "tm_quadrature_points": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, ElementTables,
                                        C.c_void_p, C.c_void_p]),
     "tm_morton_order": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]),
+    "tm_facet_vector_workspace_bytes": (C.c_size_t, [C.POINTER(FacetVectorArgs)]),
+    "tm_assemble_facet_vector": (C.c_int, [C.POINTER(FacetVectorArgs), C.c_void_p]),
     "tm_condense": (C.c_int, [C.POINTER(CondenseArgs), C.c_void_p]),
     "tm_project_reduce": (C.c_int, [C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -146,3 +146,127 @@ def packed_tables(etype: str, qorder: int) -> np.ndarray:
     t = element_tables(etype, qorder)
     return np.concatenate([t["w"].ravel(), t["phi"].ravel(), t["dphi"].ravel(),
                            t["mass_hat"].ravel(), t["load_hat"].ravel(), t["wsum"]]).astype(np.float64)
+
+
+# ---------------------------------------------------------------------------
+# Facets (boundary integrals, assemble/facet_assembler.py)
+#
+# The facets of an element are its edges (2-D) or faces (3-D).  A facet is
+# integrated as a simplex of its own: its nodes in facet-local order
+# (vertices, then, for P2, the midpoint of facet edge [[1,2],[0,2],[0,1]]),
+# its own Lagrange basis -- the element's basis restricted to the facet --
+# and the measure sqrt(det(F^T F)) of its map from the reference facet.
+# Line facets use Gauss-Legendre on [0, 1] (element/quadrature.py:13-66),
+# triangle facets the triangle rule above.
+
+# Gauss-Legendre nodes on [-1, 1] and weights, orders 1-7: the decimal
+# values of element/quadrature.py:36-53, mapped to [0, 1] below
+_GL = {
+    1: ([2.0], [0.0]),
+    2: ([1.0, 1.0], [-0.57735026918962576451, 0.57735026918962576451]),
+    3: ([0.55555555555555555556, 0.88888888888888888889, 0.55555555555555555556],
+        [-0.77459666924148337704, 0.0, 0.77459666924148337704]),
+    4: ([0.34785484513745385737, 0.65214515486254614263, 0.65214515486254614263, 0.34785484513745385737],
+        [-0.8611363115940526, -0.3399810435848563, 0.3399810435848563, 0.8611363115940526]),
+    5: ([0.23692688505618908751, 0.47862867049936646804, 0.56888888888888888889, 0.47862867049936646804,
+         0.23692688505618908751],
+        [-0.9061798459386640, -0.5384693101056831, 0.0, 0.5384693101056831, 0.9061798459386640]),
+    6: ([0.17132449237917034504, 0.36076157304813860757, 0.46791393457269104739, 0.46791393457269104739,
+         0.36076157304813860757, 0.17132449237917034504],
+        [-0.9324695142031521, -0.6612093864662645, -0.2386191860831969, 0.2386191860831969,
+         0.6612093864662645, 0.9324695142031521]),
+    7: ([0.12948496616886969327, 0.27970539148927666790, 0.38183005050511894495, 0.41795918367346938776,
+         0.38183005050511894495, 0.27970539148927666790, 0.12948496616886969327],
+        [-0.9491079123427585, -0.7415311855993945, -0.4058451513773972, 0.0, 0.4058451513773972,
+         0.7415311855993945, 0.9491079123427585]),
+}
+
+
+def line_quadrature(order: int) -> Tuple[np.ndarray, np.ndarray]:
+    """Gauss-Legendre rule on [0, 1]: weights (sum 1) and points [Q, 1]."""
+    if order not in _GL:
+        raise NotImplementedError(f"line quadrature order {order} is not tabulated (orders 1-7)")
+    w, p = _GL[order]
+    return np.array(w, dtype=np.float64) / 2.0, ((np.array(p, dtype=np.float64) + 1.0) / 2.0)[:, None]
+
+
+def _edge_node(a: int, b: int, edges, base: int) -> int:
+    for k, (x, y) in enumerate(edges):
+        if {x, y} == {a, b}:
+            return base + k
+    raise ValueError((a, b))
+
+
+def _facet_nodes(etype: str):
+    """Local node lists of the element's facets, each in facet-local order."""
+    if etype == "triangle":
+        return [(0, 1), (1, 2), (2, 0)]
+    if etype == "tetra":
+        return [(0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)]
+    if etype == "triangle6":
+        return [(a, b, _edge_node(a, b, TRI_EDGES, 3)) for a, b in [(0, 1), (1, 2), (2, 0)]]
+    if etype == "tetra10":
+        out = []
+        for a, b, c in [(0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)]:
+            out.append((a, b, c, _edge_node(b, c, TET_EDGES, 4), _edge_node(a, c, TET_EDGES, 4),
+                        _edge_node(a, b, TET_EDGES, 4)))
+        return out
+    raise NotImplementedError(f"facets of {etype!r}")
+
+
+# facet code of the C ABI: (facet dimension, facet order) -> TM_FACET_*
+FACET_CODES = {(1, 1): 0, (1, 2): 1, (2, 1): 2, (2, 2): 3}
+
+
+@dataclass(frozen=True)
+class FacetInfo:
+    element: str
+    facet_dim: int     # 1 (lines, in 2-D) or 2 (triangles, in 3-D)
+    order: int
+    n_basis: int       # nodes per facet
+    code: int          # TM_FACET_*
+    nodes: tuple       # local node lists of the element's facets
+
+
+def facet_info(etype: str) -> FacetInfo:
+    info = element_info(etype)
+    fd = info.dim - 1
+    nodes = tuple(_facet_nodes(etype))
+    return FacetInfo(etype, fd, info.order, len(nodes[0]), FACET_CODES[(fd, info.order)], nodes)
+
+
+def facet_shape_functions(facet_dim: int, order: int, t: np.ndarray):
+    """psi [Q, Bf] and dpsi [Q, facet_dim, Bf] of the facet's own Lagrange
+    basis at facet-local points t [Q, facet_dim]."""
+    t = np.asarray(t, dtype=np.float64)
+    if facet_dim == 1:
+        s = t[:, 0]
+        lam = np.stack([1.0 - s, s], 1)
+        dlam = np.array([[-1.0, 1.0]])
+        if order == 1:
+            return lam, np.broadcast_to(dlam, (len(s), 1, 2)).copy()
+        psi = np.stack([lam[:, 0] * (2 * lam[:, 0] - 1), lam[:, 1] * (2 * lam[:, 1] - 1), 4 * lam[:, 0] * lam[:, 1]], 1)
+        d = np.stack([(4 * lam[:, 0] - 1) * dlam[0, 0], (4 * lam[:, 1] - 1) * dlam[0, 1],
+                      4 * (lam[:, 0] * dlam[0, 1] + lam[:, 1] * dlam[0, 0])], 1)
+        return psi, d[:, None, :]
+    return shape_functions("triangle" if order == 1 else "triangle6", t)
+
+
+@lru_cache(maxsize=None)
+def facet_tables(etype: str, qorder: int) -> Dict[str, np.ndarray]:
+    """Weights, psi and dpsi of the facets of ``etype`` at the facet
+    quadrature of order ``qorder``."""
+    fi = facet_info(etype)
+    if fi.facet_dim == 1:
+        w, t = line_quadrature(qorder)
+    else:
+        w, t = quadrature("triangle", qorder)
+    psi, dpsi = facet_shape_functions(fi.facet_dim, fi.order, t)
+    return {"w": w, "t": t, "psi": psi, "dpsi": dpsi}
+
+
+def packed_facet_tables(etype: str, qorder: int) -> np.ndarray:
+    """[w(Q) | psi(Q*Bf) | dpsi(Q*(D-1)*Bf)] float64, the layout of
+    ``tm_facet_tables``."""
+    t = facet_tables(etype, qorder)
+    return np.concatenate([t["w"].ravel(), t["psi"].ravel(), t["dpsi"].ravel()]).astype(np.float64)

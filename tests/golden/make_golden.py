@@ -4,13 +4,15 @@ CPU in float64.
 
 Usage (from the repository root, with the reference source tree available)::
 
-    python tests/golden/make_golden.py /path/to/TensorMesh
+    python tests/golden/make_golden.py /path/to/TensorMesh [--only=facet]
 
 Writes
 
 * ``tests/golden/small_<case>.npz``: small meshes with every input and the
   reference's outputs (pattern, slot map, values, load vectors, layout
   hash, adjoint gradients).
+* ``tests/golden/small_facet.npz``: the reference's FacetAssembler on the
+  small meshes (``--only=facet`` writes this file alone).
 * ``tests/golden/full_checksums.json``: fingerprints (``checksum()`` of
   ``oracle/fem_oracle.py``) of the reference's outputs on the full-size
   workloads of ``tensormesh_gb300/workloads.py``.
@@ -35,7 +37,57 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
 
-def main(reference_root):
+def facet_golden(tm, to_ref):
+    """small_facet.npz: the reference's FacetAssembler (integrand forms as its
+    docstring writes them: ``forward(v)``, ``forward(v, f)``, a function of
+    ``x`` and a constant traction vector) on the small meshes."""
+    from tensormesh_gb300.mesh import gen_unit_square, gen_unit_cube
+
+    class Unit(tm.FacetAssembler):
+        def forward(self, v):
+            return v
+
+    class Nodal(tm.FacetAssembler):
+        def forward(self, v, f):
+            return f * v
+
+    class Func(tm.FacetAssembler):
+        def forward(self, v, x):
+            return torch.sin(math.pi * x[0]) * (1 + x[1]) * v
+
+    out = {}
+    cases = {
+        "tri3": (gen_unit_square(5, jitter=0.2, seed=111), [1, 2, 3]),
+        "tri6": (gen_unit_square(3, order=2, jitter=0.1, seed=112), [2, 3]),
+        "tet4": (gen_unit_cube(3, jitter=0.2, seed=113), [1, 2, 3]),
+        "tet10": (gen_unit_cube(2, order=2, jitter=0.1, seed=114), [2, 3]),
+    }
+    for name, (m, qorders) in cases.items():
+        rm = to_ref(m)
+        D = m.points.shape[1]
+        traction = torch.tensor([0.5, -1.0] if D == 2 else [0.5, -1.0, 0.25])
+
+        class Traction(tm.FacetAssembler):
+            def forward(self, v):
+                return v[:, None] * traction
+
+        f = torch.from_numpy(np.random.default_rng(12).uniform(-1.0, 1.0, m.n_points))
+        out[f"{name}_points"] = m.points.numpy()
+        out[f"{name}_conn"] = m.elements().numpy()
+        out[f"{name}_boundary"] = m.boundary_mask.numpy()
+        out[f"{name}_f"] = f.numpy()
+        out[f"{name}_traction"] = traction.numpy()
+        out[f"{name}_qorders"] = np.array(qorders)
+        for qo in qorders:
+            out[f"{name}_q{qo}_unit"] = Unit.from_mesh(rm, quadrature_order=qo)(rm.points).numpy()
+            out[f"{name}_q{qo}_nodal"] = Nodal.from_mesh(rm, quadrature_order=qo)(rm.points, point_data={"f": f}).numpy()
+            out[f"{name}_q{qo}_func"] = Func.from_mesh(rm, quadrature_order=qo)(rm.points).numpy()
+            out[f"{name}_q{qo}_traction"] = Traction.from_mesh(rm, quadrature_order=qo)(rm.points).numpy()
+    np.savez_compressed(os.path.join(HERE, "small_facet.npz"), **out)
+    print("wrote facet")
+
+
+def main(reference_root, only=None):
     import refshim
     refshim.install(reference_root)
     torch.set_default_dtype(torch.float64)   # the reference builds C at the default dtype
@@ -71,6 +123,10 @@ def main(reference_root):
         mm = meshio.Mesh(m.points.numpy(), [meshio.CellBlock(et, m.elements().numpy())],
                          point_data={"is_boundary": m.point_data["is_boundary"].numpy()})
         return tm.Mesh(mm)
+
+    if only == "facet":
+        facet_golden(tm, to_ref)
+        return
 
     # ------------------------------------------------------------------ small
     cases = {
@@ -218,4 +274,6 @@ def main(reference_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TENSORMESH_REF", "reference"))
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = next((a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")), None)
+    main(args[0] if args else os.environ.get("TENSORMESH_REF", "reference"), only)
