@@ -484,6 +484,9 @@ typedef struct tm_batched_pcg_args {
     void* work;
     int32_t* queue;
     tm_pcg_status* status;
+    const int32_t* order;           /* device [n_systems]: the queue's order of the systems
+                                       (largest first keeps the longest solves off the end);
+                                       NULL = 0, 1, ... */
 } tm_batched_pcg_args;
 int tm_batched_pcg(const tm_batched_pcg_args* args, tm_stream_t stream);
 

@@ -128,7 +128,7 @@ class BatchedPcgArgs(C.Structure):
     _fields_ = [("n_systems", C.c_int32), ("max_iter", C.c_int32), ("rtol", C.c_double),
                 ("system_offset", C.c_void_p), ("A", LinearOperator), ("dirichlet", C.c_void_p),
                 ("b", C.c_void_p), ("x", C.c_void_p), ("work", C.c_void_p), ("queue", C.c_void_p),
-                ("status", C.c_void_p)]
+                ("status", C.c_void_p), ("order", C.c_void_p)]
 
 
 TM_PCG_CONVERGED, TM_PCG_MAX_ITER, TM_PCG_BREAKDOWN = 1, 2, 3

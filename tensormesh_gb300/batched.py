@@ -59,6 +59,9 @@ class BatchedDiffusion:
         self.b_asm = LoadNodeAssembler.from_mesh(self.mesh, quadrature_order)
         self.device, self.dtype = dev, dtype
         self.system_offset = torch.from_numpy(self.node_offset).to(dev)
+        # the solver's queue takes the largest systems first
+        sizes = np.diff(self.node_offset)
+        self.order = torch.from_numpy(np.argsort(-sizes, kind="stable").astype(np.int32)).to(dev)
         self.dirichlet = bnd.to(torch.uint8).to(dev)
         self._graph = None
 
@@ -96,6 +99,7 @@ class BatchedDiffusion:
         a.dirichlet = _lib.ptr(self.dirichlet)
         a.b, a.x, a.work = _lib.ptr(b), _lib.ptr(x), _lib.ptr(work)
         a.queue, a.status = _lib.ptr(queue), _lib.ptr(status)
+        a.order = _lib.ptr(self.order)
         x.zero_()
         _lib.check(lib.tm_batched_pcg(C.byref(a), _lib.stream_handle(self.device)), "tm_batched_pcg")
         return values, b

@@ -8,9 +8,14 @@
 // preconditioned Krylov loops of torch SpMVs as its in-tree templates
 // (sparse/solve/torch_solve.py:70-248).
 //
-// Persistent CTAs take systems from a queue (one integer counter) and run
-// the whole PCG of a system with __syncthreads only: no grid-wide barrier,
-// no waiting on other CTAs.  Every loop is bounded by max_iter.  Reductions
+// Persistent CTAs take systems from a queue (one integer counter, over an
+// optional largest-first order) and run the whole PCG of a system with
+// __syncthreads only: no grid-wide barrier, no waiting on other CTAs.  The
+// batch time is set by its largest systems on one CTA each, so the loops
+// keep several rows per thread in flight: the SpMV interleaves the loads of
+// four rows, the vector updates load four elements before using them
+// (measured on 512 uneven meshes: 79 ms per batch against 122 ms one row at
+// a time).  Every loop is bounded by max_iter.  Reductions
 // are per thread in row order and then a fixed tree in shared memory, so the
 // result of a system does not depend on which CTA solved it.  Dirichlet rows
 // (dirichlet[i] != 0) keep x_i as given on input and are excluded from the
@@ -64,7 +69,10 @@ __global__ void __launch_bounds__(kBatchThreads) k_batched_pcg(const tm_batched_
     const uint8_t* fixed = a.dirichlet;
     const double tol2 = a.rtol * a.rtol;
     for (;;) {
-        if (threadIdx.x == 0) sys_s = atomicAdd(a.queue, 1);
+        if (threadIdx.x == 0) {
+            const int k = atomicAdd(a.queue, 1);
+            sys_s = k < a.n_systems ? (a.order ? a.order[k] : k) : a.n_systems;
+        }
         __syncthreads();
         const int sys = sys_s;
         __syncthreads();
@@ -108,14 +116,35 @@ __global__ void __launch_bounds__(kBatchThreads) k_batched_pcg(const tm_batched_
                 flag = TM_PCG_MAX_ITER;
                 break;
             }
-            // q = A p, pq
+            // q = A p, pq: four rows per thread at a time, their loads
+            // interleaved (rows r, r + T, r + 2T, r + 3T), each row summed in
+            // its entry order
             double v1[1] = {0.0};
-            for (int64_t i = r0 + threadIdx.x; i < r1; i += kBatchThreads) {
-                if (fixed && fixed[i]) continue;
-                double s = 0.0;
-                for (int64_t k = rp[i]; k < rp[i + 1]; ++k) s += (double)val[k] * (double)p[col[k]];
-                q[i] = (R)s;
-                v1[0] += (double)p[i] * s;
+            constexpr int RU = 4;
+            for (int64_t i0 = r0 + threadIdx.x; i0 < r1; i0 += RU * kBatchThreads) {
+                int64_t beg[RU], len[RU];
+                int64_t maxlen = 0;
+#pragma unroll
+                for (int u = 0; u < RU; ++u) {
+                    const int64_t i = i0 + (int64_t)u * kBatchThreads;
+                    const bool on = i < r1 && !(fixed && fixed[i]);
+                    beg[u] = on ? rp[i] : 0;
+                    len[u] = on ? rp[i + 1] - beg[u] : 0;
+                    maxlen = len[u] > maxlen ? len[u] : maxlen;
+                }
+                double s[RU] = {};
+                for (int64_t k = 0; k < maxlen; ++k)
+#pragma unroll
+                    for (int u = 0; u < RU; ++u)
+                        if (k < len[u]) s[u] += (double)val[beg[u] + k] * (double)p[col[beg[u] + k]];
+#pragma unroll
+                for (int u = 0; u < RU; ++u) {
+                    const int64_t i = i0 + (int64_t)u * kBatchThreads;
+                    if (i < r1 && !(fixed && fixed[i])) {
+                        q[i] = (R)s[u];
+                        v1[0] += (double)p[i] * s[u];
+                    }
+                }
             }
             block_sum<1>(v1, red);
             const double pq = v1[0];
@@ -125,23 +154,44 @@ __global__ void __launch_bounds__(kBatchThreads) k_batched_pcg(const tm_batched_
             }
             const double alpha = rz / pq;
             double v2[2] = {0.0, 0.0};
-            for (int64_t i = r0 + threadIdx.x; i < r1; i += kBatchThreads) {
-                if (fixed && fixed[i]) continue;
-                x[i] = (R)((double)x[i] + alpha * (double)p[i]);
-                const double ri = (double)r[i] - alpha * (double)q[i];
-                r[i] = (R)ri;
-                const double zi = ri * (double)dinv[i];
-                z[i] = (R)zi;
-                v2[0] += ri * zi;
-                v2[1] += ri * ri;
+            for (int64_t i0 = r0 + threadIdx.x; i0 < r1; i0 += 4 * kBatchThreads) {
+                double xv[4], pv[4], rv[4], qv[4], dv[4];
+                bool on[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int64_t i = i0 + (int64_t)u * kBatchThreads;
+                    on[u] = i < r1 && !(fixed && fixed[i]);
+                    if (on[u]) { xv[u] = (double)x[i]; pv[u] = (double)p[i]; rv[u] = (double)r[i]; qv[u] = (double)q[i]; dv[u] = (double)dinv[i]; }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (!on[u]) continue;
+                    const int64_t i = i0 + (int64_t)u * kBatchThreads;
+                    x[i] = (R)(xv[u] + alpha * pv[u]);
+                    const double ri = rv[u] - alpha * qv[u];
+                    r[i] = (R)ri;
+                    const double zi = ri * dv[u];
+                    z[i] = (R)zi;
+                    v2[0] += ri * zi;
+                    v2[1] += ri * ri;
+                }
             }
             block_sum<2>(v2, red);
             const double beta = rz != 0.0 ? v2[0] / rz : 0.0;
             rz = v2[0];
             rr = v2[1];
-            for (int64_t i = r0 + threadIdx.x; i < r1; i += kBatchThreads) {
-                if (fixed && fixed[i]) continue;
-                p[i] = (R)((double)z[i] + beta * (double)p[i]);
+            for (int64_t i0 = r0 + threadIdx.x; i0 < r1; i0 += 4 * kBatchThreads) {
+                double zv[4], pv[4];
+                bool on[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int64_t i = i0 + (int64_t)u * kBatchThreads;
+                    on[u] = i < r1 && !(fixed && fixed[i]);
+                    if (on[u]) { zv[u] = (double)z[i]; pv[u] = (double)p[i]; }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (on[u]) p[i0 + (int64_t)u * kBatchThreads] = (R)(zv[u] + beta * pv[u]);
             }
             __syncthreads();
             ++it;
@@ -179,10 +229,15 @@ extern "C" int tm_batched_pcg(const tm_batched_pcg_args* a, tm_stream_t stream) 
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_batched_pcg: null pointer");
     const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(a->queue, 0, sizeof(int32_t), st) != cudaSuccess) return bstatus("cudaMemsetAsync");
-    int dev = 0, sms = 0;
+    int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int grid = 2 * (sms > 0 ? sms : 152);
+    if (a->A.dtype == TM_F64)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batched_pcg<double>, kBatchThreads, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batched_pcg<float>, kBatchThreads, 0);
+    // resident CTAs only: each one loops over the queue
+    int grid = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 152);
     if (grid > a->n_systems) grid = a->n_systems;
     if (a->A.dtype == TM_F64)
         k_batched_pcg<double><<<grid, kBatchThreads, 0, st>>>(*a);
