@@ -12,6 +12,7 @@ the cached index arrays and their CSR structure.
 import ctypes
 from typing import Optional, Tuple
 
+import numpy as np
 import torch
 import torch.nn as nn
 
@@ -172,11 +173,15 @@ class Condenser(nn.Module):
         io_row / io_col their inner row and outer column) re-listed by inner
         row, stably, as positions in the full values (row_src) and in the
         K_io values (row_src_io)."""
-        order = torch.sort(io_row, stable=True).indices
-        counts = torch.bincount(io_row, minlength=n_inner) if io_row.numel() else \
-            torch.zeros(n_inner, dtype=torch.long, device=io_row.device)
+        # one-time host work (a stable sort and a count of the K_io rows)
+        dev = io_row.device
+        row_np = io_row.detach().cpu().numpy().astype(np.int64)
+        order_np = np.argsort(row_np, kind="stable")
+        counts = np.bincount(row_np, minlength=n_inner) if row_np.size else np.zeros(n_inner, dtype=np.int64)
+        row_ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        order = torch.from_numpy(order_np).to(dev)
         self._k_inner_dof = inner_dof.long().contiguous()
-        self._k_row_ptr = torch.cat([counts.new_zeros(1), torch.cumsum(counts, 0)]).long().contiguous()
+        self._k_row_ptr = torch.from_numpy(row_ptr).to(dev)
         self._k_row_src_io = order.long().contiguous()
         self._k_row_src = self.ou2in_idx[order].long().contiguous()
         self._k_row_col = io_col[order].long().contiguous()
