@@ -410,6 +410,181 @@ def run_inverse(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+ELASTIC_WORKLOAD = ("elasticity_p2tet_32: P2 tet isotropic elasticity (10-node tets, E ~ U[0.5, 2] per element, "
+                    "nu = 0.3), 32^3 cubes x 6 Kuhn, 196,608 elements, 274,625 nodes, 3x3 blocks, FP64")
+
+
+def elasticity_bytes(N, E, nnz, B=10):
+    """Inputs read once, outputs written once: 24N (points) + 4BE (int32
+    connectivity) + 8E (Young's modulus) + 4B^2 E (int32 block slot map) +
+    8 nnz (scalar values of the 3x3 blocks)."""
+    return 24 * N + 4 * B * E + 8 * E + 4 * B * B * E + 8 * nnz
+
+
+# FP64 flops per P2-tet elasticity element in the fewest-op formulation
+# (4 quadrature points; Jacobian, cofactors and 10 gradients per point; the
+# 55 unique 3x3 blocks of B_i^T C B_j per point), the figure the FP64 roof of
+# this workload is quoted on
+ELASTIC_FLOPS_PER_ELEMENT = 13000.0
+
+
+def run_elasticity(args, ws, rank, local):
+    """C3: one step = the 3x3 block values of K(E) for 196,608 P2 tets
+    (FP64).  Also times the set-up (from_mesh), the end-to-end call with host
+    buffers, and the solve that follows in the reference's examples:
+    condensation of the clamped face z = 0 and Jacobi-PCG to 1e-10."""
+    import tensormesh_gb300 as tg
+    from tensormesh_gb300 import workloads as W
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    wl = W.elasticity_p2tet(32)
+    mesh = wl.mesh.to(dev)
+    Ey = wl.data["E"].to(dev)
+    t0 = time.perf_counter()
+    asm = tg.LinearElasticityElementAssembler.from_mesh(mesh, nu=0.3)
+    setup_s = time.perf_counter() - t0
+    N, E = mesh.n_points, mesh.n_elements
+    nnz = asm.edges.shape[1] * 9
+    ed = {"E": Ey}
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        tg.assemble_forms([asm], mesh.points, ed)
+    torch.cuda.synchronize()
+    kbeg = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kdone = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for ev in kbeg + kdone:
+        ev.record()                              # torch creates an event's handle on its first record
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    _barrier(ws)
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        tg.assemble_forms([asm], mesh.points, ed, _events=(kbeg[k], None, kdone[k]))
+    torch.cuda.synchronize()
+    _barrier(ws)
+    clocks = sampler.stop()
+    ms = _max_over_ranks(statistics.mean(s.elapsed_time(e) for s, e in zip(kbeg, kdone)), ws, dev)
+
+    # e2e: points and E from pinned host memory, the block values back
+    pts_h = wl.mesh.points.clone().pin_memory()
+    E_h = wl.data["E"].clone().pin_memory()
+    vals_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    pts_d, E_d = torch.empty_like(mesh.points), torch.empty_like(Ey)
+
+    def e2e_step():
+        pts_d.copy_(pts_h, non_blocking=True)
+        E_d.copy_(E_h, non_blocking=True)
+        (K,) = tg.assemble_forms([asm], pts_d, {"E": E_d})
+        vals_h.copy_(K.reshape(-1), non_blocking=True)
+
+    for _ in range(max(2, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e_s, e_e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_s.record()
+    for _ in range(args.steps):
+        e2e_step()
+    e_e.record()
+    torch.cuda.synchronize()
+    e2e_ms = _max_over_ranks(e_s.elapsed_time(e_e) / args.steps, ws, dev)
+
+    # the solve: condense the clamped face, Jacobi-PCG (3x3 block rows)
+    K = asm(mesh.points, element_data=ed)
+    b = tg.const_node_assembler(torch.tensor([0.0, 0.0, -1.0])).from_mesh(mesh)(mesh.points)
+    clamp = (mesh.points[:, 2] == 0.0).repeat_interleave(3)
+    cond = tg.Condenser(clamp)
+    Kc, bc = cond(K, b)
+    tg.pcg_solve(Kc, bc, rtol=1e-10, max_iter=50000, check_every=100)
+    t_c, (Kc, bc) = _time_ms(lambda: cond(K, b), dev)
+    t_s, (uc, info) = _time_ms(lambda: tg.pcg_solve(Kc, bc, rtol=1e-10, max_iter=50000, check_every=100,
+                                                    return_info=True), dev)
+    n_c, nnz_c = bc.numel(), Kc.values.numel()
+    it_bytes = 8 * nnz_c + 4 * (nnz_c // 9) + 4 * (n_c // 3 + 1) + 7 * 8 * n_c
+    it_ms = t_s / max(1, info.iterations)
+
+    peak, peak_kind = _peaks()
+    abytes = elasticity_bytes(N, E, nnz)
+    achieved = abytes / (ms * 1e-3) / 1e9
+    line = {"metric": "P2-tet elasticity elements assembled/s (FP64, <=1e-12 rel)",
+            "value": E * ws / (ms * 1e-3), "unit": "elements/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kuhn-split cube, uniform E)",
+            "config": {"workload": ELASTIC_WORKLOAD, "elements": E, "nodes": N, "nnz": nnz,
+                       "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas x{ws}"},
+            "e2e": {"value": E * ws / (e2e_ms * 1e-3), "unit": "elements/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": pts_h.numel() * 8 + E_h.numel() * 8, "d2h_bytes_per_step": nnz * 8},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "k_matrix + k_matrix_finalize (one assembly pass)", "algorithmic_bytes": abytes,
+                         "fp64_gflops": ELASTIC_FLOPS_PER_ELEMENT * E / (ms * 1e-3) / 1e9},
+            "setup_s": setup_s,
+            "solve": {"condense_ms": t_c, "pcg_ms": t_s, "iterations": info.iterations,
+                      "relative_residual": info.relative_residual, "converged": info.converged,
+                      "ms_per_iteration": it_ms, "bytes_per_iteration": it_bytes,
+                      "hbm_frac_per_iteration": it_bytes / (it_ms * 1e-3) / 1e9 / peak,
+                      "unknowns": n_c, "nnz": nnz_c},
+            "clocks": clocks, "gpu_launches": 2 * args.steps}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_reference_elasticity(args, ws, rank, local):
+    """The reference's per-call elasticity work (restated in torch,
+    oracle/fem_oracle.py) on the host cores over a bounded sample (1/16 of
+    the elements, scattered into the full pattern, with the full layout
+    hash) and, whole, on the GPU."""
+    if rank != 0:
+        return
+    from oracle import fem_oracle as O
+    from tensormesh_gb300 import workloads as W
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    wl = W.elasticity_p2tet(32)
+    pts, conn, Ey = wl.mesh.points, wl.mesh.elements(), wl.data["E"]
+    edges, slot = O.element_pattern(conn, wl.mesh.n_points)
+    E = conn.shape[0]
+    Es = max(1, E // 16)
+    sample = (conn[:Es], Ey[:Es], slot[:Es * 100])
+    O.reference_call_elasticity(pts, *sample, edges, with_hash=False)
+    times = []
+    for _ in range(min(args.steps, 5)):
+        t0 = time.perf_counter()
+        O.reference_call_elasticity(pts, *sample, edges)
+        times.append(time.perf_counter() - t0)
+    s = statistics.mean(times)
+    line = {"metric": "P2-tet elasticity elements assembled/s (FP64, <=1e-12 rel)", "impl": "reference",
+            "value": Es / s, "unit": "elements/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded Kuhn-split cube, uniform E)",
+            "config": {"workload": ELASTIC_WORKLOAD, "elements": E, "parallelism": "host cores"},
+            "cpu_baseline": {"value": Es / s, "unit": "elements/s", "cores": threads, "kind": "port",
+                             "sample": f"{Es} of {E} elements per step (block K into the full pattern, incl. "
+                                       f"the per-call from_block_coo layout hash), reference op sequence restated "
+                                       f"in torch on {threads} host threads"},
+            "e2e": {"value": Es / s, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if torch.cuda.is_available() and not args.no_gpu_reference:
+        dev = torch.device("cuda", local)
+        pd, cd, Ed, sd, ed = pts.to(dev), conn.to(dev), Ey.to(dev), slot.to(dev), edges.to(dev)
+        for _ in range(max(3, args.warmup)):
+            O.reference_call_elasticity(pd, cd, Ed, sd, ed, with_hash=False)
+        torch.cuda.synchronize()
+        res = {}
+        for with_hash in (True, False):
+            ts = []
+            for _ in range(max(3, min(args.steps, 5))):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                O.reference_call_elasticity(pd, cd, Ed, sd, ed, with_hash=with_hash)
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+            res[with_hash] = E / statistics.median(ts)
+        line["torch_gpu"] = {"value": res[True], "value_without_hash": res[False], "unit": "elements/s",
+                             "note": "the reference op sequence (torch einsum/inverse/det/index_add_) on the GPU"}
+    print(json.dumps(line), flush=True)
+
+
 def run_batched(args, ws, rank, local):
     """C5: 512 uneven P1 triangle meshes, one graph launch (assembly + load +
     batched Jacobi-PCG to 1e-10) against per-mesh calls of the same library."""
@@ -478,13 +653,18 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-gpu-reference", action="store_true")
     ap.add_argument("--cubes", type=int, default=64, help="cubes per side of the Kuhn-split cube (64: 1,572,864 elements)")
-    ap.add_argument("--workload", default="diffusion_mass", choices=["diffusion_mass", "inverse", "batched"])
+    ap.add_argument("--workload", default="diffusion_mass",
+                    choices=["diffusion_mass", "elasticity", "inverse", "batched"])
     ap.add_argument("--meshes", type=int, default=512)
     ap.add_argument("--sample", type=int, default=32)
     args = ap.parse_args()
     ws, rank, local = _dist()
-    if args.impl == "reference":
+    if args.impl == "reference" and args.workload == "elasticity":
+        run_reference_elasticity(args, ws, rank, local)
+    elif args.impl == "reference":
         run_reference(args, ws, rank, local)
+    elif args.workload == "elasticity":
+        run_elasticity(args, ws, rank, local)
     elif args.workload == "inverse":
         run_inverse(args, ws, rank, local)
     elif args.workload == "batched":

@@ -459,3 +459,37 @@ def reference_call_diffusion_mass(points, conn, kappa, slot, edges, etype="tetra
             r.long(), c.long()
             hashes.append(layout_hash(r, c))
     return K, M, hashes
+
+
+# ---------------------------------------------------------------------------
+# The reference's per-call work for the P2-tet elasticity benchmark, restated
+# op for op: element_assembler.py:390-445 with the integrand of
+# builtin.py:172-178 (Ba^T C Bb per basis pair and quadrature point), the
+# quadrature contraction (element_assembler.py:199), the reduce projection
+# into [n_edge, D, D] (projector.py:95-123) and SparseMatrix.from_block_coo's
+# expansion and layout hash (sparse/matrix.py:76-86, :332-381).  A
+# per-element Young's modulus scales C element by element.
+# ---------------------------------------------------------------------------
+def reference_call_elasticity(points, conn, E, slot, edges, nu=0.3, etype="tetra10", qorder=2,
+                              with_hash=True):
+    dev = points.device
+    w, _, dphi = shape_tables(etype, qorder)
+    w, dphi = w.to(dev), dphi.to(dev)
+    D = points.shape[1]
+    nnz = edges.shape[1]
+    X = points[conn]
+    J = torch.einsum("ebj,qib->eqij", X, dphi)
+    grad = torch.einsum("qib,eqji->eqbj", dphi, torch.inverse(J))
+    jxw = torch.einsum("q,eq->eq", w, torch.linalg.det(J).abs())
+    Bm = voigt_B(grad)                                               # [e,q,b,k,a]
+    C1 = voigt_C(torch.ones(1, dtype=DT), nu, D)[0].to(dev)           # unit-E stiffness
+    integ = torch.einsum("eqika,kl,eqjlb->eqijab", Bm, C1, Bm) * E[:, None, None, None, None, None]
+    Ke = torch.einsum("eqijab,eq->eijab", integ, jxw)
+    K = torch.zeros(nnz, D, D, dtype=points.dtype, device=dev).index_add_(0, slot, Ke.reshape(-1, D, D))
+    h = None
+    if with_hash:
+        i, j = torch.meshgrid(torch.arange(D, device=dev), torch.arange(D, device=dev), indexing="ij")
+        r = (edges[0][:, None].repeat(1, D * D) * D + i.flatten()).flatten()
+        c = (edges[1][:, None].repeat(1, D * D) * D + j.flatten()).flatten()
+        h = layout_hash(r, c)
+    return K, h

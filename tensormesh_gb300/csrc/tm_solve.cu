@@ -25,6 +25,7 @@ namespace tmk {
 
 constexpr int kSolveThreads = 256;
 constexpr int kDotBlocks = 608;   // 4 x 152 SMs
+constexpr int kBlockLanes = 4;    // lanes per block row of a block (H > 1) operator
 
 // scalar slots
 enum { S_RZ = 0, S_PQ = 1, S_RZ_NEW = 2, S_RR = 3, S_BB = 4, S_ITER = 5, S_FLAG = 6 };
@@ -60,6 +61,41 @@ __device__ __forceinline__ double group_sum(double s) {
     return s;
 }
 
+// the H partial sums of block row `br` of A x: lane l of the L-lane group
+// takes blocks row_ptr[br] + l, + 2L, ...; each block is read once (its H*H
+// values, one column index, H entries of x), and every scalar row sums its
+// terms in the same order as row_partial_cg
+template <typename R, int H, int L, bool kL2 = true>
+__device__ __forceinline__ void block_row_cg(const tm_linear_operator& A, const R* x, int64_t br, int lane,
+                                             double (&s)[H]) {
+    const R* val = static_cast<const R*>(A.values);
+#pragma unroll
+    for (int a = 0; a < H; ++a) s[a] = 0;
+    const int64_t end = A.row_ptr[br + 1];
+#pragma unroll 2
+    for (int64_t p = A.row_ptr[br] + lane; p < end; p += L) {
+        const int64_t c = A.col[p];
+        R v[H * H];
+#pragma unroll
+        for (int k = 0; k < H * H; ++k) v[k] = ld(val + p * H * H + k);
+        double xb[H];
+#pragma unroll
+        for (int b = 0; b < H; ++b) xb[b] = (double)(kL2 ? __ldcg(x + c * H + b) : ld(x + c * H + b));
+#pragma unroll
+        for (int a = 0; a < H; ++a)
+#pragma unroll
+            for (int b = 0; b < H; ++b) s[a] += (double)v[a * H + b] * xb[b];
+    }
+}
+
+// butterfly sum over the L lanes of a group; every lane of the warp calls it
+template <int L>
+__device__ __forceinline__ double lane_sum(double s) {
+#pragma unroll
+    for (int m = L / 2; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m, L);
+    return s;
+}
+
 // q = A p ; partial[blk] = sum p.q over this block's rows (in row order)
 template <typename R, int H>
 __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A, const R* p, R* q,
@@ -69,7 +105,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A
     const int lane = threadIdx.x & 7, grp = threadIdx.x >> 3;
     const bool stop = scal && scal[S_FLAG] != 0.0;
     double acc = 0;
-    if (!stop) {
+    if (!stop && H == 1) {
         const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
         for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
             const int64_t r = base + grp;
@@ -80,6 +116,32 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A
                 acc += s * (double)p[r];
             }
         }
+    } else if (!stop) {
+        // 4-lane groups, one block row each; the 8-lane slots of red hold
+        // the sums of pairs of groups
+        constexpr int L = kBlockLanes;
+        const int bl = threadIdx.x & (L - 1), bg = threadIdx.x / L;
+        const int64_t nb = A.n_rows, groups_total = (int64_t)gridDim.x * (kSolveThreads / L);
+        for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
+            const int64_t bi = base + bg;
+            double s[H];
+            if (bi < nb) {
+                block_row_cg<R, H, L, false>(A, p, bi, bl, s);
+            } else {
+#pragma unroll
+                for (int c = 0; c < H; ++c) s[c] = 0;
+            }
+#pragma unroll
+            for (int c = 0; c < H; ++c) s[c] = lane_sum<L>(s[c]);
+            if (bi < nb && bl == 0) {
+#pragma unroll
+                for (int c = 0; c < H; ++c) {
+                    q[bi * H + c] = (R)s[c];
+                    acc += s[c] * (double)p[bi * H + c];
+                }
+            }
+        }
+        acc += __shfl_xor_sync(0xffffffffu, acc, 4, 8);   // lane 0 of each 8-lane slot: both groups' sums
     }
     if (lane == 0) red[grp] = acc;
     __syncthreads();
@@ -294,12 +356,37 @@ template <typename R, int H>
 __global__ void __launch_bounds__(kSolveThreads) k_spmv_op(tm_linear_operator A, const R* x, R* y, double alpha,
                                                            double beta) {
     const int64_t n = A.n_rows * H;
-    const int lane = threadIdx.x & 7, grp = threadIdx.x >> 3;
-    const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
-    for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
-        const int64_t r = base + grp;
-        const double s = group_sum(r < n ? row_partial<R, H>(A, x, r, lane) : 0.0);
-        if (r < n && lane == 0) y[r] = (R)(beta == 0.0 ? alpha * s : alpha * s + beta * (double)y[r]);
+    if constexpr (H == 1) {
+        const int lane = threadIdx.x & 7, grp = threadIdx.x >> 3;
+        const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
+        for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
+            const int64_t r = base + grp;
+            const double s = group_sum(r < n ? row_partial<R, H>(A, x, r, lane) : 0.0);
+            if (r < n && lane == 0) y[r] = (R)(beta == 0.0 ? alpha * s : alpha * s + beta * (double)y[r]);
+        }
+    } else {
+        constexpr int L = kBlockLanes;
+        const int lane = threadIdx.x & (L - 1), grp = threadIdx.x / L;
+        const int64_t nb = A.n_rows, groups_total = (int64_t)gridDim.x * (kSolveThreads / L);
+        for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
+            const int64_t bi = base + grp;
+            double s[H];
+            if (bi < nb) {
+                block_row_cg<R, H, L, false>(A, x, bi, lane, s);
+            } else {
+#pragma unroll
+                for (int c = 0; c < H; ++c) s[c] = 0;
+            }
+#pragma unroll
+            for (int c = 0; c < H; ++c) s[c] = lane_sum<L>(s[c]);
+            if (bi < nb && lane == 0) {
+#pragma unroll
+                for (int c = 0; c < H; ++c) {
+                    const int64_t r = bi * H + c;
+                    y[r] = (R)(beta == 0.0 ? alpha * s[c] : alpha * s[c] + beta * (double)y[r]);
+                }
+            }
+        }
     }
 }
 
@@ -429,14 +516,6 @@ __device__ __forceinline__ double row_partial_cg(const tm_linear_operator& A, co
     return s;
 }
 
-// butterfly sum over the L lanes of a group; every lane of the warp calls it
-template <int L>
-__device__ __forceinline__ double lane_sum(double s) {
-#pragma unroll
-    for (int m = L / 2; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m, L);
-    return s;
-}
-
 template <typename R, int H, int L>
 __global__ void __launch_bounds__(kSolveThreads, 4) k_pcg_persistent(const tm_pcg_args a, int max_iter, double tol2) {
     __shared__ double red[kSolveThreads];
@@ -465,12 +544,36 @@ __global__ void __launch_bounds__(kSolveThreads, 4) k_pcg_persistent(const tm_pc
     for (int it = 0; it < max_iter && flag == 0; ++it) {
         // q = A p and this block's part of p.q
         double acc = 0;
-        for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < n; base += groups_total) {
-            const int64_t i = base + grp;
-            const double s = lane_sum<L>(i < n ? row_partial_cg<R, H, L>(a.A, p, i, lane) : 0.0);
-            if (i < n && lane == 0) {
-                __stcg(q + i, (R)s);
-                acc += s * (double)__ldcg(p + i);
+        if constexpr (H == 1) {
+            for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < n; base += groups_total) {
+                const int64_t i = base + grp;
+                const double s = lane_sum<L>(i < n ? row_partial_cg<R, H, L>(a.A, p, i, lane) : 0.0);
+                if (i < n && lane == 0) {
+                    __stcg(q + i, (R)s);
+                    acc += s * (double)__ldcg(p + i);
+                }
+            }
+        } else {
+            // one group per block row: H rows of q from one pass over the blocks
+            const int64_t nb = a.A.n_rows;
+            for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
+                const int64_t bi = base + grp;
+                double s[H];
+                if (bi < nb) {
+                    block_row_cg<R, H, L>(a.A, p, bi, lane, s);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < H; ++c) s[c] = 0;
+                }
+#pragma unroll
+                for (int c = 0; c < H; ++c) s[c] = lane_sum<L>(s[c]);
+                if (bi < nb && lane == 0) {
+#pragma unroll
+                    for (int c = 0; c < H; ++c) {
+                        __stcg(q + bi * H + c, (R)s[c]);
+                        acc += s[c] * (double)__ldcg(p + bi * H + c);
+                    }
+                }
             }
         }
         if (lane == 0) red2[grp] = acc;
