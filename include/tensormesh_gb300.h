@@ -402,7 +402,12 @@ int tm_adjoint_p1(const tm_adjoint_args* args, tm_stream_t stream);
 /* ---- sparse linear algebra (SparseMatrix @ and solve) ------------------- */
 /*
  * CSR (block == 1) or block-CSR (block == H, HxH row-major blocks) operator.
- * Rows sorted by column are not required.
+ * Rows sorted by column are not required.  row_order (optional) is the
+ * order in which the SpMV and PCG kernels take the (block) rows, a
+ * permutation of [0, n_rows): longest rows first keeps the lanes of a warp
+ * on rows of equal length.  It changes which lanes compute a row, not the
+ * order of the terms of its sum; the dot products of tm_pcg_* follow it.
+ * NULL: natural order.  Entries outside [0, n_rows) are skipped.
  */
 typedef struct tm_linear_operator {
     int32_t dtype;             /* TM_F64 / TM_F32 */
@@ -411,6 +416,7 @@ typedef struct tm_linear_operator {
     const int64_t* row_ptr;    /* device [n_rows+1] */
     const int32_t* col;        /* device [nnz_blocks] block columns */
     const void* values;        /* device [nnz_blocks*block*block] */
+    const int32_t* row_order;  /* device [n_rows] or NULL */
 } tm_linear_operator;
 
 /* y = alpha A x + beta y  (SparseMatrix.__matmul__, inherited from torch-sla) */

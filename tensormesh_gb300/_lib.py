@@ -111,7 +111,8 @@ class CondenseArgs(C.Structure):
 
 class LinearOperator(C.Structure):
     _fields_ = [("dtype", C.c_int32), ("block", C.c_int32), ("n_rows", C.c_int64),
-                ("row_ptr", C.c_void_p), ("col", C.c_void_p), ("values", C.c_void_p)]
+                ("row_ptr", C.c_void_p), ("col", C.c_void_p), ("values", C.c_void_p),
+                ("row_order", C.c_void_p)]
 
 
 class PcgArgs(C.Structure):

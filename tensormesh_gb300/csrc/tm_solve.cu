@@ -33,6 +33,14 @@ enum { S_RZ = 0, S_PQ = 1, S_RZ_NEW = 2, S_RR = 3, S_BB = 4, S_ITER = 5, S_FLAG 
 template <typename R>
 __device__ __forceinline__ R ld(const R* p) { return __ldg(p); }
 
+// the (block) row taken at position i of the operator's row order; -1 for
+// an entry outside [0, n_rows)
+__device__ __forceinline__ int64_t row_at(const tm_linear_operator& A, int64_t i) {
+    if (!A.row_order) return i;
+    const int64_t r = __ldg(A.row_order + i);
+    return (r >= 0 && r < A.n_rows) ? r : -1;
+}
+
 // lane-partial of row `row` of A x for scalar CSR (H == 1) or block CSR rows:
 // lane l of the 8-lane group sums entries l, l+8, ... of the (block) row
 template <typename R, int H>
@@ -108,10 +116,10 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A
     if (!stop && H == 1) {
         const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
         for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
-            const int64_t r = base + grp;
+            const int64_t r = base + grp < n ? row_at(A, base + grp) : -1;
             // all 8 lanes of a group share r; the loop bound is uniform per block
-            const double s = group_sum(r < n ? row_partial<R, H>(A, p, r, lane) : 0.0);
-            if (r < n && lane == 0) {
+            const double s = group_sum(r >= 0 ? row_partial<R, H>(A, p, r, lane) : 0.0);
+            if (r >= 0 && lane == 0) {
                 q[r] = (R)s;
                 acc += s * (double)p[r];
             }
@@ -123,9 +131,9 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A
         const int bl = threadIdx.x & (L - 1), bg = threadIdx.x / L;
         const int64_t nb = A.n_rows, groups_total = (int64_t)gridDim.x * (kSolveThreads / L);
         for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
-            const int64_t bi = base + bg;
+            const int64_t bi = base + bg < nb ? row_at(A, base + bg) : -1;
             double s[H];
-            if (bi < nb) {
+            if (bi >= 0) {
                 block_row_cg<R, H, L, false>(A, p, bi, bl, s);
             } else {
 #pragma unroll
@@ -133,7 +141,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A
             }
 #pragma unroll
             for (int c = 0; c < H; ++c) s[c] = lane_sum<L>(s[c]);
-            if (bi < nb && bl == 0) {
+            if (bi >= 0 && bl == 0) {
 #pragma unroll
                 for (int c = 0; c < H; ++c) {
                     q[bi * H + c] = (R)s[c];
@@ -360,18 +368,18 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_op(tm_linear_operator A,
         const int lane = threadIdx.x & 7, grp = threadIdx.x >> 3;
         const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
         for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
-            const int64_t r = base + grp;
-            const double s = group_sum(r < n ? row_partial<R, H>(A, x, r, lane) : 0.0);
-            if (r < n && lane == 0) y[r] = (R)(beta == 0.0 ? alpha * s : alpha * s + beta * (double)y[r]);
+            const int64_t r = base + grp < n ? row_at(A, base + grp) : -1;
+            const double s = group_sum(r >= 0 ? row_partial<R, H>(A, x, r, lane) : 0.0);
+            if (r >= 0 && lane == 0) y[r] = (R)(beta == 0.0 ? alpha * s : alpha * s + beta * (double)y[r]);
         }
     } else {
         constexpr int L = kBlockLanes;
         const int lane = threadIdx.x & (L - 1), grp = threadIdx.x / L;
         const int64_t nb = A.n_rows, groups_total = (int64_t)gridDim.x * (kSolveThreads / L);
         for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
-            const int64_t bi = base + grp;
+            const int64_t bi = base + grp < nb ? row_at(A, base + grp) : -1;
             double s[H];
-            if (bi < nb) {
+            if (bi >= 0) {
                 block_row_cg<R, H, L, false>(A, x, bi, lane, s);
             } else {
 #pragma unroll
@@ -379,7 +387,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_op(tm_linear_operator A,
             }
 #pragma unroll
             for (int c = 0; c < H; ++c) s[c] = lane_sum<L>(s[c]);
-            if (bi < nb && lane == 0) {
+            if (bi >= 0 && lane == 0) {
 #pragma unroll
                 for (int c = 0; c < H; ++c) {
                     const int64_t r = bi * H + c;
@@ -546,9 +554,9 @@ __global__ void __launch_bounds__(kSolveThreads, 4) k_pcg_persistent(const tm_pc
         double acc = 0;
         if constexpr (H == 1) {
             for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < n; base += groups_total) {
-                const int64_t i = base + grp;
-                const double s = lane_sum<L>(i < n ? row_partial_cg<R, H, L>(a.A, p, i, lane) : 0.0);
-                if (i < n && lane == 0) {
+                const int64_t i = base + grp < n ? row_at(a.A, base + grp) : -1;
+                const double s = lane_sum<L>(i >= 0 ? row_partial_cg<R, H, L>(a.A, p, i, lane) : 0.0);
+                if (i >= 0 && lane == 0) {
                     __stcg(q + i, (R)s);
                     acc += s * (double)__ldcg(p + i);
                 }
@@ -557,9 +565,9 @@ __global__ void __launch_bounds__(kSolveThreads, 4) k_pcg_persistent(const tm_pc
             // one group per block row: H rows of q from one pass over the blocks
             const int64_t nb = a.A.n_rows;
             for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
-                const int64_t bi = base + grp;
+                const int64_t bi = base + grp < nb ? row_at(a.A, base + grp) : -1;
                 double s[H];
-                if (bi < nb) {
+                if (bi >= 0) {
                     block_row_cg<R, H, L>(a.A, p, bi, lane, s);
                 } else {
 #pragma unroll
@@ -567,7 +575,7 @@ __global__ void __launch_bounds__(kSolveThreads, 4) k_pcg_persistent(const tm_pc
                 }
 #pragma unroll
                 for (int c = 0; c < H; ++c) s[c] = lane_sum<L>(s[c]);
-                if (bi < nb && lane == 0) {
+                if (bi >= 0 && lane == 0) {
 #pragma unroll
                     for (int c = 0; c < H; ++c) {
                         __stcg(q + bi * H + c, (R)s[c]);

@@ -36,7 +36,9 @@ def operator_of(A) -> tuple:
     op.block = H
     op.n_rows = rp.numel() - 1
     op.row_ptr, op.col, op.values = _lib.ptr(rp), _lib.ptr(col), _lib.ptr(vals)
-    return op, (rp, col, vals)
+    order = A._row_order()
+    op.row_order = _lib.ptr(order)
+    return op, (rp, col, vals, order)
 
 
 def spmv(A, x: torch.Tensor, out: Optional[torch.Tensor] = None, alpha: float = 1.0,

@@ -61,6 +61,7 @@ class SparseMatrix:
         self._hash = None
         self._sorted = _sorted
         self._csr = None
+        self._order = None
 
     # ------------------------------------------------------------ attributes
     @property
@@ -163,6 +164,7 @@ class SparseMatrix:
                          _block=self._block, _block_row=self._block_row, _block_col=self._block_col,
                          _sorted=self._sorted)
         m._hash, m._row64, m._col64, m._csr = self._hash, self._row64, self._col64, self._csr
+        m._order = self._order
         return m
 
     # ------------------------------------------------------------ CSR view
@@ -195,6 +197,16 @@ class SparseMatrix:
             torch.cumsum(counts, 0, out=rp[1:])
         self._csr = (rp, bc.to(torch.int32).contiguous(), perm, H)
         return self._csr
+
+    def _row_order(self) -> torch.Tensor:
+        """int32 [n_rows] on the values' device: the (block) rows by
+        decreasing length, ties in row order (computed once, on the host)."""
+        if self._order is None:
+            rp = self._csr_structure()[0]
+            lens = np.diff(rp.cpu().numpy())
+            order = np.argsort(-lens, kind="stable").astype(np.int32)
+            self._order = torch.from_numpy(order).to(rp.device)
+        return self._order
 
     def matvec(self, x: torch.Tensor, out: Optional[torch.Tensor] = None, alpha: float = 1.0,
                beta: float = 0.0) -> torch.Tensor:
