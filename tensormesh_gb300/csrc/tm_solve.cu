@@ -26,6 +26,7 @@ namespace tmk {
 constexpr int kSolveThreads = 256;
 constexpr int kDotBlocks = 608;   // 4 x 152 SMs
 constexpr int kBlockLanes = 4;    // lanes per block row of a block (H > 1) operator
+constexpr int kVecUnroll = 2;     // vector elements per thread and pass in the persistent PCG
 
 // scalar slots
 enum { S_RZ = 0, S_PQ = 1, S_RZ_NEW = 2, S_RR = 3, S_BB = 4, S_ITER = 5, S_FLAG = 6 };
@@ -437,77 +438,80 @@ int dispatch_op(const tm_linear_operator& A, F&& f) {
 __device__ int g_solve_fault = 0;
 
 constexpr unsigned kBarrierTries = 1u << 22;   // L2 round trips: about a second
-constexpr int kBarrierGroups = 32;
 
-// Two-level grid barrier: bar[0] top counter, bar[1] generation,
-// bar[2 + g] the counter of group g (blocks with blockIdx % 32 == g); all
-// zero before the launch.  The last block of a group reports to the top
-// counter, the last group flips the generation, so at most 32 + 19 atomic
-// adds serialise on one address.  False when the wait ran out, in which case
-// the caller returns.
-__device__ bool grid_barrier(unsigned* bar, unsigned nblocks) {
+// Grid barrier on one arrival counter (bar[0], zero before the launch, never
+// reset within it): the barrier of epoch e completes when the counter
+// reaches (e + 1) * nblocks (modulo 2^32).  Thread 0 of each block releases
+// the block's writes (fence, then the arrival add) and polls with acquire
+// loads; no reset or generation word sits on the critical path.  False when
+// the wait ran out, in which case the caller returns.
+__device__ bool grid_barrier(unsigned* bar, unsigned nblocks, unsigned& epoch) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned* gen = bar + 1;
-        const unsigned g = *gen;
-        const unsigned groups = nblocks < (unsigned)kBarrierGroups ? nblocks : (unsigned)kBarrierGroups;
-        const unsigned grp = blockIdx.x % groups;
-        const unsigned in_grp = nblocks / groups + (grp < nblocks % groups ? 1u : 0u);
+        const unsigned target = (epoch + 1u) * nblocks;
         __threadfence();
-        bool last = false;
-        if (atomicAdd(bar + 2 + grp, 1u) == in_grp - 1) {
-            atomicExch(bar + 2 + grp, 0u);
-            __threadfence();
-            if (atomicAdd(bar, 1u) == groups - 1) {
-                atomicExch(bar, 0u);
-                __threadfence();
-                atomicAdd(bar + 1, 1u);
-                last = true;
-            }
-        }
-        if (last) {
-            ok = 1;
-        } else {
-            unsigned it = 0;
-            while (*gen == g && ++it < kBarrierTries) {
-            }
-            ok = *gen != g;
-            if (!ok) atomicExch(&g_solve_fault, 1);
-        }
-        __threadfence();
+        unsigned v;
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(v) : "l"(bar) : "memory");
+        v += 1u;
+        unsigned it = 0;
+        while ((int)(v - target) < 0 && ++it < kBarrierTries)
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+        ok = (int)(v - target) >= 0;
+        if (!ok) atomicExch(&g_solve_fault, 1);
     }
     __syncthreads();
+    ++epoch;
     return ok != 0;
 }
 
-// sum of part[0..n) in a fixed order (strided per thread, then a tree): the
-// same value in every block
-__device__ double ordered_sum(const double* part, int n, double* red) {
-    double s = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(part + i);
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    const double t = red[0];
-    __syncthreads();
-    return t;
+// butterfly sum over the 32 lanes of a warp; every lane ends with the same
+// value (both lanes of a pair add the same two operands)
+__device__ __forceinline__ double warp_sum(double s) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+    return s;
 }
 
-// tree sum of one value per thread (fixed order)
-__device__ double ordered_sum_local(double v, double* red) {
-    red[threadIdx.x] = v;
+// Fixed-order block sums of K values per thread (blockDim.x ==
+// kSolveThreads): staged in shared memory and summed by warp 0 alone (a
+// pairwise tree over each lane's 8 entries, then a butterfly), so that few
+// FP64 instructions and a short chain of dependent adds are spent; every
+// thread returns the same sums
+template <int K>
+__device__ __forceinline__ void block_sums(const double (&v)[K], double (&out)[K], double (*red)[kSolveThreads],
+                                           double* res) {
+    static_assert(kSolveThreads == 256, "block_sums sums 8 entries per lane of warp 0");
+#pragma unroll
+    for (int k = 0; k < K; ++k) red[k][threadIdx.x] = v[k];
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const double* e = red[k] + threadIdx.x;
+            const double t = ((e[0] + e[32]) + (e[64] + e[96])) + ((e[128] + e[160]) + (e[192] + e[224]));
+            const double w = warp_sum(t);
+            if (threadIdx.x == 0) res[k] = w;
+        }
     }
-    const double t = red[0];
     __syncthreads();
-    return t;
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = res[k];
+}
+
+// sums of the K arrays part[k * stride + 0..n) in a fixed order (strided per
+// thread, then block_sums): the same values in every block of the launch
+template <int K>
+__device__ __forceinline__ void ordered_sums(const double* part, int stride, int n, double (&out)[K],
+                                             double (*red)[kSolveThreads], double* res) {
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double t = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) t += __ldcg(part + k * stride + i);
+        v[k] = t;
+    }
+    block_sums<K>(v, out, red, res);
 }
 
 template <typename R, int H, int L>
@@ -525,11 +529,12 @@ __device__ __forceinline__ double row_partial_cg(const tm_linear_operator& A, co
 }
 
 template <typename R, int H, int L>
-__global__ void __launch_bounds__(kSolveThreads, 4) k_pcg_persistent(const tm_pcg_args a, int max_iter, double tol2) {
-    __shared__ double red[kSolveThreads];
-    __shared__ double red2[kSolveThreads / L];
+__global__ void __launch_bounds__(kSolveThreads, 2) k_pcg_persistent(const tm_pcg_args a, int max_iter, double tol2) {
+    __shared__ double red[2][kSolveThreads];
+    __shared__ double res[2];
     const int64_t n = a.A.n_rows * H;
     const unsigned G = gridDim.x;
+    unsigned epoch = 0;
     unsigned* bar = reinterpret_cast<unsigned*>(a.partials + 3 * kDotBlocks);
     double* part_pq = a.partials;
     double* part_rz = a.partials + kDotBlocks;
@@ -584,48 +589,92 @@ __global__ void __launch_bounds__(kSolveThreads, 4) k_pcg_persistent(const tm_pc
                 }
             }
         }
-        if (lane == 0) red2[grp] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0;
-            for (int g = 0; g < kSolveThreads / L; ++g) t += red2[g];
-            __stcg(part_pq + blockIdx.x, t);
+        {
+            const double v[1] = {acc};
+            double o[1];
+            block_sums<1>(v, o, red, res);
+            if (threadIdx.x == 0) __stcg(part_pq + blockIdx.x, o[0]);
         }
-        if (!grid_barrier(bar, G)) return;
-        pq = ordered_sum(part_pq, G, red);
+        if (!grid_barrier(bar, G, epoch)) return;
+        {
+            double o[1];
+            ordered_sums<1>(part_pq, 0, (int)G, o, red, res);
+            pq = o[0];
+        }
         if (!(pq > 0.0)) {   // breakdown (p^T A p <= 0 or NaN): x stays as it is
             flag = 2;
             break;
         }
         const double alpha = rz / pq;
         // x += alpha p ; r -= alpha q ; z = dinv r ; partials r.z and r.r
+        // (kVecUnroll elements per thread and pass, all loads issued first)
         double lrz = 0, lrr = 0;
-        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-            __stcg(x + i, (R)((double)__ldcg(x + i) + alpha * (double)__ldcg(p + i)));
-            const double ri = (double)__ldcg(r + i) - alpha * (double)__ldcg(q + i);
-            __stcg(r + i, (R)ri);
-            const double zi = ri * (double)dinv[i];
-            __stcg(z + i, (R)zi);
-            lrz += ri * zi;
-            lrr += ri * ri;
+        for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += kVecUnroll * stride) {
+            double xv[kVecUnroll], pv[kVecUnroll], rv[kVecUnroll], qv[kVecUnroll], dv[kVecUnroll];
+#pragma unroll
+            for (int u = 0; u < kVecUnroll; ++u) {
+                const int64_t i = i0 + u * stride;
+                if (i < n) {
+                    xv[u] = (double)__ldcg(x + i);
+                    pv[u] = (double)__ldcg(p + i);
+                    rv[u] = (double)__ldcg(r + i);
+                    qv[u] = (double)__ldcg(q + i);
+                    dv[u] = (double)ld(dinv + i);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kVecUnroll; ++u) {
+                const int64_t i = i0 + u * stride;
+                if (i < n) {
+                    __stcg(x + i, (R)(xv[u] + alpha * pv[u]));
+                    const double ri = rv[u] - alpha * qv[u];
+                    __stcg(r + i, (R)ri);
+                    const double zi = ri * dv[u];
+                    __stcg(z + i, (R)zi);
+                    lrz += ri * zi;
+                    lrr += ri * ri;
+                }
+            }
         }
-        const double brz = ordered_sum_local(lrz, red);
-        const double brr = ordered_sum_local(lrr, red);
-        if (threadIdx.x == 0) {
-            __stcg(part_rz + blockIdx.x, brz);
-            __stcg(part_rr + blockIdx.x, brr);
+        {
+            const double v[2] = {lrz, lrr};
+            double o[2];
+            block_sums<2>(v, o, red, res);
+            if (threadIdx.x == 0) {
+                __stcg(part_rz + blockIdx.x, o[0]);
+                __stcg(part_rr + blockIdx.x, o[1]);
+            }
         }
-        if (!grid_barrier(bar, G)) return;
-        const double rz_new = ordered_sum(part_rz, G, red);
-        rr = ordered_sum(part_rr, G, red);
+        if (!grid_barrier(bar, G, epoch)) return;
+        double rz_new;
+        {
+            double o[2];
+            ordered_sums<2>(part_rz, kDotBlocks, (int)G, o, red, res);
+            rz_new = o[0];
+            rr = o[1];
+        }
         const double beta = rz != 0.0 ? rz_new / rz : 0.0;
         rz = rz_new;
         iters += 1.0;
         if (rr <= tol2 * bb) flag = 1;
         if (flag == 0) {
-            for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
-                __stcg(p + i, (R)((double)__ldcg(z + i) + beta * (double)__ldcg(p + i)));
-            if (!grid_barrier(bar, G)) return;
+            for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += kVecUnroll * stride) {
+                double zv[kVecUnroll], pv[kVecUnroll];
+#pragma unroll
+                for (int u = 0; u < kVecUnroll; ++u) {
+                    const int64_t i = i0 + u * stride;
+                    if (i < n) {
+                        zv[u] = (double)__ldcg(z + i);
+                        pv[u] = (double)__ldcg(p + i);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kVecUnroll; ++u) {
+                    const int64_t i = i0 + u * stride;
+                    if (i < n) __stcg(p + i, (R)(zv[u] + beta * pv[u]));
+                }
+            }
+            if (!grid_barrier(bar, G, epoch)) return;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -648,7 +697,7 @@ int pcg_iterate_until_l(const tm_pcg_args& a, int max_iter, double rtol, cudaStr
     int64_t g = std::min<int64_t>((int64_t)sms * std::max(1, std::min(per_sm, 2)), kDotBlocks);
     g = std::min<int64_t>(g, std::max<int64_t>(1, (n + kSolveThreads / L - 1) / (kSolveThreads / L)));
     // barrier words after the three partial arrays start at zero
-    if (cudaMemsetAsync(a.partials + 3 * kDotBlocks, 0, (2 + kBarrierGroups) * sizeof(unsigned), st) != cudaSuccess)
+    if (cudaMemsetAsync(a.partials + 3 * kDotBlocks, 0, sizeof(unsigned), st) != cudaSuccess)
         return status("tm_pcg_iterate_until: memset");
     const double tol2 = rtol * rtol;
     void* params[] = {const_cast<tm_pcg_args*>(&a), &max_iter, const_cast<double*>(&tol2)};
