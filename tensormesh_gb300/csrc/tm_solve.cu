@@ -105,6 +105,24 @@ __device__ __forceinline__ double lane_sum(double s) {
     return s;
 }
 
+// reduce-scatter of the H (<= 4) sums s[] over the 4 lanes of a group: lane
+// k < H returns the group's sum of s[k], grouped (s_k[0] + s_k[2]) +
+// (s_k[1] + s_k[3]) exactly as lane_sum<4> groups it, with 3 adds per lane
+// instead of 2H (float64 adds are the scarce resource of this kernel)
+template <int H>
+__device__ __forceinline__ double group4_scatter(const double (&s)[H], int lane) {
+    static_assert(H >= 1 && H <= 4, "group4_scatter takes 1..4 sums");
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int c = 0; c < H; ++c) t[c] = s[c];
+    const bool hi = (lane & 2) != 0, odd = (lane & 1) != 0;
+    // lanes l and l^2: the low lane keeps sums 0 and 1, the high lane 2 and 3
+    const double ta = (hi ? t[2] : t[0]) + __shfl_xor_sync(0xffffffffu, hi ? t[0] : t[2], 2, 4);
+    const double tb = (hi ? t[3] : t[1]) + __shfl_xor_sync(0xffffffffu, hi ? t[1] : t[3], 2, 4);
+    // lanes l and l^1: the even lane keeps the first, the odd lane the second
+    return (odd ? tb : ta) + __shfl_xor_sync(0xffffffffu, odd ? ta : tb, 1, 4);
+}
+
 // q = A p ; partial[blk] = sum p.q over this block's rows (in row order)
 template <typename R, int H>
 __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A, const R* p, R* q,
@@ -129,6 +147,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A
         // 4-lane groups, one block row each; the 8-lane slots of red hold
         // the sums of pairs of groups
         constexpr int L = kBlockLanes;
+        static_assert(L == 4, "block rows are summed by group4_scatter");
         const int bl = threadIdx.x & (L - 1), bg = threadIdx.x / L;
         const int64_t nb = A.n_rows, groups_total = (int64_t)gridDim.x * (kSolveThreads / L);
         for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
@@ -140,17 +159,13 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A
 #pragma unroll
                 for (int c = 0; c < H; ++c) s[c] = 0;
             }
-#pragma unroll
-            for (int c = 0; c < H; ++c) s[c] = lane_sum<L>(s[c]);
-            if (bi >= 0 && bl == 0) {
-#pragma unroll
-                for (int c = 0; c < H; ++c) {
-                    q[bi * H + c] = (R)s[c];
-                    acc += s[c] * (double)p[bi * H + c];
-                }
+            const double u = group4_scatter<H>(s, bl);     // row bi * H + bl on lanes bl < H
+            if (bi >= 0 && bl < H) {
+                q[bi * H + bl] = (R)u;
+                acc += u * (double)p[bi * H + bl];
             }
         }
-        acc += __shfl_xor_sync(0xffffffffu, acc, 4, 8);   // lane 0 of each 8-lane slot: both groups' sums
+        acc = lane_sum<8>(acc);   // lane 0 of each 8-lane slot: both groups' sums
     }
     if (lane == 0) red[grp] = acc;
     __syncthreads();
@@ -375,6 +390,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_op(tm_linear_operator A,
         }
     } else {
         constexpr int L = kBlockLanes;
+        static_assert(L == 4, "block rows are summed by group4_scatter");
         const int lane = threadIdx.x & (L - 1), grp = threadIdx.x / L;
         const int64_t nb = A.n_rows, groups_total = (int64_t)gridDim.x * (kSolveThreads / L);
         for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
@@ -386,14 +402,10 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_op(tm_linear_operator A,
 #pragma unroll
                 for (int c = 0; c < H; ++c) s[c] = 0;
             }
-#pragma unroll
-            for (int c = 0; c < H; ++c) s[c] = lane_sum<L>(s[c]);
-            if (bi >= 0 && lane == 0) {
-#pragma unroll
-                for (int c = 0; c < H; ++c) {
-                    const int64_t r = bi * H + c;
-                    y[r] = (R)(beta == 0.0 ? alpha * s[c] : alpha * s[c] + beta * (double)y[r]);
-                }
+            const double u = group4_scatter<H>(s, lane);   // row bi * H + lane on lanes < H
+            if (bi >= 0 && lane < H) {
+                const int64_t r = bi * H + lane;
+                y[r] = (R)(beta == 0.0 ? alpha * u : alpha * u + beta * (double)y[r]);
             }
         }
     }
@@ -578,14 +590,20 @@ __global__ void __launch_bounds__(kSolveThreads, 2) k_pcg_persistent(const tm_pc
 #pragma unroll
                     for (int c = 0; c < H; ++c) s[c] = 0;
                 }
-#pragma unroll
-                for (int c = 0; c < H; ++c) s[c] = lane_sum<L>(s[c]);
-                if (bi >= 0 && lane == 0) {
+                double u;
+                if constexpr (L == 4) {
+                    u = group4_scatter<H>(s, lane);          // row bi * H + lane on lanes < H
+                } else {
+                    u = 0;
 #pragma unroll
                     for (int c = 0; c < H; ++c) {
-                        __stcg(q + bi * H + c, (R)s[c]);
-                        acc += s[c] * (double)__ldcg(p + bi * H + c);
+                        const double t = lane_sum<L>(s[c]);
+                        if (lane == c) u = t;
                     }
+                }
+                if (bi >= 0 && lane < H) {
+                    __stcg(q + bi * H + lane, (R)u);
+                    acc += u * (double)__ldcg(p + bi * H + lane);
                 }
             }
         }
