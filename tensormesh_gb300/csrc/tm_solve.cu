@@ -70,6 +70,15 @@ __device__ __forceinline__ double group_sum(double s) {
     return s;
 }
 
+// first row position of this block's chunk of `per` rows in pass `pass`:
+// odd passes hand the chunks out in reverse block order, so that with rows
+// sorted longest first no block takes the longest chunk of every pass; a
+// block whose chunk starts past the end has none in later passes either
+__device__ __forceinline__ int64_t serpentine_base(int64_t pass, int per) {
+    const int64_t b = (pass & 1) ? (int64_t)(gridDim.x - 1 - blockIdx.x) : (int64_t)blockIdx.x;
+    return (pass * gridDim.x + b) * per;
+}
+
 // the H partial sums of block row `br` of A x: lane l of the L-lane group
 // takes blocks row_ptr[br] + l, + 2L, ...; each block is read once (its H*H
 // values, one column index, H entries of x), and every scalar row sums its
@@ -133,8 +142,9 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A
     const bool stop = scal && scal[S_FLAG] != 0.0;
     double acc = 0;
     if (!stop && H == 1) {
-        const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
-        for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
+        for (int64_t pass = 0;; ++pass) {
+            const int64_t base = serpentine_base(pass, kSolveThreads / 8);
+            if (base >= n) break;
             const int64_t r = base + grp < n ? row_at(A, base + grp) : -1;
             // all 8 lanes of a group share r; the loop bound is uniform per block
             const double s = group_sum(r >= 0 ? row_partial<R, H>(A, p, r, lane) : 0.0);
@@ -149,8 +159,10 @@ __global__ void __launch_bounds__(kSolveThreads) k_spmv_dot(tm_linear_operator A
         constexpr int L = kBlockLanes;
         static_assert(L == 4, "block rows are summed by group4_scatter");
         const int bl = threadIdx.x & (L - 1), bg = threadIdx.x / L;
-        const int64_t nb = A.n_rows, groups_total = (int64_t)gridDim.x * (kSolveThreads / L);
-        for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
+        const int64_t nb = A.n_rows;
+        for (int64_t pass = 0;; ++pass) {
+            const int64_t base = serpentine_base(pass, kSolveThreads / L);
+            if (base >= nb) break;
             const int64_t bi = base + bg < nb ? row_at(A, base + bg) : -1;
             double s[H];
             if (bi >= 0) {
@@ -564,13 +576,14 @@ __global__ void __launch_bounds__(kSolveThreads, 2) k_pcg_persistent(const tm_pc
     int flag = (int)scal[S_FLAG];
     if (flag == 0 && rr <= tol2 * bb) flag = 1;
     const int lane = threadIdx.x & (L - 1), grp = threadIdx.x / L;
-    const int64_t groups_total = (int64_t)G * (kSolveThreads / L);
     const int64_t stride = (int64_t)G * blockDim.x;
     for (int it = 0; it < max_iter && flag == 0; ++it) {
         // q = A p and this block's part of p.q
         double acc = 0;
         if constexpr (H == 1) {
-            for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < n; base += groups_total) {
+            for (int64_t pass = 0;; ++pass) {
+                const int64_t base = serpentine_base(pass, kSolveThreads / L);
+                if (base >= n) break;
                 const int64_t i = base + grp < n ? row_at(a.A, base + grp) : -1;
                 const double s = lane_sum<L>(i >= 0 ? row_partial_cg<R, H, L>(a.A, p, i, lane) : 0.0);
                 if (i >= 0 && lane == 0) {
@@ -581,7 +594,9 @@ __global__ void __launch_bounds__(kSolveThreads, 2) k_pcg_persistent(const tm_pc
         } else {
             // one group per block row: H rows of q from one pass over the blocks
             const int64_t nb = a.A.n_rows;
-            for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
+            for (int64_t pass = 0;; ++pass) {
+                const int64_t base = serpentine_base(pass, kSolveThreads / L);
+                if (base >= nb) break;
                 const int64_t bi = base + grp < nb ? row_at(a.A, base + grp) : -1;
                 double s[H];
                 if (bi >= 0) {
