@@ -410,8 +410,9 @@ def run_inverse(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
-ELASTIC_WORKLOAD = ("elasticity_p2tet_32: P2 tet isotropic elasticity (10-node tets, E ~ U[0.5, 2] per element, "
-                    "nu = 0.3), 32^3 cubes x 6 Kuhn, 196,608 elements, 274,625 nodes, 3x3 blocks, FP64")
+def _elastic_name(n):
+    return (f"elasticity_p2tet_{n}: P2 tet isotropic elasticity (10-node tets, E ~ U[0.5, 2] per element, "
+            f"nu = 0.3), {n}^3 cubes x 6 Kuhn, {6 * n ** 3:,} elements, {(2 * n + 1) ** 3:,} nodes, 3x3 blocks, FP64")
 
 
 def elasticity_bytes(N, E, nnz, B=10):
@@ -437,7 +438,7 @@ def run_elasticity(args, ws, rank, local):
     from tensormesh_gb300 import workloads as W
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    wl = W.elasticity_p2tet(32)
+    wl = W.elasticity_p2tet(args.elastic_n)
     mesh = wl.mesh.to(dev)
     Ey = wl.data["E"].to(dev)
     t0 = time.perf_counter()
@@ -511,7 +512,7 @@ def run_elasticity(args, ws, rank, local):
             "value": E * ws / (ms * 1e-3), "unit": "elements/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kuhn-split cube, uniform E)",
-            "config": {"workload": ELASTIC_WORKLOAD, "elements": E, "nodes": N, "nnz": nnz,
+            "config": {"workload": _elastic_name(args.elastic_n), "elements": E, "nodes": N, "nnz": nnz,
                        "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas x{ws}"},
             "e2e": {"value": E * ws / (e2e_ms * 1e-3), "unit": "elements/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": pts_h.numel() * 8 + E_h.numel() * 8, "d2h_bytes_per_step": nnz * 8},
@@ -530,6 +531,65 @@ def run_elasticity(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def _elastic_system(n, dev):
+    """The condensed P2-tet elasticity system (clamped face z = 0, body force
+    (0, 0, -1)) at n^3 cubes x 6."""
+    import tensormesh_gb300 as tg
+    from tensormesh_gb300 import workloads as W
+    wl = W.elasticity_p2tet(n)
+    mesh = wl.mesh.to(dev)
+    K = tg.LinearElasticityElementAssembler.from_mesh(mesh, nu=0.3)(mesh.points, element_data={"E": wl.data["E"].to(dev)})
+    b = tg.const_node_assembler(torch.tensor([0.0, 0.0, -1.0])).from_mesh(mesh)(mesh.points)
+    clamp = (mesh.points[:, 2] == 0.0).repeat_interleave(3)
+    return tg.Condenser(clamp)(K, b)
+
+
+def run_spmv(args, ws, rank, local):
+    """The solver's operator kernel: y = A x on the condensed P2-tet
+    elasticity system (3x3 block rows, FP64), one step = one SpMV through
+    tm_spmv.  Its roofline: the values, block columns, row pointers and
+    row order once, x and y once (bytes), against 2 flops per stored value
+    (float64 FMAs, which bind first on this GPU)."""
+    from tensormesh_gb300 import solve as S
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    Kc, bc = _elastic_system(args.elastic_n, dev)
+    x = torch.randn(bc.numel(), dtype=torch.float64, device=dev)
+    y = torch.empty_like(x)
+    for _ in range(args.warmup):
+        S.spmv(Kc, x, y)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        starts[k].record()
+        S.spmv(Kc, x, y)
+        ends[k].record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = statistics.mean(s.elapsed_time(e) for s, e in zip(starts, ends))
+    n, nnz = bc.numel(), Kc.values.numel()
+    nb = n // 3
+    abytes = 8 * nnz + 4 * (nnz // 9) + 8 * (nb + 1) + 4 * nb + 16 * n
+    peak, peak_kind = _peaks()
+    line = {"metric": "condensed P2-tet elasticity SpMVs/s (3x3 block rows, FP64)", "value": 1e3 / ms,
+            "unit": "SpMV/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Kuhn-split cube, uniform E; random x)",
+            "config": {"workload": f"elasticity_p2tet_{args.elastic_n} condensed operator: {n} unknowns, "
+                                   f"{nnz} values", "l2": "inputs larger than L2 (values alone)"},
+            "roofline": {"bound": "hbm", "achieved": abytes / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": abytes / (ms * 1e-3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "k_spmv_op", "algorithmic_bytes": abytes,
+                         "fp64_gflops": 2.0 * nnz / (ms * 1e-3) / 1e9},
+            "clocks": clocks, "gpu_launches": args.steps}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_reference_elasticity(args, ws, rank, local):
     """The reference's per-call elasticity work (restated in torch,
     oracle/fem_oracle.py) on the host cores over a bounded sample (1/16 of
@@ -541,7 +601,7 @@ def run_reference_elasticity(args, ws, rank, local):
     from tensormesh_gb300 import workloads as W
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
-    wl = W.elasticity_p2tet(32)
+    wl = W.elasticity_p2tet(args.elastic_n)
     pts, conn, Ey = wl.mesh.points, wl.mesh.elements(), wl.data["E"]
     edges, slot = O.element_pattern(conn, wl.mesh.n_points)
     E = conn.shape[0]
@@ -558,7 +618,7 @@ def run_reference_elasticity(args, ws, rank, local):
             "value": Es / s, "unit": "elements/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded Kuhn-split cube, uniform E)",
-            "config": {"workload": ELASTIC_WORKLOAD, "elements": E, "parallelism": "host cores"},
+            "config": {"workload": _elastic_name(args.elastic_n), "elements": E, "parallelism": "host cores"},
             "cpu_baseline": {"value": Es / s, "unit": "elements/s", "cores": threads, "kind": "port",
                              "sample": f"{Es} of {E} elements per step (block K into the full pattern, incl. "
                                        f"the per-call from_block_coo layout hash), reference op sequence restated "
@@ -654,7 +714,9 @@ def main():
     ap.add_argument("--no-gpu-reference", action="store_true")
     ap.add_argument("--cubes", type=int, default=64, help="cubes per side of the Kuhn-split cube (64: 1,572,864 elements)")
     ap.add_argument("--workload", default="diffusion_mass",
-                    choices=["diffusion_mass", "elasticity", "inverse", "batched"])
+                    choices=["diffusion_mass", "elasticity", "spmv", "inverse", "batched"])
+    ap.add_argument("--elastic-n", type=int, default=32,
+                    help="cubes per side of the P2-tet elasticity workload (32: 196,608 elements)")
     ap.add_argument("--meshes", type=int, default=512)
     ap.add_argument("--sample", type=int, default=32)
     args = ap.parse_args()
@@ -665,6 +727,8 @@ def main():
         run_reference(args, ws, rank, local)
     elif args.workload == "elasticity":
         run_elasticity(args, ws, rank, local)
+    elif args.workload == "spmv":
+        run_spmv(args, ws, rank, local)
     elif args.workload == "inverse":
         run_inverse(args, ws, rank, local)
     elif args.workload == "batched":
