@@ -39,6 +39,8 @@ typedef struct CUstream_st* tm_stream_t;   /* == cudaStream_t */
 #define TM_TET4   1   /* "tetra"     */
 #define TM_TRI6   2   /* "triangle6" */
 #define TM_TET10  3   /* "tetra10"   */
+#define TM_QUAD4  4   /* "quad": bilinear on [0,1]^2, nodes (0,0) (1,0) (0,1) (1,1) (element/element.py:1801-1816) */
+#define TM_QUAD9  5   /* "quad9": biquadratic; vertices, mid-points of edges [[0,1],[0,2],[1,3],[2,3]], centre */
 
 /* ---- floating types ---------------------------------------------------- */
 #define TM_F64 0

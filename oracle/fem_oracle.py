@@ -73,21 +73,48 @@ _TET_P = {
 ELEMENT = {  # type -> (dim, order, n_basis)   (element/element_type.py:57-87)
     "triangle": (2, 1, 3), "triangle6": (2, 2, 6),
     "tetra": (3, 1, 4), "tetra10": (3, 2, 10),
+    "quad": (2, 1, 4), "quad9": (2, 2, 9),
 }
+_QUADS = ("quad", "quad9")
+_QUAD_VERTS = [[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [1.0, 1.0]]  # element.py:1811
+_QUAD_EDGE = [[0, 1], [0, 2], [1, 3], [2, 3]]                   # element.py:1813
 _TRI_EDGE = [[1, 2], [0, 2], [0, 1]]                          # element.py:1684
 _TET_EDGE = [[2, 3], [1, 3], [1, 2], [0, 3], [0, 2], [0, 1]]  # element.py:1949
 
 
 def quadrature(etype: str, order: int) -> Tuple[torch.Tensor, torch.Tensor]:
+    if etype in _QUADS:
+        return quad_quadrature(order)
     dim = ELEMENT[etype][0]
     w, p = (_TRI_W, _TRI_P) if dim == 2 else (_TET_W, _TET_P)
     return torch.tensor(w[order], dtype=DT), torch.tensor(p[order], dtype=DT)
 
 
+def quad_quadrature(order: int) -> Tuple[torch.Tensor, torch.Tensor]:
+    """element/quadrature.py:169-203: the line rule on [0, 1] in each
+    direction, torch.meshgrid(..., indexing='xy') flattened (x fastest)."""
+    w1, p1 = _facet_rule(2, order)
+    wx, wy = torch.meshgrid(w1, w1, indexing="xy")
+    px, py = torch.meshgrid(p1[:, 0], p1[:, 0], indexing="xy")
+    return (wx * wy).flatten(), torch.stack([px.flatten(), py.flatten()], -1)
+
+
+def n_vertices(etype: str) -> int:
+    return 4 if etype in _QUADS else ELEMENT[etype][0] + 1
+
+
 def basis_nodes(etype: str) -> torch.Tensor:
     """Reference-element nodes: vertices, then edge mid-points in the
-    element's edge order (element/basis.py:639-695, 750-860)."""
+    element's edge order (element/basis.py:639-695, 750-860); for
+    quadrilaterals the lexicographic vertices, the mid-points of their edges
+    and the centre (element/basis.py:697-748)."""
     dim, order, _ = ELEMENT[etype]
+    if etype in _QUADS:
+        verts = torch.tensor(_QUAD_VERTS, dtype=DT)
+        if order == 1:
+            return verts
+        mids = torch.stack([(verts[a] + verts[b]) / 2 for a, b in _QUAD_EDGE])
+        return torch.cat([verts, mids, verts.mean(0, keepdim=True)], 0)
     verts = torch.cat([torch.zeros(1, dim, dtype=DT), torch.eye(dim, dtype=DT)], 0)
     if order == 1:
         return verts
@@ -96,17 +123,26 @@ def basis_nodes(etype: str) -> torch.Tensor:
     return torch.cat([verts, mids], 0)
 
 
-def _monomials(dim: int, order: int):
+def _monomials(dim: int, order: int, tensor: bool = False):
+    """Exponents by total degree (element/polynomial.py): complete
+    polynomials of degree ``order`` for simplices, every exponent up to
+    ``order`` in each variable for the tensor-product (quadrilateral) space."""
     exps = []
-    for tot in range(order + 1):
+    for tot in range((dim if tensor else 1) * order + 1):
         if dim == 2:
             for a in range(tot, -1, -1):
-                exps.append((a, tot - a))
+                if not tensor or (a <= order and tot - a <= order):
+                    exps.append((a, tot - a))
         else:
             for a in range(tot, -1, -1):
                 for b in range(tot - a, -1, -1):
                     exps.append((a, b, tot - a - b))
     return exps
+
+
+def element_monomials(etype: str):
+    dim, order, _ = ELEMENT[etype]
+    return _monomials(dim, order, tensor=etype in _QUADS)
 
 
 def _eval_monomials(exps, pts: torch.Tensor) -> torch.Tensor:
@@ -135,7 +171,7 @@ def shape_tables(etype: str, qorder: int):
     matrix at the basis nodes (element/element.py:557-716, 804-872)."""
     dim, order, nb = ELEMENT[etype]
     w, q = quadrature(etype, qorder)
-    exps = _monomials(dim, order)
+    exps = element_monomials(etype)
     V = _eval_monomials(exps, basis_nodes(etype))        # [B, n_mono]
     coef = torch.linalg.inv(V).T                          # element.py:657
     phi = _eval_monomials(exps, q) @ coef.T               # [Q, B]
@@ -307,11 +343,20 @@ def assemble_load(points, conn, etype, n_points, f_nodes=None, const=None, func=
 # Gauss-Legendre on [-1, 1] (element/quadrature.py:36-53), mapped to [0, 1]
 _GL_W = {1: [2.0], 2: [1.0, 1.0],
          3: [0.55555555555555555556, 0.88888888888888888889, 0.55555555555555555556],
-         4: [0.34785484513745385737, 0.65214515486254614263, 0.65214515486254614263, 0.34785484513745385737]}
+         4: [0.34785484513745385737, 0.65214515486254614263, 0.65214515486254614263, 0.34785484513745385737],
+         5: [0.23692688505618908751, 0.47862867049936646804, 0.56888888888888888889, 0.47862867049936646804,
+             0.23692688505618908751]}
 _GL_P = {1: [0.0], 2: [-0.57735026918962576451, 0.57735026918962576451],
          3: [-0.77459666924148337704, 0.0, 0.77459666924148337704],
-         4: [-0.8611363115940526, -0.3399810435848563, 0.3399810435848563, 0.8611363115940526]}
+         4: [-0.8611363115940526, -0.3399810435848563, 0.3399810435848563, 0.8611363115940526],
+         5: [-0.9061798459386640, -0.5384693101056831, 0.0, 0.5384693101056831, 0.9061798459386640]}
 _FACET_VERTS = {2: [[0, 1], [1, 2], [2, 0]], 3: [[0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]]}
+
+
+def facet_vertices(etype):
+    """Vertex lists of the element's facets (quadrilaterals: its edges,
+    element.py:1813)."""
+    return _QUAD_EDGE if etype in _QUADS else _FACET_VERTS[ELEMENT[etype][0]]
 
 
 def _facet_rule(dim, qorder):
@@ -327,12 +372,13 @@ def facet_nodes(etype):
     """Local nodes of each facet: its vertices, then (P2) the element's edge
     nodes whose two ends are both facet vertices."""
     dim, order, _ = ELEMENT[etype]
-    edges = _TRI_EDGE if dim == 2 else _TET_EDGE
+    edges = _QUAD_EDGE if etype in _QUADS else (_TRI_EDGE if dim == 2 else _TET_EDGE)
+    nv = n_vertices(etype)
     out = []
-    for vs in _FACET_VERTS[dim]:
+    for vs in facet_vertices(etype):
         nodes = list(vs)
         if order == 2:
-            nodes += [dim + 1 + k for k, (a, b) in enumerate(edges) if a in vs and b in vs]
+            nodes += [nv + k for k, (a, b) in enumerate(edges) if a in vs and b in vs]
         out.append(nodes)
     return out
 
@@ -350,8 +396,8 @@ def assemble_facet_load(points, conn, etype, boundary, n_points, qorder=2, f_nod
     length W, ``func`` a function of x_q."""
     dim, order, nb = ELEMENT[etype]
     conn = conn.long()
-    verts = basis_nodes(etype)[:dim + 1]                 # reference vertex coordinates
-    exps = _monomials(dim, order)
+    verts = basis_nodes(etype)[:n_vertices(etype)]       # reference vertex coordinates
+    exps = element_monomials(etype)
     coef = torch.linalg.inv(_eval_monomials(exps, basis_nodes(etype))).T
     wf, tf = _facet_rule(dim, qorder)
     width = 1
@@ -360,7 +406,7 @@ def assemble_facet_load(points, conn, etype, boundary, n_points, qorder=2, f_nod
     if const is not None and torch.as_tensor(const).dim() == 1:
         width = torch.as_tensor(const).numel()
     out = torch.zeros(n_points, width, dtype=DT)
-    for k, (vs, fnodes) in enumerate(zip(_FACET_VERTS[dim], facet_nodes(etype))):
+    for k, (vs, fnodes) in enumerate(zip(facet_vertices(etype), facet_nodes(etype))):
         sel = boundary[conn[:, fnodes]].all(1)
         if not bool(sel.any()):
             continue

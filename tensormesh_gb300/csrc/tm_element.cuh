@@ -17,6 +17,8 @@ template <> struct Traits<TM_TRI3>  { static constexpr int D = 2, B = 3,  P1 = 1
 template <> struct Traits<TM_TET4>  { static constexpr int D = 3, B = 4,  P1 = 1; };
 template <> struct Traits<TM_TRI6>  { static constexpr int D = 2, B = 6,  P1 = 0; };
 template <> struct Traits<TM_TET10> { static constexpr int D = 3, B = 10, P1 = 0; };
+template <> struct Traits<TM_QUAD4> { static constexpr int D = 2, B = 4,  P1 = 0; };
+template <> struct Traits<TM_QUAD9> { static constexpr int D = 2, B = 9,  P1 = 0; };
 
 // offsets (in doubles) of the packed reference tables
 struct TableLayout {

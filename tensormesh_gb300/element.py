@@ -3,16 +3,24 @@ tables the CUDA kernels read.
 
 Element types follow the reference's strings (``element/element_type.py``):
 ``"triangle"`` (P1, 3 nodes), ``"triangle6"`` (P2, 6 nodes), ``"tetra"``
-(P1, 4 nodes), ``"tetra10"`` (P2, 10 nodes).  Node order is vertices first,
-then one node per edge in the order ``Triangle.edge`` = [[1,2],[0,2],[0,1]]
+(P1, 4 nodes), ``"tetra10"`` (P2, 10 nodes), ``"quad"`` (Q1, 4 nodes) and
+``"quad9"`` (Q2, 9 nodes).  Simplex node order is vertices first, then one
+node per edge in the order ``Triangle.edge`` = [[1,2],[0,2],[0,1]]
 (``element/element.py:1684``) and ``Tetrahedron.edge`` =
 [[2,3],[1,3],[1,2],[0,3],[0,2],[0,1]] (``element/element.py:1949``).
+Quadrilaterals live on [0,1]^2 with the vertices in lexicographic order
+(0,0), (1,0), (0,1), (1,1), then for Q2 the mid-points of
+``Quadrilateral.edge`` = [[0,1],[0,2],[1,3],[2,3]] and the centre
+(``element/element.py:1801-1816``, ``element/basis.py:697-748``); their
+rule is the tensor product of the Gauss-Legendre line rule of the same
+order (``element/quadrature.py:169-203``: points x fastest).
 
-Shape functions are written in barycentric form (lambda_0 = 1 - sum xi,
-lambda_k = xi_k): vertex ``i`` has ``lambda_i (2 lambda_i - 1)`` and edge
-``(a,b)`` has ``4 lambda_a lambda_b`` for P2.  The reference obtains the
-same polynomials by inverting a monomial Vandermonde matrix
-(``element/element.py:557-659``); the two agree to rounding.
+Shape functions are written in barycentric form for simplices (lambda_0 =
+1 - sum xi, lambda_k = xi_k): vertex ``i`` has ``lambda_i (2 lambda_i - 1)``
+and edge ``(a,b)`` has ``4 lambda_a lambda_b`` for P2; quadrilaterals use
+products of the 1-D Lagrange polynomials on the nodes 0, 1 (and 1/2).  The
+reference obtains the same polynomials by inverting a monomial Vandermonde
+matrix (``element/element.py:557-659``); the two agree to rounding.
 
 Quadrature tables are the reference's decimal tables for orders 1-4
 (``element/quadrature.py:68-166``), kept identical so that both sides
@@ -55,6 +63,13 @@ TET_QUAD = {
 
 TRI_EDGES = ((1, 2), (0, 2), (0, 1))
 TET_EDGES = ((2, 3), (1, 3), (1, 2), (0, 3), (0, 2), (0, 1))
+QUAD_EDGES = ((0, 1), (0, 2), (1, 3), (2, 3))
+# reference coordinates of the quadrilateral nodes (element/basis.py:697-748)
+QUAD_NODES = {
+    1: ((0.0, 0.0), (1.0, 0.0), (0.0, 1.0), (1.0, 1.0)),
+    2: ((0.0, 0.0), (1.0, 0.0), (0.0, 1.0), (1.0, 1.0),
+        (0.5, 0.0), (0.0, 0.5), (1.0, 0.5), (0.5, 1.0), (0.5, 0.5)),
+}
 
 
 @dataclass(frozen=True)
@@ -71,7 +86,10 @@ ELEMENTS: Dict[str, ElementInfo] = {
     "tetra": ElementInfo("tetra", 1, 3, 1, 4),
     "triangle6": ElementInfo("triangle6", 2, 2, 2, 6),
     "tetra10": ElementInfo("tetra10", 3, 3, 2, 10),
+    "quad": ElementInfo("quad", 4, 2, 1, 4),
+    "quad9": ElementInfo("quad9", 5, 2, 2, 9),
 }
+QUADRILATERALS = ("quad", "quad9")
 # element_type2dimension / element_type2order of the reference, for the
 # types this package assembles
 element_type2dimension = {k: v.dim for k, v in ELEMENTS.items()}
@@ -88,6 +106,11 @@ def element_info(etype: str) -> ElementInfo:
 
 def quadrature(etype: str, order: int) -> Tuple[np.ndarray, np.ndarray]:
     info = element_info(etype)
+    if etype in QUADRILATERALS:
+        w1, p1 = line_quadrature(order)
+        wx, wy = np.meshgrid(w1, w1, indexing="xy")
+        px, py = np.meshgrid(p1[:, 0], p1[:, 0], indexing="xy")
+        return (wx * wy).ravel(), np.stack([px.ravel(), py.ravel()], 1)
     table = TRI_QUAD if info.dim == 2 else TET_QUAD
     if order not in table:
         raise NotImplementedError(f"quadrature order {order} is not tabulated (orders {sorted(table)})")
@@ -103,9 +126,37 @@ def _barycentric(xi: np.ndarray):
     return lam, dlam
 
 
+def _lagrange_1d(order: int, node: float, s: np.ndarray):
+    """The 1-D Lagrange polynomial of ``node`` on the nodes {0, 1} (order 1)
+    or {0, 1, 1/2} (order 2) and its derivative, at s."""
+    if order == 1:
+        return (s, np.ones_like(s)) if node == 1.0 else (1.0 - s, -np.ones_like(s))
+    if node == 0.0:
+        return (1.0 - s) * (1.0 - 2.0 * s), 4.0 * s - 3.0
+    if node == 1.0:
+        return s * (2.0 * s - 1.0), 4.0 * s - 1.0
+    return 4.0 * s * (1.0 - s), 4.0 - 8.0 * s
+
+
+def _quad_shape_functions(order: int, xi: np.ndarray):
+    Q = xi.shape[0]
+    nodes = QUAD_NODES[order]
+    phi = np.zeros((Q, len(nodes)))
+    dphi = np.zeros((Q, 2, len(nodes)))
+    for b, (nx, ny) in enumerate(nodes):
+        lx, dx = _lagrange_1d(order, nx, xi[:, 0])
+        ly, dy = _lagrange_1d(order, ny, xi[:, 1])
+        phi[:, b] = lx * ly
+        dphi[:, 0, b] = dx * ly
+        dphi[:, 1, b] = lx * dy
+    return phi, dphi
+
+
 def shape_functions(etype: str, xi: np.ndarray):
     """phi [Q, B] and dphi [Q, D, B] (dphi[q, i, b] = d phi_b / d xi_i)."""
     info = element_info(etype)
+    if etype in QUADRILATERALS:
+        return _quad_shape_functions(info.order, np.asarray(xi, dtype=np.float64))
     lam, dlam = _barycentric(np.asarray(xi, dtype=np.float64))
     Q, D = xi.shape
     if info.order == 1:
@@ -211,6 +262,10 @@ def _facet_nodes(etype: str):
             out.append((a, b, c, _edge_node(b, c, TET_EDGES, 4), _edge_node(a, c, TET_EDGES, 4),
                         _edge_node(a, b, TET_EDGES, 4)))
         return out
+    if etype == "quad":
+        return list(QUAD_EDGES)
+    if etype == "quad9":
+        return [(a, b, 4 + k) for k, (a, b) in enumerate(QUAD_EDGES)]
     raise NotImplementedError(f"facets of {etype!r}")
 
 

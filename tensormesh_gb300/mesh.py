@@ -12,7 +12,8 @@ use; the generators below produce the structured meshes the benchmark
 workloads are defined on:
 
 * ``gen_unit_square(n)``: an (n+1)x(n+1) grid on [0,1]^2, every cell split
-  into two triangles along its (0,0)-(1,1) diagonal.
+  into two triangles along its (0,0)-(1,1) diagonal, or kept as one
+  quadrilateral (``cell="quad"``).
 * ``gen_unit_cube(n)``: an (n+1)^3 grid on [0,1]^3, every cube split into
   six tetrahedra that share the cube's main diagonal (Kuhn split).
 * ``order=2`` adds the edge mid-points in the reference's node order:
@@ -38,9 +39,10 @@ _CUBE_VERTS = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
 _KUHN_TETS = np.array([[0, 1, 2, 6], [0, 2, 3, 6], [0, 3, 7, 6],
                        [0, 7, 4, 6], [0, 4, 5, 6], [0, 5, 1, 6]], dtype=np.int64)
 _TRI_EDGES = np.array([[1, 2], [0, 2], [0, 1]], dtype=np.int64)
+_QUAD_EDGES = ((0, 1), (0, 2), (1, 3), (2, 3))
 _TET_EDGES = np.array([[2, 3], [1, 3], [1, 2], [0, 3], [0, 2], [0, 1]], dtype=np.int64)
 
-ELEMENT_DIM = {"triangle": 2, "triangle6": 2, "tetra": 3, "tetra10": 3}
+ELEMENT_DIM = {"triangle": 2, "triangle6": 2, "tetra": 3, "tetra10": 3, "quad": 2, "quad9": 2}
 
 
 class Mesh:
@@ -53,7 +55,7 @@ class Mesh:
     cells : dict
         ``{element_type: LongTensor[E, B]}``; element types are the
         reference's strings ``"triangle"``, ``"triangle6"``, ``"tetra"``,
-        ``"tetra10"``.
+        ``"tetra10"``, ``"quad"``, ``"quad9"``.
     point_data : dict, optional
         Nodal fields; ``"is_boundary"`` is what ``boundary_mask`` returns.
     """
@@ -153,12 +155,16 @@ def _jitter(points: np.ndarray, boundary: np.ndarray, amount: float, h: float,
 
 
 def gen_unit_square(n: int, order: int = 1, jitter: float = 0.0, seed: int = 0,
-                    dtype: torch.dtype = torch.float64, device="cpu") -> Mesh:
-    """Triangulated unit square with ``n`` cells per side.
+                    dtype: torch.dtype = torch.float64, device="cpu", cell: str = "triangle") -> Mesh:
+    """Unit square with ``n`` cells per side, triangulated (``cell=
+    "triangle"``) or as quadrilaterals (``cell="quad"``).
 
     Cell (i, j) with corners a=(i,j), b=(i+1,j), c=(i+1,j+1), d=(i,j+1)
-    becomes the triangles (a,b,c) and (a,c,d). ``jitter`` moves interior
-    vertices by U(-jitter*h, jitter*h) per coordinate (h = 1/n).
+    becomes the triangles (a,b,c) and (a,c,d), or the quadrilateral
+    (a,b,d,c) in the reference's lexicographic vertex order (for ``order=2``
+    followed by the mid-points of its edges [[0,1],[0,2],[1,3],[2,3]] and
+    its centre: types ``"quad"`` / ``"quad9"``).  ``jitter`` moves interior
+    nodes by U(-jitter*h, jitter*h) per coordinate (h = 1/(order*n)).
     """
     s = order                      # node grid has s*n cells per side
     m = s * n
@@ -166,6 +172,24 @@ def gen_unit_square(n: int, order: int = 1, jitter: float = 0.0, seed: int = 0,
     idx = lambda i, j: j * (m + 1) + i
     i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="xy")
     i, j = i.ravel() * s, j.ravel() * s
+    if cell == "quad":
+        h = s // 2
+        corners = [(i, j), (i + s, j), (i, j + s), (i + s, j + s)]
+        conn = [idx(x, y) for x, y in corners]
+        etype = "quad"
+        if order == 2:
+            for (p, q) in _QUAD_EDGES:
+                conn.append(idx((corners[p][0] + corners[q][0]) // 2, (corners[p][1] + corners[q][1]) // 2))
+            conn.append(idx(i + h, j + h))
+            etype = "quad9"
+        conn = np.stack(conn, axis=1)
+        bnd = _boundary(pts)
+        pts = _jitter(pts, bnd, jitter, 1.0 / m, seed)
+        return Mesh(torch.tensor(pts, dtype=dtype, device=device),
+                    {etype: torch.from_numpy(conn).to(device)},
+                    {"is_boundary": torch.from_numpy(bnd).to(device)})
+    if cell != "triangle":
+        raise ValueError(f"cell must be 'triangle' or 'quad', got {cell!r}")
     a, b, c, d = (np.array([i, j]), np.array([i + s, j]),
                   np.array([i + s, j + s]), np.array([i, j + s]))
     tris = []

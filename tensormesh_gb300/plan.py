@@ -144,8 +144,34 @@ CHUNK_ELEMS = {
     ("tetra", False): 384, ("tetra", True): 128,
     ("triangle6", False): 64, ("triangle6", True): 64,
     ("tetra10", False): 32, ("tetra10", True): 32,
+    ("quad", False): 128, ("quad", True): 128,
+    ("quad9", False): 64, ("quad9", True): 64,
 }
-NODE_CHUNK_ELEMS = {"triangle": 256, "tetra": 256, "triangle6": 128, "tetra10": 128}
+NODE_CHUNK_ELEMS = {"triangle": 256, "tetra": 256, "triangle6": 128, "tetra10": 128, "quad": 256, "quad9": 128}
+
+# shared memory a k_matrix chunk may fill (of the 227 KB a CTA can have)
+_CHUNK_SMEM_BUDGET = 200 * 1024
+
+
+def chunk_elems(etype: str, block: bool, qorder: int) -> int:
+    """Elements per k_matrix chunk: the default of ``CHUNK_ELEMS``, halved
+    while the chunk's shared memory would exceed the budget.  Elements whose
+    Jacobian varies (P2, quadrilaterals) keep the shape gradients of every
+    quadrature point in shared memory, so high quadrature orders need
+    smaller chunks; the estimate follows the kernel's layout (tables,
+    coordinates, gradients and weights per point, locals, staged plan)."""
+    ch = CHUNK_ELEMS[(etype, block)]
+    if etype in ("triangle", "tetra"):
+        return ch
+    info = element_info(etype)
+    B, D = info.n_basis, info.dim
+    Q = len(element_tables(etype, qorder)["w"])
+    NL = B * (B + 1) // 2
+    fixed = 8 * (Q + Q * B + Q * D * B + B * B + B + 1) + 16 * NL + 64
+    per = 8 * (B * D + Q * B * D + Q) + (8 * NL * D * D if block else 16 * NL) + 6 * B * B
+    while ch > 8 and fixed + ch * per > _CHUNK_SMEM_BUDGET:
+        ch //= 2
+    return ch
 
 
 class Topology:
@@ -171,7 +197,7 @@ class Topology:
         self._layout_hash = None
         self._row_ptr: Dict[torch.device, torch.Tensor] = {}
         if matrix:
-            ch = CHUNK_ELEMS[(etype, False)]
+            ch = chunk_elems(etype, False, quadrature_order)
             host = HostPlan(conn_np, self.n_points, _lib.TM_PLAN_KIND_MATRIX, ch, self.perm)
             self.edges = torch.from_numpy(np.stack([host.arrays["edge_row"], host.arrays["edge_col"]]))
             self.slot = torch.from_numpy(host.arrays["slot"])
@@ -203,7 +229,7 @@ class Topology:
         return self._conn32[device]
 
     def matrix_plan(self, device: torch.device, block: bool = False) -> DevicePlan:
-        ch = CHUNK_ELEMS[(self.etype, block)]
+        ch = chunk_elems(self.etype, block, self.quadrature_order)
         key = ("matrix", ch, device)
         if key not in self._plans:
             host = self._pending.pop(("matrix", ch), None)

@@ -4,7 +4,7 @@ CPU in float64.
 
 Usage (from the repository root, with the reference source tree available)::
 
-    python tests/golden/make_golden.py /path/to/TensorMesh [--only=facet]
+    python tests/golden/make_golden.py /path/to/TensorMesh [--only=facet|--only=quad]
 
 Writes
 
@@ -13,6 +13,9 @@ Writes
   hash, adjoint gradients).
 * ``tests/golden/small_facet.npz``: the reference's FacetAssembler on the
   small meshes (``--only=facet`` writes this file alone).
+* ``tests/golden/small_quad.npz``, ``small_quad9.npz`` and
+  ``small_facet_quad.npz``: the same cases on quadrilateral meshes
+  (``--only=quad`` writes these three alone).
 * ``tests/golden/full_checksums.json``: fingerprints (``checksum()`` of
   ``oracle/fem_oracle.py``) of the reference's outputs on the full-size
   workloads of ``tensormesh_gb300/workloads.py``.
@@ -37,10 +40,11 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
 
-def facet_golden(tm, to_ref):
+def facet_golden(tm, to_ref, quads=False):
     """small_facet.npz: the reference's FacetAssembler (integrand forms as its
     docstring writes them: ``forward(v)``, ``forward(v, f)``, a function of
-    ``x`` and a constant traction vector) on the small meshes."""
+    ``x`` and a constant traction vector) on the small meshes
+    (small_facet_quad.npz: on the quadrilateral meshes)."""
     from tensormesh_gb300.mesh import gen_unit_square, gen_unit_cube
 
     class Unit(tm.FacetAssembler):
@@ -62,6 +66,11 @@ def facet_golden(tm, to_ref):
         "tet4": (gen_unit_cube(3, jitter=0.2, seed=113), [1, 2, 3]),
         "tet10": (gen_unit_cube(2, order=2, jitter=0.1, seed=114), [2, 3]),
     }
+    if quads:
+        cases = {
+            "quad": (gen_unit_square(4, jitter=0.2, seed=115, cell="quad"), [1, 2, 3]),
+            "quad9": (gen_unit_square(3, order=2, jitter=0.1, seed=116, cell="quad"), [2, 3]),
+        }
     for name, (m, qorders) in cases.items():
         rm = to_ref(m)
         D = m.points.shape[1]
@@ -83,8 +92,9 @@ def facet_golden(tm, to_ref):
             out[f"{name}_q{qo}_nodal"] = Nodal.from_mesh(rm, quadrature_order=qo)(rm.points, point_data={"f": f}).numpy()
             out[f"{name}_q{qo}_func"] = Func.from_mesh(rm, quadrature_order=qo)(rm.points).numpy()
             out[f"{name}_q{qo}_traction"] = Traction.from_mesh(rm, quadrature_order=qo)(rm.points).numpy()
-    np.savez_compressed(os.path.join(HERE, "small_facet.npz"), **out)
-    print("wrote facet")
+    name = "small_facet_quad.npz" if quads else "small_facet.npz"
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    print("wrote", name)
 
 
 def main(reference_root, only=None):
@@ -135,6 +145,12 @@ def main(reference_root, only=None):
         "tet4": (gen_unit_cube(3, jitter=0.2, seed=103), [1, 2, 3]),
         "tet10": (gen_unit_cube(2, order=2, jitter=0.1, seed=104), [2, 3]),
     }
+    if only == "quad":
+        # quadrilaterals (written by --only=quad, with their facet file)
+        cases = {
+            "quad": (gen_unit_square(5, jitter=0.2, seed=107, cell="quad"), [1, 2, 3]),
+            "quad9": (gen_unit_square(3, order=2, jitter=0.1, seed=108, cell="quad"), [2, 3, 4]),
+        }
     for name, (m, qorders) in cases.items():
         rm = to_ref(m)
         et = m.default_element_type
@@ -174,6 +190,9 @@ def main(reference_root, only=None):
             out[f"q{qo}_El_hash"] = np.array(El.layout_hash)
         np.savez_compressed(os.path.join(HERE, f"small_{name}.npz"), **out)
         print("wrote", name)
+    if only == "quad":
+        facet_golden(tm, to_ref, quads=True)
+        return
 
     # -------------------------------------------------------- small adjoint
     m = gen_unit_cube(3, jitter=0.2, seed=105)

@@ -1,8 +1,9 @@
 """Boundary-facet loads on CPU: the oracle's restatement of the reference's
 FacetAssembler against the reference's own outputs (golden fixtures; the
 reference evaluates its facet quadrature rule in float32, so the bound is
-1e-6 relative, and 1e-14 for order-1 line facets, whose rule float32 holds
-exactly), and the facet selection of the package against the oracle's."""
+1e-6 relative, and 1e-14 for order-1 triangle edges, whose rule float32
+holds exactly; its quadrilateral edge maps round in float32 even there),
+and the facet selection of the package against the oracle's."""
 import math
 
 import numpy as np
@@ -14,7 +15,10 @@ from oracle import fem_oracle as O
 from tensormesh_gb300.element import facet_info, facet_tables
 from tensormesh_gb300.facet import FacetAssembler
 
-ET = {"tri3": "triangle", "tri6": "triangle6", "tet4": "tetra", "tet10": "tetra10"}
+ET = {"tri3": "triangle", "tri6": "triangle6", "tet4": "tetra", "tet10": "tetra10", "quad": "quad",
+      "quad9": "quad9"}
+# the quadrilateral cases live in their own fixture file
+FIXTURE = {name: ("facet_quad" if name.startswith("quad") else "facet") for name in ET}
 
 
 def _func(x):
@@ -23,7 +27,7 @@ def _func(x):
 
 @pytest.mark.parametrize("name", list(ET))
 def test_oracle_matches_reference_facets(name):
-    g = load_golden("facet")
+    g = load_golden(FIXTURE[name])
     et = ET[name]
     P = torch.from_numpy(g[f"{name}_points"])
     Cn = torch.from_numpy(g[f"{name}_conn"])
@@ -46,7 +50,7 @@ def test_oracle_matches_reference_facets(name):
 
 @pytest.mark.parametrize("name", list(ET))
 def test_selection_matches_oracle(name):
-    g = load_golden("facet")
+    g = load_golden(FIXTURE[name])
     et = ET[name]
     conn = g[f"{name}_conn"].astype(np.int64)
     bnd = g[f"{name}_boundary"].astype(bool)

@@ -1,9 +1,9 @@
 """Boundary-facet loads on the GPU (tm_assemble_facet_vector through the
 FacetAssembler built-ins) against the oracle's restatement (1e-12 relative)
 and the reference's outputs (golden fixtures, 1e-6 relative: the reference
-evaluates its facet quadrature rule in float32; 1e-14 for order-1 lines),
-on all four element types, scalar and vector loads; multi-chunk
-determinism and float32."""
+evaluates its facet quadrature rule in float32; 1e-14 for order-1
+triangle edges), on all six element types, scalar and vector loads;
+multi-chunk determinism and float32."""
 import math
 
 import numpy as np
@@ -15,7 +15,9 @@ from conftest import load_golden, rel_fro
 from oracle import fem_oracle as O
 
 pytestmark = pytest.mark.gpu
-ET = {"tri3": "triangle", "tri6": "triangle6", "tet4": "tetra", "tet10": "tetra10"}
+ET = {"tri3": "triangle", "tri6": "triangle6", "tet4": "tetra", "tet10": "tetra10", "quad": "quad",
+      "quad9": "quad9"}
+FIXTURE = {name: ("facet_quad" if name.startswith("quad") else "facet") for name in ET}
 
 
 def _func(x):
@@ -24,7 +26,7 @@ def _func(x):
 
 @pytest.mark.parametrize("name", list(ET))
 def test_facet_loads_match_oracle_and_reference(name, cuda):
-    g = load_golden("facet")
+    g = load_golden(FIXTURE[name])
     et = ET[name]
     P = torch.from_numpy(g[f"{name}_points"])
     Cn = torch.from_numpy(g[f"{name}_conn"])

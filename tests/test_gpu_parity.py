@@ -16,8 +16,9 @@ from oracle import fem_oracle as O
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["tri3", "tri6", "tet4", "tet10"]
-ETYPE = {"tri3": "triangle", "tri6": "triangle6", "tet4": "tetra", "tet10": "tetra10"}
+CASES = ["tri3", "tri6", "tet4", "tet10", "quad", "quad9"]
+ETYPE = {"tri3": "triangle", "tri6": "triangle6", "tet4": "tetra", "tet10": "tetra10", "quad": "quad",
+         "quad9": "quad9"}
 TOL = 1e-12
 
 
@@ -106,7 +107,7 @@ def test_linear_forms_match_reference(case, cuda):
         assert rel_fro(bv, ref) <= 1e-14
 
 
-@pytest.mark.parametrize("case", ["tri3", "tet4", "tet10"])
+@pytest.mark.parametrize("case", ["tri3", "tet4", "tet10", "quad9"])
 def test_float32(case, cuda):
     g = load_golden(case)
     mesh = _mesh(g, case, cuda).to(dtype=torch.float32)

@@ -11,8 +11,9 @@ import torch
 from conftest import GOLDEN, load_golden, rel_fro
 from oracle import fem_oracle as O
 
-CASES = ["tri3", "tri6", "tet4", "tet10"]
-ETYPE = {"tri3": "triangle", "tri6": "triangle6", "tet4": "tetra", "tet10": "tetra10"}
+CASES = ["tri3", "tri6", "tet4", "tet10", "quad", "quad9"]
+ETYPE = {"tri3": "triangle", "tri6": "triangle6", "tet4": "tetra", "tet10": "tetra10", "quad": "quad",
+         "quad9": "quad9"}
 
 
 @pytest.mark.parametrize("case", CASES)
