@@ -425,11 +425,26 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
             }
             if constexpr (ELAST) {
                 const R Ey = (yng ? ldg(yng + e) : R(1)) * yscale;
-                R* blk = LE + (size_t)k * HH;
+                // A = sum_q jw_q g_a g_b^T, then the block in one step
+                R A[D][D];
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int c = 0; c < D; ++c) A[r][c] = 0;
                 for (int q = 0; q < Q; ++q) {
                     const R* g = G + (size_t)(el * Q + q) * B * D;
-                    elastic_block<R, D>(g + pa * D, g + pb * D, Ey * clam, Ey * cmu, JW[el * Q + q], blk, q > 0);
+                    const R jw = JW[el * Q + q];
+                    R t[D];
+#pragma unroll
+                    for (int c = 0; c < D; ++c) t[c] = jw * g[pb * D + c];
+#pragma unroll
+                    for (int r = 0; r < D; ++r) {
+                        const R ar = g[pa * D + r];
+#pragma unroll
+                        for (int c = 0; c < D; ++c) A[r][c] += ar * t[c];
+                    }
                 }
+                elastic_block_outer<R, D>(A, Ey * clam, Ey * cmu, LE + (size_t)k * HH);
             }
         }
     }
