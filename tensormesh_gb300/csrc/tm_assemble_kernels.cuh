@@ -96,7 +96,9 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q, int MS, int MC) {
     else if (MASS)
         o = align16(o + sizeof(R) * CH * (T::P1 ? 1 : NL));
     L.le = o;
-    if (ELAST) o = align16(o + sizeof(R) * CH * NL * D * D);
+    // affine elements: the element blocks; the others: {E lam, E mu} per
+    // element, the blocks being formed from the gradients during the reduction
+    if (ELAST) o = align16(o + sizeof(R) * CH * (T::P1 ? NL * D * D : 2));
     // the chunk's plan: an mbarrier, then 16-byte windows of slot_ptr and
     // contrib
     L.bar = o;
@@ -161,6 +163,9 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
     R* LS = reinterpret_cast<R*>(sm + L.ls);
     R* LM = reinterpret_cast<R*>(sm + L.lm);
     R* LE = reinterpret_cast<R*>(sm + L.le);
+    // per (element, quadrature point) gradients and weights (non-affine elements)
+    [[maybe_unused]] R* G = reinterpret_cast<R*>(sm + L.g);
+    [[maybe_unused]] R* JW = reinterpret_cast<R*>(sm + L.jw);
 
     // per-CTA constants of the double-float path, computed once by thread 0:
     // the range check of the scales and of the mass template, and the
@@ -367,8 +372,6 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
         }
     } else {
         R* X = reinterpret_cast<R*>(sm + L.x);
-        R* G = reinterpret_cast<R*>(sm + L.g);
-        R* JW = reinterpret_cast<R*>(sm + L.jw);
         for (int k = threadIdx.x; k < ne * B; k += blockDim.x) {
             const int64_t node = P.conn[i0 * B + k];
 #pragma unroll
@@ -404,7 +407,16 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
             JW[k] = (R)tab[TL.w + q] * rabs(det);
         }
         __syncthreads();
-        for (int k = threadIdx.x; k < ne * NL; k += blockDim.x) {
+        if constexpr (ELAST) {
+            // the element's scaled Lame constants; its blocks are formed from
+            // G and JW during the reduction (elasticity is never fused)
+            for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+                const R Ey = (yng ? ldg(yng + P.elem_perm[i0 + el]) : R(1)) * yscale;
+                LE[2 * el] = Ey * clam;
+                LE[2 * el + 1] = Ey * cmu;
+            }
+        }
+        for (int k = threadIdx.x; k < (DIFF || MASS ? ne * NL : 0); k += blockDim.x) {
             const int el = k / NL, l = k - el * NL;
             int pa, pb;
             upper_pair<B>(l, pa, pb);
@@ -422,29 +434,6 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                 for (int q = 0; q < Q; ++q)
                     s += JW[el * Q + q] * (R)tab[TL.phi + q * B + pa] * (R)tab[TL.phi + q * B + pb];
                 LM[k] = s * mscale;
-            }
-            if constexpr (ELAST) {
-                const R Ey = (yng ? ldg(yng + e) : R(1)) * yscale;
-                // A = sum_q jw_q g_a g_b^T, then the block in one step
-                R A[D][D];
-#pragma unroll
-                for (int r = 0; r < D; ++r)
-#pragma unroll
-                    for (int c = 0; c < D; ++c) A[r][c] = 0;
-                for (int q = 0; q < Q; ++q) {
-                    const R* g = G + (size_t)(el * Q + q) * B * D;
-                    const R jw = JW[el * Q + q];
-                    R t[D];
-#pragma unroll
-                    for (int c = 0; c < D; ++c) t[c] = jw * g[pb * D + c];
-#pragma unroll
-                    for (int r = 0; r < D; ++r) {
-                        const R ar = g[pa * D + r];
-#pragma unroll
-                        for (int c = 0; c < D; ++c) A[r][c] += ar * t[c];
-                    }
-                }
-                elastic_block_outer<R, D>(A, Ey * clam, Ey * cmu, LE + (size_t)k * HH);
             }
         }
     }
@@ -597,7 +586,36 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                 }
             }
             if constexpr (ELAST) {
-                const R* blk = LE + (size_t)idx * HH;
+                [[maybe_unused]] R tmp[HH];
+                const R* blk;
+                if constexpr (T::P1 != 0) {
+                    blk = LE + (size_t)idx * HH;
+                } else {
+                    // A = sum_q jw_q g_a g_b^T of (element, pair), then its block
+                    const int el = idx / NL;
+                    int pa, pb;
+                    upper_pair<B>(idx - el * NL, pa, pb);
+                    R A[D][D];
+#pragma unroll
+                    for (int r = 0; r < D; ++r)
+#pragma unroll
+                        for (int c = 0; c < D; ++c) A[r][c] = 0;
+                    for (int q = 0; q < Q; ++q) {
+                        const R* g = G + (size_t)(el * Q + q) * B * D;
+                        const R jw = JW[el * Q + q];
+                        R t[D];
+#pragma unroll
+                        for (int c = 0; c < D; ++c) t[c] = jw * g[pb * D + c];
+#pragma unroll
+                        for (int r = 0; r < D; ++r) {
+                            const R ar = g[pa * D + r];
+#pragma unroll
+                            for (int c = 0; c < D; ++c) A[r][c] += ar * t[c];
+                        }
+                    }
+                    elastic_block_outer<R, D>(A, LE[2 * el], LE[2 * el + 1], tmp);
+                    blk = tmp;
+                }
                 if (code & 1) {
 #pragma unroll
                     for (int r = 0; r < D; ++r)

@@ -168,7 +168,9 @@ def chunk_elems(etype: str, block: bool, qorder: int) -> int:
     Q = len(element_tables(etype, qorder)["w"])
     NL = B * (B + 1) // 2
     fixed = 8 * (Q + Q * B + Q * D * B + B * B + B + 1) + 16 * NL + 64
-    per = 8 * (B * D + Q * B * D + Q) + (8 * NL * D * D if block else 16 * NL) + 6 * B * B
+    # elasticity keeps two scalars per element (its blocks are formed during
+    # the reduction), the scalar forms one value per local pair and form
+    per = 8 * (B * D + Q * B * D + Q) + (16 if block else 16 * NL) + 6 * B * B
     while ch > 8 and fixed + ch * per > _CHUNK_SMEM_BUDGET:
         ch //= 2
     return ch
