@@ -15,9 +15,11 @@
 // keep several rows per thread in flight: the SpMV interleaves the loads of
 // four rows, the vector updates load four elements before using them
 // (measured on 512 uneven meshes: 79 ms per batch against 122 ms one row at
-// a time).  Every loop is bounded by max_iter.  Reductions
-// are per thread in row order and then a fixed tree in shared memory, so the
-// result of a system does not depend on which CTA solved it.  Dirichlet rows
+// a time).  Every loop is bounded by max_iter.  Reductions are per thread
+// in row order, then summed in a fixed order by one warp, so the result of
+// a system does not depend on which CTA solved it.  (Keeping the search
+// direction in shared memory instead measured slower, 93 ms against 79: it
+// takes L1 capacity that the matrix and vector streams hit in.)  Dirichlet rows
 // (dirichlet[i] != 0) keep x_i as given on input and are excluded from the
 // iteration (p_i = r_i = 0), which solves the condensed system
 // K_ii x_i = b_i - K_io x_o without extracting K_ii.
@@ -33,22 +35,40 @@ namespace tmk {
 
 constexpr int kBatchThreads = 512;
 
+// butterfly sum over the 32 lanes of a warp (both lanes of a pair add the
+// same two operands, so every lane ends with the same value)
+__device__ __forceinline__ double warp_sum(double s) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+    return s;
+}
+
+// Fixed-order block sums of N values per thread: staged in shared memory
+// (red: [N][kBatchThreads]) and summed by warp 0 alone, each lane a pairwise
+// tree over its 16 entries, then a butterfly (float64 adds are scarce on this
+// GPU: the other warps issue none); every thread returns the same sums
 template <int N>
 __device__ __forceinline__ void block_sum(double (&v)[N], double* red) {
-    // red: [N][kBatchThreads] scratch; fixed-order tree
+    static_assert(kBatchThreads == 512, "block_sum sums 16 entries per lane of warp 0");
+    __shared__ double res[N];
 #pragma unroll
     for (int k = 0; k < N; ++k) red[k * kBatchThreads + threadIdx.x] = v[k];
     __syncthreads();
-    for (int w = kBatchThreads / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
+    if (threadIdx.x < 32) {
 #pragma unroll
-            for (int k = 0; k < N; ++k) red[k * kBatchThreads + threadIdx.x] += red[k * kBatchThreads + threadIdx.x + w];
+        for (int k = 0; k < N; ++k) {
+            const double* e = red + k * kBatchThreads + threadIdx.x;
+            double t8[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) t8[j] = e[64 * j] + e[64 * j + 32];
+            const double t = ((t8[0] + t8[1]) + (t8[2] + t8[3])) + ((t8[4] + t8[5]) + (t8[6] + t8[7]));
+            const double w = warp_sum(t);
+            if (threadIdx.x == 0) res[k] = w;
         }
-        __syncthreads();
     }
-#pragma unroll
-    for (int k = 0; k < N; ++k) v[k] = red[k * kBatchThreads];
     __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = res[k];
 }
 
 template <typename R>
