@@ -96,9 +96,10 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q, int MS, int MC) {
     else if (MASS)
         o = align16(o + sizeof(R) * CH * (T::P1 ? 1 : NL));
     L.le = o;
-    // affine elements: the element blocks; the others: {E lam, E mu} per
-    // element, the blocks being formed from the gradients during the reduction
-    if (ELAST) o = align16(o + sizeof(R) * CH * (T::P1 ? NL * D * D : 2));
+    // affine elements: the element blocks; the others: {E lam, E mu, scale}
+    // per element, the blocks being formed from the gradients during the
+    // reduction
+    if (ELAST) o = align16(o + sizeof(R) * CH * (T::P1 ? NL * D * D : 3));
     // the chunk's plan: an mbarrier, then 16-byte windows of slot_ptr and
     // contrib
     L.bar = o;
@@ -129,6 +130,9 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
     constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
     constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
     constexpr bool DF64 = use_df64<R, ET, FORMS>();
+    // float64 elasticity on non-affine elements: geometry in FP64, blocks
+    // and their sums in double-float arithmetic on the FP32 pipes
+    constexpr bool DFE = std::is_same<R, double>::value && !T::P1 && ELAST;
     constexpr int HH = ELAST ? D * D : 1;
     const tm_chunk_plan& P = a.plan;
     const int CH = P.chunk_elems, Q = a.tables.n_quad;
@@ -219,6 +223,7 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
     const R cmu = R(1) / (R(2) * (R(1) + nu));
 
     bool use_df = false;
+    [[maybe_unused]] bool use_dfe = false;
     if constexpr (T::P1 != 0) {
         const R wsum = (R)tab[TL.wsum];
         // P1 simplices in the arithmetic of R: unscaled gradients C_b (g_b = C_b / det)
@@ -412,8 +417,62 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
             // G and JW during the reduction (elasticity is never fused)
             for (int el = threadIdx.x; el < ne; el += blockDim.x) {
                 const R Ey = (yng ? ldg(yng + P.elem_perm[i0 + el]) : R(1)) * yscale;
-                LE[2 * el] = Ey * clam;
-                LE[2 * el + 1] = Ey * cmu;
+                LE[3 * el] = Ey * clam;
+                LE[3 * el + 1] = Ey * cmu;
+            }
+        }
+        if constexpr (DFE) {
+            // Per element, powers of two that bring the largest gradient
+            // entry, weight and modulus to [1/2, 1): the element's blocks are
+            // then formed in double-float from values of order one and
+            // scaled back by 2^S (S = 2 sg + sw + se) before they are summed.
+            // A chunk with an element outside the window below (or a value
+            // that is not finite) keeps the FP64 path.
+            bool ok = true;
+            for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+                int eg = 0, ew = 0;
+                const R* g = G + (size_t)el * Q * B * D;
+                for (int t = 0; t < Q * B * D; ++t) eg = max(eg, biased_exponent(g[t]));
+                for (int q = 0; q < Q; ++q) ew = max(ew, biased_exponent(JW[el * Q + q]));
+                const int ee = max(biased_exponent(LE[3 * el]), biased_exponent(LE[3 * el + 1]));
+                const int sg = eg - 1022, sw = ew - 1022, se = ee - 1022;
+                const int S = 2 * sg + sw + se;
+                ok = ok && eg < 2047 && ew < 2047 && ee < 2047 && S > -70 && S < 100;
+                reinterpret_cast<int*>(LE + 3 * el + 2)[0] = sg;
+                reinterpret_cast<int*>(LE + 3 * el + 2)[1] = S;
+                reinterpret_cast<int*>(LE + 3 * el)[0] = sw;       // read back below, before LE is converted
+                reinterpret_cast<int*>(LE + 3 * el)[1] = se;
+            }
+            use_dfe = !__syncthreads_or(!ok);
+            if (!use_dfe && threadIdx.x == 0 && a.stats) atomicAdd(a.stats, 1);
+            if (!use_dfe) {
+                // restore the moduli the scale pass overwrote
+                for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+                    const R Ey = (yng ? ldg(yng + P.elem_perm[i0 + el]) : R(1)) * yscale;
+                    LE[3 * el] = Ey * clam;
+                    LE[3 * el + 1] = Ey * cmu;
+                }
+            } else {
+                // convert in place: the gradients, weights and moduli become
+                // scaled double-float pairs (8 bytes, as the doubles were)
+                f2* G2 = reinterpret_cast<f2*>(G);
+                f2* JW2 = reinterpret_cast<f2*>(JW);
+                for (int t = threadIdx.x; t < ne * Q * B * D; t += blockDim.x) {
+                    const int el = t / (Q * B * D);
+                    G2[t] = split_scaled(G[t], reinterpret_cast<const int*>(LE + 3 * el + 2)[0]);
+                }
+                for (int t = threadIdx.x; t < ne * Q; t += blockDim.x) {
+                    const int el = t / Q;
+                    JW2[t] = split_scaled(JW[t], reinterpret_cast<const int*>(LE + 3 * el)[0]);
+                }
+                __syncthreads();
+                for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+                    const int se = reinterpret_cast<const int*>(LE + 3 * el)[1];
+                    const R Ey = (yng ? ldg(yng + P.elem_perm[i0 + el]) : R(1)) * yscale;
+                    f2* m = reinterpret_cast<f2*>(LE + 3 * el);
+                    m[0] = split_scaled(Ey * clam, se);
+                    m[1] = split_scaled(Ey * cmu, se);
+                }
             }
         }
         for (int k = threadIdx.x; k < (DIFF || MASS ? ne * NL : 0); k += blockDim.x) {
@@ -566,6 +625,84 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
         }
     }
 
+    if constexpr (DFE) {
+        if (use_dfe) {
+            // each contribution's block from its (element, pair): A = sum_q
+            // jw g_a g_b^T and lam A + mu (A^T + tr A I) in double-float on
+            // the element's scaled values, scaled back by 2^S exactly, then
+            // a compensated sum per target in element order, rounded once
+            const f2* G2 = reinterpret_cast<const f2*>(G);
+            const f2* JW2 = reinterpret_cast<const f2*>(JW);
+            for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+                const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
+                const int32_t tgt = __ldcs(P.slot_target + s0 + j), mir = __ldcs(P.slot_mirror + s0 + j);
+                acc2 sum[HH];
+#pragma unroll
+                for (int k = 0; k < HH; ++k) sum[k] = {0.0f, 0.0f};
+                for (int p = p0; p < p1; ++p) {
+                    const int code = CT[p];
+                    const int idx = code >> 1;
+                    const int el = idx / NL;
+                    int pa, pb;
+                    upper_pair<B>(idx - el * NL, pa, pb);
+                    acc2 A[D][D];
+#pragma unroll
+                    for (int r = 0; r < D; ++r)
+#pragma unroll
+                        for (int c = 0; c < D; ++c) A[r][c] = {0.0f, 0.0f};
+                    for (int q = 0; q < Q; ++q) {
+                        const f2* g = G2 + (size_t)(el * Q + q) * B * D;
+                        const f2 w = JW2[el * Q + q];
+                        f2 t[D];
+#pragma unroll
+                        for (int c = 0; c < D; ++c) t[c] = f2_mul(w, g[pb * D + c]);
+#pragma unroll
+                        for (int r = 0; r < D; ++r) {
+                            const f2 ar = g[pa * D + r];
+#pragma unroll
+                            for (int c = 0; c < D; ++c) acc_fma(A[r][c], ar, t[c]);
+                        }
+                    }
+                    const f2* m = reinterpret_cast<const f2*>(LE + 3 * el);
+                    const float sc = pow2f(reinterpret_cast<const int*>(LE + 3 * el + 2)[1]);
+                    f2 Av[D][D];
+#pragma unroll
+                    for (int r = 0; r < D; ++r)
+#pragma unroll
+                        for (int c = 0; c < D; ++c) Av[r][c] = acc_value(A[r][c]);
+                    f2 tr = Av[0][0];
+#pragma unroll
+                    for (int d = 1; d < D; ++d) tr = f2_add(tr, Av[d][d]);
+                    f2 blk[HH];
+#pragma unroll
+                    for (int r = 0; r < D; ++r)
+#pragma unroll
+                        for (int c = 0; c < D; ++c) {
+                            const f2 u = r == c ? f2_add(Av[c][r], tr) : Av[c][r];
+                            f2 v = f2_add(f2_mul(m[0], Av[r][c]), f2_mul(m[1], u));
+                            v.hi = __fmul_rn(v.hi, sc);
+                            v.lo = __fmul_rn(v.lo, sc);
+                            blk[r * D + c] = v;
+                        }
+                    if (code & 1) {
+#pragma unroll
+                        for (int r = 0; r < D; ++r)
+#pragma unroll
+                            for (int c = 0; c < D; ++c) acc_add(sum[r * D + c], blk[c * D + r]);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < HH; ++k) acc_add(sum[k], blk[k]);
+                    }
+                }
+                R ae[HH];
+#pragma unroll
+                for (int k = 0; k < HH; ++k) ae[k] = (R)f2_to_double(acc_value(sum[k]));
+                emit(tgt, mir, R(0), R(0), ae);
+            }
+            return;
+        }
+    }
+
     for (int j = threadIdx.x; j < ns; j += blockDim.x) {
         const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
         const int32_t tgt = __ldcs(P.slot_target + s0 + j), mir = __ldcs(P.slot_mirror + s0 + j);
@@ -613,7 +750,7 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                             for (int c = 0; c < D; ++c) A[r][c] += ar * t[c];
                         }
                     }
-                    elastic_block_outer<R, D>(A, LE[2 * el], LE[2 * el + 1], tmp);
+                    elastic_block_outer<R, D>(A, LE[3 * el], LE[3 * el + 1], tmp);
                     blk = tmp;
                 }
                 if (code & 1) {

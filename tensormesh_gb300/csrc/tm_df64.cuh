@@ -171,6 +171,48 @@ __device__ __forceinline__ f2 split_double(double x) {
     return {__uint_as_float(hib), lo};
 }
 
+// x * 2^-s as hi + lo (split_double of the scaled value); the exponent is
+// moved on the integer pipe, so that the scaling is exact, and a scaled
+// value below the double range becomes 0.  The caller picks s so that
+// |x| 2^-s < 1.
+__device__ __forceinline__ f2 split_scaled(double x, int s) {
+    const uint64_t u = (uint64_t)__double_as_longlong(x);
+    const int e = (int)((u >> 52) & 0x7FF);
+    const int ne = e - s;
+    if (e == 0 || ne <= 0) return {0.0f, 0.0f};
+    const uint64_t v = (u & ~(0x7FFull << 52)) | ((uint64_t)ne << 52);
+    return split_double(__longlong_as_double((long long)v));
+}
+
+// 2^k as a float, k in [-126, 127]
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
+
+// an unnormalised double-float accumulator: s + e, where every term's
+// rounding error is collected in e (TwoSum on the leading parts)
+struct acc2 {
+    float s, e;
+};
+
+// acc += a * b for double-float a, b (a.lo * b.lo dropped: below 2^-96)
+__device__ __forceinline__ void acc_fma(acc2& acc, f2 a, f2 b) {
+    const f2 p = two_prod(a.hi, b.hi);
+    const f2 t = two_sum(acc.s, p.hi);
+    float e = __fadd_rn(acc.e, __fadd_rn(t.lo, p.lo));
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    acc.s = t.hi;
+    acc.e = e;
+}
+
+// acc += a for double-float a
+__device__ __forceinline__ void acc_add(acc2& acc, f2 a) {
+    const f2 t = two_sum(acc.s, a.hi);
+    acc.s = t.hi;
+    acc.e = __fadd_rn(acc.e, __fadd_rn(t.lo, a.lo));
+}
+
+__device__ __forceinline__ f2 acc_value(acc2 acc) { return fast_two_sum(acc.s, acc.e); }
+
 // float -> double, exact, on the integer pipe (normal floats and zero)
 __device__ __forceinline__ double float_to_double(float f) {
     const uint32_t b = __float_as_uint(f);

@@ -143,7 +143,7 @@ CHUNK_ELEMS = {
     ("triangle", False): 256, ("triangle", True): 256,
     ("tetra", False): 384, ("tetra", True): 128,
     ("triangle6", False): 64, ("triangle6", True): 64,
-    ("tetra10", False): 32, ("tetra10", True): 32,
+    ("tetra10", False): 32, ("tetra10", True): 64,
     ("quad", False): 128, ("quad", True): 128,
     ("quad9", False): 64, ("quad9", True): 64,
 }
@@ -168,9 +168,9 @@ def chunk_elems(etype: str, block: bool, qorder: int) -> int:
     Q = len(element_tables(etype, qorder)["w"])
     NL = B * (B + 1) // 2
     fixed = 8 * (Q + Q * B + Q * D * B + B * B + B + 1) + 16 * NL + 64
-    # elasticity keeps two scalars per element (its blocks are formed during
-    # the reduction), the scalar forms one value per local pair and form
-    per = 8 * (B * D + Q * B * D + Q) + (16 if block else 16 * NL) + 6 * B * B
+    # elasticity keeps three scalars per element (its blocks are formed
+    # during the reduction), the scalar forms one value per local pair and form
+    per = 8 * (B * D + Q * B * D + Q) + (24 if block else 16 * NL) + 6 * B * B
     while ch > 8 and fixed + ch * per > _CHUNK_SMEM_BUDGET:
         ch //= 2
     return ch

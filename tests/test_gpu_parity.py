@@ -198,6 +198,45 @@ def test_double_float_path_and_fp64_fallback(etype, cuda):
 
 
 @pytest.mark.parametrize("etype,make", [
+    ("tetra10", lambda: tg.gen_unit_cube(3, order=2, jitter=0.1, seed=34)),
+    ("triangle6", lambda: tg.gen_unit_square(8, order=2, jitter=0.1, seed=35)),
+    ("quad9", lambda: tg.gen_unit_square(8, order=2, jitter=0.1, seed=36, cell="quad")),
+])
+def test_elasticity_double_float_path_and_fp64_fallback(etype, make, cuda):
+    """Float64 elasticity on non-affine elements forms its blocks in
+    double-float arithmetic on per-element power-of-two scaled values;
+    chunks whose scales leave the window keep FP64.  Both match the oracle
+    to 1e-12, and the stats counter tells which path ran."""
+    base = make()
+    E = base.n_elements
+    Ey = np.random.default_rng(37).uniform(0.5, 2.0, E)
+    cases = {
+        "plain": (1.0, 0.0, 1.0, False),
+        "scaled": (1.0e-3, 0.0, 1.0e4, False),
+        # (a larger shift makes the FP64 Jacobian of any summation order
+        # lose ~shift/h ulps to cancellation, as the reference's does)
+        "translated": (1.0, 10.0, 1.0, False),
+        # in 3-D the blocks scale with h (S = -84 here: FP64); in 2-D they do
+        # not depend on the size, and the scaled double-float path keeps them
+        "tiny": (1.0e-25, 0.0, 1.0, base.points.shape[1] == 3),
+        "huge_modulus": (1.0, 0.0, 1.0e35, True),
+    }
+    for name, (scale, shift, emul, expect_fallback) in cases.items():
+        pts = base.points * scale + shift
+        conn = base.elements()
+        Et = torch.from_numpy(Ey * emul)
+        mesh = tg.Mesh(pts, {etype: conn}).to(cuda)
+        asm = tg.LinearElasticityElementAssembler.from_mesh(mesh, nu=0.3)
+        stats = torch.zeros(1, dtype=torch.int32, device=cuda)
+        (K,) = tg.assemble_forms([asm], mesh.points, {"E": Et.to(cuda)}, _stats=stats)
+        _, _, Ko = O.assemble_matrix(pts, conn, base.n_points,
+                                     lambda p, c, E: O.element_locals_elasticity(p, c, etype, E, 0.3, 2), E=Et)
+        assert rel_fro(K, Ko) <= TOL, (name, rel_fro(K, Ko))
+        fell_back = int(stats.item())
+        assert (fell_back > 0) == expect_fallback, (name, fell_back)
+
+
+@pytest.mark.parametrize("etype,make", [
     ("tetra", lambda: tg.gen_unit_cube(12, jitter=0.2, seed=71)),
     ("tetra10", lambda: tg.gen_unit_cube(5, order=2, jitter=0.1, seed=72)),
     ("triangle6", lambda: tg.gen_unit_square(20, order=2, jitter=0.1, seed=73)),
