@@ -163,6 +163,52 @@ def test_spmv_and_pcg(cuda):
     assert rel_fro(ui, ref) <= 1e-11
 
 
+@pytest.mark.parametrize("block", [False, True])
+def test_spmv_row_order(block, cuda):
+    """tm_spmv through the C ABI: the longest-first row order changes which
+    lanes sum a row, not its value (bitwise equal to the natural order, and
+    within 1e-14 of a dense product); an order entry outside [0, n_rows)
+    is skipped, leaving that row of y as it was."""
+    import ctypes
+    from tensormesh_gb300 import _lib, solve as S
+    if block:
+        mesh = tg.gen_unit_cube(3, order=2, jitter=0.1, seed=95).to(cuda)
+        E = torch.from_numpy(np.random.default_rng(96).uniform(0.5, 2.0, mesh.n_elements)).to(cuda)
+        K = tg.LinearElasticityElementAssembler.from_mesh(mesh, nu=0.3)(mesh.points, element_data={"E": E})
+    else:
+        mesh = tg.gen_unit_cube(6, jitter=0.2, seed=97).to(cuda)
+        K = tg.LaplaceElementAssembler.from_mesh(mesh)(mesh.points)
+    lib = _lib.load()
+    st = _lib.stream_handle(torch.device(cuda))
+    x = torch.from_numpy(np.random.default_rng(98).standard_normal(K.shape[0])).to(cuda)
+    op, keep = S.operator_of(K)
+    assert op.row_order
+
+    def run(op):
+        y = torch.full_like(x, float("nan"))
+        _lib.check(lib.tm_spmv(ctypes.byref(op), _lib.ptr(x), _lib.ptr(y), 1.0, 0.0, st), "tm_spmv")
+        torch.cuda.synchronize()
+        return y
+
+    y_ordered = run(op)
+    natural = S.operator_of(K)[0]
+    natural.row_order = None
+    y_natural = run(natural)
+    assert torch.equal(y_ordered, y_natural)
+    assert rel_fro(y_ordered, K.to_dense() @ x) <= 1e-14
+    order = K._row_order().clone()
+    first = int(order[0])
+    order[0] = op.n_rows                     # outside [0, n_rows): skipped
+    op.row_order = _lib.ptr(order)
+    y_skip = run(op)
+    H = K._block
+    rows = torch.arange(first * H, first * H + H, device=cuda)
+    assert bool(torch.isnan(y_skip[rows]).all())
+    keep_rows = torch.ones_like(x, dtype=torch.bool)
+    keep_rows[rows] = False
+    assert torch.equal(y_skip[keep_rows], y_ordered[keep_rows])
+
+
 @pytest.mark.parametrize("etype", ["tetra", "triangle"])
 def test_double_float_path_and_fp64_fallback(etype, cuda):
     """Float64 P1 diffusion/mass runs in double-float arithmetic; chunks whose
