@@ -410,6 +410,55 @@ def run_inverse(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_poisson(args, ws, rank, local):
+    """C1: P1 triangles on the unit square, 256 x 256 cells x 2 (131,072
+    elements, 66,049 nodes), f = 2 pi^2 sin(pi x) sin(pi y), zero Dirichlet
+    data.  One step = the whole solve through the public API: K and b
+    assembled, the boundary condensed, Jacobi-PCG to 1e-12, the solution
+    recovered; the L2 error against sin(pi x) sin(pi y) is reported (the
+    reference's own pipeline gives 3.7935e-05 on this mesh).  A small,
+    launch-bound workload: no roofline is claimed for it."""
+    import tensormesh_gb300 as tg
+    from tensormesh_gb300 import workloads as W
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    wl = W.poisson_tri(256)
+    mesh = wl.mesh.to(dev)
+    f = wl.data["f"].to(dev)
+    exact = wl.data["exact"].to(dev)
+    K_asm = tg.LaplaceElementAssembler.from_mesh(mesh)
+    b_asm = tg.LoadNodeAssembler.from_mesh(mesh)
+    cond = tg.Condenser(mesh.boundary_mask)
+
+    def step():
+        K = K_asm(mesh.points)
+        b = b_asm(mesh.points, point_data={"f": f})
+        Ki, bi = cond(K, b)
+        ui, info = tg.pcg_solve(Ki, bi, rtol=1e-12, return_info=True)
+        return cond.recover(ui), info
+
+    for _ in range(args.warmup):
+        step()
+    times, asm_times = [], []
+    for _ in range(args.steps):
+        t, (u, info) = _time_ms(step, dev)
+        times.append(t)
+        ta, _ = _time_ms(lambda: (K_asm(mesh.points), b_asm(mesh.points, point_data={"f": f})), dev)
+        asm_times.append(ta)
+    ms = statistics.median(times)
+    err = float((u - exact).norm() / exact.norm())
+    line = {"metric": "P1-triangle Poisson solves/s (assemble K and b, condense, Jacobi-PCG to 1e-12, FP64)",
+            "value": 1e3 / ms, "unit": "solves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (structured unit square, f = 2 pi^2 sin(pi x) sin(pi y))",
+            "config": {"workload": "poisson_tri_256: 131,072 P1 triangles, 66,049 nodes, zero Dirichlet data"},
+            "assembly_ms": statistics.median(asm_times), "iterations": info.iterations,
+            "converged": info.converged, "l2_relative_error": err,
+            "reference_l2_relative_error": 3.7935219e-05}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def _elastic_name(n):
     return (f"elasticity_p2tet_{n}: P2 tet isotropic elasticity (10-node tets, E ~ U[0.5, 2] per element, "
             f"nu = 0.3), {n}^3 cubes x 6 Kuhn, {6 * n ** 3:,} elements, {(2 * n + 1) ** 3:,} nodes, 3x3 blocks, FP64")
@@ -714,7 +763,7 @@ def main():
     ap.add_argument("--no-gpu-reference", action="store_true")
     ap.add_argument("--cubes", type=int, default=64, help="cubes per side of the Kuhn-split cube (64: 1,572,864 elements)")
     ap.add_argument("--workload", default="diffusion_mass",
-                    choices=["diffusion_mass", "elasticity", "spmv", "inverse", "batched"])
+                    choices=["diffusion_mass", "poisson", "elasticity", "spmv", "inverse", "batched"])
     ap.add_argument("--elastic-n", type=int, default=32,
                     help="cubes per side of the P2-tet elasticity workload (32: 196,608 elements)")
     ap.add_argument("--meshes", type=int, default=512)
@@ -725,6 +774,8 @@ def main():
         run_reference_elasticity(args, ws, rank, local)
     elif args.impl == "reference":
         run_reference(args, ws, rank, local)
+    elif args.workload == "poisson":
+        run_poisson(args, ws, rank, local)
     elif args.workload == "elasticity":
         run_elasticity(args, ws, rank, local)
     elif args.workload == "spmv":
