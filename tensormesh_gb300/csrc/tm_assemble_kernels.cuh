@@ -52,10 +52,13 @@ constexpr int matrix_threads() {
 
 // resident CTAs per SM the compiler must allow: four 384-thread CTAs of the
 // double-float tet kernel (40 registers), five 256-thread CTAs of the
-// double-float triangle kernel (48 registers)
+// double-float triangle kernel (48 registers), three of the double-float
+// elasticity kernel on non-affine elements (80 registers, 32-element chunks)
 template <typename R, int ET, int FORMS>
 constexpr int matrix_min_blocks() {
-    return use_df64<R, ET, FORMS>() ? (ET == TM_TET4 ? 4 : 5) : 1;
+    if (use_df64<R, ET, FORMS>()) return ET == TM_TET4 ? 4 : 5;
+    if (std::is_same<R, double>::value && !Traits<ET>::P1 && (FORMS & TM_FORM_ELASTICITY)) return 3;
+    return 1;
 }
 
 struct MatLayout {

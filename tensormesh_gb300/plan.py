@@ -143,7 +143,7 @@ CHUNK_ELEMS = {
     ("triangle", False): 256, ("triangle", True): 256,
     ("tetra", False): 384, ("tetra", True): 128,
     ("triangle6", False): 64, ("triangle6", True): 64,
-    ("tetra10", False): 32, ("tetra10", True): 64,
+    ("tetra10", False): 32, ("tetra10", True): 32,
     ("quad", False): 128, ("quad", True): 128,
     ("quad9", False): 64, ("quad9", True): 64,
 }
