@@ -135,6 +135,11 @@ def _traffic():
     return None
 
 
+# float64 FMA rate of this GPU, measured with an FMA-chain probe (1:62 of
+# FP32): the roof of any kernel that does its arithmetic in native float64
+FP64_PEAK_GFLOPS = 1254.0
+
+
 def algorithmic_bytes(N, E, nnz):
     """Inputs read once, outputs written once, int32 indices, slot map
     included: 24N (points) + 16E (connectivity) + 8E (kappa) + 64E (4x4 int32
@@ -288,7 +293,8 @@ def run_ours(args, ws, rank, local):
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_matrix + k_matrix_finalize (one assembly pass)",
                      "algorithmic_bytes": abytes, "k_matrix_ms": kms,
-                     "fp64_gflops": 125.0 * E / (ms * 1e-3) / 1e9},
+                     "fp64_gflops": 125.0 * E / (ms * 1e-3) / 1e9, "fp64_peak_gflops": FP64_PEAK_GFLOPS,
+                     "fp64_frac": 125.0 * E / (ms * 1e-3) / 1e9 / FP64_PEAK_GFLOPS},
         "clocks": clocks,
         "gpu_launches": 2 * args.steps,
         "wall_s_timed_region": wall,
@@ -568,7 +574,9 @@ def run_elasticity(args, ws, rank, local):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                          "kernel": "k_matrix + k_matrix_finalize (one assembly pass)", "algorithmic_bytes": abytes,
-                         "fp64_gflops": ELASTIC_FLOPS_PER_ELEMENT * E / (ms * 1e-3) / 1e9},
+                         "fp64_gflops": ELASTIC_FLOPS_PER_ELEMENT * E / (ms * 1e-3) / 1e9,
+                         "fp64_peak_gflops": FP64_PEAK_GFLOPS,
+                         "fp64_frac": ELASTIC_FLOPS_PER_ELEMENT * E / (ms * 1e-3) / 1e9 / FP64_PEAK_GFLOPS},
             "setup_s": setup_s,
             "solve": {"condense_ms": t_c, "pcg_ms": t_s, "iterations": info.iterations,
                       "relative_residual": info.relative_residual, "converged": info.converged,
@@ -633,7 +641,8 @@ def run_spmv(args, ws, rank, local):
             "roofline": {"bound": "hbm", "achieved": abytes / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": abytes / (ms * 1e-3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
                          "kernel": "k_spmv_op", "algorithmic_bytes": abytes,
-                         "fp64_gflops": 2.0 * nnz / (ms * 1e-3) / 1e9},
+                         "fp64_gflops": 2.0 * nnz / (ms * 1e-3) / 1e9, "fp64_peak_gflops": FP64_PEAK_GFLOPS,
+                         "fp64_frac": 2.0 * nnz / (ms * 1e-3) / 1e9 / FP64_PEAK_GFLOPS},
             "clocks": clocks, "gpu_launches": args.steps}
     if rank == 0:
         print(json.dumps(line), flush=True)
