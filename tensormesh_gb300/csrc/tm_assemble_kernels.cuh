@@ -62,7 +62,7 @@ constexpr int matrix_min_blocks() {
 }
 
 struct MatLayout {
-    size_t tab, mhl, x, g, jw, ld, ls, lm, le, bar, sp, ct, total;
+    size_t tab, mhl, x, g, jw, ph, ld, ls, lm, le, bar, sp, ct, total;
 };
 
 // MS / MC: the plan's largest chunk in slots / contributions (staged copies)
@@ -74,6 +74,7 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q, int MS, int MC) {
     constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
     constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
     constexpr bool DF64 = use_df64<R, ET, FORMS>();
+    constexpr bool DFS = std::is_same<R, double>::value && !T::P1 && (DIFF || MASS);
     MatLayout L;
     size_t o = 0;
     L.tab = o;
@@ -89,10 +90,13 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q, int MS, int MC) {
         L.jw = o;
         o = align16(o + sizeof(R) * CH * Q);
     }
+    L.ph = o;   // double-float scalar forms: phi at the quadrature points as pairs
+    if (DFS && MASS) o = align16(o + 8 * (size_t)Q * B);
     L.ld = o;
     if (DIFF) o = align16(o + sizeof(R) * CH * NL);
-    L.ls = o;   // double-float path: per element {scale, |det| rho} as four floats
-    if (DF64) o = align16(o + 16 * (size_t)CH);
+    L.ls = o;   // double-float paths: per element {scale, |det| rho} as four floats
+                // (affine) or four exponents (the scalar forms on other elements)
+    if (DF64 || DFS) o = align16(o + 16 * (size_t)CH);
     L.lm = o;   // the double-float path's FP64 fallback keeps its masses in the records' space
     if (DF64)
         L.lm = L.ls;
@@ -136,6 +140,9 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
     // float64 elasticity on non-affine elements: geometry in FP64, blocks
     // and their sums in double-float arithmetic on the FP32 pipes
     constexpr bool DFE = std::is_same<R, double>::value && !T::P1 && ELAST;
+    // float64 diffusion / mass on non-affine elements: geometry in FP64, the
+    // pair integrals and the target sums in double-float
+    constexpr bool DFS = std::is_same<R, double>::value && !T::P1 && (DIFF || MASS);
     constexpr int HH = ELAST ? D * D : 1;
     const tm_chunk_plan& P = a.plan;
     const int CH = P.chunk_elems, Q = a.tables.n_quad;
@@ -227,6 +234,11 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
 
     bool use_df = false;
     [[maybe_unused]] bool use_dfe = false;
+    [[maybe_unused]] bool use_dfs = false;
+    // per element (double-float scalar forms): the exponents sg, sw, sk, sm
+    // of its gradient, weight, kappa and mass scalings
+    [[maybe_unused]] int* SI = reinterpret_cast<int*>(sm + L.ls);
+    [[maybe_unused]] f2* PH2 = reinterpret_cast<f2*>(sm + L.ph);
     if constexpr (T::P1 != 0) {
         const R wsum = (R)tab[TL.wsum];
         // P1 simplices in the arithmetic of R: unscaled gradients C_b (g_b = C_b / det)
@@ -478,11 +490,82 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                 }
             }
         }
+        if constexpr (DFS) {
+            // Per element, the powers of two of its largest gradient entry,
+            // weight, kappa and the mass scale (a zero scales by 1); a pair
+            // integral is formed in double-float from the scaled values and
+            // scaled back by 2^(2 sg + sw + sk) (diffusion) or 2^(sw + sm)
+            // (mass) before its target's sum.  A chunk with an element whose
+            // shifts leave (-70, 100), or a value that is not finite, keeps
+            // the FP64 path.
+            if constexpr (MASS)
+                for (int t = threadIdx.x; t < Q * B; t += blockDim.x) PH2[t] = split_double(tab[TL.phi + t]);
+            auto shift = [](double v) {
+                const int e = biased_exponent(v);
+                return e == 0 ? 0 : e - 1022;
+            };
+            bool ok = true;
+            for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+                int eg = 0, ew = 0;
+                const R* g = G + (size_t)el * Q * B * D;
+                for (int t = 0; t < Q * B * D; ++t) eg = max(eg, biased_exponent(g[t]));
+                for (int q = 0; q < Q; ++q) ew = max(ew, biased_exponent(JW[el * Q + q]));
+                const int sg = eg == 0 ? 0 : eg - 1022, sw = ew == 0 ? 0 : ew - 1022;
+                ok = ok && eg < 2047 && ew < 2047;
+                int sk = 0, smv = 0;
+                if constexpr (DIFF) {
+                    const double kv = (kap ? ldg(kap + P.elem_perm[i0 + el]) : 1.0) * kscale;
+                    sk = shift(kv);
+                    const int S = 2 * sg + sw + sk;
+                    ok = ok && biased_exponent(kv) < 2047 && S > -70 && S < 100;
+                }
+                if constexpr (MASS) {
+                    smv = shift(mscale);
+                    const int S = sw + smv;
+                    ok = ok && biased_exponent(mscale) < 2047 && S > -70 && S < 100;
+                }
+                SI[4 * el] = sg;
+                SI[4 * el + 1] = sw;
+                SI[4 * el + 2] = sk;
+                SI[4 * el + 3] = smv;
+            }
+            use_dfs = !__syncthreads_or(!ok);
+            if (!use_dfs && threadIdx.x == 0 && a.stats) atomicAdd(a.stats, 1);
+            if (use_dfs) {
+                f2* G2 = reinterpret_cast<f2*>(G);
+                f2* JW2 = reinterpret_cast<f2*>(JW);
+                for (int t = threadIdx.x; t < ne * Q * B * D; t += blockDim.x)
+                    G2[t] = split_scaled(G[t], SI[4 * (t / (Q * B * D))]);
+                for (int t = threadIdx.x; t < ne * Q; t += blockDim.x) JW2[t] = split_scaled(JW[t], SI[4 * (t / Q) + 1]);
+                __syncthreads();
+            }
+        }
         for (int k = threadIdx.x; k < (DIFF || MASS ? ne * NL : 0); k += blockDim.x) {
             const int el = k / NL, l = k - el * NL;
             int pa, pb;
             upper_pair<B>(l, pa, pb);
             const int e = P.elem_perm[i0 + el];
+            if (DFS && use_dfs) {
+                // the scaled pair integrals in double-float
+                const f2* G2 = reinterpret_cast<const f2*>(G);
+                const f2* JW2 = reinterpret_cast<const f2*>(JW);
+                if constexpr (DIFF) {
+                    acc2 sd = {0.0f, 0.0f};
+                    for (int q = 0; q < Q; ++q) {
+                        const f2* g = G2 + (size_t)(el * Q + q) * B * D;
+                        const f2 d = D == 3 ? f2_dot3(g + pa * D, g + pb * D) : f2_dot2(g + pa * D, g + pb * D);
+                        acc_fma(sd, JW2[el * Q + q], d);
+                    }
+                    const double kv = (kap ? ldg(kap + e) : 1.0) * kscale;
+                    reinterpret_cast<f2*>(LD)[k] = f2_mul(split_scaled(kv, SI[4 * el + 2]), acc_value(sd));
+                }
+                if constexpr (MASS) {
+                    acc2 sv = {0.0f, 0.0f};
+                    for (int q = 0; q < Q; ++q) acc_fma(sv, JW2[el * Q + q], f2_mul(PH2[q * B + pa], PH2[q * B + pb]));
+                    reinterpret_cast<f2*>(LM)[k] = f2_mul(split_scaled(mscale, SI[4 * el + 3]), acc_value(sv));
+                }
+                continue;
+            }
             if constexpr (DIFF) {
                 R s = 0;
                 for (int q = 0; q < Q; ++q) {
@@ -624,6 +707,44 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                 reduce(std::true_type{});
             else
                 reduce(std::false_type{});
+            return;
+        }
+    }
+
+    if constexpr (DFS) {
+        if (use_dfs) {
+            // compensated sums of the scaled pair integrals, scaled back by
+            // their element's power of two, in element order; one FP64 add
+            // rounds each target
+            const f2* LD2 = reinterpret_cast<const f2*>(LD);
+            const f2* LM2 = reinterpret_cast<const f2*>(LM);
+            for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+                const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
+                const int32_t tgt = __ldcs(P.slot_target + s0 + j), mir = __ldcs(P.slot_mirror + s0 + j);
+                acc2 sd = {0.0f, 0.0f}, sv = {0.0f, 0.0f};
+                for (int p = p0; p < p1; ++p) {
+                    const int idx = CT[p] >> 1;
+                    const int el = idx / NL;
+                    const int4 sh = reinterpret_cast<const int4*>(SI)[el];
+                    if constexpr (DIFF) {
+                        f2 v = LD2[idx];
+                        const float sc = pow2f(2 * sh.x + sh.y + sh.z);
+                        v.hi = __fmul_rn(v.hi, sc);
+                        v.lo = __fmul_rn(v.lo, sc);
+                        acc_add(sd, v);
+                    }
+                    if constexpr (MASS) {
+                        f2 v = LM2[idx];
+                        const float sc = pow2f(sh.y + sh.w);
+                        v.hi = __fmul_rn(v.hi, sc);
+                        v.lo = __fmul_rn(v.lo, sc);
+                        acc_add(sv, v);
+                    }
+                }
+                const R ad = DIFF ? (R)f2_to_double(acc_value(sd)) : R(0);
+                const R am = MASS ? (R)f2_to_double(acc_value(sv)) : R(0);
+                emit(tgt, mir, ad, am, nullptr);
+            }
             return;
         }
     }

@@ -283,6 +283,50 @@ def test_elasticity_double_float_path_and_fp64_fallback(etype, make, cuda):
 
 
 @pytest.mark.parametrize("etype,make", [
+    ("tetra10", lambda: tg.gen_unit_cube(3, order=2, jitter=0.1, seed=38)),
+    ("triangle6", lambda: tg.gen_unit_square(8, order=2, jitter=0.1, seed=39)),
+    ("quad9", lambda: tg.gen_unit_square(8, order=2, jitter=0.1, seed=40, cell="quad")),
+])
+def test_scalar_forms_double_float_path_and_fp64_fallback(etype, make, cuda):
+    """Float64 diffusion and mass on non-affine elements integrate each local
+    pair in double-float arithmetic on per-element power-of-two scaled
+    values; chunks whose scales leave the window keep FP64.  Fused K + M and
+    K alone match the oracle to 1e-12, and the stats counter tells which path
+    ran (kappa = 0 on some elements stays on the double-float path)."""
+    base = make()
+    E = base.n_elements
+    rng = np.random.default_rng(41)
+    kap0 = rng.lognormal(0.0, 1.0, E)
+    zeros = kap0.copy()
+    zeros[::7] = 0.0
+    cases = {
+        "plain": (1.0, kap0, False),
+        "scaled": (1.0e-3, kap0 * 1e4, False),
+        "zero_kappa": (1.0, zeros, False),
+        "tiny": (1.0e-25, kap0, True),
+        "huge_kappa": (1.0, kap0 * 1e35, True),
+    }
+    for name, (scale, kap, expect_fallback) in cases.items():
+        pts = base.points * scale
+        conn = base.elements()
+        kappa = torch.from_numpy(kap)
+        mesh = tg.Mesh(pts, {etype: conn}).to(cuda)
+        K_asm = tg.LaplaceElementAssembler.from_mesh(mesh)
+        M_asm = tg.MassElementAssembler.from_assembler(K_asm)
+        stats = torch.zeros(1, dtype=torch.int32, device=cuda)
+        K, M = tg.assemble_forms([K_asm, M_asm], mesh.points, {"kappa": kappa.to(cuda)}, _stats=stats)
+        (K1,) = tg.assemble_forms([K_asm], mesh.points, {"kappa": kappa.to(cuda)})
+        _, _, Ko = O.assemble_matrix(pts, conn, base.n_points,
+                                     lambda p, c, kappa: O.element_locals_diffusion(p, c, etype, kappa, 2), kappa=kappa)
+        _, _, Mo = O.assemble_matrix(pts, conn, base.n_points, lambda p, c: O.element_locals_mass(p, c, etype, 2))
+        assert rel_fro(K, Ko) <= TOL, (name, rel_fro(K, Ko))
+        assert rel_fro(M, Mo) <= TOL, (name, rel_fro(M, Mo))
+        assert rel_fro(K1, Ko) <= TOL, (name, rel_fro(K1, Ko))
+        fell_back = int(stats.item())
+        assert (fell_back > 0) == expect_fallback, (name, fell_back)
+
+
+@pytest.mark.parametrize("etype,make", [
     ("tetra", lambda: tg.gen_unit_cube(12, jitter=0.2, seed=71)),
     ("tetra10", lambda: tg.gen_unit_cube(5, order=2, jitter=0.1, seed=72)),
     ("triangle6", lambda: tg.gen_unit_square(20, order=2, jitter=0.1, seed=73)),
