@@ -53,11 +53,11 @@ constexpr int matrix_threads() {
 // resident CTAs per SM the compiler must allow: four 384-thread CTAs of the
 // double-float tet kernel (40 registers), five 256-thread CTAs of the
 // double-float triangle kernel (48 registers), three of the double-float
-// elasticity kernel on non-affine elements (80 registers, 32-element chunks)
+// kernels on non-affine elements (at most 85 registers)
 template <typename R, int ET, int FORMS>
 constexpr int matrix_min_blocks() {
     if (use_df64<R, ET, FORMS>()) return ET == TM_TET4 ? 4 : 5;
-    if (std::is_same<R, double>::value && !Traits<ET>::P1 && (FORMS & TM_FORM_ELASTICITY)) return 3;
+    if (std::is_same<R, double>::value && !Traits<ET>::P1) return 3;
     return 1;
 }
 
@@ -74,7 +74,7 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q, int MS, int MC) {
     constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
     constexpr bool ELAST = (FORMS & TM_FORM_ELASTICITY) != 0;
     constexpr bool DF64 = use_df64<R, ET, FORMS>();
-    constexpr bool DFS = std::is_same<R, double>::value && !T::P1 && (DIFF || MASS);
+    constexpr bool DFG = std::is_same<R, double>::value && !T::P1;
     MatLayout L;
     size_t o = 0;
     L.tab = o;
@@ -90,23 +90,23 @@ __host__ __device__ inline MatLayout mat_layout(int CH, int Q, int MS, int MC) {
         L.jw = o;
         o = align16(o + sizeof(R) * CH * Q);
     }
-    L.ph = o;   // double-float scalar forms: phi at the quadrature points as pairs
-    if (DFS && MASS) o = align16(o + 8 * (size_t)Q * B);
+    L.ph = o;   // double-float path: dphi and w, then (mass) phi, at the quadrature points as pairs
+    if (DFG) o = align16(o + 8 * (size_t)Q * (D * B + 1 + (MASS ? B : 0)));
     L.ld = o;
     if (DIFF) o = align16(o + sizeof(R) * CH * NL);
     L.ls = o;   // double-float paths: per element {scale, |det| rho} as four floats
                 // (affine) or four exponents (the scalar forms on other elements)
-    if (DF64 || DFS) o = align16(o + 16 * (size_t)CH);
+    if (DF64 || DFG) o = align16(o + 16 * (size_t)CH);
     L.lm = o;   // the double-float path's FP64 fallback keeps its masses in the records' space
     if (DF64)
         L.lm = L.ls;
     else if (MASS)
         o = align16(o + sizeof(R) * CH * (T::P1 ? 1 : NL));
     L.le = o;
-    // affine elements: the element blocks; the others: {E lam, E mu, scale}
-    // per element, the blocks being formed from the gradients during the
+    // affine elements: the element blocks; the others: {E lam, E mu} per
+    // element, the blocks being formed from the gradients during the
     // reduction
-    if (ELAST) o = align16(o + sizeof(R) * CH * (T::P1 ? NL * D * D : 3));
+    if (ELAST) o = align16(o + sizeof(R) * CH * (T::P1 ? NL * D * D : 2));
     // the chunk's plan: an mbarrier, then 16-byte windows of slot_ptr and
     // contrib
     L.bar = o;
@@ -140,9 +140,11 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
     // float64 elasticity on non-affine elements: geometry in FP64, blocks
     // and their sums in double-float arithmetic on the FP32 pipes
     constexpr bool DFE = std::is_same<R, double>::value && !T::P1 && ELAST;
-    // float64 diffusion / mass on non-affine elements: geometry in FP64, the
-    // pair integrals and the target sums in double-float
+    // float64 diffusion / mass on non-affine elements: the pair integrals
+    // and the target sums in double-float
     constexpr bool DFS = std::is_same<R, double>::value && !T::P1 && (DIFF || MASS);
+    // any float64 form on non-affine elements: geometry in double-float too
+    constexpr bool DFG = DFE || DFS;
     constexpr int HH = ELAST ? D * D : 1;
     const tm_chunk_plan& P = a.plan;
     const int CH = P.chunk_elems, Q = a.tables.n_quad;
@@ -233,12 +235,15 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
     const R cmu = R(1) / (R(2) * (R(1) + nu));
 
     bool use_df = false;
-    [[maybe_unused]] bool use_dfe = false;
-    [[maybe_unused]] bool use_dfs = false;
-    // per element (double-float scalar forms): the exponents sg, sw, sk, sm
-    // of its gradient, weight, kappa and mass scalings
+    [[maybe_unused]] bool use_dfg = false;
+    // per element (double-float, non-affine): the exponents {sg, sw, sk, sm}
+    // of its gradient, weight, kappa and mass scalings (elasticity: {sg, sw,
+    // se, S})
     [[maybe_unused]] int* SI = reinterpret_cast<int*>(sm + L.ls);
-    [[maybe_unused]] f2* PH2 = reinterpret_cast<f2*>(sm + L.ph);
+    // dphi [Q][D][B], w [Q] and (mass) phi [Q][B] as double-float pairs
+    [[maybe_unused]] f2* DP2 = reinterpret_cast<f2*>(sm + L.ph);
+    [[maybe_unused]] f2* W2 = DP2 + Q * D * B;
+    [[maybe_unused]] f2* PH2 = W2 + Q;
     if constexpr (T::P1 != 0) {
         const R wsum = (R)tab[TL.wsum];
         // P1 simplices in the arithmetic of R: unscaled gradients C_b (g_b = C_b / det)
@@ -392,160 +397,211 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
         }
     } else {
         R* X = reinterpret_cast<R*>(sm + L.x);
-        for (int k = threadIdx.x; k < ne * B; k += blockDim.x) {
-            const int64_t node = P.conn[i0 * B + k];
+        auto stage_x = [&]() {
+            for (int k = threadIdx.x; k < ne * B; k += blockDim.x) {
+                const int64_t node = P.conn[i0 * B + k];
 #pragma unroll
-            for (int d = 0; d < D; ++d) X[k * D + d] = ldg(pts + node * D + d);
-        }
-        __syncthreads();
-        for (int k = threadIdx.x; k < ne * Q; k += blockDim.x) {
-            const int el = k / Q, q = k - el * Q;
-            const double* dphi = tab + TL.dphi + q * D * B;
-            R J[D][D];
-#pragma unroll
-            for (int r = 0; r < D; ++r)
-#pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    R s = 0;
-#pragma unroll
-                    for (int b = 0; b < B; ++b) s += (R)dphi[r * B + b] * X[(el * B + b) * D + c];
-                    J[r][c] = s;
-                }
-            R cof[D][D];
-            const R det = cofactors<R>(J, cof);
-            const R inv = R(1) / det;
-            R* g = G + (size_t)k * B * D;
-#pragma unroll
-            for (int b = 0; b < B; ++b)
-#pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    R s = 0;
-#pragma unroll
-                    for (int r = 0; r < D; ++r) s += (R)dphi[r * B + b] * cof[r][c];
-                    g[b * D + c] = s * inv;
-                }
-            JW[k] = (R)tab[TL.w + q] * rabs(det);
-        }
-        __syncthreads();
-        if constexpr (ELAST) {
-            // the element's scaled Lame constants; its blocks are formed from
-            // G and JW during the reduction (elasticity is never fused)
-            for (int el = threadIdx.x; el < ne; el += blockDim.x) {
-                const R Ey = (yng ? ldg(yng + P.elem_perm[i0 + el]) : R(1)) * yscale;
-                LE[3 * el] = Ey * clam;
-                LE[3 * el + 1] = Ey * cmu;
+                for (int d = 0; d < D; ++d) X[k * D + d] = ldg(pts + node * D + d);
             }
-        }
-        if constexpr (DFE) {
-            // Per element, powers of two that bring the largest gradient
-            // entry, weight and modulus to [1/2, 1): the element's blocks are
-            // then formed in double-float from values of order one and
-            // scaled back by 2^S (S = 2 sg + sw + se) before they are summed.
-            // A chunk with an element outside the window below (or a value
-            // that is not finite) keeps the FP64 path.
-            bool ok = true;
-            for (int el = threadIdx.x; el < ne; el += blockDim.x) {
-                int eg = 0, ew = 0;
-                const R* g = G + (size_t)el * Q * B * D;
-                for (int t = 0; t < Q * B * D; ++t) eg = max(eg, biased_exponent(g[t]));
-                for (int q = 0; q < Q; ++q) ew = max(ew, biased_exponent(JW[el * Q + q]));
-                const int ee = max(biased_exponent(LE[3 * el]), biased_exponent(LE[3 * el + 1]));
-                const int sg = eg - 1022, sw = ew - 1022, se = ee - 1022;
-                const int S = 2 * sg + sw + se;
-                ok = ok && eg < 2047 && ew < 2047 && ee < 2047 && S > -70 && S < 100;
-                reinterpret_cast<int*>(LE + 3 * el + 2)[0] = sg;
-                reinterpret_cast<int*>(LE + 3 * el + 2)[1] = S;
-                reinterpret_cast<int*>(LE + 3 * el)[0] = sw;       // read back below, before LE is converted
-                reinterpret_cast<int*>(LE + 3 * el)[1] = se;
+            __syncthreads();
+        };
+        // geometry per (element, quadrature point) in the arithmetic of R
+        auto geometry_native = [&]() {
+            for (int k = threadIdx.x; k < ne * Q; k += blockDim.x) {
+                const int el = k / Q, q = k - el * Q;
+                const double* dphi = tab + TL.dphi + q * D * B;
+                R J[D][D];
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int c = 0; c < D; ++c) {
+                        R s = 0;
+#pragma unroll
+                        for (int b = 0; b < B; ++b) s += (R)dphi[r * B + b] * X[(el * B + b) * D + c];
+                        J[r][c] = s;
+                    }
+                R cof[D][D];
+                const R det = cofactors<R>(J, cof);
+                const R inv = R(1) / det;
+                R* g = G + (size_t)k * B * D;
+#pragma unroll
+                for (int b = 0; b < B; ++b)
+#pragma unroll
+                    for (int c = 0; c < D; ++c) {
+                        R s = 0;
+#pragma unroll
+                        for (int r = 0; r < D; ++r) s += (R)dphi[r * B + b] * cof[r][c];
+                        g[b * D + c] = s * inv;
+                    }
+                JW[k] = (R)tab[TL.w + q] * rabs(det);
             }
-            use_dfe = !__syncthreads_or(!ok);
-            if (!use_dfe && threadIdx.x == 0 && a.stats) atomicAdd(a.stats, 1);
-            if (!use_dfe) {
-                // restore the moduli the scale pass overwrote
+            if constexpr (ELAST) {
+                // the element's scaled Lame constants; its blocks are formed
+                // from G and JW during the reduction (elasticity is never fused)
                 for (int el = threadIdx.x; el < ne; el += blockDim.x) {
                     const R Ey = (yng ? ldg(yng + P.elem_perm[i0 + el]) : R(1)) * yscale;
-                    LE[3 * el] = Ey * clam;
-                    LE[3 * el + 1] = Ey * cmu;
-                }
-            } else {
-                // convert in place: the gradients, weights and moduli become
-                // scaled double-float pairs (8 bytes, as the doubles were)
-                f2* G2 = reinterpret_cast<f2*>(G);
-                f2* JW2 = reinterpret_cast<f2*>(JW);
-                for (int t = threadIdx.x; t < ne * Q * B * D; t += blockDim.x) {
-                    const int el = t / (Q * B * D);
-                    G2[t] = split_scaled(G[t], reinterpret_cast<const int*>(LE + 3 * el + 2)[0]);
-                }
-                for (int t = threadIdx.x; t < ne * Q; t += blockDim.x) {
-                    const int el = t / Q;
-                    JW2[t] = split_scaled(JW[t], reinterpret_cast<const int*>(LE + 3 * el)[0]);
-                }
-                __syncthreads();
-                for (int el = threadIdx.x; el < ne; el += blockDim.x) {
-                    const int se = reinterpret_cast<const int*>(LE + 3 * el)[1];
-                    const R Ey = (yng ? ldg(yng + P.elem_perm[i0 + el]) : R(1)) * yscale;
-                    f2* m = reinterpret_cast<f2*>(LE + 3 * el);
-                    m[0] = split_scaled(Ey * clam, se);
-                    m[1] = split_scaled(Ey * cmu, se);
+                    LE[2 * el] = Ey * clam;
+                    LE[2 * el + 1] = Ey * cmu;
                 }
             }
-        }
-        if constexpr (DFS) {
-            // Per element, the powers of two of its largest gradient entry,
-            // weight, kappa and the mass scale (a zero scales by 1); a pair
-            // integral is formed in double-float from the scaled values and
-            // scaled back by 2^(2 sg + sw + sk) (diffusion) or 2^(sw + sm)
-            // (mass) before its target's sum.  A chunk with an element whose
-            // shifts leave (-70, 100), or a value that is not finite, keeps
-            // the FP64 path.
+            __syncthreads();
+        };
+        stage_x();
+        if constexpr (DFG) {
+            // Float64 on non-affine elements, in double-float on the FP32
+            // pipes.  (1) Per element, the coordinate differences to its
+            // first node (FP64 subtractions) scaled by the power of two of
+            // the largest one and split.  (2) Per (element, quadrature
+            // point): Jacobian, cofactors, determinant, its reciprocal, the
+            // gradients and the weight |det| w, on those scaled coordinates.
+            // (3) Per element, powers of two that bring its largest gradient
+            // entry and weight to [1/2, 1), and the form's scales: kappa and
+            // the mass scale (pair integrals scaled back by 2^(2 sg + sw +
+            // sk), 2^(sw + sm)) or the moduli (blocks by 2^S, S = 2 sg + sw +
+            // se).  A chunk with a degenerate element, a value that is not
+            // finite or a shift outside (-70, 100) runs in FP64 instead.
+            for (int t = threadIdx.x; t < Q * D * B; t += blockDim.x) DP2[t] = split_double(tab[TL.dphi + t]);
+            for (int t = threadIdx.x; t < Q; t += blockDim.x) W2[t] = split_double(tab[TL.w + t]);
             if constexpr (MASS)
                 for (int t = threadIdx.x; t < Q * B; t += blockDim.x) PH2[t] = split_double(tab[TL.phi + t]);
+            f2* X2 = reinterpret_cast<f2*>(X);
+            f2* G2 = reinterpret_cast<f2*>(G);
+            f2* JW2 = reinterpret_cast<f2*>(JW);
+            bool ok = true;
+            for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+                const R* xe = X + el * B * D;
+                int ex = 0;
+#pragma unroll
+                for (int b = 1; b < B; ++b)
+#pragma unroll
+                    for (int c = 0; c < D; ++c) ex = max(ex, biased_exponent(xe[b * D + c] - xe[c]));
+                ok = ok && ex > 0 && ex < 2047;
+                const int sx = ex - 1022;
+                // in place, node 0 last (the others are taken relative to it)
+                for (int b = B - 1; b >= 0; --b)
+#pragma unroll
+                    for (int c = 0; c < D; ++c) X2[(el * B + b) * D + c] = split_scaled(xe[b * D + c] - xe[c], sx);
+                SI[4 * el] = sx;
+            }
+            __syncthreads();
+            for (int k = threadIdx.x; k < ne * Q; k += blockDim.x) {
+                const int el = k / Q, q = k - el * Q;
+                const f2* dp = DP2 + q * D * B;
+                const f2* xe = X2 + el * B * D;
+                f2 J[D][D];
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int c = 0; c < D; ++c) {
+                        acc2 t = {0.0f, 0.0f};
+#pragma unroll
+                        for (int b = 1; b < B; ++b) acc_fma(t, dp[r * B + b], xe[b * D + c]);
+                        J[r][c] = acc_value(t);
+                    }
+                f2 cof[D][D];
+                f2 det;
+                if constexpr (D == 3) {
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        const int r1 = (r + 1) % 3, r2 = (r + 2) % 3;
+                        cof[r][0] = f2_diff_of_products(J[r1][1], J[r2][2], J[r1][2], J[r2][1]);
+                        cof[r][1] = f2_diff_of_products(J[r1][2], J[r2][0], J[r1][0], J[r2][2]);
+                        cof[r][2] = f2_diff_of_products(J[r1][0], J[r2][1], J[r1][1], J[r2][0]);
+                    }
+                    det = f2_dot3(J[0], cof[0]);
+                } else {
+                    cof[0][0] = J[1][1];
+                    cof[0][1] = f2_neg(J[1][0]);
+                    cof[1][0] = f2_neg(J[0][1]);
+                    cof[1][1] = J[0][0];
+                    det = f2_diff_of_products(J[0][0], J[1][1], J[0][1], J[1][0]);
+                }
+                const f2 adet = f2_abs(det);
+                const f2 inv = f2_recip(det);
+                ok = ok && adet.hi > 0.0f && f2_in_band(adet, -60, 60) && f2_finite(inv);
+                if constexpr (DIFF || ELAST) {    // (mass needs only the weights)
+                    f2* g = G2 + (size_t)k * B * D;
+#pragma unroll
+                    for (int b = 0; b < B; ++b)
+#pragma unroll
+                        for (int c = 0; c < D; ++c) {
+                            acc2 t = {0.0f, 0.0f};
+#pragma unroll
+                            for (int r = 0; r < D; ++r) acc_fma(t, dp[r * B + b], cof[r][c]);
+                            g[b * D + c] = f2_mul(acc_value(t), inv);
+                        }
+                }
+                JW2[k] = f2_mul(W2[q], adet);
+            }
+            __syncthreads();
+            auto fexp = [](f2 v) { return (int)((__float_as_uint(v.hi) >> 23) & 0xFF); };
             auto shift = [](double v) {
                 const int e = biased_exponent(v);
                 return e == 0 ? 0 : e - 1022;
             };
-            bool ok = true;
             for (int el = threadIdx.x; el < ne; el += blockDim.x) {
-                int eg = 0, ew = 0;
-                const R* g = G + (size_t)el * Q * B * D;
-                for (int t = 0; t < Q * B * D; ++t) eg = max(eg, biased_exponent(g[t]));
-                for (int q = 0; q < Q; ++q) ew = max(ew, biased_exponent(JW[el * Q + q]));
-                const int sg = eg == 0 ? 0 : eg - 1022, sw = ew == 0 ? 0 : ew - 1022;
-                ok = ok && eg < 2047 && ew < 2047;
-                int sk = 0, smv = 0;
+                const int sx = SI[4 * el];
+                f2* g = G2 + (size_t)el * Q * B * D;
+                f2* w = JW2 + el * Q;
+                int fg = 126, fw = 0;    // (126: a mass-only kernel has no gradients to scale)
+                if constexpr (DIFF || ELAST) {
+                    fg = 0;
+                    for (int t = 0; t < Q * B * D; ++t) fg = max(fg, fexp(g[t]));
+                }
+                for (int q = 0; q < Q; ++q) fw = max(fw, fexp(w[q]));
+                // (float exponents in [2^-125, 2^124): the scale factors
+                // below stay normal floats)
+                ok = ok && fg >= 2 && fg <= 251 && fw >= 2 && fw <= 251;
+                const float cg = pow2f(126 - fg), cw = pow2f(126 - fw);    // max to [1/2, 1)
+                if constexpr (DIFF || ELAST)
+                    for (int t = 0; t < Q * B * D; ++t) g[t] = {__fmul_rn(g[t].hi, cg), __fmul_rn(g[t].lo, cg)};
+                for (int q = 0; q < Q; ++q) w[q] = {__fmul_rn(w[q].hi, cw), __fmul_rn(w[q].lo, cw)};
+                const int sg = fg - 126 - sx, sw = fw - 126 + D * sx;
+                const int e = P.elem_perm[i0 + el];
+                int s2 = 0, s3 = 0;
+                if constexpr (ELAST) {
+                    const double Ey = (yng ? ldg(yng + e) : 1.0) * yscale;
+                    const double lam = Ey * clam, mu = Ey * cmu;
+                    const int ee = max(biased_exponent(lam), biased_exponent(mu));
+                    const int se = ee == 0 ? 0 : ee - 1022;
+                    s2 = se;
+                    s3 = 2 * sg + sw + se;
+                    ok = ok && ee < 2047 && s3 > -70 && s3 < 100;
+                    f2* m = reinterpret_cast<f2*>(LE + 2 * el);
+                    m[0] = split_scaled(lam, se);
+                    m[1] = split_scaled(mu, se);
+                }
                 if constexpr (DIFF) {
-                    const double kv = (kap ? ldg(kap + P.elem_perm[i0 + el]) : 1.0) * kscale;
-                    sk = shift(kv);
-                    const int S = 2 * sg + sw + sk;
+                    const double kv = (kap ? ldg(kap + e) : 1.0) * kscale;
+                    s2 = shift(kv);
+                    const int S = 2 * sg + sw + s2;
                     ok = ok && biased_exponent(kv) < 2047 && S > -70 && S < 100;
                 }
                 if constexpr (MASS) {
-                    smv = shift(mscale);
-                    const int S = sw + smv;
+                    s3 = shift(mscale);
+                    const int S = sw + s3;
                     ok = ok && biased_exponent(mscale) < 2047 && S > -70 && S < 100;
                 }
                 SI[4 * el] = sg;
                 SI[4 * el + 1] = sw;
-                SI[4 * el + 2] = sk;
-                SI[4 * el + 3] = smv;
+                SI[4 * el + 2] = s2;
+                SI[4 * el + 3] = s3;
             }
-            use_dfs = !__syncthreads_or(!ok);
-            if (!use_dfs && threadIdx.x == 0 && a.stats) atomicAdd(a.stats, 1);
-            if (use_dfs) {
-                f2* G2 = reinterpret_cast<f2*>(G);
-                f2* JW2 = reinterpret_cast<f2*>(JW);
-                for (int t = threadIdx.x; t < ne * Q * B * D; t += blockDim.x)
-                    G2[t] = split_scaled(G[t], SI[4 * (t / (Q * B * D))]);
-                for (int t = threadIdx.x; t < ne * Q; t += blockDim.x) JW2[t] = split_scaled(JW[t], SI[4 * (t / Q) + 1]);
-                __syncthreads();
+            use_dfg = !__syncthreads_or(!ok);
+            if (!use_dfg) {
+                if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats, 1);
+                stage_x();
+                geometry_native();
             }
+        } else {
+            geometry_native();
         }
         for (int k = threadIdx.x; k < (DIFF || MASS ? ne * NL : 0); k += blockDim.x) {
             const int el = k / NL, l = k - el * NL;
             int pa, pb;
             upper_pair<B>(l, pa, pb);
             const int e = P.elem_perm[i0 + el];
-            if (DFS && use_dfs) {
+            if (DFS && use_dfg) {
                 // the scaled pair integrals in double-float
                 const f2* G2 = reinterpret_cast<const f2*>(G);
                 const f2* JW2 = reinterpret_cast<const f2*>(JW);
@@ -712,7 +768,7 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
     }
 
     if constexpr (DFS) {
-        if (use_dfs) {
+        if (use_dfg) {
             // compensated sums of the scaled pair integrals, scaled back by
             // their element's power of two, in element order; one FP64 add
             // rounds each target
@@ -750,7 +806,7 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
     }
 
     if constexpr (DFE) {
-        if (use_dfe) {
+        if (use_dfg) {
             // each contribution's block from its (element, pair): A = sum_q
             // jw g_a g_b^T and lam A + mu (A^T + tr A I) in double-float on
             // the element's scaled values, scaled back by 2^S exactly, then
@@ -787,8 +843,8 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                             for (int c = 0; c < D; ++c) acc_fma(A[r][c], ar, t[c]);
                         }
                     }
-                    const f2* m = reinterpret_cast<const f2*>(LE + 3 * el);
-                    const float sc = pow2f(reinterpret_cast<const int*>(LE + 3 * el + 2)[1]);
+                    const f2* m = reinterpret_cast<const f2*>(LE + 2 * el);
+                    const float sc = pow2f(SI[4 * el + 3]);
                     f2 Av[D][D];
 #pragma unroll
                     for (int r = 0; r < D; ++r)
@@ -874,7 +930,7 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                             for (int c = 0; c < D; ++c) A[r][c] += ar * t[c];
                         }
                     }
-                    elastic_block_outer<R, D>(A, LE[3 * el], LE[3 * el + 1], tmp);
+                    elastic_block_outer<R, D>(A, LE[2 * el], LE[2 * el + 1], tmp);
                     blk = tmp;
                 }
                 if (code & 1) {

@@ -167,10 +167,12 @@ def chunk_elems(etype: str, block: bool, qorder: int) -> int:
     B, D = info.n_basis, info.dim
     Q = len(element_tables(etype, qorder)["w"])
     NL = B * (B + 1) // 2
-    fixed = 8 * (Q + Q * B + Q * D * B + B * B + B + 1) + 16 * NL + 64
-    # elasticity keeps three scalars per element (its blocks are formed
-    # during the reduction), the scalar forms one value per local pair and form
-    per = 8 * (B * D + Q * B * D + Q) + (24 if block else 16 * NL) + 6 * B * B
+    # tables, mass template and their double-float copies
+    fixed = 8 * (Q + Q * B + Q * D * B + B * B + B + 1) + 16 * NL + 8 * Q * (D * B + 1 + B) + 64
+    # per element: coordinates, gradients and weights per quadrature point,
+    # 16 bytes of scale exponents, then two moduli (elasticity, whose blocks
+    # are formed during the reduction) or one value per local pair and form
+    per = 8 * (B * D + Q * B * D + Q) + 16 + (16 if block else 16 * NL) + 6 * B * B
     while ch > 8 and fixed + ch * per > _CHUNK_SMEM_BUDGET:
         ch //= 2
     return ch
