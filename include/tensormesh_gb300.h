@@ -214,8 +214,9 @@ typedef struct tm_matrix_args {
     tm_chunk_plan plan;
     void* event_begin;         /* optional cudaEvent_t recorded before the element-chunk kernel */
     void* event_end;           /* optional cudaEvent_t recorded after it (before finalisation) */
-    int32_t* stats;            /* optional device int32 [1]: += chunks whose float64 P1 locals left the
-                                  double-float range and were recomputed in FP64 arithmetic */
+    int32_t* stats;            /* optional device int32 [1]: += chunks whose float64 data left the
+                                  double-float range (P1 diffusion / mass, and every form on
+                                  P2 and quadrilateral elements) and ran in FP64 arithmetic */
     void* event_done;          /* optional cudaEvent_t recorded after the call's last launch */
 } tm_matrix_args;
 size_t tm_matrix_workspace_bytes(const tm_matrix_args* args);

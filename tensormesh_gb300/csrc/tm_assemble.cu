@@ -3,19 +3,29 @@
 // One CTA per element chunk (tm_chunk_plan).  Phase 1 computes the element
 // locals of the chunk into shared memory: the geometry of
 // element/element.py:875-968 and element/transformation.py:1219-1276 (for P1
-// simplices once per element, the Jacobian being constant; for P2 per
-// quadrature point), then the integrand of the form summed over quadrature
-// points (assemble/element_assembler.py:190-209, builtin.py:61-178).
-// Phase 2 walks the chunk's targets (CSR positions or nodes) in increasing
-// order and adds their contributions from shared memory in a fixed order
-// (element, then local entry), replacing ReduceProjector's index_add_
-// (assemble/projector.py:95-123).  Targets touched by one chunk only are
-// written directly -- for symmetric forms the value is also written to the
-// transposed CSR position.  For the others each chunk writes a partial, and
-// k_matrix_finalize sums each shared target's partials in chunk order (the
-// node-plan kernels instead let the last chunk to deliver a partial do that
-// sum, see tm_reduce.cuh).  No floating-point value is accumulated
-// atomically: results are bitwise reproducible run to run.
+// simplices once per element, the Jacobian being constant; for P2 and
+// quadrilaterals per quadrature point), then the integrand of the form
+// summed over quadrature points (assemble/element_assembler.py:190-209,
+// builtin.py:61-178).  Phase 2 walks the chunk's targets (CSR positions or
+// nodes) in increasing order and adds their contributions from shared
+// memory in a fixed order (element, then local entry), replacing
+// ReduceProjector's index_add_ (assemble/projector.py:95-123).  Targets
+// touched by one chunk only are written directly -- for symmetric forms the
+// value is also written to the transposed CSR position.  For the others
+// each chunk writes a partial, and k_matrix_finalize sums each shared
+// target's partials in chunk order (the node-plan kernels instead let the
+// last chunk to deliver a partial do that sum, see tm_reduce.cuh).  No
+// floating-point value is accumulated atomically: results are bitwise
+// reproducible run to run.
+//
+// Float64 forms do their arithmetic in double-float on the FP32 pipes
+// (tm_df64.cuh; the FP64 rate of this GPU is 1/62 of its FP32 rate): the P1
+// diffusion / mass kernels from the FP64 coordinate differences on, and on
+// every other element type all forms, on per-element power-of-two scaled
+// values, scaled back exactly before the compensated target sums.  A chunk
+// whose data leave the double-float range runs the same computation in
+// FP64 (counted in tm_matrix_args.stats).  Elasticity on P1 simplices and
+// all float32 forms use the arithmetic of their type.
 #include "tm_assemble_kernels.cuh"
 #include "tm_assemble_quad.h"
 
