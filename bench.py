@@ -15,6 +15,15 @@ the host cores) and the SM clocks seen during the timed region.  The
 reference arm times the reference's op sequence (a restatement in torch) on
 the host cores.  With torchrun, every rank assembles its own copy of the
 mesh ("replicas only": the path has no exchange step).
+
+The other workloads of the path, each printing its own line
+(``--workload``): ``poisson`` (131,072 P1 triangles: a whole solve through
+the public API and its L2 error), ``elasticity`` (196,608 P2 tets: the
+assembly pass, its e2e, condensation and Jacobi-PCG; ``--impl reference
+--workload elasticity`` for the reference's op sequence), ``spmv`` (the
+condensed elasticity operator's SpMV), ``inverse`` (663,552 P1 tets:
+forward solve against the adjoint gradient) and ``batched`` (512 uneven
+triangle meshes in one graph replay against per-mesh calls).
 """
 import argparse
 import json
