@@ -206,8 +206,8 @@ typedef struct tm_matrix_args {
     const void* young;         /* device [E] per-element Young's modulus, or NULL */
     double young_scale;        /* multiplies young (or is E when NULL) */
     double poisson;            /* nu */
-    void* out_diffusion;
-    void* out_mass;
+    void* out_diffusion;       /* outputs of the forms asked for: [nnz] values, [nnz, D, D] for */
+    void* out_mass;            /* elasticity; may be NULL when the plan has no elements */
     void* out_elasticity;
     void* workspace;
     tm_element_tables tables;

@@ -142,8 +142,9 @@ extern "C" int tm_assemble_matrix(const tm_matrix_args* a, tm_stream_t stream) {
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: missing element tables");
     if (a->plan.n_elements > 0 && !a->points)
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: points is null");
-    if (((a->forms & TM_FORM_DIFFUSION) && !a->out_diffusion) || ((a->forms & TM_FORM_MASS) && !a->out_mass) ||
-        ((a->forms & TM_FORM_ELASTICITY) && !a->out_elasticity))
+    if (a->plan.n_elements > 0 &&
+        (((a->forms & TM_FORM_DIFFUSION) && !a->out_diffusion) || ((a->forms & TM_FORM_MASS) && !a->out_mass) ||
+         ((a->forms & TM_FORM_ELASTICITY) && !a->out_elasticity)))
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: output pointer is null");
     if (a->plan.n_partials > 0 && !a->workspace)
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: workspace is null");
@@ -310,8 +311,9 @@ extern "C" int tm_assemble_matrix_noalloc(const tm_matrix_args* a, tm_stream_t s
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: missing element tables");
     if (a->plan.n_elements > 0 && !a->points)
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: points is null");
-    if (((a->forms & TM_FORM_DIFFUSION) && !a->out_diffusion) || ((a->forms & TM_FORM_MASS) && !a->out_mass) ||
-        ((a->forms & TM_FORM_ELASTICITY) && !a->out_elasticity))
+    if (a->plan.n_elements > 0 &&
+        (((a->forms & TM_FORM_DIFFUSION) && !a->out_diffusion) || ((a->forms & TM_FORM_MASS) && !a->out_mass) ||
+         ((a->forms & TM_FORM_ELASTICITY) && !a->out_elasticity)))
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: output pointer is null");
     if (a->dtype != TM_F64 && a->dtype != TM_F32)
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix_noalloc: dtype must be TM_F64 or TM_F32");
