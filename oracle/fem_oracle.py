@@ -345,11 +345,19 @@ _GL_W = {1: [2.0], 2: [1.0, 1.0],
          3: [0.55555555555555555556, 0.88888888888888888889, 0.55555555555555555556],
          4: [0.34785484513745385737, 0.65214515486254614263, 0.65214515486254614263, 0.34785484513745385737],
          5: [0.23692688505618908751, 0.47862867049936646804, 0.56888888888888888889, 0.47862867049936646804,
-             0.23692688505618908751]}
+             0.23692688505618908751],
+         6: [0.17132449237917034504, 0.36076157304813860757, 0.46791393457269104739, 0.46791393457269104739,
+             0.36076157304813860757, 0.17132449237917034504],
+         7: [0.12948496616886969327, 0.27970539148927666790, 0.38183005050511894495, 0.41795918367346938776,
+             0.38183005050511894495, 0.27970539148927666790, 0.12948496616886969327]}
 _GL_P = {1: [0.0], 2: [-0.57735026918962576451, 0.57735026918962576451],
          3: [-0.77459666924148337704, 0.0, 0.77459666924148337704],
          4: [-0.8611363115940526, -0.3399810435848563, 0.3399810435848563, 0.8611363115940526],
-         5: [-0.9061798459386640, -0.5384693101056831, 0.0, 0.5384693101056831, 0.9061798459386640]}
+         5: [-0.9061798459386640, -0.5384693101056831, 0.0, 0.5384693101056831, 0.9061798459386640],
+         6: [-0.9324695142031521, -0.6612093864662645, -0.2386191860831969, 0.2386191860831969,
+             0.6612093864662645, 0.9324695142031521],
+         7: [-0.9491079123427585, -0.7415311855993945, -0.4058451513773972, 0.0, 0.4058451513773972,
+             0.7415311855993945, 0.9491079123427585]}
 _FACET_VERTS = {2: [[0, 1], [1, 2], [2, 0]], 3: [[0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]]}
 
 

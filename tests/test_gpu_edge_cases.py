@@ -72,3 +72,35 @@ def test_empty_mesh(cuda):
     assert K.values.numel() == 0 and K.shape == (3, 3)
     b = tg.const_node_assembler(1.0).from_mesh(mesh)(mesh.points)
     assert b.shape == (3,) and float(b.abs().sum()) == 0.0
+
+
+@pytest.mark.parametrize("etype,make,qorder", [
+    ("tetra10", lambda: tg.gen_unit_cube(3, order=2, jitter=0.1, seed=141), 4),
+    ("triangle6", lambda: tg.gen_unit_square(6, order=2, jitter=0.1, seed=142), 4),
+    ("quad9", lambda: tg.gen_unit_square(6, order=2, jitter=0.1, seed=143, cell="quad"), 7),
+    ("quad", lambda: tg.gen_unit_square(8, jitter=0.2, seed=144, cell="quad"), 7),
+])
+def test_highest_quadrature_orders(etype, make, qorder, cuda):
+    """The largest tabulated rules (tet and triangle order 4, quadrilateral
+    order 7: 49 points) shrink the chunks until their shared memory fits;
+    every form still matches the oracle."""
+    from tensormesh_gb300.plan import chunk_elems, CHUNK_ELEMS
+    base = make()
+    mesh = base.to(cuda)
+    E = base.n_elements
+    kappa = torch.from_numpy(np.random.default_rng(145).lognormal(0.0, 1.0, E))
+    Ey = torch.from_numpy(np.random.default_rng(146).uniform(0.5, 2.0, E))
+    K_asm = tg.LaplaceElementAssembler.from_mesh(mesh, quadrature_order=qorder)
+    K, M = tg.assemble_forms([K_asm, tg.MassElementAssembler.from_assembler(K_asm)], mesh.points,
+                             {"kappa": kappa.to(cuda)})
+    El = tg.LinearElasticityElementAssembler.from_assembler(K_asm, nu=0.3)(mesh.points, element_data={"E": Ey.to(cuda)})
+    pts, conn = base.points, base.elements()
+    _, _, Ko = O.assemble_matrix(pts, conn, base.n_points,
+                                 lambda p, c, kappa: O.element_locals_diffusion(p, c, etype, kappa, qorder), kappa=kappa)
+    _, _, Mo = O.assemble_matrix(pts, conn, base.n_points, lambda p, c: O.element_locals_mass(p, c, etype, qorder))
+    _, _, Eo = O.assemble_matrix(pts, conn, base.n_points,
+                                 lambda p, c, E: O.element_locals_elasticity(p, c, etype, E, 0.3, qorder), E=Ey)
+    assert rel_fro(K, Ko) <= 1e-12 and rel_fro(M, Mo) <= 1e-12
+    assert rel_fro(El.values, Eo) <= 1e-12
+    if etype == "quad9":
+        assert chunk_elems(etype, True, qorder) < CHUNK_ELEMS[(etype, True)]
