@@ -1,5 +1,5 @@
-"""Batched assembly and solve of many P1 diffusion problems on meshes of
-uneven size.
+"""Batched assembly and solve of many diffusion problems on meshes of
+uneven size (one element type per batch: any type the assemblers take).
 
 The reference handles a set of different meshes by looping: build the mesh,
 ``from_mesh``, assemble, condense, solve, one mesh after another
@@ -36,14 +36,16 @@ class BatchStatus:
 
 class BatchedDiffusion:
     """K_m(kappa_m) u_m = b_m(f_m) with zero Dirichlet data on each mesh's
-    boundary, for a list of meshes of one P1 element type."""
+    boundary, for a list of meshes of one element type."""
 
     def __init__(self, meshes: Sequence[Mesh], quadrature_order: int = 2,
                  device: Optional[torch.device] = None, dtype: torch.dtype = torch.float64):
         from .builtin import LaplaceElementAssembler, LoadNodeAssembler
+        from .element import element_info
         types = {m.default_element_type for m in meshes}
-        if len(types) != 1 or next(iter(types)) not in ("triangle", "tetra"):
-            raise NotImplementedError("a batch holds meshes of one P1 element type")
+        if len(types) != 1:
+            raise NotImplementedError("a batch holds meshes of one element type")
+        element_info(next(iter(types)))             # raises for a type the assemblers do not take
         etype = next(iter(types))
         dev = torch.device(device) if device is not None else meshes[0].device
         self.n_systems = len(meshes)
