@@ -19,19 +19,45 @@
 #include <new>
 #include <numeric>
 #include <thread>
+#include <type_traits>
 #include <utility>
 #include <vector>
+
+// Allocator whose value-less construct leaves an element uninitialised:
+// resize() then does not zero the pages on one thread, and the parallel
+// loops that fill the arrays are the first to touch them.
+template <class T>
+struct uninit_alloc : std::allocator<T> {
+    using value_type = T;
+    template <class U>
+    struct rebind {
+        using other = uninit_alloc<U>;
+    };
+    uninit_alloc() = default;
+    template <class U>
+    uninit_alloc(const uninit_alloc<U>&) noexcept {}
+    template <class U>
+    void construct(U* q) noexcept(std::is_nothrow_default_constructible<U>::value) {
+        ::new ((void*)q) U;
+    }
+    template <class U, class... A>
+    void construct(U* q, A&&... a) {
+        ::new ((void*)q) U(std::forward<A>(a)...);
+    }
+};
+template <class T>
+using buffer = std::vector<T, uninit_alloc<T>>;
 
 struct tm_host_plan {
     int32_t kind = 0, n_basis = 0, n_local = 0, chunk_elems = 0, n_chunks = 0;
     int64_t n_elements = 0, n_points = 0, nnz = 0, n_partials = 0;
-    std::vector<int32_t> edge_row, edge_col;
-    std::vector<int64_t> slot;
-    std::vector<int32_t> chunk_begin, chunk_contrib, slot_ptr, slot_target, slot_mirror;
+    buffer<int32_t> edge_row, edge_col;
+    buffer<int64_t> slot;
+    buffer<int32_t> chunk_begin, chunk_contrib, slot_ptr, slot_target, slot_mirror;
     int32_t max_chunk_slots = 0, max_chunk_contrib = 0;
-    std::vector<uint16_t> contrib;
-    std::vector<int32_t> shared_ptr, shared_target, shared_mirror;
-    std::vector<int32_t> conn, perm;
+    buffer<uint16_t> contrib;
+    buffer<int32_t> shared_ptr, shared_target, shared_mirror;
+    buffer<int32_t> conn, perm;
 };
 
 namespace {
@@ -52,7 +78,8 @@ int host_threads() {
 }
 
 // f(begin, end) over T contiguous ranges of [0, n) on T threads (the calling
-// thread takes the first); an allocation failure on any thread is rethrown
+// thread takes the first, and the ranges of threads that could not be
+// started); an allocation failure on any thread is rethrown as bad_alloc
 template <class F>
 void parallel_for(int64_t n, int T, F&& f) {
     if (n <= 0) return;
@@ -71,11 +98,19 @@ void parallel_for(int64_t n, int T, F&& f) {
         }
     };
     std::vector<std::thread> pool;
-    for (int t = 1; t < T; ++t) {
-        const int64_t b = t * step, e = std::min(n, b + step);
-        if (b < e) pool.emplace_back(run, b, e);
+    int64_t rest = std::min(n, step);   // [rest, n) has no thread: the calling thread runs it
+    try {
+        pool.reserve(T - 1);
+        for (int t = 1; t < T; ++t) {
+            const int64_t b = t * step, e = std::min(n, b + step);
+            if (b >= e) break;
+            pool.emplace_back(run, b, e);
+            rest = e;
+        }
+    } catch (...) {
     }
     run(0, std::min(n, step));
+    if (rest < n) run(rest, n);
     for (auto& th : pool) th.join();
     if (failed) throw std::bad_alloc();
 }
@@ -104,7 +139,7 @@ void build_pattern(tm_host_plan& p, const int64_t* conn) {
         }
         row_ptr[r + 1] = row_ptr[r] + o;
     }
-    std::vector<int32_t> cols(row_ptr[N]);
+    buffer<int32_t> cols(row_ptr[N]);
     parallel_for(T, T, [&](int64_t t0, int64_t t1) {
         for (int64_t t = t0; t < t1; ++t)
             for (int64_t e = t * estep; e < std::min(E, (t + 1) * estep); ++e)
@@ -175,9 +210,18 @@ int build_chunks(tm_host_plan& p) {
     const int n_parts = (int)((p.n_chunks + per - 1) / per);
     std::vector<Part> parts(n_parts);
     parallel_for(n_parts, T, [&](int64_t part_begin, int64_t part_end) {
+        // A chunk holds fewer than 65536 contributions (codes are 16-bit),
+        // so a group's count and number fit in 16 bits.  Targets are grouped
+        // in an open-addressing table (target -> group, groups numbered by
+        // first appearance) of at least twice that many entries.
         std::vector<Contribution> buf;
-        std::vector<int32_t> order;
-        std::vector<std::pair<int32_t, int32_t>> groups;   // (first position in order, count)
+        int bits = 4;
+        while ((int64_t(1) << bits) < 4 * (int64_t)CH * NL) ++bits;
+        std::vector<int32_t> hkey(size_t(1) << bits, -1), hgroup(size_t(1) << bits);
+        std::vector<uint32_t> gslot;
+        std::vector<int32_t> group_of, gtarget, gmirror, gcount;
+        std::vector<uint64_t> gorder;   // (65535 - count, target, group), ascending
+        std::vector<size_t> gstart;
         for (int64_t pi = part_begin; pi < part_end; ++pi) {
             Part& out = parts[pi];
             const int64_t k0 = pi * per, k1 = std::min<int64_t>(p.n_chunks, k0 + per);
@@ -208,32 +252,52 @@ int build_chunks(tm_host_plan& p) {
                         for (int a = 0; a < B; ++a) buf.push_back({c[a], -1, (uint16_t)((el * NL + a) << 1)});
                     }
                 }
-                order.resize(buf.size());
-                std::iota(order.begin(), order.end(), 0);
-                std::stable_sort(order.begin(), order.end(),
-                                 [&](int32_t x, int32_t y) { return buf[x].target < buf[y].target; });
-                // runs of one target, then emitted by decreasing contribution
-                // count so that the threads of a warp (one target each) loop
-                // equally long; a target's own contributions keep their
-                // (element, entry) order
-                groups.clear();
-                for (size_t q = 0; q < order.size(); ++q)
-                    if (q == 0 || buf[order[q - 1]].target != buf[order[q]].target) groups.push_back({(int32_t)q, 0});
-                for (size_t g = 0; g < groups.size(); ++g)
-                    groups[g].second =
-                        (g + 1 < groups.size() ? groups[g + 1].first : (int32_t)order.size()) - groups[g].first;
-                std::stable_sort(groups.begin(), groups.end(),
-                                 [](const std::pair<int32_t, int32_t>& x, const std::pair<int32_t, int32_t>& y) {
-                                     return x.second > y.second;
-                                 });
-                for (const auto& g : groups) {
-                    const Contribution& head = buf[order[g.first]];
-                    out.slot_target.push_back(head.target);
-                    out.slot_mirror.push_back(head.mirror);
-                    out.slot_len.push_back(g.second);
-                    for (int32_t q = g.first; q < g.first + g.second; ++q) out.contrib.push_back(buf[order[q]].code);
+                // one group (slot) per target; targets are non-negative
+                gslot.clear();
+                gtarget.clear();
+                gmirror.clear();
+                gcount.clear();
+                group_of.resize(buf.size());
+                for (size_t q = 0; q < buf.size(); ++q) {
+                    const int32_t t = buf[q].target;
+                    uint32_t h = ((uint32_t)t * 2654435761u) >> (32 - bits);
+                    while (hkey[h] != -1 && hkey[h] != t) h = (h + 1) & ((1u << bits) - 1);
+                    if (hkey[h] == -1) {
+                        hkey[h] = t;
+                        hgroup[h] = (int32_t)gtarget.size();
+                        gslot.push_back(h);
+                        gtarget.push_back(t);
+                        gmirror.push_back(buf[q].mirror);
+                        gcount.push_back(0);
+                    }
+                    group_of[q] = hgroup[h];
+                    ++gcount[hgroup[h]];
                 }
-                out.chunk_slots.push_back((int32_t)groups.size());
+                for (const uint32_t h : gslot) hkey[h] = -1;
+                // slots by decreasing contribution count, so that the threads
+                // of a warp (one slot each) loop equally long, then by target;
+                // a slot's contributions keep their (element, entry) order
+                const size_t G = gtarget.size();
+                gorder.resize(G);
+                for (size_t g = 0; g < G; ++g)
+                    gorder[g] = (uint64_t)(65535 - gcount[g]) << 48 | (uint64_t)gtarget[g] << 16 | g;
+                std::sort(gorder.begin(), gorder.end());
+                const size_t s0 = out.slot_target.size(), c0 = out.contrib.size();
+                out.slot_target.resize(s0 + G);
+                out.slot_mirror.resize(s0 + G);
+                out.slot_len.resize(s0 + G);
+                out.contrib.resize(c0 + buf.size());
+                gstart.resize(G);
+                for (size_t i = 0, c = c0; i < G; ++i) {
+                    const size_t g = gorder[i] & 0xFFFF;
+                    out.slot_target[s0 + i] = gtarget[g];
+                    out.slot_mirror[s0 + i] = gmirror[g];
+                    out.slot_len[s0 + i] = gcount[g];
+                    gstart[g] = c;
+                    c += gcount[g];
+                }
+                for (size_t q = 0; q < buf.size(); ++q) out.contrib[gstart[group_of[q]]++] = buf[q].code;
+                out.chunk_slots.push_back((int32_t)G);
             }
         }
     });
@@ -248,7 +312,8 @@ int build_chunks(tm_host_plan& p) {
     p.chunk_begin.assign(p.n_chunks + 1, 0);
     p.slot_target.resize(n_slots);
     p.slot_mirror.resize(n_slots);
-    p.slot_ptr.assign(n_slots + 1, 0);
+    p.slot_ptr.resize(n_slots + 1);
+    p.slot_ptr[0] = 0;
     p.contrib.resize(n_contrib);
     parallel_for(n_parts, T, [&](int64_t q0, int64_t q1) {
         for (int64_t q = q0; q < q1; ++q) {
@@ -272,12 +337,23 @@ int build_chunks(tm_host_plan& p) {
             }
     }
     parts.clear();
-    std::vector<int32_t> chunks_per_target(n_targets, 0);
-    std::vector<int32_t> mirror_of(matrix ? n_targets : 0, -1);
-    for (size_t j = 0; j < n_slots; ++j) {
-        chunks_per_target[p.slot_target[j]] += 1;
-        if (matrix) mirror_of[p.slot_target[j]] = p.slot_mirror[j];
-    }
+    // partials per target (the chunks that touch it) and, for the matrix,
+    // the mirror of every target: counts commute, so relaxed atomic adds on
+    // host threads give the same counts for any number of threads, and all
+    // slots of one target carry the same mirror
+    buffer<int32_t> chunks_per_target(n_targets);
+    buffer<int32_t> mirror_of(matrix ? n_targets : 0);
+    parallel_for(n_targets, T, [&](int64_t t0, int64_t t1) {
+        std::fill(chunks_per_target.begin() + t0, chunks_per_target.begin() + t1, 0);
+        if (matrix) std::fill(mirror_of.begin() + t0, mirror_of.begin() + t1, -1);
+    });
+    parallel_for((int64_t)n_slots, T, [&](int64_t s0, int64_t s1) {
+        for (int64_t s = s0; s < s1; ++s) {
+            const int32_t t = p.slot_target[s];
+            __atomic_fetch_add(&chunks_per_target[t], 1, __ATOMIC_RELAXED);
+            if (matrix) __atomic_store_n(&mirror_of[t], p.slot_mirror[s], __ATOMIC_RELAXED);
+        }
+    });
     // first contribution of every chunk, and the largest chunk, for kernels
     // that stage a chunk's slots and contributions in shared memory
     p.chunk_contrib.resize(p.chunk_begin.size());
@@ -286,34 +362,86 @@ int build_chunks(tm_host_plan& p) {
         p.max_chunk_slots = std::max(p.max_chunk_slots, p.chunk_begin[k + 1] - p.chunk_begin[k]);
         p.max_chunk_contrib = std::max(p.max_chunk_contrib, p.chunk_contrib[k + 1] - p.chunk_contrib[k]);
     }
-    // shared targets, numbered by decreasing partial count and then by
-    // target (neighbouring threads of the finalizing kernel loop equally
-    // long); their partials are contiguous per target and ordered by chunk
-    std::vector<int32_t> shared_index(n_targets, -1);
-    std::vector<int32_t> by_count;
-    for (int64_t t = 0; t < n_targets; ++t)
-        if (chunks_per_target[t] > 1) by_count.push_back((int32_t)t);
-    std::stable_sort(by_count.begin(), by_count.end(), [&](int32_t x, int32_t y) {
-        return chunks_per_target[x] > chunks_per_target[y];
+    // shared targets (touched by more than one chunk), numbered by
+    // decreasing partial count and then by target (neighbouring threads of
+    // the finalizing kernel loop equally long); their partials are
+    // contiguous per target and ordered by chunk.  The numbering is a stable
+    // counting sort on the count over ranges of targets on host threads; the
+    // histograms (ranges x counts) stay within n_targets entries.
+    int32_t max_count = 0;
+    for (int64_t t = 0; t < n_targets; ++t) max_count = std::max(max_count, chunks_per_target[t]);
+    const int64_t W = (int64_t)max_count + 1;
+    const int64_t R = std::max<int64_t>(1, std::min<int64_t>(T, n_targets / W));
+    const int64_t tstep = std::max<int64_t>(1, (n_targets + R - 1) / R);
+    std::vector<int64_t> hist((size_t)(R * W), 0);
+    parallel_for(R, T, [&](int64_t r0, int64_t r1) {
+        for (int64_t r = r0; r < r1; ++r)
+            for (int64_t t = r * tstep; t < std::min(n_targets, (r + 1) * tstep); ++t)
+                if (chunks_per_target[t] > 1) ++hist[r * W + chunks_per_target[t]];
     });
-    p.shared_ptr.assign(1, 0);
-    for (const int32_t t : by_count) {
-        shared_index[t] = (int32_t)p.shared_target.size();
-        p.shared_target.push_back(t);
-        p.shared_mirror.push_back(matrix ? mirror_of[t] : -1);
-        p.shared_ptr.push_back(p.shared_ptr.back() + chunks_per_target[t]);
-    }
-    p.n_partials = p.shared_ptr.back();
-    std::vector<int32_t> used(p.shared_target.size(), 0);
-    for (size_t s = 0; s < p.slot_target.size(); ++s) {
-        const int32_t t = p.slot_target[s];
-        const int32_t sh = shared_index[t];
-        if (sh >= 0) {
-            const int32_t part = p.shared_ptr[sh] + used[sh]++;
-            p.slot_target[s] = -(part + 1);
-            p.slot_mirror[s] = sh;
+    // offsets in the order (count descending, range, target), and the first
+    // index and first partial of every count
+    std::vector<int64_t> class_first(W, 0), class_partial(W, 0);
+    int64_t n_shared = 0, n_partials = 0;
+    for (int64_t c = W - 1; c >= 2; --c) {
+        class_first[c] = n_shared;
+        class_partial[c] = n_partials;
+        for (int64_t r = 0; r < R; ++r) {
+            const int64_t h = hist[r * W + c];
+            hist[r * W + c] = n_shared;
+            n_shared += h;
         }
+        n_partials += (n_shared - class_first[c]) * c;
     }
+    buffer<int32_t> shared_index(n_targets);
+    p.shared_target.resize(n_shared);
+    p.shared_mirror.resize(n_shared);
+    p.shared_ptr.resize(n_shared + 1);
+    parallel_for(R, T, [&](int64_t r0, int64_t r1) {
+        for (int64_t r = r0; r < r1; ++r)
+            for (int64_t t = r * tstep; t < std::min(n_targets, (r + 1) * tstep); ++t) {
+                const int32_t c = chunks_per_target[t];
+                if (c > 1) {
+                    const int64_t i = hist[r * W + c]++;
+                    shared_index[t] = (int32_t)i;
+                    p.shared_target[i] = (int32_t)t;
+                    p.shared_mirror[i] = matrix ? mirror_of[t] : -1;
+                    p.shared_ptr[i] = (int32_t)(class_partial[c] + (i - class_first[c]) * c);
+                } else {
+                    shared_index[t] = -1;
+                }
+            }
+    });
+    p.shared_ptr[n_shared] = (int32_t)n_partials;
+    p.n_partials = n_partials;
+    // a shared slot's partial is the next one of its target in slot (=
+    // chunk) order.  Host threads own ranges of shared targets holding about
+    // equal numbers of partials and each scans all slots, so the counter of
+    // every target advances in slot order on one thread.
+    buffer<int32_t> slot_shared(n_slots);
+    parallel_for((int64_t)n_slots, T, [&](int64_t s0, int64_t s1) {
+        for (int64_t s = s0; s < s1; ++s) slot_shared[s] = shared_index[p.slot_target[s]];
+    });
+    const int64_t TO = std::max<int64_t>(1, std::min<int64_t>(T, n_shared));
+    std::vector<int64_t> own(TO + 1, n_shared);
+    for (int64_t o = 0; o < TO; ++o)
+        own[o] = std::lower_bound(p.shared_ptr.begin(), p.shared_ptr.begin() + n_shared, n_partials * o / TO) -
+                 p.shared_ptr.begin();
+    buffer<int32_t> next(n_shared);
+    parallel_for(TO, T, [&](int64_t o0, int64_t o1) {
+        for (int64_t o = o0; o < o1; ++o) {
+            const int32_t lo = (int32_t)own[o], n_own = (int32_t)(own[o + 1] - own[o]);
+            if (n_own <= 0) continue;
+            for (int32_t sh = lo; sh < lo + n_own; ++sh) next[sh] = p.shared_ptr[sh];
+            for (size_t s = 0; s < n_slots; ++s) {
+                const int32_t sh = slot_shared[s];
+                if ((uint32_t)(sh - lo) < (uint32_t)n_own) {
+                    p.slot_target[s] = -(next[sh]++ + 1);
+                    p.slot_mirror[s] = sh;
+                }
+            }
+        }
+    });
     return TM_OK;
 }
 
@@ -426,11 +554,19 @@ extern "C" int tm_plan_build(const int64_t* conn, int64_t n_elements, int32_t n_
         p->n_points = n_points;
         p->chunk_elems = chunk_elems;
         p->n_local = kind == TM_PLAN_KIND_MATRIX ? n_basis * (n_basis + 1) / 2 : n_basis;
-        for (int64_t k = 0; k < n_elements * n_basis; ++k)
-            if (conn[k] < 0 || conn[k] >= n_points) {
-                delete p;
-                return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_build: connectivity index out of range");
-            }
+        const int T = host_threads();
+        std::atomic<bool> bad_index(false);
+        parallel_for(n_elements * n_basis, T, [&](int64_t k0, int64_t k1) {
+            for (int64_t k = k0; k < k1; ++k)
+                if (conn[k] < 0 || conn[k] >= n_points) {
+                    bad_index = true;
+                    return;
+                }
+        });
+        if (bad_index) {
+            delete p;
+            return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_build: connectivity index out of range");
+        }
         p->perm.resize(n_elements);
         if (perm) {
             std::vector<char> seen(n_elements, 0);
@@ -446,15 +582,32 @@ extern "C" int tm_plan_build(const int64_t* conn, int64_t n_elements, int32_t n_
             std::iota(p->perm.begin(), p->perm.end(), 0);
         }
         p->conn.resize((size_t)n_elements * n_basis);
-        for (int64_t i = 0; i < n_elements; ++i)
-            for (int a = 0; a < n_basis; ++a)
-                p->conn[i * n_basis + a] = (int32_t)conn[(int64_t)p->perm[i] * n_basis + a];
+        parallel_for(n_elements, T, [&](int64_t i0, int64_t i1) {
+            for (int64_t i = i0; i < i1; ++i)
+                for (int a = 0; a < n_basis; ++a)
+                    p->conn[i * n_basis + a] = (int32_t)conn[(int64_t)p->perm[i] * n_basis + a];
+        });
         if (kind == TM_PLAN_KIND_MATRIX) {
             if (slot_map) {
-                p->slot.assign(slot_map, slot_map + (size_t)n_elements * n_basis * n_basis);
-                int64_t mx = -1;
-                for (int64_t v : p->slot) mx = std::max(mx, v);
-                p->nnz = mx + 1;
+                const int64_t n_slot = n_elements * n_basis * n_basis;
+                p->slot.resize(n_slot);
+                std::vector<int64_t> range_max(T, -1), range_min(T, 0);
+                const int64_t step = (n_slot + T - 1) / T;
+                parallel_for(T, T, [&](int64_t t0, int64_t t1) {
+                    for (int64_t t = t0; t < t1; ++t) {
+                        const int64_t b = std::min(n_slot, t * step), e = std::min(n_slot, b + step);
+                        std::copy(slot_map + b, slot_map + e, p->slot.begin() + b);
+                        for (int64_t k = b; k < e; ++k) {
+                            range_max[t] = std::max(range_max[t], slot_map[k]);
+                            range_min[t] = std::min(range_min[t], slot_map[k]);
+                        }
+                    }
+                });
+                if (*std::min_element(range_min.begin(), range_min.end()) < 0) {
+                    delete p;
+                    return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_build: negative slot_map entry");
+                }
+                p->nnz = *std::max_element(range_max.begin(), range_max.end()) + 1;
             } else {
                 build_pattern(*p, conn);
             }
@@ -497,9 +650,19 @@ extern "C" int64_t tm_plan_array_size(const tm_host_plan* p, int32_t id) {
     }
 }
 
+// copies in 4 MB pieces on host threads: the caller's fresh destination
+// pages are first touched in parallel
 template <typename T>
-static int copy_vec(const std::vector<T>& v, void* dst) {
-    if (!v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(T));
+static int copy_vec(const buffer<T>& v, void* dst) {
+    const int64_t n = (int64_t)v.size() * (int64_t)sizeof(T), piece = 4 << 20;
+    try {
+        parallel_for((n + piece - 1) / piece, host_threads(), [&](int64_t q0, int64_t q1) {
+            const int64_t b = q0 * piece, e = std::min(n, q1 * piece);
+            std::memcpy((char*)dst + b, (const char*)v.data() + b, (size_t)(e - b));
+        });
+    } catch (...) {
+        return tm_set_error(TM_ERR_PLAN, "tm_plan_copy_array: out of host memory");
+    }
     return TM_OK;
 }
 

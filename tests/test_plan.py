@@ -123,6 +123,36 @@ def test_degenerate_repeated_node():
     np.testing.assert_allclose(emulate_matrix(h, loc), ref, atol=1e-13)
 
 
+def _fan(n):
+    """n triangles around node 0 (one node in every element: its targets
+    are shared by every chunk), ring nodes in shuffled numbering."""
+    ang = np.linspace(0.0, 2 * np.pi, n, endpoint=False)
+    pts = np.concatenate([[[0.0, 0.0]], np.stack([np.cos(ang), np.sin(ang)], 1)])
+    ring = 1 + np.random.default_rng(3).permutation(n)
+    conn = np.stack([np.zeros(n, np.int64), ring, np.roll(ring, -1)], 1)
+    return torch.from_numpy(pts), torch.from_numpy(conn)
+
+
+@pytest.mark.parametrize("chunk", [3, 16, 128])
+def test_fan_mesh_high_partial_counts(chunk):
+    """A node in all of 600 elements: its shared targets have a partial from
+    every chunk, and both reductions still match the oracle."""
+    pts, conn_t = _fan(600)
+    conn = conn_t.numpy()
+    perm = morton_order(pts.numpy(), conn)
+    h = HostPlan(conn, pts.shape[0], _lib.TM_PLAN_KIND_MATRIX, chunk, perm)
+    assert np.diff(h.arrays["shared_ptr"]).max() == h.n_chunks
+    E = torch.rand(conn.shape[0], dtype=torch.float64, generator=torch.Generator().manual_seed(2)) + 0.5
+    loc = O.element_locals_elasticity(pts, conn_t, "triangle", E, 0.3, 2).numpy()
+    _, _, ref = O.assemble_matrix(pts, conn_t, pts.shape[0],
+                                  lambda p, c, E: O.element_locals_elasticity(p, c, "triangle", E, 0.3, 2), E=E)
+    np.testing.assert_allclose(emulate_matrix(h, loc), ref.numpy(), rtol=0, atol=1e-13 * np.abs(ref.numpy()).max())
+    hn = HostPlan(conn, pts.shape[0], _lib.TM_PLAN_KIND_NODE, chunk, perm)
+    locv = np.random.default_rng(4).standard_normal((conn.shape[0], 3, 1))
+    refv = O.reduce_project(conn_t.reshape(-1), torch.from_numpy(locv.reshape(-1, 1)), pts.shape[0])
+    np.testing.assert_allclose(emulate_vector(hn, locv, pts.shape[0]), refv.numpy(), atol=1e-12)
+
+
 def test_empty_mesh():
     h = HostPlan(np.zeros((0, 4), dtype=np.int64), 5, _lib.TM_PLAN_KIND_MATRIX, 16)
     assert h.nnz == 0 and h.n_chunks == 0 and h.n_partials == 0
@@ -135,6 +165,8 @@ def test_rejects_bad_input():
         HostPlan(np.array([[0, 1, 2], [0, 2, 1]]), 3, _lib.TM_PLAN_KIND_MATRIX, 4, perm=np.array([1, 1]))
     with pytest.raises(_lib.TmError):
         HostPlan(np.zeros((10, 10), dtype=np.int64), 10, _lib.TM_PLAN_KIND_MATRIX, 1000)  # u16 overflow
+    with pytest.raises(_lib.TmError):
+        HostPlan(np.array([[0, 1, 2]]), 3, _lib.TM_PLAN_KIND_MATRIX, 4, slot_map=np.array([0, 1, 2, -1, 3, 4, 5, 6, 7]))
 
 
 @pytest.mark.parametrize("kind", [_lib.TM_PLAN_KIND_MATRIX, _lib.TM_PLAN_KIND_NODE])
@@ -170,15 +202,17 @@ def test_plan_independent_of_host_threads(kind, monkeypatch):
     """The plan is built on host threads (TM_HOST_THREADS, default all
     cores); every array is the same whatever their number."""
     m = gen_unit_cube(6, jitter=0.2, seed=7)
-    conn = m.elements().numpy()
-    perm = morton_order(m.points.numpy(), conn)
-    built = []
-    for threads in ("1", "3", "8"):
-        monkeypatch.setenv("TM_HOST_THREADS", threads)
-        built.append(HostPlan(conn, m.n_points, kind, 64, perm))
-    for h in built[1:]:
-        for name, arr in built[0].arrays.items():
-            assert np.array_equal(arr, h.arrays[name]), name
+    fan_pts, fan_conn = _fan(900)
+    for pts, conn, n_points in ((m.points.numpy(), m.elements().numpy(), m.n_points),
+                                (fan_pts.numpy(), fan_conn.numpy(), fan_pts.shape[0])):
+        perm = morton_order(pts, conn)
+        built = []
+        for threads in ("1", "3", "8"):
+            monkeypatch.setenv("TM_HOST_THREADS", threads)
+            built.append(HostPlan(conn, n_points, kind, 64, perm))
+        for h in built[1:]:
+            for name, arr in built[0].arrays.items():
+                assert np.array_equal(arr, h.arrays[name]), name
 
 
 def _spread(x, dims):
