@@ -17,6 +17,7 @@ from .facet import FacetAssembler, LoadFacetAssembler, const_facet_assembler, fu
 from .solve import pcg_solve
 from .condense import Condenser
 from .adjoint import solve_diffusion
+from . import autotune
 
 __version__ = "0.1.0"
 

@@ -32,7 +32,7 @@ def _adjoint_call(topo, points, kappa, kappa_scale, k_mode, weights=None, slot=N
     dev = points.device
     pts = points.detach().to(torch.float64).contiguous()
     E = topo.n_elements
-    plan = topo.node_plan(dev)
+    plan = topo.node_plan(dev)          # static chunk size (the tuner times assembly calls only)
     a = _lib.AdjointArgs()
     a.dtype = _lib.TM_F64
     a.k_mode = k_mode

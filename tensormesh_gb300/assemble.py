@@ -349,7 +349,7 @@ def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_da
                 out[i] = torch.empty(topo.nnz, D, D, dtype=dt, device=dev)
                 args.out_elasticity = _lib.ptr(out[i])
         args.forms = bits
-        plan = topo.matrix_plan(dev, block=block)
+        plan = topo.matrix_plan(dev, block=block, dtype=dt)
         args.plan = plan.struct()
         args.tables = topo.table_struct(dev)
         ws_bytes = lib.tm_matrix_workspace_bytes(C_byref(args))
@@ -563,7 +563,7 @@ def _run_vector(topo: Topology, pts: torch.Tensor, source: int, values: Optional
         raise NotImplementedError("linear forms with more than 3 components per node are not supported")
     lib = _lib.load()
     dev, dt = pts.device, pts.dtype
-    plan = topo.node_plan(dev)
+    plan = topo.node_plan(dev, dtype=dt)
     args = _lib.VectorArgs()
     args.dtype = _lib.dtype_code(dt)
     args.source = source

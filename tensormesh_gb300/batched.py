@@ -11,6 +11,10 @@ launch all load vectors, and a single ``tm_batched_pcg`` launch solves every
 system (Dirichlet nodes masked, no extraction of the condensed blocks).
 ``capture()`` records the three launches in one CUDA graph; ``replay()``
 copies new coefficients and sources into its static buffers and runs it.
+With ``autotune=True`` the elements per chunk of the stiffness and load
+launches are timed over the candidate sizes on the batch itself
+(``autotune.tune_matrix`` / ``tune_vector``) before anything is captured;
+``chunks`` holds the sizes used.
 """
 import ctypes as C
 from dataclasses import dataclass
@@ -39,7 +43,8 @@ class BatchedDiffusion:
     boundary, for a list of meshes of one element type."""
 
     def __init__(self, meshes: Sequence[Mesh], quadrature_order: int = 2,
-                 device: Optional[torch.device] = None, dtype: torch.dtype = torch.float64):
+                 device: Optional[torch.device] = None, dtype: torch.dtype = torch.float64,
+                 autotune: bool = False):
         from .builtin import LaplaceElementAssembler, LoadNodeAssembler
         from .element import element_info
         types = {m.default_element_type for m in meshes}
@@ -66,6 +71,16 @@ class BatchedDiffusion:
         self.order = torch.from_numpy(np.argsort(-sizes, kind="stable").astype(np.int32)).to(dev)
         self.dirichlet = bnd.to(torch.uint8).to(dev)
         self._graph = None
+        if autotune:
+            from . import autotune as tuner
+            pts = self.mesh.points.to(dtype)
+            ones = torch.ones(self.n_elements, dtype=dtype, device=dev)
+            zeros = torch.zeros(self.n_points, dtype=dtype, device=dev)
+            tuner.tune_matrix([self.K_asm], pts, {"kappa": ones})
+            tuner.tune_vector(self.b_asm, pts, {"f": zeros})
+        topo = self.K_asm._topo(True)
+        self.chunks = {"matrix": topo.chunk_for("scalar", dev, dtype),
+                       "node": self.b_asm._topo(False).chunk_for("node", dev, dtype)}
 
     @property
     def n_points(self) -> int:

@@ -153,27 +153,37 @@ NODE_CHUNK_ELEMS = {"triangle": 256, "tetra": 256, "triangle6": 128, "tetra10": 
 _CHUNK_SMEM_BUDGET = 200 * 1024
 
 
-def chunk_elems(etype: str, block: bool, qorder: int) -> int:
-    """Elements per k_matrix chunk: the default of ``CHUNK_ELEMS``, halved
-    while the chunk's shared memory would exceed the budget.  Elements whose
-    Jacobian varies (P2, quadrilaterals) keep the shape gradients of every
-    quadrature point in shared memory, so high quadrature orders need
-    smaller chunks; the estimate follows the kernel's layout (tables,
-    coordinates, gradients and weights per point, locals, staged plan)."""
-    ch = CHUNK_ELEMS[(etype, block)]
-    if etype in ("triangle", "tetra"):
-        return ch
+def chunk_fits(etype: str, block: bool, qorder: int, ch: int) -> bool:
+    """Whether a k_matrix chunk of ``ch`` elements fits: contribution codes
+    are 16-bit (ch * n_local * 2 <= 65536), and for elements whose Jacobian
+    varies (P2, quadrilaterals), which keep the shape gradients of every
+    quadrature point in shared memory, the estimate of the kernel's layout
+    (tables, coordinates, gradients and weights per point, locals, staged
+    plan) stays within the budget.  P1 chunks hold only their locals and
+    staged plan, which the default sizes leave well inside it."""
     info = element_info(etype)
     B, D = info.n_basis, info.dim
-    Q = len(element_tables(etype, qorder)["w"])
     NL = B * (B + 1) // 2
+    if ch < 1 or ch * NL * 2 > 65536:
+        return False
+    if etype in ("triangle", "tetra"):
+        return True
+    Q = len(element_tables(etype, qorder)["w"])
     # tables, mass template and their double-float copies
     fixed = 8 * (Q + Q * B + Q * D * B + B * B + B + 1) + 16 * NL + 8 * Q * (D * B + 1 + B) + 64
     # per element: coordinates, gradients and weights per quadrature point,
     # 16 bytes of scale exponents, then two moduli (elasticity, whose blocks
     # are formed during the reduction) or one value per local pair and form
     per = 8 * (B * D + Q * B * D + Q) + 16 + (16 if block else 16 * NL) + 6 * B * B
-    while ch > 8 and fixed + ch * per > _CHUNK_SMEM_BUDGET:
+    return fixed + ch * per <= _CHUNK_SMEM_BUDGET
+
+
+def chunk_elems(etype: str, block: bool, qorder: int) -> int:
+    """Elements per k_matrix chunk: the default of ``CHUNK_ELEMS``, halved
+    while the chunk does not fit (``chunk_fits``): high quadrature orders of
+    P2 and quadrilateral elements need smaller chunks."""
+    ch = CHUNK_ELEMS[(etype, block)]
+    while ch > 8 and not chunk_fits(etype, block, qorder, ch):
         ch //= 2
     return ch
 
@@ -232,8 +242,21 @@ class Topology:
             self._conn32[device] = torch.from_numpy(self._conn_np.astype(np.int32)).to(device)
         return self._conn32[device]
 
-    def matrix_plan(self, device: torch.device, block: bool = False) -> DevicePlan:
-        ch = chunk_elems(self.etype, block, self.quadrature_order)
+    def chunk_for(self, kind: str, device: torch.device, dtype: Optional[torch.dtype] = None) -> int:
+        """Elements per chunk for kind "scalar", "block" (matrix forms) or
+        "node": the autotuned size for this GPU and dtype when one is
+        recorded, else the static default."""
+        from . import autotune
+        tuned = autotune.lookup(device, self.etype, kind, self.quadrature_order, dtype)
+        if tuned is not None:
+            return tuned
+        if kind == "node":
+            return NODE_CHUNK_ELEMS[self.etype]
+        return chunk_elems(self.etype, kind == "block", self.quadrature_order)
+
+    def matrix_plan(self, device: torch.device, block: bool = False,
+                    dtype: Optional[torch.dtype] = None) -> DevicePlan:
+        ch = self.chunk_for("block" if block else "scalar", device, dtype)
         key = ("matrix", ch, device)
         if key not in self._plans:
             host = self._pending.pop(("matrix", ch), None)
@@ -243,8 +266,8 @@ class Topology:
             self._plans[key] = DevicePlan(host, device)
         return self._plans[key]
 
-    def node_plan(self, device: torch.device) -> DevicePlan:
-        ch = NODE_CHUNK_ELEMS[self.etype]
+    def node_plan(self, device: torch.device, dtype: Optional[torch.dtype] = None) -> DevicePlan:
+        ch = self.chunk_for("node", device, dtype)
         key = ("node", ch, device)
         if key not in self._plans:
             host = HostPlan(self._conn_np, self.n_points, _lib.TM_PLAN_KIND_NODE, ch, self.perm)
