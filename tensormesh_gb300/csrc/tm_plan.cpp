@@ -77,13 +77,23 @@ int host_threads() {
     return std::max(1, std::min(n, 64));
 }
 
-// f(begin, end) over T contiguous ranges of [0, n) on T threads (the calling
-// thread takes the first, and the ranges of threads that could not be
-// started); an allocation failure on any thread is rethrown as bad_alloc
+// items per thread below which a loop of simple per-item work stays on fewer
+// threads (starting a thread costs tens of microseconds)
+constexpr int64_t kGrain = 1 << 15;
+
+// host threads for n items of at least `grain` items each
+int threads_for(int64_t n, int64_t grain) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>(host_threads(), n / grain));
+}
+
+// f(begin, end) over at most T contiguous ranges of [0, n), of `grain` items
+// at least, on as many threads (the calling thread takes the first, and the
+// ranges of threads that could not be started); an allocation failure on
+// any thread is rethrown as bad_alloc
 template <class F>
-void parallel_for(int64_t n, int T, F&& f) {
+void parallel_for(int64_t n, int T, F&& f, int64_t grain = 1) {
     if (n <= 0) return;
-    T = (int)std::min<int64_t>(T, n);
+    T = (int)std::min<int64_t>(T, std::max<int64_t>(1, n / std::max<int64_t>(1, grain)));
     if (T <= 1) {
         f(int64_t(0), n);
         return;
@@ -121,7 +131,7 @@ void build_pattern(tm_host_plan& p, const int64_t* conn) {
     // counting sort of all E*B*B (row, col) pairs by row: contiguous element
     // ranges count their rows, then each range fills its rows after the
     // earlier ranges' entries (the sequential order), on host threads
-    const int T = (int)std::max<int64_t>(1, std::min<int64_t>(host_threads(), E / 4096 + 1));
+    const int T = threads_for(E, kGrain / 4);
     const int64_t estep = (E + T - 1) / T;
     std::vector<std::vector<int32_t>> cnt(T, std::vector<int32_t>(N, 0));
     parallel_for(T, T, [&](int64_t t0, int64_t t1) {
@@ -161,7 +171,7 @@ void build_pattern(tm_host_plan& p, const int64_t* conn) {
             std::sort(s, t);
             ucnt[r] = std::unique(s, t) - s;
         }
-    });
+    }, kGrain / 16);
     std::vector<int64_t> urow_ptr(N + 1, 0);
     for (int64_t r = 0; r < N; ++r) urow_ptr[r + 1] = urow_ptr[r] + ucnt[r];
     const int64_t nnz = urow_ptr[N];
@@ -173,7 +183,7 @@ void build_pattern(tm_host_plan& p, const int64_t* conn) {
             std::copy(cols.begin() + row_ptr[r], cols.begin() + row_ptr[r] + ucnt[r], p.edge_col.begin() + urow_ptr[r]);
             std::fill(p.edge_row.begin() + urow_ptr[r], p.edge_row.begin() + urow_ptr[r + 1], (int32_t)r);
         }
-    });
+    }, kGrain);
     // slot map, element-major, i-major, j-minor
     p.slot.resize((size_t)E * B * B);
     const int32_t* ucol = p.edge_col.data();
@@ -188,7 +198,7 @@ void build_pattern(tm_host_plan& p, const int64_t* conn) {
                     p.slot[(e * B + a) * B + b] = (int64_t)(std::lower_bound(s, t, c) - ucol);
                 }
             }
-    });
+    }, kGrain / 8);
 }
 
 int build_chunks(tm_host_plan& p) {
@@ -206,10 +216,11 @@ int build_chunks(tm_host_plan& p) {
         std::vector<uint16_t> contrib;
     };
     const int T = host_threads();
-    const int64_t per = std::max<int64_t>(1, (p.n_chunks + T - 1) / T);
+    const int TP = (int)std::max<int64_t>(1, std::min<int64_t>(T, p.n_chunks / 16));   // 16 chunks a thread at least
+    const int64_t per = std::max<int64_t>(1, (p.n_chunks + TP - 1) / TP);
     const int n_parts = (int)((p.n_chunks + per - 1) / per);
     std::vector<Part> parts(n_parts);
-    parallel_for(n_parts, T, [&](int64_t part_begin, int64_t part_end) {
+    parallel_for(n_parts, TP, [&](int64_t part_begin, int64_t part_end) {
         // A chunk holds fewer than 65536 contributions (codes are 16-bit),
         // so a group's count and number fit in 16 bits.  Targets are grouped
         // in an open-addressing table (target -> group, groups numbered by
@@ -346,14 +357,14 @@ int build_chunks(tm_host_plan& p) {
     parallel_for(n_targets, T, [&](int64_t t0, int64_t t1) {
         std::fill(chunks_per_target.begin() + t0, chunks_per_target.begin() + t1, 0);
         if (matrix) std::fill(mirror_of.begin() + t0, mirror_of.begin() + t1, -1);
-    });
+    }, kGrain);
     parallel_for((int64_t)n_slots, T, [&](int64_t s0, int64_t s1) {
         for (int64_t s = s0; s < s1; ++s) {
             const int32_t t = p.slot_target[s];
             __atomic_fetch_add(&chunks_per_target[t], 1, __ATOMIC_RELAXED);
             if (matrix) __atomic_store_n(&mirror_of[t], p.slot_mirror[s], __ATOMIC_RELAXED);
         }
-    });
+    }, kGrain);
     // first contribution of every chunk, and the largest chunk, for kernels
     // that stage a chunk's slots and contributions in shared memory
     p.chunk_contrib.resize(p.chunk_begin.size());
@@ -371,7 +382,7 @@ int build_chunks(tm_host_plan& p) {
     int32_t max_count = 0;
     for (int64_t t = 0; t < n_targets; ++t) max_count = std::max(max_count, chunks_per_target[t]);
     const int64_t W = (int64_t)max_count + 1;
-    const int64_t R = std::max<int64_t>(1, std::min<int64_t>(T, n_targets / W));
+    const int64_t R = std::max<int64_t>(1, std::min<int64_t>(T, n_targets / std::max<int64_t>(W, kGrain)));
     const int64_t tstep = std::max<int64_t>(1, (n_targets + R - 1) / R);
     std::vector<int64_t> hist((size_t)(R * W), 0);
     parallel_for(R, T, [&](int64_t r0, int64_t r1) {
@@ -421,8 +432,8 @@ int build_chunks(tm_host_plan& p) {
     buffer<int32_t> slot_shared(n_slots);
     parallel_for((int64_t)n_slots, T, [&](int64_t s0, int64_t s1) {
         for (int64_t s = s0; s < s1; ++s) slot_shared[s] = shared_index[p.slot_target[s]];
-    });
-    const int64_t TO = std::max<int64_t>(1, std::min<int64_t>(T, n_shared));
+    }, kGrain);
+    const int64_t TO = std::max<int64_t>(1, std::min<int64_t>({(int64_t)T, n_shared, (int64_t)n_slots / kGrain}));
     std::vector<int64_t> own(TO + 1, n_shared);
     for (int64_t o = 0; o < TO; ++o)
         own[o] = std::lower_bound(p.shared_ptr.begin(), p.shared_ptr.begin() + n_shared, n_partials * o / TO) -
@@ -492,7 +503,7 @@ extern "C" int tm_morton_order(const double* points, int64_t n_points, int32_t d
                     for (int v = 1; v < V; ++v) s += points[conn[e * n_basis + v] * D + d];
                     cent[e * D + d] = s / (double)V;
                 }
-        });
+        }, kGrain / 4);
         double lo[3], hi[3], span[3];
         for (int d = 0; d < D; ++d) {
             lo[d] = hi[d] = cent[d];
@@ -514,11 +525,12 @@ extern "C" int tm_morton_order(const double* points, int64_t n_points, int32_t d
                 }
                 key[e] = {k, (int32_t)e};
             }
-        });
+        }, kGrain / 4);
         // sort ranges on host threads, then merge; (key, index) pairs give
         // the stable order
-        const int64_t step = (n_elements + T - 1) / T;
-        parallel_for(T, T, [&](int64_t t0, int64_t t1) {
+        const int TS = threads_for(n_elements, kGrain);
+        const int64_t step = (n_elements + TS - 1) / TS;
+        parallel_for(TS, TS, [&](int64_t t0, int64_t t1) {
             for (int64_t t = t0; t < t1; ++t) {
                 const int64_t b = std::min(n_elements, t * step), e = std::min(n_elements, (t + 1) * step);
                 std::sort(key.begin() + b, key.begin() + e);
@@ -562,7 +574,7 @@ extern "C" int tm_plan_build(const int64_t* conn, int64_t n_elements, int32_t n_
                     bad_index = true;
                     return;
                 }
-        });
+        }, kGrain);
         if (bad_index) {
             delete p;
             return tm_set_error(TM_ERR_INVALID_ARG, "tm_plan_build: connectivity index out of range");
@@ -586,14 +598,15 @@ extern "C" int tm_plan_build(const int64_t* conn, int64_t n_elements, int32_t n_
             for (int64_t i = i0; i < i1; ++i)
                 for (int a = 0; a < n_basis; ++a)
                     p->conn[i * n_basis + a] = (int32_t)conn[(int64_t)p->perm[i] * n_basis + a];
-        });
+        }, kGrain / 4);
         if (kind == TM_PLAN_KIND_MATRIX) {
             if (slot_map) {
                 const int64_t n_slot = n_elements * n_basis * n_basis;
                 p->slot.resize(n_slot);
-                std::vector<int64_t> range_max(T, -1), range_min(T, 0);
-                const int64_t step = (n_slot + T - 1) / T;
-                parallel_for(T, T, [&](int64_t t0, int64_t t1) {
+                const int TS = threads_for(n_slot, kGrain);
+                std::vector<int64_t> range_max(TS, -1), range_min(TS, 0);
+                const int64_t step = (n_slot + TS - 1) / TS;
+                parallel_for(TS, TS, [&](int64_t t0, int64_t t1) {
                     for (int64_t t = t0; t < t1; ++t) {
                         const int64_t b = std::min(n_slot, t * step), e = std::min(n_slot, b + step);
                         std::copy(slot_map + b, slot_map + e, p->slot.begin() + b);
