@@ -40,6 +40,7 @@ CANDIDATES = (16, 32, 64, 128, 256, 384, 512)
 _table: Dict[str, int] = {}
 _loaded = False
 _tags: Dict[torch.device, str] = {}
+_keys: Dict[tuple, str] = {}
 
 
 def cache_path() -> Path:
@@ -97,19 +98,31 @@ def save(path: Optional[Path] = None):
 
 
 def clear():
-    """Forget every result of this process (the cache file is kept and is
-    read again on the next lookup)."""
+    """Forget every result of this process, and the device tags and keys
+    built so far (the cache file is kept and is read again on the next
+    lookup)."""
     global _loaded
     _table.clear()
+    _tags.clear()
+    _keys.clear()
     _loaded = False
 
 
 def lookup(device, etype: str, kind: str, qorder: int, dtype: Optional[torch.dtype]) -> Optional[int]:
-    """The tuned chunk size for a CUDA device, or None."""
-    if dtype is None or device is None or torch.device(device).type != "cuda":
+    """The tuned chunk size for a CUDA device, or None (every assembly call
+    asks: the key of each argument tuple is built once)."""
+    if dtype is None or device is None:
         return None
-    _load()
-    return _table.get(make_key(device_tag(torch.device(device)), etype, kind, qorder, dtype))
+    args = (device, etype, kind, qorder, dtype)
+    key = _keys.get(args)
+    if key is None:
+        dev = torch.device(device)
+        if dev.type != "cuda":
+            return None
+        key = _keys[args] = make_key(device_tag(dev), etype, kind, qorder, dtype)
+    if not _loaded:
+        _load()
+    return _table.get(key)
 
 
 def record(device, etype: str, kind: str, qorder: int, dtype: torch.dtype, chunk: int):

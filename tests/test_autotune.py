@@ -68,6 +68,16 @@ def test_cache_round_trip_merges(fake_gpu):
     assert autotune.lookup("cuda", "tetra", "scalar", 2, torch.float64) is None
 
 
+def test_clear_forgets_memoised_keys(fake_gpu, monkeypatch):
+    cuda = torch.device("cuda", 0)
+    autotune.record(cuda, "tetra", "scalar", 2, torch.float64, 64)
+    assert autotune.lookup(cuda, "tetra", "scalar", 2, torch.float64) == 64
+    autotune.clear()
+    monkeypatch.setattr(autotune, "device_tag", lambda device: "Another GPU|8sm|cc90")
+    autotune.record(cuda, "tetra", "scalar", 2, torch.float64, 128)
+    assert autotune.lookup(cuda, "tetra", "scalar", 2, torch.float64) == 128
+
+
 def test_topology_uses_the_tuned_size(fake_gpu):
     m = gen_unit_cube(2)
     topo = Topology(m.points, m.elements(), "tetra", 2)
