@@ -156,7 +156,8 @@ class ElementAssembler(_AssemblerBase):
         assert project in ["reduce", "sparse"]
         points = mesh.points
         etype, conn = _single_type(_mesh_elements(mesh))
-        topo = Topology(points, conn, etype, quadrature_order, matrix=True)
+        topo = Topology(points, conn, etype, quadrature_order, matrix=True,
+                        element_groups=getattr(mesh, "element_groups", None))
         E, B = conn.shape
         if project == "reduce":
             proj = ReduceProjector(indices=topo.slot, from_shape=(E, B, B), to_shape=(topo.nnz,))
@@ -403,6 +404,10 @@ class NodeAssembler(_AssemblerBase):
     def from_elements(cls, points: torch.Tensor, elements: Dict[str, torch.Tensor], quadrature_order: int = 2,
                       device="cpu", dtype: torch.dtype = torch.float32, project: str = "reduce", *args, **kwargs):
         """node_assembler.py:617-698: the scatter map is conn.flatten()."""
+        return cls._build(points, elements, quadrature_order, device, dtype, project, None, *args, **kwargs)
+
+    @classmethod
+    def _build(cls, points, elements, quadrature_order, device, dtype, project, element_groups, *args, **kwargs):
         etype, conn = _single_type(elements)
         N = points.shape[0]
         E, B = conn.shape
@@ -414,14 +419,14 @@ class NodeAssembler(_AssemblerBase):
             raise ValueError(f"project should be either 'reduce' or 'sparse', but got {project}")
         trans = Transformation(points, conn, etype, quadrature_order)
         asm = cls({etype: proj}, {etype: trans}, {etype: conn}, *args, **kwargs)
-        asm._topology = Topology(points, conn, etype, quadrature_order, matrix=False)
+        asm._topology = Topology(points, conn, etype, quadrature_order, matrix=False, element_groups=element_groups)
         return asm.type(dtype).to(device)
 
     @classmethod
     def from_mesh(cls, mesh, quadrature_order: int = 2, project: str = "reduce", *args, **kwargs):
         elements = _mesh_elements(mesh)
-        return cls.from_elements(mesh.points, elements, quadrature_order, mesh.device, mesh.dtype, project,
-                                 *args, **kwargs)
+        return cls._build(mesh.points, elements, quadrature_order, mesh.device, mesh.dtype, project,
+                          getattr(mesh, "element_groups", None), *args, **kwargs)
 
     @classmethod
     def from_assembler(cls, obj, *args, **kwargs):

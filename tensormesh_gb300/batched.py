@@ -61,7 +61,9 @@ class BatchedDiffusion:
         pts = torch.cat([m.points.detach().cpu().to(dtype) for m in meshes])
         conn = torch.cat([m.elements().cpu().long() + int(self.node_offset[i]) for i, m in enumerate(meshes)])
         bnd = torch.cat([m.boundary_mask.cpu().bool() for m in meshes])
-        self.mesh = Mesh(pts, {etype: conn}, {"is_boundary": bnd}).to(dev)
+        # one element group per mesh: the meshes overlap in space, and one
+        # order over all of them would mix meshes in every chunk
+        self.mesh = Mesh(pts, {etype: conn}, {"is_boundary": bnd}, element_groups=self.elem_offset).to(dev)
         self.K_asm = LaplaceElementAssembler.from_mesh(self.mesh, quadrature_order)
         self.b_asm = LoadNodeAssembler.from_mesh(self.mesh, quadrature_order)
         self.device, self.dtype = dev, dtype

@@ -58,13 +58,20 @@ class Mesh:
         ``"tetra10"``, ``"quad"``, ``"quad9"``.
     point_data : dict, optional
         Nodal fields; ``"is_boundary"`` is what ``boundary_mask`` returns.
+    element_groups : array of int, optional
+        ``[G+1]`` element offsets of independent groups (several meshes
+        concatenated into one): the assemblers order elements by Morton code
+        within each group and keep the groups in sequence, so that a chunk
+        of elements stays within one group even where the groups overlap in
+        space.
     """
 
     def __init__(self, points: torch.Tensor, cells: Dict[str, torch.Tensor],
-                 point_data: Optional[Dict[str, torch.Tensor]] = None):
+                 point_data: Optional[Dict[str, torch.Tensor]] = None, element_groups=None):
         self.points = points
         self.cells = {k: v.long() for k, v in cells.items()}
         self.point_data = dict(point_data or {})
+        self.element_groups = None if element_groups is None else np.asarray(element_groups, dtype=np.int64)
         dims = {k: ELEMENT_DIM[k] for k in self.cells}
         top = max(dims.values())
         types = [k for k, d in dims.items() if d == top]
@@ -122,7 +129,7 @@ class Mesh:
             pts = pts.to(dtype)
         cells = {k: v.to(device) if device is not None else v for k, v in self.cells.items()}
         pd = {k: v.to(device) if device is not None else v for k, v in self.point_data.items()}
-        return Mesh(pts, cells, pd)
+        return Mesh(pts, cells, pd, self.element_groups)
 
     def __repr__(self):
         sizes = ", ".join(f"{k}:{tuple(v.shape)}" for k, v in self.cells.items())

@@ -19,12 +19,22 @@ from . import _lib
 from .element import element_info, element_tables, packed_tables
 
 
-def morton_order(points: np.ndarray, conn: np.ndarray) -> np.ndarray:
+def morton_order(points: np.ndarray, conn: np.ndarray, groups: Optional[np.ndarray] = None) -> np.ndarray:
     """Processing order of the elements: increasing Morton code of the
     centroid of their vertices, ties in element order (``tm_morton_order``,
-    on host threads)."""
+    on host threads).  With ``groups`` (``[G+1]`` element offsets from 0 to
+    E) each group is ordered on its own (within its own bounding box) and
+    the groups follow one another."""
     E = conn.shape[0]
     perm = np.zeros(E, dtype=np.int32)
+    if groups is not None:
+        g = np.asarray(groups, dtype=np.int64)
+        if g.ndim != 1 or g.size < 1 or g[0] != 0 or g[-1] != E or (np.diff(g) < 0).any():
+            raise ValueError("element groups must be non-decreasing offsets from 0 to the element count")
+        for b, e in zip(g[:-1], g[1:]):
+            if e > b:
+                perm[b:e] = morton_order(points, conn[b:e]) + np.int32(b)
+        return perm
     if E == 0:
         return perm
     pts = np.ascontiguousarray(points, dtype=np.float64)
@@ -193,14 +203,16 @@ class Topology:
     between calls: connectivity, pattern, slot map, tables, chunk plans."""
 
     def __init__(self, points: torch.Tensor, conn: torch.Tensor, etype: str, quadrature_order: int,
-                 matrix: bool = True):
+                 matrix: bool = True, element_groups: Optional[np.ndarray] = None):
         info = element_info(etype)
         self.etype, self.info, self.quadrature_order = etype, info, quadrature_order
         self.n_points = int(points.shape[0])
         self.n_elements = int(conn.shape[0])
-        conn_np = conn.detach().cpu().numpy().astype(np.int64)
+        # int64 connectivity as numpy (no copy when it is one already: the
+        # topology reads it like the assembler's own element buffer)
+        conn_np = conn.detach().to("cpu", torch.int64).contiguous().numpy()
         pts_np = points.detach().cpu().to(torch.float64).numpy()
-        self.perm = morton_order(pts_np, conn_np)
+        self.perm = morton_order(pts_np, conn_np, element_groups)
         self._conn_np = conn_np
         self._plans: Dict[tuple, DevicePlan] = {}
         self._host_node: Optional[HostPlan] = None
