@@ -15,7 +15,7 @@ from typing import Dict, Optional
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, autotune
 from .element import element_info, element_tables, packed_tables
 
 
@@ -258,13 +258,14 @@ class Topology:
         """Elements per chunk for kind "scalar", "block" (matrix forms) or
         "node": the autotuned size for this GPU and dtype when one is
         recorded, else the static default."""
-        from . import autotune
         tuned = autotune.lookup(device, self.etype, kind, self.quadrature_order, dtype)
         if tuned is not None:
             return tuned
-        if kind == "node":
-            return NODE_CHUNK_ELEMS[self.etype]
-        return chunk_elems(self.etype, kind == "block", self.quadrature_order)
+        static = self.__dict__.setdefault("_static_chunk", {})
+        if kind not in static:
+            static[kind] = (NODE_CHUNK_ELEMS[self.etype] if kind == "node"
+                            else chunk_elems(self.etype, kind == "block", self.quadrature_order))
+        return static[kind]
 
     def matrix_plan(self, device: torch.device, block: bool = False,
                     dtype: Optional[torch.dtype] = None) -> DevicePlan:
