@@ -10,6 +10,8 @@ of their centroids so that a chunk of consecutive elements is spatially
 compact and most CSR targets are reduced inside one chunk.
 """
 import ctypes as C
+import os
+from concurrent.futures import ThreadPoolExecutor
 from typing import Dict, Optional
 
 import numpy as np
@@ -17,6 +19,18 @@ import torch
 
 from . import _lib, autotune
 from .element import element_info, element_tables, packed_tables
+
+
+def _host_threads() -> int:
+    """TM_HOST_THREADS if set, else all hardware threads (at most 64), as
+    the native plan builder counts them."""
+    try:
+        n = int(os.environ.get("TM_HOST_THREADS", "0"))
+    except ValueError:
+        n = 0
+    if n <= 0:
+        n = os.cpu_count() or 1
+    return max(1, min(n, 64))
 
 
 def morton_order(points: np.ndarray, conn: np.ndarray, groups: Optional[np.ndarray] = None) -> np.ndarray:
@@ -31,9 +45,22 @@ def morton_order(points: np.ndarray, conn: np.ndarray, groups: Optional[np.ndarr
         g = np.asarray(groups, dtype=np.int64)
         if g.ndim != 1 or g.size < 1 or g[0] != 0 or g[-1] != E or (np.diff(g) < 0).any():
             raise ValueError("element groups must be non-decreasing offsets from 0 to the element count")
-        for b, e in zip(g[:-1], g[1:]):
-            if e > b:
-                perm[b:e] = morton_order(points, conn[b:e]) + np.int32(b)
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        c64 = np.ascontiguousarray(conn, dtype=np.int64)
+
+        def one(be):
+            b, e = be
+            perm[b:e] = morton_order(pts, c64[b:e]) + np.int32(b)
+
+        spans = [(int(b), int(e)) for b, e in zip(g[:-1], g[1:]) if e > b]
+        # groups on host threads (the native call releases the interpreter lock)
+        workers = min(len(spans), _host_threads())
+        if workers > 1 and E >= 1 << 16:
+            with ThreadPoolExecutor(max_workers=workers) as pool:
+                list(pool.map(one, spans))
+        else:
+            for be in spans:
+                one(be)
         return perm
     if E == 0:
         return perm
