@@ -131,7 +131,11 @@ typedef struct tm_chunk_plan {
  *       1 = node   (chunk plan onto nodes).
  * slot_map: optional host int64 [E*B*B] slot map of an earlier matrix plan of
  * the same mesh (NULL = build the pattern); lets one mesh carry chunk plans
- * of several chunk sizes.
+ * of several chunk sizes.  A negative entry is rejected (TM_ERR_INVALID_ARG),
+ * as are connectivity outside [0, n_points) and a perm that is not a
+ * permutation; chunk_elems * n_local * 2 above 65536 gives TM_ERR_TOO_LARGE
+ * (contribution codes are 16-bit; n_local = B(B+1)/2 for matrix plans, B for
+ * node plans).
  * The CSR pattern is the reference's: unique (row, col) pairs sorted
  * row-major, and the slot map is the element-major, i-major, j-minor
  * position of every local pair in that pattern.
