@@ -292,3 +292,23 @@ def test_grouped_morton_order_and_batch_topology():
     _, _, ref = O.assemble_matrix(pts, conn, pts.shape[0],
                                   lambda p, c, E: O.element_locals_elasticity(p, c, "triangle", E, 0.3, 2), E=E)
     np.testing.assert_allclose(emulate_matrix(hg, loc), ref.numpy(), rtol=0, atol=1e-13 * np.abs(ref.numpy()).max())
+
+
+def test_from_mesh_takes_the_mesh_element_groups():
+    """ElementAssembler.from_mesh and NodeAssembler.from_mesh order the
+    elements of a mesh with element groups group by group (as a batch does)."""
+    import tensormesh_gb300 as tg
+    from tensormesh_gb300.mesh import Mesh
+    parts = [gen_unit_square(n, jitter=0.1, seed=60 + n) for n in (5, 3, 8)]
+    noff = np.cumsum([0] + [m.n_points for m in parts])
+    eoff = np.cumsum([0] + [m.n_elements for m in parts])
+    pts = torch.cat([m.points for m in parts])
+    conn = torch.cat([m.elements() + int(noff[i]) for i, m in enumerate(parts)])
+    mesh = Mesh(pts, {"triangle": conn}, element_groups=eoff)
+    expect = morton_order(pts.numpy(), conn.numpy(), eoff)
+    K = tg.LaplaceElementAssembler.from_mesh(mesh)
+    b = tg.LoadNodeAssembler.from_mesh(mesh)
+    assert np.array_equal(K._topo(True).perm, expect)
+    assert np.array_equal(b._topo(False).perm, expect)
+    plain = tg.LaplaceElementAssembler.from_mesh(Mesh(pts, {"triangle": conn}))
+    assert np.array_equal(plain._topo(True).perm, morton_order(pts.numpy(), conn.numpy()))
