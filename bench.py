@@ -31,6 +31,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -82,8 +83,8 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "",
-                                 f".clocks_{os.getpid()}.csv")
+        fd, self.path = tempfile.mkstemp(prefix="tm_clocks_", suffix=".csv")
+        os.close(fd)
 
     def start(self):
         try:

@@ -234,9 +234,13 @@ int tm_assemble_matrix(const tm_matrix_args* args, tm_stream_t stream);
  * args->workspace is ignored and the partial sums live in a static device
  * array of TM_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps
  * until exit.  Plans needing more (tm_matrix_workspace_bytes) are rejected
- * with TM_ERR_TOO_LARGE.  The first call on a device looks the array up
- * (with that device current): make it before any stream capture.  Calls
- * share the array: calls whose kernels overlap on the GPU race.
+ * with TM_ERR_TOO_LARGE.  The first call on a device (and the first after
+ * its context changed, e.g. after cudaDeviceReset) looks the array up with
+ * that device current: make it before any stream capture.  Calls share the
+ * array and it keeps the last call's partials: calls whose kernels overlap
+ * on the GPU race, and a result may be used only after tm_device_fault()
+ * reports 0 (a chunk whose bounded wait ran out leaves the previous call's
+ * partials in its place).
  */
 #define TM_NOALLOC_SCRATCH_BYTES (64u << 20)
 int tm_assemble_matrix_noalloc(const tm_matrix_args* args, tm_stream_t stream);

@@ -76,8 +76,23 @@ def _load():
     except (OSError, ValueError):
         return
     for k, v in data.items():
-        if isinstance(v, int) and v > 0:
+        if isinstance(v, int) and v > 0 and _cached_size_fits(k, v):
             _table.setdefault(k, v)
+
+
+def _cached_size_fits(key: str, chunk: int) -> bool:
+    """A cached chunk size is used only if it still fits its element type,
+    kind and quadrature order (16-bit contribution codes, shared memory): a
+    stale or hand-edited entry is dropped, and the static default applies."""
+    parts = key.split("|")
+    if len(parts) < 5:
+        return False
+    etype, kind, q = parts[-4], parts[-3], parts[-2]
+    try:
+        qorder = int(q[1:]) if q.startswith("q") else None
+        return qorder is not None and bool(candidates(etype, kind, qorder, [chunk]))
+    except (KeyError, ValueError):
+        return False
 
 
 def save(path: Optional[Path] = None):

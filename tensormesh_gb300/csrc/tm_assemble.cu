@@ -258,13 +258,19 @@ extern "C" int tm_project_reduce(int32_t dtype, int64_t n_to, int64_t width, con
 // every GPU that loads the library holds until the process exits.
 //
 // The array's address is looked up once per device, with that device
-// current, by the first call on that device (cudaGetSymbolAddress); make
-// that first call before any stream capture.  Nothing in the array has to
-// start at zero: each call writes every partial it later reads.  All calls
-// share the one array, so calls whose kernels overlap on the GPU (on
-// different streams, or from different host threads) race on it; order them
-// on one stream or serialise them.
+// current, by the first call on that device (cudaGetSymbolAddress), and
+// again on the first call after the device's context changed (after a
+// cudaDeviceReset the module is loaded anew); make that first call before
+// any stream capture.  Nothing in the array has to start at zero: each call
+// writes every partial it later reads.  If a chunk's bounded wait for its
+// staged plan runs out, that chunk writes no partials and the finalising
+// kernel sums whatever the previous call left there: as with
+// tm_assemble_matrix, check tm_device_fault() before using the results.
+// All calls share the one array, so calls whose kernels overlap on the GPU
+// (on different streams, or from different host threads) race on it; order
+// them on one stream or serialise them.
 // ---------------------------------------------------------------------------
+#include <cuda.h>
 #include <mutex>
 
 namespace tmk {
@@ -273,15 +279,53 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[TM_NOALLOC_SCRA
 
 constexpr int kMaxDevices = 64;
 static void* g_noalloc_ptr[kMaxDevices] = {};
+// the context each cached address belongs to: after cudaDeviceReset the
+// device gets a new context (new id), the module is loaded again and the
+// array may sit elsewhere, so the address is looked up again
+static unsigned long long g_noalloc_ctx[kMaxDevices] = {};
 static std::mutex g_noalloc_mutex;
+
+// unique id of the calling thread's current context (0 if there is none);
+// called with g_noalloc_mutex held.
+// The driver functions are fetched through the runtime, so that the library
+// does not link the driver library (it also loads on machines without one).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+static unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+        cudaGetLastError();
+        looked_up = true;
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 static int noalloc_scratch(void** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return launch_status("cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices)
         return tm_set_error(TM_ERR_UNSUPPORTED, "tm_assemble_matrix_noalloc: device index above 63");
+    // 0 when this host thread has no current context yet: the lookup below
+    // binds the device's primary context, and its id is read after it
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_noalloc_ptr[dev] || ctx == 0 || g_noalloc_ctx[dev] != ctx) {
+        g_noalloc_ptr[dev] = nullptr;
         void* p = nullptr;
         const cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (err != cudaSuccess || !p) {
@@ -292,6 +336,7 @@ static int noalloc_scratch(void** out) {
             return tm_set_error(TM_ERR_CUDA, buf);
         }
         g_noalloc_ptr[dev] = p;
+        g_noalloc_ctx[dev] = current_context_id();
     }
     *out = g_noalloc_ptr[dev];
     return TM_OK;

@@ -235,9 +235,10 @@ class Topology:
         self.etype, self.info, self.quadrature_order = etype, info, quadrature_order
         self.n_points = int(points.shape[0])
         self.n_elements = int(conn.shape[0])
-        # int64 connectivity as numpy (no copy when it is one already: the
-        # topology reads it like the assembler's own element buffer)
-        conn_np = conn.detach().to("cpu", torch.int64).contiguous().numpy()
+        # int64 connectivity as numpy, always a private copy: plans for other
+        # chunk sizes and kinds are built from it later, and must match the
+        # pattern and slot map even if the caller edits its cells in place
+        conn_np = np.array(conn.detach().to("cpu", torch.int64).contiguous().numpy(), copy=True)
         pts_np = points.detach().cpu().to(torch.float64).numpy()
         self.perm = morton_order(pts_np, conn_np, element_groups)
         self._conn_np = conn_np
