@@ -484,6 +484,75 @@ def checksum(values: torch.Tensor) -> Dict[str, float]:
 
 
 # ---------------------------------------------------------------------------
+# Random sign sketches: a relative-Frobenius comparison with a value array
+# that is too large to store.  Sketch k of v is s_k = sum_i r_k[i] v_i with
+# Rademacher signs r_k[i] = 1 - 2 * bit k of splitmix64(i) (Vigna's
+# SplitMix64 finaliser, computed with wrapping int64 arithmetic in torch, so
+# that the signs are the same on every machine and device).  For a
+# difference d = a - b, E[(s_k(a) - s_k(b))^2] = ||d||^2 for every k, so
+# sqrt(mean_k (s_k(a) - s_k(b))^2) estimates ||a - b||_F from the 64 stored
+# numbers of b alone; with 64 sketches the estimate stays within a factor of
+# about two of the true norm (chi-square-like with 64 degrees of freedom,
+# relative spread ~0.18), and no cancellation can hide an error, unlike
+# positively weighted sums.  The sums run in float64 over blocks; their own
+# rounding (~1e-16 ||v|| for random signs) is far below the 1e-12 bar.
+# ---------------------------------------------------------------------------
+N_SKETCH = 64
+_U64 = 1 << 64
+
+
+def _s64(c: int) -> int:
+    return c - _U64 if c >= 1 << 63 else c
+
+
+def _srl(x: torch.Tensor, s: int) -> torch.Tensor:
+    """Logical right shift of int64 values (torch shifts arithmetically)."""
+    return (x >> s) & ((1 << (64 - s)) - 1)
+
+
+def splitmix64(i: torch.Tensor) -> torch.Tensor:
+    """SplitMix64 output for state increments i (int64, wrapping)."""
+    z = i + _s64(0x9E3779B97F4A7C15)
+    z = (z ^ _srl(z, 30)) * _s64(0xBF58476D1CE4E5B9)
+    z = (z ^ _srl(z, 27)) * _s64(0x94D049BB133111EB)
+    return z ^ _srl(z, 31)
+
+
+def splitmix64_py(i: int) -> int:
+    """The same function on Python integers (to check the tensor version)."""
+    z = (i + 0x9E3779B97F4A7C15) % _U64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) % _U64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) % _U64
+    return z ^ (z >> 31)
+
+
+def sketch(values: torch.Tensor, n: int = N_SKETCH, block: int = 1 << 18) -> list:
+    """The n sign sketches of the flat float64 value array (on its device)."""
+    v = values.detach().reshape(-1).to(DT)
+    dev = v.device
+    ks = torch.arange(n, device=dev, dtype=torch.int64)
+    acc = torch.zeros(n, dtype=DT, device=dev)
+    for b0 in range(0, v.shape[0], block):
+        b1 = min(v.shape[0], b0 + block)
+        h = splitmix64(torch.arange(b0, b1, device=dev, dtype=torch.int64))
+        signs = 1.0 - 2.0 * ((h[:, None] >> ks[None, :]) & 1).to(DT)
+        acc += v[b0:b1] @ signs
+    return [float(x) for x in acc.cpu()]
+
+
+def sketch_rel_error(got: Sequence[float], ref: Sequence[float], ref_fro: float) -> float:
+    """Estimated ||a - b||_F / ||b||_F from the sketches of a and b."""
+    d = np.asarray(got, dtype=np.float64) - np.asarray(ref, dtype=np.float64)
+    return float(np.sqrt(np.mean(d * d)) / ref_fro)
+
+
+def slot_hash(slot: torch.Tensor) -> str:
+    """SHA-256 of a slot map's entries as little-endian int32 bytes."""
+    s = slot.detach().reshape(-1).cpu().numpy()
+    return hashlib.sha256(s.astype("<i4").tobytes()).hexdigest()
+
+
+# ---------------------------------------------------------------------------
 # The reference's per-call work for the diffusion + mass benchmark, restated
 # op for op (element_assembler.py:390-445 with builtin.py:61-62 / :99-100 and
 # sparse/matrix.py:76-86), given the slot map of ``from_mesh``.  Used as the

@@ -4,7 +4,7 @@ CPU in float64.
 
 Usage (from the repository root, with the reference source tree available)::
 
-    python tests/golden/make_golden.py /path/to/TensorMesh [--only=facet|--only=quad]
+    python tests/golden/make_golden.py /path/to/TensorMesh [--only=facet|--only=quad|--only=full]
 
 Writes
 
@@ -16,9 +16,11 @@ Writes
 * ``tests/golden/small_quad.npz``, ``small_quad9.npz`` and
   ``small_facet_quad.npz``: the same cases on quadrilateral meshes
   (``--only=quad`` writes these three alone).
-* ``tests/golden/full_checksums.json``: fingerprints (``checksum()`` of
-  ``oracle/fem_oracle.py``) of the reference's outputs on the full-size
-  workloads of ``tensormesh_gb300/workloads.py``.
+* ``tests/golden/full_checksums.json``: the reference's outputs on the
+  full-size workloads of ``tensormesh_gb300/workloads.py``: pattern and
+  slot-map hashes, fingerprints (``checksum()`` of ``oracle/fem_oracle.py``)
+  and 64 sign sketches (``sketch()``) of every value array
+  (``--only=full`` writes this file alone).
 
 The reference's user-level forms are written exactly as its documentation
 and examples write them (a ``forward(gradu, gradv, kappa)`` diffusion form,
@@ -137,6 +139,9 @@ def main(reference_root, only=None):
     if only == "facet":
         facet_golden(tm, to_ref)
         return
+    if only == "full":
+        full_golden(tm, to_ref, KappaDiffusion, ElasticityE, Source)
+        return
 
     # ------------------------------------------------------------------ small
     cases = {
@@ -237,12 +242,32 @@ def main(reference_root, only=None):
     np.savez_compressed(os.path.join(HERE, "small_projector.npz"), **proj)
     print("wrote projector")
 
-    # ------------------------------------------------------------ full size
+    full_golden(tm, to_ref, KappaDiffusion, ElasticityE, Source)
+
+
+def _values(v):
+    """Fingerprints and sign sketches of one of the reference's value arrays."""
+    from oracle.fem_oracle import checksum, sketch
+    out = checksum(v)
+    out["sketch"] = sketch(v)
+    return out
+
+
+def full_golden(tm, to_ref, KappaDiffusion, ElasticityE, Source):
+    """full_checksums.json: for each full-size workload of
+    ``tensormesh_gb300/workloads.py``, the reference's pattern hash, the
+    SHA-256 of its slot map (int32 bytes, element-major), and for each value
+    array its fingerprints and 64 sign sketches (``oracle.fem_oracle.sketch``:
+    a relative-Frobenius estimate of any other array against it)."""
+    from oracle.fem_oracle import slot_hash
+    from tensormesh_gb300 import workloads as W
+
     full = {}
     t0 = time.time()
     wl = W.poisson_tri(256)
     rm = to_ref(wl.mesh)
-    K = tm.LaplaceElementAssembler.from_mesh(rm)(rm.points)
+    asm = tm.LaplaceElementAssembler.from_mesh(rm)
+    K = asm(rm.points)
     b = Source.from_mesh(rm)(rm.points, point_data={"f": wl.data["f"]})
     mask = wl.mesh.boundary_mask
     Kc, bc = tm.Condenser(mask)(K, b)
@@ -250,9 +275,10 @@ def main(reference_root, only=None):
     u = torch.zeros(wl.mesh.n_points)
     u[~mask] = u_i
     err = float((u - wl.data["exact"]).norm() / wl.data["exact"].norm())
-    full[wl.name] = {"nnz": int(K.nnz), "hash": K.layout_hash, "K": checksum(K.values),
-                     "b": checksum(b), "u": checksum(u), "l2_rel_error": err}
+    full[wl.name] = {"nnz": int(K.nnz), "hash": K.layout_hash, "slot_sha256": slot_hash(asm.projector["triangle"].indices),
+                     "K": _values(K.values), "b": _values(b), "u": _values(u), "l2_rel_error": err}
     print(wl.name, err, time.time() - t0)
+    del asm, K
 
     t0 = time.time()
     wl = W.diffusion_mass_tet(64)
@@ -260,8 +286,8 @@ def main(reference_root, only=None):
     asm = KappaDiffusion.from_mesh(rm)
     K = asm(rm.points, element_data={"kappa": wl.data["kappa"]})
     M = tm.MassElementAssembler.from_assembler(asm)(rm.points)
-    full[wl.name] = {"nnz": int(K.nnz), "hash": K.layout_hash, "K": checksum(K.values),
-                     "M": checksum(M.values)}
+    full[wl.name] = {"nnz": int(K.nnz), "hash": K.layout_hash, "slot_sha256": slot_hash(asm.projector["tetra"].indices),
+                     "K": _values(K.values), "M": _values(M.values)}
     print(wl.name, time.time() - t0)
     del asm, K, M
 
@@ -271,8 +297,8 @@ def main(reference_root, only=None):
     asm = KappaDiffusion.from_mesh(rm)
     K = asm(rm.points, element_data={"kappa": wl.data["kappa_true"]})
     b = Source.from_mesh(rm)(rm.points, point_data={"f": wl.data["f"]})
-    full[wl.name] = {"nnz": int(K.nnz), "hash": K.layout_hash, "K": checksum(K.values),
-                     "b": checksum(b)}
+    full[wl.name] = {"nnz": int(K.nnz), "hash": K.layout_hash, "slot_sha256": slot_hash(asm.projector["tetra"].indices),
+                     "K": _values(K.values), "b": _values(b)}
     print(wl.name, time.time() - t0)
     del asm, K
 
@@ -284,7 +310,8 @@ def main(reference_root, only=None):
     full[wl.name] = {"nnz_blocks": int(asm.edges.shape[1]), "nnz": int(El.nnz),
                      "hash_blocks": __import__("hashlib").sha256(
                          asm.edges[0].numpy().tobytes() + asm.edges[1].numpy().tobytes()).hexdigest(),
-                     "K": checksum(El.values)}
+                     "slot_sha256": slot_hash(asm.projector["tetra10"].indices),
+                     "K": _values(El.values)}
     print(wl.name, time.time() - t0)
 
     with open(os.path.join(HERE, "full_checksums.json"), "w") as fh:

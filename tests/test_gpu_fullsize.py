@@ -1,7 +1,28 @@
-"""Full-size benchmark workloads on the GPU against fingerprints of the
-reference's own outputs (tests/golden/full_checksums.json): Frobenius norm
-and two positively weighted sums of the value arrays, within 1e-12 of the
-sum of absolute values; pattern hashes bit-exact; the Poisson L2 error."""
+"""Full-size benchmark workloads on the GPU against the reference's own
+outputs at full size (tests/golden/full_checksums.json, written by
+make_golden.py from the reference itself).
+
+For every workload (C1 Poisson on 131,072 triangles, C2 diffusion + mass on
+1,572,864 P1 tets, C3 elasticity on 196,608 P2 tets, C4 diffusion on 663,552
+P1 tets):
+
+* the pattern hash and the SHA-256 of the element-major slot map are
+  bit-exact with the reference's;
+* every value array is within 1e-12 relative Frobenius of the reference's,
+  in two ways:
+  - directly against the reference: the 64 sign sketches of the array
+    (``oracle.fem_oracle.sketch``) estimate ||ours - reference||_F from the
+    reference's stored sketches; the estimate must be below 1e-13, ten times
+    under the bar (a true error of 1e-12 would give an estimate above 5e-13
+    with overwhelming probability: 64 random-sign projections, none able to
+    cancel);
+  - exactly against the oracle: the oracle's restatement of the reference's
+    op sequence runs on the same device with the (hash-checked) slot map,
+    its own sketches are checked against the reference's at 1e-13 (which
+    pins the oracle at full size), and ``rel_fro(ours, oracle) <= 1e-12`` is
+    asserted on the whole arrays;
+* the Poisson L2 error against the exact solution matches the reference
+  pipeline's."""
 import json
 import os
 
@@ -9,11 +30,14 @@ import pytest
 import torch
 
 import tensormesh_gb300 as tg
-from conftest import GOLDEN
+from conftest import GOLDEN, rel_fro
 from oracle import fem_oracle as O
 from tensormesh_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
+
+TOL = 1e-12          # the assembly bar, relative Frobenius
+SKETCH_TOL = 1e-13   # bound on the sketch estimate against the reference
 
 
 def _full():
@@ -21,11 +45,27 @@ def _full():
         return json.load(fh)
 
 
-def _close(values, ref, tol=1e-12):
-    ck = O.checksum(values.detach().cpu())
-    assert ck["n"] == ref["n"]
-    for key in ("fro", "w1", "w2"):
-        assert abs(ck[key] - ref[key]) <= tol * ref["abs"], (key, ck[key], ref[key])
+def _vs_reference(values, ref, what):
+    assert values.numel() == ref["n"], what
+    est = O.sketch_rel_error(O.sketch(values), ref["sketch"], ref["fro"])
+    assert est <= SKETCH_TOL, f"{what}: sketch estimate of the relative error {est:.3e}"
+    return est
+
+
+def _check(ours, oracle, ref, what):
+    """ours and the oracle against the reference's sketches, ours against
+    the oracle exactly."""
+    _vs_reference(oracle, ref, what + " (oracle)")
+    _vs_reference(ours, ref, what)
+    r = rel_fro(ours, oracle)
+    assert r <= TOL, f"{what}: relative Frobenius error {r:.3e} against the oracle"
+
+
+def test_sketch_signs_are_splitmix64(cuda):
+    i = torch.tensor([0, 1, 7, 123456789, (1 << 40) + 3, (1 << 62) + 11], dtype=torch.int64)
+    for dev in ("cpu", cuda):
+        h = O.splitmix64(i.to(dev)).cpu().tolist()
+        assert [x % (1 << 64) for x in h] == [O.splitmix64_py(int(x)) for x in i]
 
 
 def test_diffusion_mass_tet_64(cuda):
@@ -37,8 +77,12 @@ def test_diffusion_mass_tet_64(cuda):
     kappa = wl.data["kappa"].to(cuda)
     K, M = tg.assemble_forms([K_asm, M_asm], mesh.points, {"kappa": kappa})
     assert K_asm.edges.shape[1] == ref["nnz"]
-    _close(K, ref["K"])
-    _close(M, ref["M"])
+    slot = K_asm.projector["tetra"].indices
+    assert O.slot_hash(slot) == ref["slot_sha256"]
+    Ko, Mo, _ = O.reference_call_diffusion_mass(mesh.points, mesh.elements(), kappa, slot.to(cuda),
+                                                K_asm.edges.to(cuda), with_hash=False)
+    _check(K, Ko, ref["K"], "C2 K")
+    _check(M, Mo, ref["M"], "C2 M")
     Ks = K_asm(mesh.points, element_data={"kappa": kappa})
     assert torch.equal(Ks.values, K)
     assert Ks.layout_hash == ref["hash"]
@@ -48,11 +92,18 @@ def test_poisson_tri_256(cuda):
     ref = _full()["poisson_tri_256"]
     wl = W.poisson_tri(256)
     mesh = wl.mesh.to(cuda)
-    K = tg.LaplaceElementAssembler.from_mesh(mesh)(mesh.points)
+    asm = tg.LaplaceElementAssembler.from_mesh(mesh)
+    K = asm(mesh.points)
     b = tg.LoadNodeAssembler.from_mesh(mesh)(mesh.points, point_data={"f": wl.data["f"].to(cuda)})
     assert K.layout_hash == ref["hash"]
-    _close(K.values, ref["K"])
-    _close(b, ref["b"])
+    slot = asm.projector["triangle"].indices
+    assert O.slot_hash(slot) == ref["slot_sha256"]
+    ones = torch.ones(mesh.n_elements, dtype=torch.float64, device=cuda)
+    Ko, _, _ = O.reference_call_diffusion_mass(mesh.points, mesh.elements(), ones, slot.to(cuda),
+                                               asm.edges.to(cuda), etype="triangle", with_hash=False)
+    _check(K.values, Ko, ref["K"], "C1 K")
+    bo = O.assemble_load(wl.mesh.points, wl.mesh.elements(), "triangle", wl.mesh.n_points, f_nodes=wl.data["f"])
+    _check(b, bo, ref["b"], "C1 b")
     cond = tg.Condenser(mesh.boundary_mask)
     Ki, bi = cond(K, b)
     ui, info = tg.pcg_solve(Ki, bi, rtol=1e-13, return_info=True)
@@ -66,11 +117,18 @@ def test_inverse_diffusion_tet_48(cuda):
     ref = _full()["inverse_diffusion_tet_48"]
     wl = W.inverse_diffusion_tet(48)
     mesh = wl.mesh.to(cuda)
-    K = tg.LaplaceElementAssembler.from_mesh(mesh)(mesh.points, element_data={"kappa": wl.data["kappa_true"].to(cuda)})
+    asm = tg.LaplaceElementAssembler.from_mesh(mesh)
+    kappa = wl.data["kappa_true"].to(cuda)
+    K = asm(mesh.points, element_data={"kappa": kappa})
     b = tg.LoadNodeAssembler.from_mesh(mesh)(mesh.points, point_data={"f": wl.data["f"].to(cuda)})
     assert K.layout_hash == ref["hash"]
-    _close(K.values, ref["K"])
-    _close(b, ref["b"])
+    slot = asm.projector["tetra"].indices
+    assert O.slot_hash(slot) == ref["slot_sha256"]
+    Ko, _, _ = O.reference_call_diffusion_mass(mesh.points, mesh.elements(), kappa, slot.to(cuda),
+                                               asm.edges.to(cuda), with_hash=False)
+    _check(K.values, Ko, ref["K"], "C4 K")
+    bo = O.assemble_load(wl.mesh.points, wl.mesh.elements(), "tetra", wl.mesh.n_points, f_nodes=wl.data["f"])
+    _check(b, bo, ref["b"], "C4 b")
 
 
 def test_elasticity_p2tet_32(cuda):
@@ -78,7 +136,12 @@ def test_elasticity_p2tet_32(cuda):
     wl = W.elasticity_p2tet(32)
     mesh = wl.mesh.to(cuda)
     asm = tg.LinearElasticityElementAssembler.from_mesh(mesh, nu=0.3)
-    El = asm(mesh.points, element_data={"E": wl.data["E"].to(cuda)})
+    E = wl.data["E"].to(cuda)
+    El = asm(mesh.points, element_data={"E": E})
     assert asm.edges.shape[1] == ref["nnz_blocks"]
     assert El.nnz == ref["nnz"]
-    _close(El.values, ref["K"])
+    slot = asm.projector["tetra10"].indices
+    assert O.slot_hash(slot) == ref["slot_sha256"]
+    Ko, _ = O.reference_call_elasticity(mesh.points, mesh.elements(), E, slot.to(cuda), asm.edges.to(cuda),
+                                        with_hash=False)
+    _check(El.values, Ko, ref["K"], "C3 K")

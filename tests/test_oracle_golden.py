@@ -96,19 +96,44 @@ def _close(ck, ref, tol=1e-12):
         assert abs(ck[key] - ref[key]) <= tol * ref["abs"], (key, ck[key], ref[key])
 
 
+def test_sketch_signs_are_splitmix64():
+    i = torch.tensor([0, 1, 7, 123456789, (1 << 40) + 3, (1 << 62) + 11], dtype=torch.int64)
+    h = O.splitmix64(i).tolist()
+    assert [x % (1 << 64) for x in h] == [O.splitmix64_py(int(x)) for x in i]
+
+
+def test_sketch_estimates_the_relative_error():
+    """64 sign sketches estimate ||a - b|| / ||b|| within a factor of two,
+    whatever the sign pattern of the difference."""
+    g = torch.Generator().manual_seed(3)
+    b = torch.randn(200_000, generator=g, dtype=torch.float64)
+    sb = O.sketch(b)
+    for d in (torch.randn(200_000, generator=g, dtype=torch.float64) * 1e-12,
+              torch.full((200_000,), 1e-14, dtype=torch.float64),
+              torch.zeros(200_000, dtype=torch.float64).index_fill_(0, torch.tensor([17]), 1e-9)):
+        true = float(d.norm() / b.norm())
+        est = O.sketch_rel_error(O.sketch(b + d), sb, float(b.norm()))
+        assert 0.5 * true <= est <= 2.0 * true, (est, true)
+
+
 def test_oracle_full_poisson_tri_256():
-    """Full-size C1 through the oracle: pattern hash, K and b fingerprints and
-    the L2 error of the condensed direct solve (3.7935e-05 for the reference)."""
+    """Full-size C1 through the oracle: pattern and slot-map hashes, K and b
+    against the reference's fingerprints and sign sketches (relative
+    Frobenius estimate below 1e-13) and the L2 error of the condensed direct
+    solve (3.7935e-05 for the reference)."""
     from tensormesh_gb300 import workloads as W
     ref = _full()["poisson_tri_256"]
     wl = W.poisson_tri(256)
     m = wl.mesh
-    edges, _, K = O.assemble_matrix(m.points, m.elements(), m.n_points,
-                                    lambda p, c: O.element_locals_diffusion(p, c, "triangle", None, 2))
+    edges, slot, K = O.assemble_matrix(m.points, m.elements(), m.n_points,
+                                       lambda p, c: O.element_locals_diffusion(p, c, "triangle", None, 2))
     b = O.assemble_load(m.points, m.elements(), "triangle", m.n_points, f_nodes=wl.data["f"])
     assert O.layout_hash(edges[0], edges[1]) == ref["hash"]
+    assert O.slot_hash(slot) == ref["slot_sha256"]
     _close(O.checksum(K), ref["K"])
     _close(O.checksum(b), ref["b"])
+    for v, r in ((K, ref["K"]), (b, ref["b"])):
+        assert O.sketch_rel_error(O.sketch(v), r["sketch"], r["fro"]) <= 1e-13
     u = O.solve_dirichlet(K, edges[0], edges[1], m.n_points, m.boundary_mask, b)
     err = float((u - wl.data["exact"]).norm() / wl.data["exact"].norm())
     assert abs(err - ref["l2_rel_error"]) <= 1e-9 * ref["l2_rel_error"]
