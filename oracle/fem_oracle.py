@@ -312,6 +312,29 @@ def assemble_matrix(points, conn, n_points, local_fn, chunk=1 << 15, **kw):
     return edges, slot, out
 
 
+def assemble_mixed(points, cells, n_points, local_fns):
+    """A matrix over a mesh with several element types: the pattern of every
+    type's local pairs together (element_assembler.py:811-830 with all types'
+    pairs), and the sum over types, in type order, of each type's locals
+    reduced onto it (the projectors of element_assembler.py:832-856 summed
+    as __call__ sums them).  ``local_fns[et](points, conn)`` gives a type's
+    locals.  Returns (edges int32 [2, nnz], values)."""
+    keys = []
+    for et, conn in cells.items():
+        c = conn.cpu().numpy().astype(np.int64)
+        B = c.shape[1]
+        keys.append((np.repeat(c[:, :, None], B, 2) * n_points + np.repeat(c[:, None, :], B, 1)).reshape(-1))
+    union = np.unique(np.concatenate(keys))
+    edges = torch.from_numpy(np.stack([union // n_points, union % n_points]).astype(np.int32))
+    out = None
+    for (et, conn), k in zip(cells.items(), keys):
+        loc = local_fns[et](points, conn)
+        slot = torch.from_numpy(np.searchsorted(union, k))
+        part = reduce_project(slot, loc.reshape(slot.shape[0], *loc.shape[3:]), union.shape[0])
+        out = part if out is None else out + part
+    return edges, out
+
+
 def assemble_load(points, conn, etype, n_points, f_nodes=None, const=None, func=None, qorder=2,
                   chunk=1 << 16):
     """b_i = sum_e sum_q jxw phi_i(q) f(q)  (node_assembler.py:368-409):

@@ -5,7 +5,7 @@ A drop-in for the assembly path of TensorMesh: ``ElementAssembler`` /
 signatures and return types, and run hand-written CUDA kernels through the
 C ABI of ``libtmgb300.so`` (``include/tensormesh_gb300.h``).
 """
-from .mesh import Mesh, gen_unit_square, gen_unit_cube
+from .mesh import Mesh, gen_unit_square, gen_unit_square_mixed, gen_unit_cube
 from .element import element_type2dimension, element_type2order
 from .transformation import Transformation, ReduceProjector, SparseProjector
 from .sparse import SparseMatrix
@@ -22,7 +22,7 @@ from . import autotune
 __version__ = "0.1.0"
 
 __all__ = [
-    "Mesh", "gen_unit_square", "gen_unit_cube", "Transformation", "ReduceProjector", "SparseProjector",
+    "Mesh", "gen_unit_square", "gen_unit_square_mixed", "gen_unit_cube", "Transformation", "ReduceProjector", "SparseProjector",
     "SparseMatrix", "ElementAssembler", "NodeAssembler", "assemble_forms", "LaplaceElementAssembler",
     "DiffusionElementAssembler", "MassElementAssembler", "LinearElasticityElementAssembler",
     "const_node_assembler", "func_node_assembler", "LoadNodeAssembler", "pcg_solve",

@@ -27,7 +27,7 @@ import torch.nn as nn
 
 from . import _lib
 from .element import element_info, element_tables, element_type2dimension
-from .plan import Topology
+from .plan import MixedTopology, Topology
 from .sparse import SparseMatrix
 from .transformation import ReduceProjector, SparseProjector, Transformation
 
@@ -117,6 +117,129 @@ class _AssemblerBase(nn.Module):
 
 
 # ============================================================================
+# Recognition of user weak forms
+# ============================================================================
+class RecognisedForm:
+    """A user ``forward`` identified as a built-in family: ``form`` is
+    "diffusion", "mass" or "elasticity", ``coef`` the name of its coefficient
+    argument (or None) and ``nu`` the Poisson ratio of an elasticity form."""
+
+    def __init__(self, form: str, coef: Optional[str], nu: float = 0.3, scale: float = 1.0):
+        self.form, self.coef, self.nu, self.scale = form, coef, nu, scale
+
+    def __repr__(self):
+        return f"RecognisedForm({self.form!r}, coef={self.coef!r}, nu={self.nu}, scale={self.scale})"
+
+
+_FIELD_ARGS = ("gradu", "gradv", "u", "v", "x")
+_UNSET = object()
+
+
+def _close(a: torch.Tensor, b: torch.Tensor, tol: float = 1e-12) -> bool:
+    a, b = torch.as_tensor(a, dtype=torch.float64), torch.as_tensor(b, dtype=torch.float64)
+    if a.shape != b.shape:
+        return False
+    return bool((a - b).abs().max() <= tol * max(1.0, float(b.abs().max())))
+
+
+def recognise_form(asm) -> Optional[RecognisedForm]:
+    """Identify the ``forward`` of an ``ElementAssembler`` subclass with one
+    of the families the kernels assemble, the way the reference calls it
+    (per element, quadrature point and basis pair, arguments bound by name:
+    element_assembler.py:231-445): ``forward(gradu, gradv[, c])`` returning
+    ``c * (gradu @ gradv)`` (diffusion, e.g. the ``SIMPLaplace`` form of
+    examples/inverse_design/thermal_topology.py:48-52), ``forward(u, v[, c])``
+    returning ``c * u * v`` (mass), or ``forward(gradu, gradv[, c])`` returning
+    a D x D block ``c (lam gu gv^T + mu (gv gu^T + (gu . gv) I))`` (isotropic
+    elasticity, ``Ba^T C Bb`` of builtin.py:168-178).  ``forward`` is probed
+    on a few seeded random arguments in float64 and must reproduce the family
+    to 1e-12 on each, with a coefficient that enters linearly; anything else
+    (another argument, a nonlinear dependence) is a custom form (None).  The
+    result is cached on the assembler (a form may read its own attributes,
+    such as a Poisson ratio set by ``__post_init__``)."""
+    cached = asm.__dict__.get("_tm_recognised", _UNSET)
+    if cached is not _UNSET:
+        return cached
+    try:
+        rec = _probe(asm)
+    except Exception:
+        rec = None
+    asm.__dict__["_tm_recognised"] = rec
+    return rec
+
+
+def _probe(asm) -> Optional[RecognisedForm]:
+    if type(asm).forward is ElementAssembler.forward:
+        return None
+    params = list(inspect.signature(asm.forward).parameters.values())
+    if any(p.kind in (p.VAR_POSITIONAL, p.VAR_KEYWORD) for p in params):
+        return None
+    names = [p.name for p in params]
+    coefs = [n for n in names if n not in _FIELD_ARGS]
+    if len(coefs) > 1 or "x" in names:
+        return None
+    coef = coefs[0] if coefs else None
+    fields = set(names) - set(coefs)
+    D = asm.dimension
+    g = torch.Generator().manual_seed(1234)
+    draws = []
+    for _ in range(3):
+        c = 0.5 + float(torch.rand((), generator=g, dtype=torch.float64)) * 1.5
+        draws.append((torch.randn(D, generator=g, dtype=torch.float64),
+                      torch.randn(D, generator=g, dtype=torch.float64),
+                      torch.randn((), generator=g, dtype=torch.float64),
+                      torch.randn((), generator=g, dtype=torch.float64), c))
+
+    def call(gu, gv, u, v, c):
+        vals = {"gradu": gu, "gradv": gv, "u": u, "v": v}
+        kw = {n: vals[n] for n in fields}
+        if coef is not None:
+            kw[coef] = torch.tensor(c, dtype=torch.float64)
+        with torch.no_grad():
+            return torch.as_tensor(asm.forward(**kw))
+
+    if fields == {"u", "v"}:
+        for gu, gv, u, v, c in draws:
+            if not _close(call(gu, gv, u, v, c), (c if coef else 1.0) * u * v):
+                return None
+        return RecognisedForm("mass", coef)
+    if fields != {"gradu", "gradv"}:
+        return None
+    gu, gv, u, v, c = draws[0]
+    out = call(gu, gv, u, v, c)
+    if out.dim() == 0:
+        for gu, gv, u, v, c in draws:
+            if not _close(call(gu, gv, u, v, c), (c if coef else 1.0) * (gu @ gv)):
+                return None
+        return RecognisedForm("diffusion", coef)
+    if tuple(out.shape) != (D, D):
+        return None
+
+    def basis(gu, gv):
+        return torch.outer(gu, gv), torch.outer(gv, gu) + (gu @ gv) * torch.eye(D, dtype=torch.float64)
+
+    # lam and mu per unit coefficient from the first draw (least squares),
+    # then every draw must reproduce the block
+    a, b = basis(gu, gv)
+    scale = c if coef else 1.0
+    A = torch.stack([a.reshape(-1), b.reshape(-1)], 1) * scale
+    sol = torch.linalg.lstsq(A, out.reshape(-1, 1).to(torch.float64)).solution.reshape(-1)
+    lam, mu = float(sol[0]), float(sol[1])
+    if not (mu > 0 and lam + mu > 0):
+        return None
+    for gu, gv, u, v, c in draws:
+        a, b = basis(gu, gv)
+        if not _close(call(gu, gv, u, v, c), (c if coef else 1.0) * (lam * a + mu * b)):
+            return None
+    # the kernel's moduli: lam = E nu / ((1 + nu)(1 - 2 nu)), mu = E / (2 (1 + nu));
+    # E per unit coefficient is the form's scale
+    nu = lam / (2.0 * (lam + mu))
+    if not (-1.0 < nu < 0.5):
+        return None
+    return RecognisedForm("elasticity", coef, nu, scale=2.0 * mu * (1.0 + nu))
+
+
+# ============================================================================
 # Bilinear forms
 # ============================================================================
 class ElementAssembler(_AssemblerBase):
@@ -127,6 +250,16 @@ class ElementAssembler(_AssemblerBase):
     ``"elasticity"`` (``LinearElasticityElementAssembler``)."""
 
     _tm_form: Optional[str] = None
+
+    def _tm_kind(self) -> Optional[str]:
+        """The kernel family of this assembler: the class's ``_tm_form``, or
+        for a user subclass the family its ``forward`` is recognised as
+        (``recognise_form``), or None for a custom integrand."""
+        form = type(self)._tm_form
+        if form is not None:
+            return form
+        rec = recognise_form(self)
+        return None if rec is None else rec.form
 
     def __init__(self, projector, transformation, elements, edges, *args, **kwargs):
         super().__init__()
@@ -155,7 +288,10 @@ class ElementAssembler(_AssemblerBase):
         plan builder together with the kernels' reduction plan."""
         assert project in ["reduce", "sparse"]
         points = mesh.points
-        etype, conn = _single_type(_mesh_elements(mesh))
+        elements = _mesh_elements(mesh)
+        if len(elements) > 1:
+            return cls._from_mixed(mesh, elements, quadrature_order, project, *args, **kwargs)
+        etype, conn = _single_type(elements)
         topo = Topology(points, conn, etype, quadrature_order, matrix=True,
                         element_groups=getattr(mesh, "element_groups", None))
         E, B = conn.shape
@@ -167,6 +303,37 @@ class ElementAssembler(_AssemblerBase):
         trans = Transformation(points=points, elements=conn.long(), element_type=etype,
                                quadrature_order=quadrature_order)
         asm = cls({etype: proj}, {etype: trans}, {etype: conn.long()}, topo.edges, *args, **kwargs)
+        asm._topology = topo
+        return asm.type(mesh.dtype).to(mesh.device)
+
+    @classmethod
+    def _from_mixed(cls, mesh, elements, quadrature_order, project, *args, **kwargs):
+        """A mesh with several element types (element_assembler.py:811-866):
+        one pattern over every type's local pairs, one projector and one
+        Transformation per type.  The reference stacks the types' pair
+        columns element-major (``torch.stack(..., -1)``), which raises when
+        the types have different element counts and, with equal counts,
+        hands each type slots of the interleaved sequence; here every type's
+        slot map points at the union positions of its own pairs, and the
+        assembled matrix is the sum over types."""
+        points = mesh.points
+        for et in elements:
+            element_info(et)
+        dims = {element_type2dimension[et] for et in elements}
+        if len(dims) != 1:
+            raise ValueError(f"element types of different dimensions in one mesh: {list(elements)}")
+        topo = MixedTopology(points, {et: c for et, c in elements.items()}, quadrature_order, matrix=True)
+        proj, trans = {}, {}
+        for et, conn in elements.items():
+            E, B = conn.shape
+            if project == "reduce":
+                proj[et] = ReduceProjector(indices=topo.slot[et], from_shape=(E, B, B), to_shape=(topo.nnz,))
+            else:
+                proj[et] = SparseProjector(from_=torch.arange(E * B * B), to_=topo.slot[et], from_shape=(E, B, B),
+                                           to_shape=(topo.nnz,))
+            trans[et] = Transformation(points=points, elements=conn.long(), element_type=et,
+                                       quadrature_order=quadrature_order)
+        asm = cls(proj, trans, {et: c.long() for et, c in elements.items()}, topo.edges, *args, **kwargs)
         asm._topology = topo
         return asm.type(mesh.dtype).to(mesh.device)
 
@@ -211,12 +378,15 @@ class ElementAssembler(_AssemblerBase):
         never materialises the integrand."""
         if func is not None:
             raise NotImplementedError("custom integrands (func=...) are not assembled by tensormesh_gb300")
-        form = type(self)._tm_form
+        form = self._tm_kind()
         if form is None:
             raise NotImplementedError(
                 f"{type(self).__name__}.forward is a custom Python weak form; tensormesh_gb300 assembles the "
                 f"built-in families (LaplaceElementAssembler / DiffusionElementAssembler, "
-                f"MassElementAssembler, LinearElasticityElementAssembler)")
+                f"MassElementAssembler, LinearElasticityElementAssembler, or a forward that computes "
+                f"c * (gradu @ gradv), c * u * v or an isotropic elasticity block)")
+        if isinstance(self._topology, MixedTopology):
+            return self._call_mixed(points, point_data, element_data, scalar_data)
         et, points, ed, sd = self._prepare(points, point_data, element_data, scalar_data)
         if torch.is_grad_enabled() and (points.requires_grad or any(
                 torch.is_tensor(v) and v.requires_grad for v in list(ed.values()) + list(sd.values()))):
@@ -232,6 +402,21 @@ class ElementAssembler(_AssemblerBase):
         (values,) = assemble_forms([self], points, ed, sd)
         return self._build_output(values)
 
+    def _call_mixed(self, points, point_data, element_data, scalar_data) -> SparseMatrix:
+        et0 = self.element_types[0]
+        if points is None:
+            points = self.transformation[et0].points
+        for et in self.element_types:
+            self.transformation[et].update_points(points)
+        _lib.require_cuda(points, "points")
+        self.type(points.dtype).to(points.device)
+        ed = dict(element_data or {})
+        if torch.is_grad_enabled() and (points.requires_grad or any(
+                torch.is_tensor(v) and v.requires_grad for v in ed.values())):
+            raise NotImplementedError("gradients on meshes with several element types are not implemented")
+        (values,) = assemble_forms([self], points, ed, dict(scalar_data or {}))
+        return self._build_output(values)
+
     def _build_output(self, values: torch.Tensor) -> SparseMatrix:
         topo = self._topo(True)
         edges = self.edges
@@ -245,7 +430,26 @@ class ElementAssembler(_AssemblerBase):
 
     # -- form parameters (overridden by the built-ins) ------------------------
     def _tm_coefficients(self, ed, sd, E):
-        return {}
+        """Kernel coefficients of a recognised user form: its coefficient
+        argument is looked up by name in element_data (per element) or
+        scalar_data, as the reference binds forward's arguments."""
+        rec = recognise_form(self)
+        if rec is None:
+            return {}
+        c = None
+        if rec.coef is not None:
+            c = ed.get(rec.coef, sd.get(rec.coef))
+            if c is None:
+                raise KeyError(f"{type(self).__name__}.forward takes {rec.coef!r}: pass it in element_data "
+                               f"(one value per element) or scalar_data")
+        if rec.form == "diffusion":
+            return {"kappa": c}
+        if rec.form == "mass":
+            if torch.is_tensor(c) and c.dim() > 0 and c.numel() > 1:
+                raise NotImplementedError("a per-element coefficient of the mass form is not assembled by "
+                                          "tensormesh_gb300 (a scalar one is)")
+            return {"rho": c}
+        return {"E": 1.0 if c is None else c, "nu": rec.nu, "E_scale": rec.scale}
 
     def forward(self, *args, **kwargs):
         raise NotImplementedError("forward is not implemented")
@@ -299,12 +503,65 @@ def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_da
     topo = first._topo(True)
     ed = dict(element_data or {})
     sd = dict(scalar_data or {})
+    if isinstance(topo, MixedTopology):
+        return _assemble_mixed(assemblers, topo, points, ed, sd)
+    return _assemble_on(assemblers, topo, points, ed, sd, _events, _stats)
+
+
+def _split_element_data(topo: "MixedTopology", ed: dict) -> Dict[str, dict]:
+    """Per element type, the element data of a mixed mesh: a value given as
+    {element_type: tensor} (the reference's per-type form) or as one tensor
+    over all elements, the types' elements concatenated in type order."""
+    out = {et: {} for et in topo.types}
+    total = sum(topo.n_elements.values())
+    for key, value in ed.items():
+        if isinstance(value, dict):
+            for et in topo.types:
+                out[et][key] = value[et]
+        elif torch.is_tensor(value) and value.dim() > 0:
+            if value.shape[0] != total:
+                raise ValueError(f"{key} must be a {{element_type: tensor}} dict or have one value per element "
+                                 f"of all types ({total}), got {tuple(value.shape)}")
+            o = 0
+            for et in topo.types:
+                n = topo.n_elements[et]
+                out[et][key] = value[o:o + n]
+                o += n
+        else:
+            for et in topo.types:
+                out[et][key] = value
+    return out
+
+
+def _combine(topo: "MixedTopology", kind: str, parts, dev, dt) -> torch.Tensor:
+    """Sum per-type results into the union pattern ("matrix") or onto the
+    nodes ("node") with one deterministic gather-sum, types in order."""
+    lib = _lib.load()
+    width = int(np.prod(parts[0].shape[1:])) if parts[0].dim() > 1 else 1
+    x = torch.cat([p.reshape(p.shape[0], width) for p in parts], 0).contiguous()
+    n_to = topo.nnz if kind == "matrix" else topo.n_points
+    seg, src = topo.segments(dev, kind)
+    out = torch.empty(n_to, *parts[0].shape[1:], dtype=dt, device=dev)
+    _lib.check(lib.tm_project_reduce(_lib.dtype_code(dt), n_to, width, _lib.ptr(seg), _lib.ptr(src), _lib.ptr(x),
+                                     _lib.ptr(out), _lib.stream_handle(dev)), "tm_project_reduce")
+    return out
+
+
+def _assemble_mixed(assemblers, topo: "MixedTopology", points, ed, sd):
+    per_type = _split_element_data(topo, ed)
+    parts = [_assemble_on(assemblers, topo.topos[et], points, per_type[et], sd, None, None) for et in topo.types]
+    return [_combine(topo, "matrix", [p[i] for p in parts], points.device, points.dtype)
+            for i in range(len(assemblers))]
+
+
+def _assemble_on(assemblers, topo: Topology, points, ed, sd, _events, _stats):
+    """The fused launches of ``assemble_forms`` on one element type."""
     E = topo.n_elements
     dev, dt = points.device, points.dtype
     pts = points.detach().contiguous()
     if pts.dtype not in (torch.float64, torch.float32):
         raise TypeError(f"points must be float64 or float32, got {pts.dtype}")
-    forms = [type(a)._tm_form for a in assemblers]
+    forms = [a._tm_kind() for a in assemblers]
     scalar_group = [i for i, f in enumerate(forms) if f in ("diffusion", "mass")]
     out = [None] * len(assemblers)
     groups = []
@@ -344,7 +601,7 @@ def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_da
             else:
                 block = True
                 t, s = _coef(c.get("E"), dt, dev, E, "E")
-                args.young, args.young_scale = _lib.ptr(t), s
+                args.young, args.young_scale = _lib.ptr(t), s * float(c.get("E_scale", 1.0))
                 args.poisson = float(c.get("nu", 0.3))
                 keep.append(t)
                 out[i] = torch.empty(topo.nnz, D, D, dtype=dt, device=dev)
@@ -408,6 +665,26 @@ class NodeAssembler(_AssemblerBase):
 
     @classmethod
     def _build(cls, points, elements, quadrature_order, device, dtype, project, element_groups, *args, **kwargs):
+        if not isinstance(elements, torch.Tensor) and len(elements) > 1:
+            # several element types: one projector (conn.flatten()) and one
+            # Transformation per type, the nodal vectors summed over types
+            # in type order (node_assembler.py:617-698)
+            N = points.shape[0]
+            proj, trans = {}, {}
+            for et, conn in elements.items():
+                element_info(et)
+                E, B = conn.shape
+                if project == "reduce":
+                    proj[et] = ReduceProjector(indices=conn.flatten(), from_shape=(E, B), to_shape=(N,))
+                elif project == "sparse":
+                    proj[et] = SparseProjector(from_=torch.arange(E * B), to_=conn.flatten(), from_shape=(E, B),
+                                               to_shape=(N,))
+                else:
+                    raise ValueError(f"project should be either 'reduce' or 'sparse', but got {project}")
+                trans[et] = Transformation(points, conn, et, quadrature_order)
+            asm = cls(proj, trans, dict(elements), *args, **kwargs)
+            asm._topology = MixedTopology(points, dict(elements), quadrature_order, matrix=False)
+            return asm.type(dtype).to(device)
         etype, conn = _single_type(elements)
         N = points.shape[0]
         E, B = conn.shape
@@ -477,11 +754,25 @@ class NodeAssembler(_AssemblerBase):
             assert value.shape[0] == points.shape[0], \
                 f"the shape of {key} should be [n_point, ...], but got {tuple(value.shape)}"
         fn = self.forward if func is None else func
+        topo = self._topology
+        if isinstance(topo, MixedTopology):
+            if torch.is_grad_enabled() and (points.requires_grad or any(
+                    torch.is_tensor(v) and v.requires_grad for v in list(point_data.values()) +
+                    list(scalar_data.values()))):
+                raise NotImplementedError("gradients on meshes with several element types are not implemented")
+            for et in self.element_types[1:]:
+                self.transformation[et].update_points(points)
+            parts = [assemble_linear_form(self, fn, points, point_data, scalar_data, topo=topo.topos[et])
+                     for et in topo.types]
+            width = parts[0].numel() // topo.n_points
+            return _combine(topo, "node", [p.reshape(topo.n_points, width) for p in parts], points.device,
+                            points.dtype).reshape(-1)
         return assemble_linear_form(self, fn, points, point_data, scalar_data)
 
 
-def assemble_linear_form(asm: NodeAssembler, fn: Callable, points: torch.Tensor, point_data, scalar_data):
-    topo = asm._topo(False)
+def assemble_linear_form(asm: NodeAssembler, fn: Callable, points: torch.Tensor, point_data, scalar_data,
+                         topo: Optional[Topology] = None):
+    topo = asm._topo(False) if topo is None else topo
     dev, dt = points.device, points.dtype
     pts = points.detach().contiguous()
     params = list(inspect.signature(fn).parameters)

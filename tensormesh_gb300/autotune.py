@@ -35,7 +35,7 @@ from .element import element_info
 
 # chunk sizes tried (those that fit the element type and kind), besides the
 # static default
-CANDIDATES = (16, 32, 64, 128, 256, 384, 512)
+CANDIDATES = (16, 32, 64, 128, 256, 384, 512, 768, 1024)
 
 _table: Dict[str, int] = {}
 _loaded = False
@@ -222,7 +222,7 @@ def tune_matrix(assemblers, points: Optional[torch.Tensor] = None, element_data=
     pts = trans.points if points is None else points
     _lib.require_cuda(pts, "points")
     topo = first._topo(True)
-    kind = "block" if any(type(a)._tm_form == "elasticity" for a in assemblers) else "scalar"
+    kind = "block" if any(a._tm_kind() == "elasticity" for a in assemblers) else "scalar"
     run = lambda: assemble_forms(assemblers, pts, element_data, scalar_data)
     return _sweep(topo, (pts.device, et, kind, topo.quadrature_order, pts.dtype), "matrix", run, sizes, repeats,
                   save)

@@ -1247,8 +1247,24 @@ inline int set_smem(K kernel, size_t bytes) {
     return TM_OK;
 }
 
+// float64 diffusion / mass on P1 simplices: tm_p1df.cuh (included at the
+// end of this header)
+template <int ET, int FORMS>
+int run_p1df(const tm_matrix_args& a, cudaStream_t st);
+template <typename R, int ET, int FORMS>
+int run_matrix_general(const tm_matrix_args& a, cudaStream_t st);
+
 template <typename R, int ET, int FORMS>
 int run_matrix(const tm_matrix_args& a, cudaStream_t st) {
+    if constexpr (use_df64<R, ET, FORMS>()) {
+        return run_p1df<ET, FORMS>(a, st);
+    } else {
+        return run_matrix_general<R, ET, FORMS>(a, st);
+    }
+}
+
+template <typename R, int ET, int FORMS>
+int run_matrix_general(const tm_matrix_args& a, cudaStream_t st) {
     const MatLayout L = mat_layout<R, ET, FORMS>(a.plan.chunk_elems, a.tables.n_quad, a.plan.max_chunk_slots,
                                                  a.plan.max_chunk_contrib);
     if (L.total > 227 * 1024) return tm_set_error(TM_ERR_TOO_LARGE, "tm_assemble_matrix: chunk needs more than 227 KB of shared memory");
@@ -1334,3 +1350,5 @@ int dispatch_source(const tm_vector_args& a, cudaStream_t st) {
 }
 
 }  // namespace tmk
+
+#include "tm_p1df.cuh"

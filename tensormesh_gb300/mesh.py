@@ -219,6 +219,24 @@ def gen_unit_square(n: int, order: int = 1, jitter: float = 0.0, seed: int = 0,
                 {"is_boundary": torch.from_numpy(bnd).to(device)})
 
 
+def gen_unit_square_mixed(n: int, jitter: float = 0.0, seed: int = 0, dtype: torch.dtype = torch.float64,
+                          device="cpu") -> Mesh:
+    """Unit square with ``n`` cells per side and two element types: cells
+    whose left edge lies in the left half are quadrilaterals (``"quad"``),
+    the others are split into the triangles (a,b,c), (a,c,d) of
+    ``gen_unit_square`` (``"triangle"``).  The quadrilaterals are listed
+    first.  Same nodes, jitter and boundary flags as ``gen_unit_square``."""
+    q = gen_unit_square(n, jitter=jitter, seed=seed, dtype=dtype, cell="quad")
+    t = gen_unit_square(n, jitter=jitter, seed=seed, dtype=dtype, cell="triangle")
+    i = np.tile(np.arange(n), n)                   # cell column, cells x fastest in both generators
+    left = i < (n + 1) // 2
+    quads = q.cells["quad"].numpy()[left]
+    tris = t.cells["triangle"].numpy().reshape(n * n, 2, 3)[~left].reshape(-1, 3)
+    return Mesh(q.points.to(device), {"quad": torch.from_numpy(quads).to(device),
+                                      "triangle": torch.from_numpy(tris).to(device)},
+                {"is_boundary": q.point_data["is_boundary"].to(device)})
+
+
 def gen_unit_cube(n: int, order: int = 1, jitter: float = 0.0, seed: int = 0,
                   dtype: torch.dtype = torch.float64, device="cpu") -> Mesh:
     """Kuhn-split unit cube with ``n`` cubes per side (6 tetrahedra per cube).

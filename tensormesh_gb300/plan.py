@@ -177,8 +177,8 @@ class DevicePlan:
 # chunk sizes (elements per CTA) by element type and whether the form is a
 # DxD block form; chosen so that the locals of a chunk fit in shared memory
 CHUNK_ELEMS = {
-    ("triangle", False): 256, ("triangle", True): 256,
-    ("tetra", False): 384, ("tetra", True): 128,
+    ("triangle", False): 768, ("triangle", True): 256,
+    ("tetra", False): 768, ("tetra", True): 128,
     ("triangle6", False): 64, ("triangle6", True): 64,
     ("tetra10", False): 32, ("tetra10", True): 32,
     ("quad", False): 128, ("quad", True): 128,
@@ -196,15 +196,16 @@ def chunk_fits(etype: str, block: bool, qorder: int, ch: int) -> bool:
     varies (P2, quadrilaterals), which keep the shape gradients of every
     quadrature point in shared memory, the estimate of the kernel's layout
     (tables, coordinates, gradients and weights per point, locals, staged
-    plan) stays within the budget.  P1 chunks hold only their locals and
-    staged plan, which the default sizes leave well inside it."""
+    plan) stays within the budget.  P1 chunks hold their locals and |det|
+    rho as 8-byte values and their share of the staged plan (about two
+    slots and NL 2-byte contributions per element)."""
     info = element_info(etype)
     B, D = info.n_basis, info.dim
     NL = B * (B + 1) // 2
     if ch < 1 or ch * NL * 2 > 65536:
         return False
     if etype in ("triangle", "tetra"):
-        return True
+        return 64 + ch * (8 * NL + 8 + 4 * 3 + 2 * NL) <= _CHUNK_SMEM_BUDGET
     Q = len(element_tables(etype, qorder)["w"])
     # tables, mass template and their double-float copies
     fixed = 8 * (Q + Q * B + Q * D * B + B * B + B + 1) + 16 * NL + 8 * Q * (D * B + 1 + B) + 64
@@ -337,6 +338,90 @@ class Topology:
     def block_layout_hash(self, H: int) -> str:
         """layout_hash of the (N*H, N*H) block matrix on this pattern (its
         expanded int64 scalar rows and columns), computed once per H."""
+        cache = self.__dict__.setdefault("_block_hashes", {})
+        if H not in cache:
+            from .sparse import block_layout_hash
+            cache[H] = block_layout_hash(self.edges[0], self.edges[1], H)
+        return cache[H]
+
+
+class MixedTopology:
+    """A mesh with several element types: one ``Topology`` per type (its own
+    pattern, plans and kernels) and the union pattern the assembled matrix
+    lives on.
+
+    The union pattern is the set of distinct (row, col) pairs over all types,
+    sorted row-major (int32 ``edges``), as ``ElementAssembler.from_mesh``
+    builds it from every type's local pairs (element_assembler.py:811-830).
+    ``maps[t]`` sends type t's own CSR positions into the union, so that the
+    union slot map of type t is ``maps[t][slot_t]``.  A matrix assembled per
+    type is combined by one deterministic gather-sum (``tm_project_reduce``)
+    whose segments list, for every union position, the contributing
+    positions of the types in type order: the sum over types runs in the
+    order of the mesh's element types, as the reference sums its projectors."""
+
+    def __init__(self, points: torch.Tensor, elements: Dict[str, torch.Tensor], quadrature_order: int,
+                 matrix: bool = True):
+        self.n_points = int(points.shape[0])
+        self.quadrature_order = quadrature_order
+        self.types = list(elements.keys())
+        self.topos: Dict[str, Topology] = {
+            et: Topology(points, conn, et, quadrature_order, matrix=matrix) for et, conn in elements.items()}
+        self.n_elements = {et: t.n_elements for et, t in self.topos.items()}
+        self._row_ptr: Dict[torch.device, torch.Tensor] = {}
+        self._seg: Dict[tuple, tuple] = {}
+        self._layout_hash = None
+        self.edges = None
+        if not matrix:
+            self.nnz = 0
+            return
+        N = np.int64(self.n_points)
+        keys = {et: t.edges[0].numpy().astype(np.int64) * N + t.edges[1].numpy().astype(np.int64)
+                for et, t in self.topos.items()}
+        union = np.unique(np.concatenate(list(keys.values())))
+        self.nnz = int(union.shape[0])
+        self.edges = torch.from_numpy(np.stack([(union // N).astype(np.int32), (union % N).astype(np.int32)]))
+        self.maps = {et: np.searchsorted(union, k).astype(np.int64) for et, k in keys.items()}
+        self.slot = {et: torch.from_numpy(self.maps[et][t.slot.numpy()]) for et, t in self.topos.items()}
+
+    def segments(self, device: torch.device, kind: str) -> tuple:
+        """(seg_ptr, src) of the combine: "matrix" over the union pattern
+        (sources: the types' CSR values, concatenated in type order),
+        "node" over the nodes (sources: the types' nodal vectors)."""
+        key = (kind, device)
+        if key not in self._seg:
+            if kind == "matrix":
+                tgt = np.concatenate([self.maps[et] for et in self.types])
+                n_to = self.nnz
+            else:
+                tgt = np.tile(np.arange(self.n_points, dtype=np.int64), len(self.types))
+                n_to = self.n_points
+            src = np.argsort(tgt, kind="stable").astype(np.int64)     # type order within a target
+            seg = np.zeros(n_to + 1, dtype=np.int64)
+            np.cumsum(np.bincount(tgt, minlength=n_to), out=seg[1:])
+            self._seg[key] = (torch.from_numpy(seg).to(device), torch.from_numpy(src).to(device))
+        return self._seg[key]
+
+    def row_ptr(self, device: torch.device) -> torch.Tensor:
+        """CSR row pointer of the union pattern."""
+        if device not in self._row_ptr:
+            counts = np.bincount(self.edges[0].numpy(), minlength=self.n_points)
+            rp = np.zeros(self.n_points + 1, dtype=np.int64)
+            np.cumsum(counts, out=rp[1:])
+            self._row_ptr[device] = torch.from_numpy(rp).to(device)
+        return self._row_ptr[device]
+
+    @property
+    def layout_hash(self) -> str:
+        """SHA-256 of the union pattern's int32 rows then columns
+        (sparse/matrix.py:82-86)."""
+        if self._layout_hash is None:
+            import hashlib
+            self._layout_hash = hashlib.sha256(self.edges[0].numpy().tobytes()
+                                               + self.edges[1].numpy().tobytes()).hexdigest()
+        return self._layout_hash
+
+    def block_layout_hash(self, H: int) -> str:
         cache = self.__dict__.setdefault("_block_hashes", {})
         if H not in cache:
             from .sparse import block_layout_hash
