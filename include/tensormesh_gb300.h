@@ -182,6 +182,31 @@ int64_t tm_plan_scalar(const tm_host_plan* plan, int32_t which);
 void tm_plan_free(tm_host_plan* plan);
 
 /*
+ * Device-side construction of the CSR pattern and the slot map (replaces
+ * ElementAssembler.from_mesh's SciPy COO->CSR conversion and id lookup,
+ * assemble/element_assembler.py:811-851): the same int32 edges (unique
+ * (row, col) pairs sorted row-major) and int64 slot map (element-major,
+ * i-major, j-minor), built on the GPU by a node-incidence counting sort and
+ * per-row ranking of the candidate columns; deterministic.
+ *   conn: device int32 [n_elements*n_basis] (element order), n_basis one of
+ *         3, 4, 6, 9, 10; n_elements*n_basis and n_points below 2^31.
+ *   workspace: device, tm_pattern_workspace_bytes(...) bytes, shared by the
+ *         two calls (tm_pattern_fill reads what tm_pattern_count left there).
+ * tm_pattern_count writes row_ptr (device int64 [n_points+1]), synchronises
+ * the stream and returns nnz in *nnz (host); a node index outside
+ * [0, n_points) gives TM_ERR_INVALID_ARG, a node lying in more than
+ * 8192 / n_basis elements TM_ERR_TOO_LARGE.  tm_pattern_fill then writes
+ * edge_row, edge_col (device int32 [nnz]) and slot (device int64
+ * [n_elements*n_basis*n_basis]), stream-ordered.
+ */
+size_t tm_pattern_workspace_bytes(int64_t n_elements, int32_t n_basis, int64_t n_points);
+int tm_pattern_count(const int32_t* conn, int64_t n_elements, int32_t n_basis, int64_t n_points,
+                     void* workspace, int64_t* row_ptr, int64_t* nnz, tm_stream_t stream);
+int tm_pattern_fill(const int32_t* conn, int64_t n_elements, int32_t n_basis, int64_t n_points,
+                    const void* workspace, const int64_t* row_ptr, int32_t* edge_row, int32_t* edge_col,
+                    int64_t* slot, tm_stream_t stream);
+
+/*
  * Float64 P1 diffusion / mass locals and their reduction are computed in
  * double-float arithmetic (hi + lo pairs of floats, ~48 bits, relative
  * error ~1e-14) on the FP32 pipes; chunks whose data fall outside the

@@ -155,6 +155,11 @@ _SIGNATURES = {
     "tm_quadrature_points": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, ElementTables,
                                        C.c_void_p, C.c_void_p]),
     "tm_morton_order": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]),
+    "tm_pattern_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32, C.c_int64]),
+    "tm_pattern_count": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p,
+                                   C.POINTER(C.c_int64), C.c_void_p]),
+    "tm_pattern_fill": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "tm_facet_vector_workspace_bytes": (C.c_size_t, [C.POINTER(FacetVectorArgs)]),
     "tm_assemble_facet_vector": (C.c_int, [C.POINTER(FacetVectorArgs), C.c_void_p]),
     "tm_condense": (C.c_int, [C.POINTER(CondenseArgs), C.c_void_p]),

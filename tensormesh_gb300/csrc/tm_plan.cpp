@@ -610,10 +610,15 @@ extern "C" int tm_plan_build(const int64_t* conn, int64_t n_elements, int32_t n_
                     for (int64_t t = t0; t < t1; ++t) {
                         const int64_t b = std::min(n_slot, t * step), e = std::min(n_slot, b + step);
                         std::copy(slot_map + b, slot_map + e, p->slot.begin() + b);
+                        // the range's extremes in registers, stored once (the
+                        // per-thread entries share cache lines)
+                        int64_t mx = -1, mn = 0;
                         for (int64_t k = b; k < e; ++k) {
-                            range_max[t] = std::max(range_max[t], slot_map[k]);
-                            range_min[t] = std::min(range_min[t], slot_map[k]);
+                            mx = std::max(mx, slot_map[k]);
+                            mn = std::min(mn, slot_map[k]);
                         }
+                        range_max[t] = mx;
+                        range_min[t] = mn;
                     }
                 });
                 if (*std::min_element(range_min.begin(), range_min.end()) < 0) {

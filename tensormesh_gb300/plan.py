@@ -71,6 +71,29 @@ def morton_order(points: np.ndarray, conn: np.ndarray, groups: Optional[np.ndarr
     return perm
 
 
+def device_pattern(conn: torch.Tensor, n_points: int):
+    """CSR pattern and slot map of a connectivity on the GPU
+    (``tm_pattern_count`` / ``tm_pattern_fill``): (edges int32 [2, nnz],
+    slot int64 [E*B*B], row_ptr int64 [N+1]), all on conn's device, equal to
+    the reference's ``from_mesh`` arrays."""
+    _lib.require_cuda(conn, "conn")
+    lib = _lib.load()
+    dev = conn.device
+    c = conn.to(torch.int32).contiguous()
+    E, B = int(c.shape[0]), int(c.shape[1])
+    ws = torch.empty(max(1, lib.tm_pattern_workspace_bytes(E, B, n_points)), dtype=torch.uint8, device=dev)
+    row_ptr = torch.empty(n_points + 1, dtype=torch.int64, device=dev)
+    nnz = C.c_int64(0)
+    st = _lib.stream_handle(dev)
+    _lib.check(lib.tm_pattern_count(_lib.ptr(c), E, B, n_points, _lib.ptr(ws), _lib.ptr(row_ptr), C.byref(nnz), st),
+               "tm_pattern_count")
+    edges = torch.empty(2, nnz.value, dtype=torch.int32, device=dev)
+    slot = torch.empty(E * B * B, dtype=torch.int64, device=dev)
+    _lib.check(lib.tm_pattern_fill(_lib.ptr(c), E, B, n_points, _lib.ptr(ws), _lib.ptr(row_ptr), _lib.ptr(edges[0]),
+                                   _lib.ptr(edges[1]), _lib.ptr(slot), st), "tm_pattern_fill")
+    return edges, slot, row_ptr
+
+
 class HostPlan:
     """Arrays of one ``tm_plan_build`` call, as numpy arrays."""
 
@@ -253,10 +276,20 @@ class Topology:
         self._row_ptr: Dict[torch.device, torch.Tensor] = {}
         if matrix:
             ch = chunk_elems(etype, False, quadrature_order)
-            host = HostPlan(conn_np, self.n_points, _lib.TM_PLAN_KIND_MATRIX, ch, self.perm)
-            self.edges = torch.from_numpy(np.stack([host.arrays["edge_row"], host.arrays["edge_col"]]))
-            self.slot = torch.from_numpy(host.arrays["slot"])
-            self.nnz = int(host.nnz)
+            if conn.is_cuda and self.n_elements > 0:
+                # pattern and slot map built on the GPU (tm_pattern_*); the
+                # chunk plan follows on the host from that slot map
+                edges, slot, row_ptr = device_pattern(conn, self.n_points)
+                self._row_ptr[conn.device] = row_ptr
+                self.edges, self.slot = edges.cpu(), slot.cpu()
+                host = HostPlan(conn_np, self.n_points, _lib.TM_PLAN_KIND_MATRIX, ch, self.perm,
+                                slot_map=self.slot.numpy())
+                self.nnz = int(self.edges.shape[1])
+            else:
+                host = HostPlan(conn_np, self.n_points, _lib.TM_PLAN_KIND_MATRIX, ch, self.perm)
+                self.edges = torch.from_numpy(np.stack([host.arrays["edge_row"], host.arrays["edge_col"]]))
+                self.slot = torch.from_numpy(host.arrays["slot"])
+                self.nnz = int(host.nnz)
             self._pending = {("matrix", ch): host}
         else:
             self.nnz = 0
