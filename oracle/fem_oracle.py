@@ -639,3 +639,72 @@ def reference_call_elasticity(points, conn, E, slot, edges, nu=0.3, etype="tetra
         c = (edges[1][:, None].repeat(1, D * D) * D + j.flatten()).flatten()
         h = layout_hash(r, c)
     return K, h
+
+
+# ---------------------------------------------------------------------------
+# The reference's per-mesh solve path, restated on any device: from_mesh's
+# SciPy pattern and slot map (element_assembler.py:811-851), the diffusion
+# and load assembly op sequences (element_assembler.py:390-445,
+# node_assembler.py:242-409), the Condenser's layout and gathers
+# (operator/condense.py:182-296) and the in-tree conjugate gradient cg_py
+# (sparse/solve/torch_solve.py:70-127: torch CSR product, one host check of
+# sqrt(r.r) < atol per iteration).  The per-mesh baseline of the batched
+# benchmark.
+# ---------------------------------------------------------------------------
+def reference_cg(values, row, col, n, b, atol, max_iter=100000):
+    """cg_py: CG on the CSR operator, stopping when ||r|| < atol."""
+    A = torch.sparse_coo_tensor(torch.stack([row.long(), col.long()]), values, (n, n)).coalesce()
+    A = A.to_sparse_csr()
+    x = torch.zeros_like(b)
+    r = b - A @ x
+    p = r.clone()
+    rs_old = torch.dot(r, r)
+    it = 0
+    for it in range(max_iter):
+        Ap = A @ p
+        alpha = rs_old / torch.dot(p, Ap)
+        x = x + alpha * p
+        r = r - alpha * Ap
+        rs_new = torch.dot(r, r)
+        if torch.sqrt(rs_new) < atol:
+            break
+        p = r + (rs_new / rs_old) * p
+        rs_old = rs_new
+    return x, it + 1
+
+
+def reference_per_mesh_solve(points, conn, boundary, kappa, f, etype="triangle", qorder=2, rel=1e-10):
+    """One mesh through the reference's path on the device of ``points``:
+    pattern and slot map on the host, K(kappa) and b = int f v assembled by
+    the reference's op sequence, the Dirichlet rows condensed (zero boundary
+    values), CG to ||r|| < rel ||b_i||.  Returns (u [N], iterations)."""
+    dev = points.device
+    n = points.shape[0]
+    edges, slot = element_pattern(conn, n)
+    edges, slot = edges.to(dev), slot.to(dev)
+    w, phi, dphi = (t.to(dev) for t in shape_tables(etype, qorder))
+    X = points[conn]
+    J = torch.einsum("ebj,qib->eqij", X, dphi)
+    grad = torch.einsum("qib,eqji->eqbj", dphi, torch.inverse(J))
+    jxw = torch.einsum("q,eq->eq", w, torch.linalg.det(J).abs())
+    Ke = torch.einsum("eqij,eq->eij", kappa[:, None, None, None] * torch.einsum("eqid,eqjd->eqij", grad, grad), jxw)
+    K = torch.zeros(edges.shape[1], dtype=points.dtype, device=dev).index_add_(0, slot, Ke.reshape(-1))
+    fq = torch.einsum("eb,qb->eq", f[conn], phi)
+    be = torch.einsum("eq,qb,eq->eb", fq, phi, jxw)
+    b = torch.zeros(n, dtype=points.dtype, device=dev).index_add_(0, conn.reshape(-1), be.reshape(-1))
+    # Condenser: inner/outer masks over the pattern, local numbering
+    row, col = edges[0].long(), edges[1].long()
+    inner = ~boundary
+    ie = inner[row] & inner[col]
+    oe = inner[row] & boundary[col]
+    loc = torch.full((n,), -1, dtype=torch.long, device=dev)
+    ni, no = int(inner.sum()), int(boundary.sum())
+    loc[inner] = torch.arange(ni, device=dev)
+    loc[boundary] = torch.arange(no, device=dev)
+    uo = torch.zeros(no, dtype=points.dtype, device=dev)
+    Kio = torch.sparse_coo_tensor(torch.stack([loc[row[oe]], loc[col[oe]]]), K[oe], (ni, no))
+    bi = b[inner] - Kio @ uo
+    ui, iters = reference_cg(K[ie], loc[row[ie]], loc[col[ie]], ni, bi, rel * float(bi.norm()))
+    u = torch.zeros(n, dtype=points.dtype, device=dev)
+    u[inner] = ui
+    return u, iters

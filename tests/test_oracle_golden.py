@@ -138,3 +138,20 @@ def test_oracle_full_poisson_tri_256():
     err = float((u - wl.data["exact"]).norm() / wl.data["exact"].norm())
     assert abs(err - ref["l2_rel_error"]) <= 1e-9 * ref["l2_rel_error"]
     assert abs(err - 3.793522e-05) < 1e-11
+
+
+def test_reference_per_mesh_path_solves_the_system():
+    """The restated per-mesh path (pattern, assembly, Condenser, cg_py)
+    reaches the direct solution of the oracle's condensed system."""
+    import warnings
+    from tensormesh_gb300 import workloads as W
+    warnings.filterwarnings("ignore", category=UserWarning)
+    w = W.batched_poisson_tri(2)[0]
+    m = w.mesh
+    u, it = O.reference_per_mesh_solve(m.points, m.elements(), m.boundary_mask, w.data["kappa"], w.data["f"])
+    edges, _, K = O.assemble_matrix(m.points, m.elements(), m.n_points,
+                                    lambda p, c, kappa: O.element_locals_diffusion(p, c, "triangle", kappa, 2),
+                                    kappa=w.data["kappa"])
+    b = O.assemble_load(m.points, m.elements(), "triangle", m.n_points, f_nodes=w.data["f"])
+    ud = O.solve_dirichlet(K, edges[0], edges[1], m.n_points, m.boundary_mask, b)
+    assert it > 1 and float((u - ud).norm() / ud.norm()) < 1e-8
