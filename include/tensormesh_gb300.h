@@ -207,6 +207,60 @@ int tm_pattern_fill(const int32_t* conn, int64_t n_elements, int32_t n_basis, in
                     int64_t* slot, tm_stream_t stream);
 
 /*
+ * Device-side processing order and chunk plans: the GPU counterparts of
+ * tm_morton_order and tm_plan_build, producing the same arrays from a
+ * connectivity already on the device (no counterpart in the reference, whose
+ * from_mesh builds no such plan; they complete the device-side from_mesh).
+ *
+ * tm_morton_order_device: perm (device int32 [n_elements]) = the elements by
+ * increasing Morton code of their vertices' centroid over the bounding box of
+ * their group, ties by element index, groups in sequence (groups: device int64
+ * [n_groups+1] element offsets, or NULL for one group).  points: device
+ * float64 [n_points*dim]; conn: device int32 [n_elements*n_basis]; workspace:
+ * tm_morton_workspace_bytes(n_elements, dim, n_groups) bytes.  The order is
+ * the host function's.
+ *
+ * tm_chunk_plan_device: the plan of tm_plan_build (kind TM_PLAN_KIND_MATRIX
+ * with the device slot map of tm_pattern_fill and its nnz, or
+ * TM_PLAN_KIND_NODE), from device conn (int32, element order) and perm.
+ * Outputs go to the caller's device arrays of tm_device_chunk_plan, sized at
+ * least: conn [n_elements*n_basis], chunk_begin and chunk_contrib
+ * [n_chunks+1], slot_ptr [cap_slots+1], contrib [cap_contrib],
+ * slot_target and slot_mirror [cap_slots], shared_ptr [cap_shared+1],
+ * shared_target and shared_mirror [cap_shared] (enough: cap_slots =
+ * n_elements*n_local, cap_contrib = twice that for matrix plans (n_local for
+ * node plans), cap_shared = the number of targets).  The call synchronises
+ * its stream and writes the sizes into the struct.  chunk_elems at most
+ * 1024; a chunk with more than 8192 contributions or a capacity exceeded
+ * gives TM_ERR_TOO_LARGE (tm_plan_build on the host has no such limits).
+ */
+typedef struct tm_device_chunk_plan {
+    int32_t* conn;
+    int32_t* chunk_begin;
+    int32_t* chunk_contrib;
+    int32_t* slot_ptr;
+    uint16_t* contrib;
+    int32_t* slot_target;
+    int32_t* slot_mirror;
+    int32_t* shared_ptr;
+    int32_t* shared_target;
+    int32_t* shared_mirror;
+    int64_t cap_slots, cap_contrib, cap_shared;
+    /* written by the call */
+    int64_t n_chunks, n_slots, n_contrib, n_shared, n_partials;
+    int32_t max_chunk_slots, max_chunk_contrib;
+} tm_device_chunk_plan;
+size_t tm_morton_workspace_bytes(int64_t n_elements, int32_t dim, int32_t n_groups);
+int tm_morton_order_device(const double* points, int64_t n_points, int32_t dim, const int32_t* conn,
+                           int64_t n_elements, int32_t n_basis, const int64_t* groups, int32_t n_groups,
+                           void* workspace, int32_t* perm, tm_stream_t stream);
+size_t tm_chunk_plan_device_workspace_bytes(int64_t n_elements, int32_t n_basis, int64_t n_targets,
+                                            int32_t kind, int32_t chunk_elems);
+int tm_chunk_plan_device(const int32_t* conn, int64_t n_elements, int32_t n_basis, int64_t n_points,
+                         int32_t kind, int32_t chunk_elems, const int32_t* perm, const int64_t* slot,
+                         int64_t nnz, void* workspace, tm_device_chunk_plan* out, tm_stream_t stream);
+
+/*
  * Float64 P1 diffusion / mass locals and their reduction are computed in
  * double-float arithmetic (hi + lo pairs of floats, ~48 bits, relative
  * error ~1e-14) on the FP32 pipes; chunks whose data fall outside the

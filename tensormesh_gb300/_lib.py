@@ -48,6 +48,18 @@ class ChunkPlan(C.Structure):
     ]
 
 
+class DeviceChunkPlan(C.Structure):
+    _fields_ = [
+        ("conn", C.c_void_p), ("chunk_begin", C.c_void_p), ("chunk_contrib", C.c_void_p),
+        ("slot_ptr", C.c_void_p), ("contrib", C.c_void_p), ("slot_target", C.c_void_p),
+        ("slot_mirror", C.c_void_p), ("shared_ptr", C.c_void_p), ("shared_target", C.c_void_p),
+        ("shared_mirror", C.c_void_p), ("cap_slots", C.c_int64), ("cap_contrib", C.c_int64),
+        ("cap_shared", C.c_int64), ("n_chunks", C.c_int64), ("n_slots", C.c_int64), ("n_contrib", C.c_int64),
+        ("n_shared", C.c_int64), ("n_partials", C.c_int64), ("max_chunk_slots", C.c_int32),
+        ("max_chunk_contrib", C.c_int32),
+    ]
+
+
 class MatrixArgs(C.Structure):
     _fields_ = [
         ("dtype", C.c_int32), ("forms", C.c_int32), ("n_points", C.c_int64),
@@ -156,6 +168,13 @@ _SIGNATURES = {
                                        C.c_void_p, C.c_void_p]),
     "tm_morton_order": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]),
     "tm_pattern_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32, C.c_int64]),
+    "tm_morton_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32, C.c_int32]),
+    "tm_morton_order_device": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32,
+                                         C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "tm_chunk_plan_device_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32]),
+    "tm_chunk_plan_device": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32,
+                                       C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                       C.POINTER(DeviceChunkPlan), C.c_void_p]),
     "tm_pattern_count": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p,
                                    C.POINTER(C.c_int64), C.c_void_p]),
     "tm_pattern_fill": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p,
@@ -212,7 +231,9 @@ def check(status: int, what: str = "") -> None:
         lib = load()
         msg = lib.tm_last_error_message().decode(errors="replace")
         kind = lib.tm_error_string(status).decode(errors="replace")
-        raise TmError(f"{what}: {kind}: {msg}" if what else f"{kind}: {msg}")
+        err = TmError(f"{what}: {kind}: {msg}" if what else f"{kind}: {msg}")
+        err.status = status
+        raise err
 
 
 def ptr(t) -> int:

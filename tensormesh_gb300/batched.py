@@ -58,9 +58,12 @@ class BatchedDiffusion:
         self.elem_offset = np.zeros(self.n_systems + 1, dtype=np.int64)
         np.cumsum([m.n_points for m in meshes], out=self.node_offset[1:])
         np.cumsum([m.n_elements for m in meshes], out=self.elem_offset[1:])
-        pts = torch.cat([m.points.detach().cpu().to(dtype) for m in meshes])
-        conn = torch.cat([m.elements().cpu().long() + int(self.node_offset[i]) for i, m in enumerate(meshes)])
-        bnd = torch.cat([m.boundary_mask.cpu().bool() for m in meshes])
+        # concatenated where the meshes live (on the GPU the order, pattern
+        # and plans are then built there too)
+        src = meshes[0].device
+        pts = torch.cat([m.points.detach().to(src, dtype) for m in meshes])
+        conn = torch.cat([m.elements().to(src).long() + int(self.node_offset[i]) for i, m in enumerate(meshes)])
+        bnd = torch.cat([m.boundary_mask.to(src).bool() for m in meshes])
         # one element group per mesh: the meshes overlap in space, and one
         # order over all of them would mix meshes in every chunk
         self.mesh = Mesh(pts, {etype: conn}, {"is_boundary": bnd}, element_groups=self.elem_offset).to(dev)
@@ -71,7 +74,7 @@ class BatchedDiffusion:
         # the solver's queue takes the largest systems first
         sizes = np.diff(self.node_offset)
         self.order = torch.from_numpy(np.argsort(-sizes, kind="stable").astype(np.int32)).to(dev)
-        self.dirichlet = bnd.to(torch.uint8).to(dev)
+        self.dirichlet = bnd.to(dev).to(torch.uint8)
         self._graph = None
         if autotune:
             from . import autotune as tuner
@@ -83,6 +86,9 @@ class BatchedDiffusion:
         topo = self.K_asm._topo(True)
         self.chunks = {"matrix": topo.chunk_for("scalar", dev, dtype),
                        "node": self.b_asm._topo(False).chunk_for("node", dev, dtype)}
+        # the plans of those chunk sizes, built now (on the GPU for device meshes)
+        topo.matrix_plan(dev, dtype=dtype)
+        self.b_asm._topo(False).node_plan(dev, dtype=dtype)
 
     @property
     def n_points(self) -> int:

@@ -1,134 +1,177 @@
-// Paired double-float arithmetic: two independent double-float numbers per
-// thread, one in each lane of a float2, computed with the paired FP32
-// instructions of sm_100 and later (__fadd2_rn, __fmul2_rn, __ffma2_rn: one
-// issued instruction performs the operation on both lanes).  The error-free
-// transformations are those of tm_df64.cuh (Knuth's TwoSum, Dekker's
-// Fast2Sum, the FMA form of TwoProduct); every step is an explicit
-// round-to-nearest paired intrinsic, which the compiler does not contract.
+// Double-float arithmetic on one or two lanes: a value is an unevaluated sum
+// hi + lo of two floats (about 48 significant bits), and a "lane" type L is
+// either float (one number) or float2 (two independent numbers, one per
+// lane, computed with the paired FP32 instructions of sm_100 and later:
+// __fadd2_rn, __fmul2_rn, __ffma2_rn perform the operation on both lanes in
+// one issued instruction).  The error-free transformations are the
+// classical ones (Knuth's TwoSum, Dekker's Fast2Sum, the FMA form of
+// TwoProduct; Dekker 1971, Knuth TAOCP vol. 2 4.2.2, the double-float
+// formulation of Hida, Li & Bailey's QD library); every step is an explicit
+// round-to-nearest intrinsic, which the compiler does not contract.
 //
-// The P1 assembly kernels carry two elements per thread through these
-// operations (lane x: one element, lane y: the other) and accumulate a
-// target's stiffness and mass sums in the two lanes of one pair, so that the
-// double-float work, which bounds those kernels, issues half the
-// instructions.
+// The P1 assembly kernels use float2 lanes to carry two elements per
+// thread, or float lanes for one element per thread, and float2 lanes to
+// accumulate a target's stiffness and mass sums side by side.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace tmk {
 
-__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 p_neg(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return __fadd2_rn(a, p_neg(b)); }
-__device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 p_set(float v) { return make_float2(v, v); }
+// ------------------------------------------------------------ lane primitives
+__device__ __forceinline__ float l_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float l_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float l_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float l_neg(float a) { return -a; }
+__device__ __forceinline__ float2 l_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 l_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 l_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 l_neg(float2 a) { return make_float2(-a.x, -a.y); }
+template <class L>
+__device__ __forceinline__ L l_sub(L a, L b) { return l_add(a, l_neg(b)); }
 
-// two double-float numbers: (hi.x + lo.x, hi.y + lo.y)
-struct pf2 {
-    float2 hi, lo;
-};
+template <class L> __device__ __forceinline__ L l_set(float v);
+template <> __device__ __forceinline__ float l_set<float>(float v) { return v; }
+template <> __device__ __forceinline__ float2 l_set<float2>(float v) { return make_float2(v, v); }
 
-// s + e == a + b exactly, lane by lane (Knuth)
-__device__ __forceinline__ pf2 p_two_sum(float2 a, float2 b) {
-    const float2 s = p_add(a, b);
-    const float2 bb = p_sub(s, a);
-    const float2 e = p_add(p_sub(a, p_sub(s, bb)), p_sub(b, bb));
-    return {s, e};
+// lane access (k a compile-time constant after unrolling)
+__device__ __forceinline__ float l_get(float v, int) { return v; }
+__device__ __forceinline__ float l_get(float2 v, int k) { return k ? v.y : v.x; }
+__device__ __forceinline__ void l_put(float& v, int, float x) { v = x; }
+__device__ __forceinline__ void l_put(float2& v, int k, float x) {
+    if (k)
+        v.y = x;
+    else
+        v.x = x;
 }
 
-// s + e == a + b exactly when |a| >= |b| in each lane (Dekker)
-__device__ __forceinline__ pf2 p_fast_two_sum(float2 a, float2 b) {
-    const float2 s = p_add(a, b);
-    const float2 e = p_sub(b, p_sub(s, a));
-    return {s, e};
-}
-
-__device__ __forceinline__ pf2 p_neg(pf2 a) { return {p_neg(a.hi), p_neg(a.lo)}; }
-
-__device__ __forceinline__ pf2 p_add(pf2 a, pf2 b) {
-    const pf2 s = p_two_sum(a.hi, b.hi);
-    const float2 e = p_add(s.lo, p_add(a.lo, b.lo));
-    return p_fast_two_sum(s.hi, e);
-}
-
-__device__ __forceinline__ pf2 p_mul(pf2 a, pf2 b) {
-    const float2 p = p_mul(a.hi, b.hi);
-    float2 e = p_fma(a.hi, b.hi, p_neg(p));
-    e = p_fma(a.hi, b.lo, e);
-    e = p_fma(a.lo, b.hi, e);
-    return p_fast_two_sum(p, e);
-}
-
-// a * b - c * d with one normalisation
-__device__ __forceinline__ pf2 p_diff_of_products(pf2 a, pf2 b, pf2 c, pf2 d) {
-    const float2 p = p_mul(a.hi, b.hi);
-    const float2 pe = p_fma(a.hi, b.hi, p_neg(p));
-    const float2 q = p_mul(c.hi, d.hi);
-    const float2 qe = p_fma(c.hi, d.hi, p_neg(q));
-    const pf2 s = p_two_sum(p, p_neg(q));
-    float2 e = p_add(s.lo, p_sub(pe, qe));
-    e = p_fma(a.hi, b.lo, e);
-    e = p_fma(a.lo, b.hi, e);
-    e = p_fma(p_neg(c.hi), d.lo, e);
-    e = p_fma(p_neg(c.lo), d.hi, e);
-    return p_fast_two_sum(s.hi, e);
-}
-
-// a0 b0 + a1 b1 + a2 b2 with one normalisation
-__device__ __forceinline__ pf2 p_dot3(const pf2* a, const pf2* b) {
-    const float2 p0 = p_mul(a[0].hi, b[0].hi), p1 = p_mul(a[1].hi, b[1].hi), p2 = p_mul(a[2].hi, b[2].hi);
-    const float2 e0 = p_fma(a[0].hi, b[0].hi, p_neg(p0));
-    const float2 e1 = p_fma(a[1].hi, b[1].hi, p_neg(p1));
-    const float2 e2 = p_fma(a[2].hi, b[2].hi, p_neg(p2));
-    const pf2 s01 = p_two_sum(p0, p1);
-    const pf2 s = p_two_sum(s01.hi, p2);
-    float2 e = p_add(p_add(s01.lo, s.lo), p_add(p_add(e0, e1), e2));
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        e = p_fma(a[k].hi, b[k].lo, e);
-        e = p_fma(a[k].lo, b[k].hi, e);
-    }
-    return p_fast_two_sum(s.hi, e);
-}
-
-// a0 b0 + a1 b1 with one normalisation
-__device__ __forceinline__ pf2 p_dot2(const pf2* a, const pf2* b) {
-    const float2 p0 = p_mul(a[0].hi, b[0].hi), p1 = p_mul(a[1].hi, b[1].hi);
-    const float2 e0 = p_fma(a[0].hi, b[0].hi, p_neg(p0));
-    const float2 e1 = p_fma(a[1].hi, b[1].hi, p_neg(p1));
-    const pf2 s = p_two_sum(p0, p1);
-    float2 e = p_add(s.lo, p_add(e0, e1));
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        e = p_fma(a[k].hi, b[k].lo, e);
-        e = p_fma(a[k].lo, b[k].hi, e);
-    }
-    return p_fast_two_sum(s.hi, e);
-}
-
-// 1 / a for a.hi > 0 normal: the hardware approximation of 1 / a.hi
-// (rcp.approx, relative error below 2^-22), one Newton step in float that
-// brings it to about 2^-24, and one in double-float, r + r (1 - a r): the
-// relative error of the result is about 2^-47
+// hardware approximation of 1 / x (rcp.approx, relative error below 2^-22)
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
-__device__ __forceinline__ pf2 p_recip(pf2 a) {
-    float2 r = make_float2(rcp_approx(a.hi.x), rcp_approx(a.hi.y));
-    float2 e = p_fma(p_neg(a.hi), r, p_set(1.0f));
-    r = p_fma(r, e, r);
-    e = p_fma(p_neg(a.hi), r, p_set(1.0f));       // 1 - a.hi r: exact up to the FMA's rounding of a tiny value
-    e = p_fma(p_neg(a.lo), r, e);
-    return p_fast_two_sum(r, p_mul(r, e));
+__device__ __forceinline__ float l_rcp(float x) { return rcp_approx(x); }
+__device__ __forceinline__ float2 l_rcp(float2 x) { return make_float2(rcp_approx(x.x), rcp_approx(x.y)); }
+
+// v with the sign flipped where s is negative
+__device__ __forceinline__ float l_abs_sel(float v, float s) { return s < 0.0f ? -v : v; }
+__device__ __forceinline__ float2 l_abs_sel(float2 v, float2 s) {
+    return make_float2(s.x < 0.0f ? -v.x : v.x, s.y < 0.0f ? -v.y : v.y);
 }
 
-__device__ __forceinline__ pf2 p_abs(pf2 a) {
-    const bool nx = a.hi.x < 0.0f, ny = a.hi.y < 0.0f;
-    return {make_float2(nx ? -a.hi.x : a.hi.x, ny ? -a.hi.y : a.hi.y),
-            make_float2(nx ? -a.lo.x : a.lo.x, ny ? -a.lo.y : a.lo.y)};
+// ------------------------------------------------------------ double-float
+template <class L>
+struct ddv {
+    L hi, lo;
+};
+using pf2 = ddv<float2>;
+
+// s + e == a + b exactly, lane by lane (Knuth)
+template <class L>
+__device__ __forceinline__ ddv<L> p_two_sum(L a, L b) {
+    const L s = l_add(a, b);
+    const L bb = l_sub(s, a);
+    const L e = l_add(l_sub(a, l_sub(s, bb)), l_sub(b, bb));
+    return {s, e};
+}
+
+// s + e == a + b exactly when |a| >= |b| in each lane (Dekker)
+template <class L>
+__device__ __forceinline__ ddv<L> p_fast_two_sum(L a, L b) {
+    const L s = l_add(a, b);
+    const L e = l_sub(b, l_sub(s, a));
+    return {s, e};
+}
+
+template <class L>
+__device__ __forceinline__ ddv<L> p_neg(ddv<L> a) { return {l_neg(a.hi), l_neg(a.lo)}; }
+
+template <class L>
+__device__ __forceinline__ ddv<L> p_const(float hi, float lo) { return {l_set<L>(hi), l_set<L>(lo)}; }
+
+template <class L>
+__device__ __forceinline__ ddv<L> p_add(ddv<L> a, ddv<L> b) {
+    const ddv<L> s = p_two_sum(a.hi, b.hi);
+    const L e = l_add(s.lo, l_add(a.lo, b.lo));
+    return p_fast_two_sum(s.hi, e);
+}
+
+template <class L>
+__device__ __forceinline__ ddv<L> p_mul(ddv<L> a, ddv<L> b) {
+    const L p = l_mul(a.hi, b.hi);
+    L e = l_fma(a.hi, b.hi, l_neg(p));
+    e = l_fma(a.hi, b.lo, e);
+    e = l_fma(a.lo, b.hi, e);
+    return p_fast_two_sum(p, e);
+}
+
+// a * b - c * d with one normalisation
+template <class L>
+__device__ __forceinline__ ddv<L> p_diff_of_products(ddv<L> a, ddv<L> b, ddv<L> c, ddv<L> d) {
+    const L p = l_mul(a.hi, b.hi);
+    const L pe = l_fma(a.hi, b.hi, l_neg(p));
+    const L q = l_mul(c.hi, d.hi);
+    const L qe = l_fma(c.hi, d.hi, l_neg(q));
+    const ddv<L> s = p_two_sum(p, l_neg(q));
+    L e = l_add(s.lo, l_sub(pe, qe));
+    e = l_fma(a.hi, b.lo, e);
+    e = l_fma(a.lo, b.hi, e);
+    e = l_fma(l_neg(c.hi), d.lo, e);
+    e = l_fma(l_neg(c.lo), d.hi, e);
+    return p_fast_two_sum(s.hi, e);
+}
+
+// a0 b0 + a1 b1 + a2 b2 with one normalisation
+template <class L>
+__device__ __forceinline__ ddv<L> p_dot3(const ddv<L>* a, const ddv<L>* b) {
+    const L p0 = l_mul(a[0].hi, b[0].hi), p1 = l_mul(a[1].hi, b[1].hi), p2 = l_mul(a[2].hi, b[2].hi);
+    const L e0 = l_fma(a[0].hi, b[0].hi, l_neg(p0));
+    const L e1 = l_fma(a[1].hi, b[1].hi, l_neg(p1));
+    const L e2 = l_fma(a[2].hi, b[2].hi, l_neg(p2));
+    const ddv<L> s01 = p_two_sum(p0, p1);
+    const ddv<L> s = p_two_sum(s01.hi, p2);
+    L e = l_add(l_add(s01.lo, s.lo), l_add(l_add(e0, e1), e2));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        e = l_fma(a[k].hi, b[k].lo, e);
+        e = l_fma(a[k].lo, b[k].hi, e);
+    }
+    return p_fast_two_sum(s.hi, e);
+}
+
+// a0 b0 + a1 b1 with one normalisation
+template <class L>
+__device__ __forceinline__ ddv<L> p_dot2(const ddv<L>* a, const ddv<L>* b) {
+    const L p0 = l_mul(a[0].hi, b[0].hi), p1 = l_mul(a[1].hi, b[1].hi);
+    const L e0 = l_fma(a[0].hi, b[0].hi, l_neg(p0));
+    const L e1 = l_fma(a[1].hi, b[1].hi, l_neg(p1));
+    const ddv<L> s = p_two_sum(p0, p1);
+    L e = l_add(s.lo, l_add(e0, e1));
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        e = l_fma(a[k].hi, b[k].lo, e);
+        e = l_fma(a[k].lo, b[k].hi, e);
+    }
+    return p_fast_two_sum(s.hi, e);
+}
+
+// 1 / a for a.hi > 0 normal: the hardware approximation, one Newton step in
+// float (relative error about 2^-24), one in double-float, r + r (1 - a r):
+// relative error of the result about 2^-47
+template <class L>
+__device__ __forceinline__ ddv<L> p_recip(ddv<L> a) {
+    L r = l_rcp(a.hi);
+    L e = l_fma(l_neg(a.hi), r, l_set<L>(1.0f));
+    r = l_fma(r, e, r);
+    e = l_fma(l_neg(a.hi), r, l_set<L>(1.0f));
+    e = l_fma(l_neg(a.lo), r, e);
+    return p_fast_two_sum(r, l_mul(r, e));
+}
+
+template <class L>
+__device__ __forceinline__ ddv<L> p_abs(ddv<L> a) {
+    return {l_abs_sel(a.hi, a.hi), l_abs_sel(a.lo, a.hi)};
 }
 
 // ------------------------------------------------------------ conversions

@@ -15,15 +15,18 @@
 // relative, in double-float arithmetic on the FP32 pipes (FP64 runs at 1/62
 // of the FP32 rate on GB300).
 //
-// One CTA of kNT threads per chunk of the plan (Morton-ordered elements):
+// One CTA per chunk of the plan (Morton-ordered elements):
 //  * phase 0: one thread issues the bulk copies of the chunk's slot_ptr and
 //    contrib windows into shared memory (they land during phase 1);
-//  * phase 1: each thread takes two elements (e and e + kNT) through paired
-//    double-float instructions (one lane per element): the coordinate
+//  * phase 1: each thread takes NE elements (NE = 2: elements e and e + NT
+//    through paired double-float instructions, one lane per element, at most
+//    384 threads; NE = 1: one element per thread, at most 768 threads and
+//    about half the registers, so twice the resident warps): the coordinate
 //    differences (one FP64 subtraction each, then split on the integer
 //    pipe), cofactors, determinant, the Gram entries C_a . C_b, the scale
 //    kappa W / |det| and the scaled locals K_e[a][b] (upper triangle), and
-//    |det| rho; both go to shared memory as hi/lo float pairs;
+//    |det| rho; both go to shared memory as hi/lo float pairs, one record of
+//    NL + 1 pairs per element;
 //  * phase 2: one thread per target (CSR position) of the chunk, targets
 //    ordered by contribution count so that a warp's loops are equally long,
 //    sums its contributions in element order: the stiffness sum in lane x and
@@ -40,19 +43,24 @@
 // is not two-valued to 1e-14) runs the whole chunk in FP64 arithmetic instead
 // (tm_matrix_args.stats counts those chunks).
 #pragma once
+#include <algorithm>
+
 #include "tm_df2.cuh"
 
 namespace tmk {
 
-constexpr int kP1NT = 384;   // threads of a k_p1df CTA (two elements each per pass)
+// most threads of a k_p1df CTA for NE elements per thread
+template <int NE>
+__host__ __device__ constexpr int p1_threads() { return NE == 2 ? 384 : 768; }
 
 struct P1Layout {
-    size_t bar, sp, ct, lk, lm, total;
+    size_t bar, sp, ct, rec, total;
 };
 
-// LK: the chunk's scaled locals (upper triangle, element-major), LM: |det|
-// rho per element; both 8 bytes per value (a hi/lo float pair, or a double
-// on the FP64 path)
+// REC: per element a record of NL + 1 values of 8 bytes (a hi/lo float
+// pair, or a double on the FP64 path): the scaled locals (upper triangle)
+// and |det| rho.  The odd record stride (88 bytes for a tetrahedron) spreads
+// a warp's stores over the banks.
 template <int ET>
 __host__ __device__ inline P1Layout p1_layout(int CH, int MS, int MC) {
     constexpr int B = Traits<ET>::B, NL = B * (B + 1) / 2;
@@ -65,10 +73,8 @@ __host__ __device__ inline P1Layout p1_layout(int CH, int MS, int MC) {
     L.ct = o;
     o += stage_capacity(MC, 2);
     o = align16(o);
-    L.lk = o;
-    o = align16(o + 8 * (size_t)CH * NL);
-    L.lm = o;
-    o = align16(o + 8 * (size_t)CH);
+    L.rec = o;
+    o = align16(o + 8 * (size_t)CH * (NL + 1));
     L.total = o;
     return L;
 }
@@ -78,10 +84,13 @@ __device__ __forceinline__ uint32_t exp_field(double x) {
     return ((uint32_t)__double2hiint(x) >> 20) & 0x7FFu;
 }
 
-template <int ET, int FORMS>
-__global__ void __launch_bounds__(kP1NT, 2) k_p1df(const tm_matrix_args a) {
+template <int ET, int FORMS, int NE>
+__global__ void __launch_bounds__(p1_threads<NE>(), 2) k_p1df(const tm_matrix_args a) {
     using T = Traits<ET>;
-    constexpr int D = T::D, B = T::B, NL = B * (B + 1) / 2;
+    using Ln = typename std::conditional<NE == 2, float2, float>::type;   // lane type
+    using V = ddv<Ln>;
+    constexpr int D = T::D, B = T::B, NL = B * (B + 1) / 2, NR = NL + 1;
+    const int NT = blockDim.x;
     constexpr bool DIFF = (FORMS & TM_FORM_DIFFUSION) != 0;
     constexpr bool MASS = (FORMS & TM_FORM_MASS) != 0;
     const tm_chunk_plan& P = a.plan;
@@ -106,10 +115,8 @@ __global__ void __launch_bounds__(kP1NT, 2) k_p1df(const tm_matrix_args a) {
     }
     const int32_t* SP = reinterpret_cast<const int32_t*>(sm + L.sp) + w_sp.skip;   // slot_ptr[s0 + j]
     const uint16_t* CT = reinterpret_cast<const uint16_t*>(sm + L.ct) + w_ct.skip;  // contrib[c0 + q]
-    float2* LK = reinterpret_cast<float2*>(sm + L.lk);
-    float2* LM = reinterpret_cast<float2*>(sm + L.lm);
-    double* LKd = reinterpret_cast<double*>(sm + L.lk);
-    double* LMd = reinterpret_cast<double*>(sm + L.lm);
+    float2* REC = reinterpret_cast<float2*>(sm + L.rec);
+    double* RECd = reinterpret_cast<double*>(sm + L.rec);
 
     // per-CTA constants: the mass template's two class values (diagonal and
     // off-diagonal entries) and whether the template has that structure
@@ -152,53 +159,63 @@ __global__ void __launch_bounds__(kP1NT, 2) k_p1df(const tm_matrix_args a) {
     split_to_pair(pk[TL.wsum], ws_h, ws_l);
 
     // ---------------------------------------------------------------- phase 1
-    for (int base = 0; base < ne; base += 2 * kP1NT) {
-        const int ea = base + threadIdx.x, eb = ea + kP1NT;
-        if (ea >= ne) break;
-        const bool has_b = eb < ne;
-        const int64_t ia = i0 + ea, ib = i0 + (has_b ? eb : ea);
-        int na[B], nb[B];
+    for (int base = 0; base < ne; base += NE * NT) {
+        int el[NE];
+        bool has[NE];
+#pragma unroll
+        for (int k = 0; k < NE; ++k) {
+            el[k] = base + threadIdx.x + k * NT;
+            has[k] = el[k] < ne;
+        }
+        if (!has[0]) break;
+#pragma unroll
+        for (int k = 1; k < NE; ++k)
+            if (!has[k]) el[k] = el[0];              // a copy of element 0 fills the lane, unstored
+        int nd[NE][B];
         if constexpr (B == 4) {
-            const int4 ca = __ldcs(reinterpret_cast<const int4*>(P.conn) + ia);
-            const int4 cb = __ldcs(reinterpret_cast<const int4*>(P.conn) + ib);
-            na[0] = ca.x, na[1] = ca.y, na[2] = ca.z, na[3] = ca.w;
-            nb[0] = cb.x, nb[1] = cb.y, nb[2] = cb.z, nb[3] = cb.w;
+#pragma unroll
+            for (int k = 0; k < NE; ++k) {
+                const int4 c = __ldcs(reinterpret_cast<const int4*>(P.conn) + i0 + el[k]);
+                nd[k][0] = c.x, nd[k][1] = c.y, nd[k][2] = c.z, nd[k][3] = c.w;
+            }
         } else {
 #pragma unroll
-            for (int k = 0; k < B; ++k) {
-                na[k] = __ldcs(P.conn + ia * B + k);
-                nb[k] = __ldcs(P.conn + ib * B + k);
-            }
-        }
-        double kva = 1.0, kvb = 1.0;
-        if (DIFF && kap) {
-            kva = __ldg(kap + __ldcs(P.elem_perm + ia));
-            kvb = __ldg(kap + __ldcs(P.elem_perm + ib));
-        }
-        double Xa[B][D], Xb[B][D];
+            for (int k = 0; k < NE; ++k)
 #pragma unroll
-        for (int k = 0; k < B; ++k)
+                for (int b = 0; b < B; ++b) nd[k][b] = __ldcs(P.conn + (i0 + el[k]) * B + b);
+        }
+        double kv[NE];
 #pragma unroll
-            for (int d = 0; d < D; ++d) {
-                Xa[k][d] = __ldg(pts + (int64_t)na[k] * D + d);
-                Xb[k][d] = __ldg(pts + (int64_t)nb[k] * D + d);
-            }
+        for (int k = 0; k < NE; ++k) kv[k] = (DIFF && kap) ? __ldg(kap + __ldcs(P.elem_perm + i0 + el[k])) : 1.0;
+        double X[NE][B][D];
+#pragma unroll
+        for (int k = 0; k < NE; ++k)
+#pragma unroll
+            for (int b = 0; b < B; ++b)
+#pragma unroll
+                for (int d = 0; d < D; ++d) X[k][b][d] = __ldg(pts + (int64_t)nd[k][b] * D + d);
         // J[r][c] = x_{r+1,c} - x_{0,c}: the one FP64 step, then split
-        pf2 J[D][D];
-        uint32_t ea_max = 0, eb_max = 0;
+        V J[D][D];
+        uint32_t emax[NE];
+#pragma unroll
+        for (int k = 0; k < NE; ++k) emax[k] = 0;
 #pragma unroll
         for (int r = 0; r < D; ++r)
 #pragma unroll
-            for (int c = 0; c < D; ++c) {
-                const double da = Xa[r + 1][c] - Xa[0][c], db = Xb[r + 1][c] - Xb[0][c];
-                ea_max = max(ea_max, exp_field(da));
-                eb_max = max(eb_max, exp_field(db));
-                split_to_pair(da, J[r][c].hi.x, J[r][c].lo.x);
-                split_to_pair(db, J[r][c].hi.y, J[r][c].lo.y);
-            }
-        bad |= ea_max < 1023 - 20 || ea_max >= 1023 + 20 || eb_max < 1023 - 20 || eb_max >= 1023 + 20;
-        pf2 cof[D][D];
-        pf2 det;
+            for (int c = 0; c < D; ++c)
+#pragma unroll
+                for (int k = 0; k < NE; ++k) {
+                    const double dd = X[k][r + 1][c] - X[k][0][c];
+                    emax[k] = max(emax[k], exp_field(dd));
+                    float h, l;
+                    split_to_pair(dd, h, l);
+                    l_put(J[r][c].hi, k, h);
+                    l_put(J[r][c].lo, k, l);
+                }
+#pragma unroll
+        for (int k = 0; k < NE; ++k) bad |= emax[k] < 1023 - 20 || emax[k] >= 1023 + 20;
+        V cof[D][D];
+        V det;
         if constexpr (D == 3) {
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
@@ -215,14 +232,18 @@ __global__ void __launch_bounds__(kP1NT, 2) k_p1df(const tm_matrix_args a) {
             cof[1][1] = J[0][0];
             det = p_diff_of_products(J[0][0], J[1][1], J[0][1], J[1][0]);
         }
-        const pf2 adet = p_abs(det);
-        bad |= !f2_in_band({adet.hi.x, 0.0f}, -100, 100) || !f2_in_band({adet.hi.y, 0.0f}, -100, 100) ||
-               !(adet.hi.x > 0.0f) || !(adet.hi.y > 0.0f);
+        const V adet = p_abs(det);
+#pragma unroll
+        for (int k = 0; k < NE; ++k) {
+            const float ad = l_get(adet.hi, k);
+            bad |= !f2_in_band({ad, 0.0f}, -100, 100) || !(ad > 0.0f);
+        }
         if constexpr (DIFF) {
-            bad |= !exponent_in_band(kva, 30) || !exponent_in_band(kvb, 30);
+#pragma unroll
+            for (int k = 0; k < NE; ++k) bad |= !exponent_in_band(kv[k], 30);
             // Gram entries of the cofactor rows; C_0 = -sum_r cof_r gives
             // C_0.C_0 = sum_rc G_rc and C_0.C_{c+1} = -sum_r G_rc
-            pf2 G[D][D];
+            V G[D][D];
 #pragma unroll
             for (int r = 0; r < D; ++r)
 #pragma unroll
@@ -230,54 +251,61 @@ __global__ void __launch_bounds__(kP1NT, 2) k_p1df(const tm_matrix_args a) {
                     G[r][c] = D == 3 ? p_dot3(cof[r], cof[c]) : p_dot2(cof[r], cof[c]);
                     G[c][r] = G[r][c];
                 }
-            pf2 rs[D];
+            V rs[D];
 #pragma unroll
             for (int c = 0; c < D; ++c) {
-                pf2 acc = G[0][c];
+                V acc = G[0][c];
 #pragma unroll
                 for (int r = 1; r < D; ++r) acc = p_add(acc, G[r][c]);
                 rs[c] = acc;
             }
-            pf2 tot = rs[0];
+            V tot = rs[0];
 #pragma unroll
             for (int c = 1; c < D; ++c) tot = p_add(tot, rs[c]);
             // scale kappa * kappa_scale * W / |det|
-            pf2 kv;
-            split_to_pair(kva, kv.hi.x, kv.lo.x);
-            split_to_pair(kvb, kv.hi.y, kv.lo.y);
-            const pf2 kw = p_mul(kv, pf2{p_set(ks_h), p_set(ks_l)});
-            const pf2 sc = p_mul(kw, p_mul(pf2{p_set(ws_h), p_set(ws_l)}, p_recip(adet)));
-            // largest local: the trace-dominant entries; its exponent with
-            // the scale's must keep every product a normal float
-            float gx = fabsf(tot.hi.x), gy = fabsf(tot.hi.y);
+            V kd;
 #pragma unroll
-            for (int c = 0; c < D; ++c) {
-                gx = fmaxf(gx, fabsf(G[c][c].hi.x));
-                gy = fmaxf(gy, fabsf(G[c][c].hi.y));
+            for (int k = 0; k < NE; ++k) {
+                float h, l;
+                split_to_pair(kv[k], h, l);
+                l_put(kd.hi, k, h);
+                l_put(kd.lo, k, l);
             }
-            const int lx = (int)((__float_as_uint(gx) >> 23) & 0xFF) + (int)((__float_as_uint(sc.hi.x) >> 23) & 0xFF) - 254;
-            const int ly = (int)((__float_as_uint(gy) >> 23) & 0xFF) + (int)((__float_as_uint(sc.hi.y) >> 23) & 0xFF) - 254;
-            bad |= lx < -80 || lx >= 100 || ly < -80 || ly >= 100 || !isfinite(sc.hi.x) || !isfinite(sc.hi.y);
-            pf2 k[NL];
-            int l = 0;
-            k[l++] = p_mul(sc, tot);
+            const V sc = p_mul(p_mul(kd, p_const<Ln>(ks_h, ks_l)), p_mul(p_const<Ln>(ws_h, ws_l), p_recip(adet)));
+            // largest local: the diagonal entries; its exponent with the
+            // scale's must keep every product a normal float
 #pragma unroll
-            for (int q = 0; q < D; ++q) k[l++] = p_neg(p_mul(sc, rs[q]));
+            for (int k = 0; k < NE; ++k) {
+                float g = fabsf(l_get(tot.hi, k));
+#pragma unroll
+                for (int c = 0; c < D; ++c) g = fmaxf(g, fabsf(l_get(G[c][c].hi, k)));
+                const float sh = l_get(sc.hi, k);
+                const int le = (int)((__float_as_uint(g) >> 23) & 0xFF) + (int)((__float_as_uint(sh) >> 23) & 0xFF) - 254;
+                bad |= le < -80 || le >= 100 || !isfinite(sh);
+            }
+            V kl[NL];
+            int l = 0;
+            kl[l++] = p_mul(sc, tot);
+#pragma unroll
+            for (int q = 0; q < D; ++q) kl[l++] = p_neg(p_mul(sc, rs[q]));
 #pragma unroll
             for (int p = 0; p < D; ++p)
 #pragma unroll
-                for (int q = p; q < D; ++q) k[l++] = p_mul(sc, G[p][q]);
+                for (int q = p; q < D; ++q) kl[l++] = p_mul(sc, G[p][q]);
 #pragma unroll
-            for (int m = 0; m < NL; ++m) {
-                LK[ea * NL + m] = make_float2(k[m].hi.x, k[m].lo.x);
-                if (has_b) LK[eb * NL + m] = make_float2(k[m].hi.y, k[m].lo.y);
-            }
+            for (int k = 0; k < NE; ++k)
+                if (has[k])
+#pragma unroll
+                    for (int m = 0; m < NL; ++m)
+                        REC[el[k] * NR + m] = make_float2(l_get(kl[m].hi, k), l_get(kl[m].lo, k));
         }
         if constexpr (MASS) {
-            const pf2 v = p_mul(adet, pf2{p_set(ms_h), p_set(ms_l)});
-            bad |= !f2_in_band({v.hi.x, 0.0f}, -80, 100) || !f2_in_band({v.hi.y, 0.0f}, -80, 100);
-            LM[ea] = make_float2(v.hi.x, v.lo.x);
-            if (has_b) LM[eb] = make_float2(v.hi.y, v.lo.y);
+            const V v = p_mul(adet, p_const<Ln>(ms_h, ms_l));
+#pragma unroll
+            for (int k = 0; k < NE; ++k) {
+                bad |= !f2_in_band({l_get(v.hi, k), 0.0f}, -80, 100);
+                if (has[k]) REC[el[k] * NR + NL] = make_float2(l_get(v.hi, k), l_get(v.lo, k));
+            }
         }
     }
     const bool use_df = !__syncthreads_or(bad);
@@ -286,7 +314,7 @@ __global__ void __launch_bounds__(kP1NT, 2) k_p1df(const tm_matrix_args a) {
         // same shared-memory slots
         if (threadIdx.x == 0 && a.stats) atomicAdd(a.stats, 1);
         const double wsum = pk[TL.wsum];
-        for (int el = threadIdx.x; el < ne; el += kP1NT) {
+        for (int el = threadIdx.x; el < ne; el += NT) {
             const int64_t i = i0 + el;
             double X[B][D];
 #pragma unroll
@@ -305,9 +333,9 @@ __global__ void __launch_bounds__(kP1NT, 2) k_p1df(const tm_matrix_args a) {
 #pragma unroll
                 for (int p = 0; p < B; ++p)
 #pragma unroll
-                    for (int q = p; q < B; ++q, ++l) LKd[el * NL + l] = s * dot<double, D>(C[p], C[q]);
+                    for (int q = p; q < B; ++q, ++l) RECd[el * NR + l] = s * dot<double, D>(C[p], C[q]);
             }
-            if constexpr (MASS) LMd[el] = adet * a.mass_scale;
+            if constexpr (MASS) RECd[el * NR + NL] = adet * a.mass_scale;
         }
         __syncthreads();
     }
@@ -353,7 +381,7 @@ __global__ void __launch_bounds__(kP1NT, 2) k_p1df(const tm_matrix_args a) {
             split_to_pair(cta.m_diag, mdh, mdl);
             split_to_pair(cta.m_off, moh, mol);
         }
-        for (int j = threadIdx.x; j < ns; j += kP1NT) {
+        for (int j = threadIdx.x; j < ns; j += NT) {
             const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
             const int32_t tgt = __ldcs(P.slot_target + s0 + j), mir = __ldcs(P.slot_mirror + s0 + j);
             // lane x: the stiffness sum, lane y: the sum of |det| rho; TwoSum
@@ -361,11 +389,12 @@ __global__ void __launch_bounds__(kP1NT, 2) k_p1df(const tm_matrix_args a) {
             float2 acc = make_float2(0.0f, 0.0f), err = make_float2(0.0f, 0.0f);
             for (int p = p0; p < p1; ++p) {
                 const unsigned idx = (unsigned)CT[p] >> 1;
-                const float2 kv = DIFF ? LK[idx] : make_float2(0.0f, 0.0f);
-                const float2 mv = MASS ? LM[idx / (unsigned)NL] : make_float2(0.0f, 0.0f);
+                const unsigned e = idx / (unsigned)NL;       // record e, entry idx - e NL
+                const float2 kv = DIFF ? REC[idx + e] : make_float2(0.0f, 0.0f);
+                const float2 mv = MASS ? REC[e * NR + NL] : make_float2(0.0f, 0.0f);
                 const pf2 t = p_two_sum(acc, make_float2(kv.x, mv.x));
                 acc = t.hi;
-                err = p_add(err, p_add(t.lo, make_float2(kv.y, mv.y)));
+                err = l_add(err, l_add(t.lo, make_float2(kv.y, mv.y)));
             }
             const pf2 r = p_fast_two_sum(acc, err);
             double kd = 0.0, md = 0.0;
@@ -391,15 +420,15 @@ __global__ void __launch_bounds__(kP1NT, 2) k_p1df(const tm_matrix_args a) {
         mhl[threadIdx.x] = pk[TL.mhat + pa * B + pb];
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < ns; j += kP1NT) {
+    for (int j = threadIdx.x; j < ns; j += NT) {
         const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
         const int32_t tgt = P.slot_target[s0 + j], mir = P.slot_mirror[s0 + j];
         double kd = 0.0, md = 0.0;
         for (int p = p0; p < p1; ++p) {
             const unsigned idx = (unsigned)CT[p] >> 1;
             const unsigned el = idx / (unsigned)NL;
-            if constexpr (DIFF) kd += LKd[idx];
-            if constexpr (MASS) md += LMd[el] * mhl[idx - el * (unsigned)NL];
+            if constexpr (DIFF) kd += RECd[idx + el];
+            if constexpr (MASS) md += RECd[el * NR + NL] * mhl[idx - el * (unsigned)NL];
         }
         emit(tgt, mir, kd, md);
     }
@@ -451,19 +480,22 @@ namespace tmk {
 
 // k_p1df, then (when the plan has shared targets) k_p1df_finalize as its
 // programmatic dependent
-template <int ET, int FORMS>
-int run_p1df(const tm_matrix_args& a, cudaStream_t st) {
+template <int ET, int FORMS, int NE>
+int run_p1df_ne(const tm_matrix_args& a, cudaStream_t st) {
     const P1Layout L = p1_layout<ET>(a.plan.chunk_elems, a.plan.max_chunk_slots, a.plan.max_chunk_contrib);
     if (L.total > 227 * 1024)
         return tm_set_error(TM_ERR_TOO_LARGE, "tm_assemble_matrix: chunk needs more than 227 KB of shared memory");
     if (Traits<ET>::B == 4 && (reinterpret_cast<uintptr_t>(a.plan.conn) & 15) != 0)
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_matrix: plan.conn must start on a 16-byte boundary");
     if (a.plan.n_chunks == 0) return TM_OK;
-    int s = set_smem(k_p1df<ET, FORMS>, L.total);
+    int s = set_smem(k_p1df<ET, FORMS, NE>, L.total);
     if (s) return s;
     if (a.event_begin && cudaEventRecord(static_cast<cudaEvent_t>(a.event_begin), st) != cudaSuccess)
         return launch_status("cudaEventRecord");
-    k_p1df<ET, FORMS><<<a.plan.n_chunks, kP1NT, L.total, st>>>(a);
+    // threads: enough for the chunk's elements (NE each), at most the bound
+    const int want = (a.plan.chunk_elems + NE - 1) / NE;
+    const int threads = std::min(p1_threads<NE>(), std::max(32, (want + 31) / 32 * 32));
+    k_p1df<ET, FORMS, NE><<<a.plan.n_chunks, threads, L.total, st>>>(a);
     if ((s = launch_status("k_p1df"))) return s;
     if (a.event_end && cudaEventRecord(static_cast<cudaEvent_t>(a.event_end), st) != cudaSuccess)
         return launch_status("cudaEventRecord");
@@ -485,6 +517,14 @@ int run_p1df(const tm_matrix_args& a, cudaStream_t st) {
     if (a.event_done && cudaEventRecord(static_cast<cudaEvent_t>(a.event_done), st) != cudaSuccess)
         return launch_status("cudaEventRecord");
     return TM_OK;
+}
+
+// one element per thread: twice the resident warps of the paired variant
+// (NE = 2), which the latency-bound phases need more than its halved
+// double-float instruction count
+template <int ET, int FORMS>
+int run_p1df(const tm_matrix_args& a, cudaStream_t st) {
+    return run_p1df_ne<ET, FORMS, 1>(a, st);
 }
 
 }  // namespace tmk

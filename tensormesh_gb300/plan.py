@@ -94,6 +94,76 @@ def device_pattern(conn: torch.Tensor, n_points: int):
     return edges, slot, row_ptr
 
 
+def device_morton_order(points: torch.Tensor, conn: torch.Tensor, groups: Optional[np.ndarray] = None) -> torch.Tensor:
+    """``morton_order`` on the GPU (``tm_morton_order_device``): the same
+    permutation, as a device int32 tensor."""
+    lib = _lib.load()
+    dev = conn.device
+    c = conn.to(torch.int32).contiguous()
+    E, B = int(c.shape[0]), int(c.shape[1])
+    pts = points.detach().to(device=dev, dtype=torch.float64).contiguous()
+    D = int(pts.shape[1])
+    perm = torch.empty(E, dtype=torch.int32, device=dev)
+    if E == 0:
+        return perm
+    g = None if groups is None else torch.as_tensor(np.asarray(groups, dtype=np.int64)).to(dev)
+    G = 1 if g is None else int(g.shape[0]) - 1
+    if g is not None and (G < 1 or int(groups[0]) != 0 or int(groups[-1]) != E or (np.diff(groups) < 0).any()):
+        raise ValueError("element groups must be non-decreasing offsets from 0 to the element count")
+    ws = torch.empty(max(1, lib.tm_morton_workspace_bytes(E, D, G)), dtype=torch.uint8, device=dev)
+    _lib.check(lib.tm_morton_order_device(_lib.ptr(pts), int(pts.shape[0]), D, _lib.ptr(c), E, B, _lib.ptr(g), G,
+                                          _lib.ptr(ws), _lib.ptr(perm), _lib.stream_handle(dev)),
+               "tm_morton_order_device")
+    return perm
+
+
+def device_chunk_plan(conn: torch.Tensor, perm: torch.Tensor, n_points: int, kind: int, chunk_elems: int,
+                      slot: Optional[torch.Tensor] = None, nnz: int = 0) -> "DevicePlan":
+    """``tm_plan_build``'s chunk plan built on the GPU (``tm_chunk_plan_device``)
+    from device conn (element order), perm and, for matrix plans, the device
+    slot map: the same arrays, kept on the device."""
+    lib = _lib.load()
+    dev = conn.device
+    c = conn.to(torch.int32).contiguous()
+    E, B = int(c.shape[0]), int(c.shape[1])
+    matrix = kind == _lib.TM_PLAN_KIND_MATRIX
+    NL = B * (B + 1) // 2 if matrix else B
+    n_targets = nnz if matrix else n_points
+    n_chunks = (E + chunk_elems - 1) // chunk_elems
+    cap_slots, cap_contrib, cap_shared = E * NL, (2 * E * NL if matrix else E * NL), max(1, n_targets)
+    i32 = lambda n: torch.empty(max(1, n), dtype=torch.int32, device=dev)
+    arrays = {"conn": i32(E * B), "chunk_begin": i32(n_chunks + 1), "chunk_contrib": i32(n_chunks + 1),
+              "slot_ptr": i32(cap_slots + 1), "contrib": torch.empty(max(1, cap_contrib), dtype=torch.int16, device=dev),
+              "slot_target": i32(cap_slots), "slot_mirror": i32(cap_slots), "shared_ptr": i32(cap_shared + 1),
+              "shared_target": i32(cap_shared), "shared_mirror": i32(cap_shared)}
+    out = _lib.DeviceChunkPlan()
+    for k, v in arrays.items():
+        setattr(out, k, _lib.ptr(v))
+    out.cap_slots, out.cap_contrib, out.cap_shared = cap_slots, cap_contrib, cap_shared
+    ws = torch.empty(max(1, lib.tm_chunk_plan_device_workspace_bytes(E, B, n_targets, kind, chunk_elems)),
+                     dtype=torch.uint8, device=dev)
+    _lib.check(lib.tm_chunk_plan_device(_lib.ptr(c), E, B, n_points, kind, chunk_elems, _lib.ptr(perm), _lib.ptr(slot),
+                                        nnz, _lib.ptr(ws), C.byref(out), _lib.stream_handle(dev)),
+               "tm_chunk_plan_device")
+    del ws
+    ns, nc, nsh = int(out.n_slots), int(out.n_contrib), int(out.n_shared)
+    # exact sizes; the arrays staged by bulk copies keep 16 zero bytes past their end
+    pad = lambda x, n: torch.cat([x[:n], torch.zeros(16 // x.element_size(), dtype=x.dtype, device=dev)])
+    sizes = {"n_elements": E, "n_basis": B, "n_local": NL, "chunk_elems": chunk_elems, "n_chunks": int(out.n_chunks),
+             "n_targets": n_targets, "n_shared": nsh, "n_partials": int(out.n_partials), "n_chunk_slots": ns,
+             "n_contrib": nc, "max_chunk_slots": int(out.max_chunk_slots),
+             "max_chunk_contrib": int(out.max_chunk_contrib)}
+    dev_arrays = {"elem_perm": perm.to(torch.int32).contiguous(), "conn": arrays["conn"][:E * B],
+                  "chunk_begin": arrays["chunk_begin"][:n_chunks + 1],
+                  "chunk_contrib": arrays["chunk_contrib"][:n_chunks + 1],
+                  "slot_ptr": pad(arrays["slot_ptr"], ns + 1), "contrib": pad(arrays["contrib"], nc),
+                  "slot_target": arrays["slot_target"][:ns].clone(), "slot_mirror": arrays["slot_mirror"][:ns].clone(),
+                  "shared_ptr": arrays["shared_ptr"][:nsh + 1].clone(),
+                  "shared_target": arrays["shared_target"][:nsh].clone(),
+                  "shared_mirror": arrays["shared_mirror"][:nsh].clone()}
+    return DevicePlan.from_device(dev_arrays, sizes, dev)
+
+
 class HostPlan:
     """Arrays of one ``tm_plan_build`` call, as numpy arrays."""
 
@@ -180,6 +250,17 @@ class DevicePlan:
         self.max_chunk_slots, self.max_chunk_contrib = host.max_chunk_slots, host.max_chunk_contrib
         self.device = device
 
+    @classmethod
+    def from_device(cls, arrays: Dict[str, torch.Tensor], sizes: Dict[str, int], device: torch.device) -> "DevicePlan":
+        """A plan whose arrays were built on the device (``device_chunk_plan``)."""
+        p = cls.__new__(cls)
+        for k, v in arrays.items():
+            setattr(p, k, v)
+        for k, v in sizes.items():
+            setattr(p, k, v)
+        p.device = device
+        return p
+
     def struct(self) -> _lib.ChunkPlan:
         if getattr(self, "_struct", None) is not None:
             return self._struct
@@ -263,8 +344,15 @@ class Topology:
         # chunk sizes and kinds are built from it later, and must match the
         # pattern and slot map even if the caller edits its cells in place
         conn_np = np.array(conn.detach().to("cpu", torch.int64).contiguous().numpy(), copy=True)
-        pts_np = points.detach().cpu().to(torch.float64).numpy()
-        self.perm = morton_order(pts_np, conn_np, element_groups)
+        # a mesh on the GPU is ordered, patterned and planned on the GPU
+        self._dev = conn.device if (conn.is_cuda and self.n_elements > 0) else None
+        if self._dev is not None:
+            self._conn_dev = conn.detach().to(torch.int32).contiguous().clone()
+            self._perm_dev = device_morton_order(points, self._conn_dev, element_groups)
+            self.perm = self._perm_dev.cpu().numpy()   # host copy, for plans the host builds
+        else:
+            pts_np = points.detach().cpu().to(torch.float64).numpy()
+            self.perm = morton_order(pts_np, conn_np, element_groups)
         self._conn_np = conn_np
         self._plans: Dict[tuple, DevicePlan] = {}
         self._host_node: Optional[HostPlan] = None
@@ -276,21 +364,21 @@ class Topology:
         self._row_ptr: Dict[torch.device, torch.Tensor] = {}
         if matrix:
             ch = chunk_elems(etype, False, quadrature_order)
-            if conn.is_cuda and self.n_elements > 0:
-                # pattern and slot map built on the GPU (tm_pattern_*); the
-                # chunk plan follows on the host from that slot map
-                edges, slot, row_ptr = device_pattern(conn, self.n_points)
+            if self._dev is not None:
+                # pattern and slot map on the GPU (tm_pattern_*); chunk
+                # plans follow on the GPU from that slot map, per chunk size
+                edges, slot, row_ptr = device_pattern(self._conn_dev, self.n_points)
                 self._row_ptr[conn.device] = row_ptr
+                self._slot_dev = slot
                 self.edges, self.slot = edges.cpu(), slot.cpu()
-                host = HostPlan(conn_np, self.n_points, _lib.TM_PLAN_KIND_MATRIX, ch, self.perm,
-                                slot_map=self.slot.numpy())
                 self.nnz = int(self.edges.shape[1])
+                self._pending = {}
             else:
                 host = HostPlan(conn_np, self.n_points, _lib.TM_PLAN_KIND_MATRIX, ch, self.perm)
                 self.edges = torch.from_numpy(np.stack([host.arrays["edge_row"], host.arrays["edge_col"]]))
                 self.slot = torch.from_numpy(host.arrays["slot"])
                 self.nnz = int(host.nnz)
-            self._pending = {("matrix", ch): host}
+                self._pending = {("matrix", ch): host}
         else:
             self.nnz = 0
             self._pending = {}
@@ -334,19 +422,41 @@ class Topology:
         ch = self.chunk_for("block" if block else "scalar", device, dtype)
         key = ("matrix", ch, device)
         if key not in self._plans:
-            host = self._pending.pop(("matrix", ch), None)
-            if host is None:
-                host = HostPlan(self._conn_np, self.n_points, _lib.TM_PLAN_KIND_MATRIX, ch, self.perm,
-                                slot_map=self.slot.numpy())
-            self._plans[key] = DevicePlan(host, device)
+            plan = self._device_plan(device, _lib.TM_PLAN_KIND_MATRIX, ch)
+            if plan is None:
+                host = self._pending.pop(("matrix", ch), None)
+                if host is None:
+                    host = HostPlan(self._conn_np, self.n_points, _lib.TM_PLAN_KIND_MATRIX, ch, self.perm,
+                                    slot_map=self.slot.numpy())
+                plan = DevicePlan(host, device)
+            self._plans[key] = plan
         return self._plans[key]
+
+    def _device_plan(self, device: torch.device, kind: int, ch: int) -> Optional[DevicePlan]:
+        """The chunk plan built on the GPU, for a mesh that lives on this
+        device; None where the device builder does not apply (another device,
+        chunks above 1024 elements or 8192 contributions), and the host
+        builder takes over."""
+        if self._dev is None or torch.device(device) != self._dev or ch > 1024:
+            return None
+        try:
+            if kind == _lib.TM_PLAN_KIND_MATRIX:
+                return device_chunk_plan(self._conn_dev, self._perm_dev, self.n_points, kind, ch, self._slot_dev,
+                                         self.nnz)
+            return device_chunk_plan(self._conn_dev, self._perm_dev, self.n_points, kind, ch)
+        except _lib.TmError as err:
+            if getattr(err, "status", None) == _lib.TM_ERR_TOO_LARGE:
+                return None
+            raise
 
     def node_plan(self, device: torch.device, dtype: Optional[torch.dtype] = None) -> DevicePlan:
         ch = self.chunk_for("node", device, dtype)
         key = ("node", ch, device)
         if key not in self._plans:
-            host = HostPlan(self._conn_np, self.n_points, _lib.TM_PLAN_KIND_NODE, ch, self.perm)
-            self._plans[key] = DevicePlan(host, device)
+            plan = self._device_plan(device, _lib.TM_PLAN_KIND_NODE, ch)
+            if plan is None:
+                plan = DevicePlan(HostPlan(self._conn_np, self.n_points, _lib.TM_PLAN_KIND_NODE, ch, self.perm), device)
+            self._plans[key] = plan
         return self._plans[key]
 
     def row_ptr(self, device: torch.device) -> torch.Tensor:
