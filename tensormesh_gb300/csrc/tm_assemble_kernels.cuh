@@ -12,7 +12,6 @@
 
 #include "../../include/tensormesh_gb300.h"
 #include "tm_df64.cuh"
-#include "tm_df2.cuh"
 #include "tm_element.cuh"
 #include "tm_reduce.cuh"
 #include "tm_status.h"
@@ -58,7 +57,7 @@ constexpr int matrix_threads() {
 template <typename R, int ET, int FORMS>
 constexpr int matrix_min_blocks() {
     if (use_df64<R, ET, FORMS>()) return ET == TM_TET4 ? 4 : 5;
-    if (std::is_same<R, double>::value && !Traits<ET>::P1) return (FORMS & TM_FORM_ELASTICITY) ? 2 : 3;
+    if (std::is_same<R, double>::value && !Traits<ET>::P1) return 3;
     return 1;
 }
 
@@ -811,116 +810,74 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
             // each contribution's block from its (element, pair): A = sum_q
             // jw g_a g_b^T and lam A + mu (A^T + tr A I) in double-float on
             // the element's scaled values, scaled back by 2^S exactly, then
-            // a compensated sum per target in element order, rounded once.
-            // A thread takes two neighbouring targets (counts sorted, so
-            // their loops are about equally long) in the two lanes of the
-            // paired FP32 instructions; the shorter one's missing steps add
-            // exact zeros (a zero weight and zero moduli), which leave its
-            // sums bitwise unchanged.
+            // a compensated sum per target in element order, rounded once
             const f2* G2 = reinterpret_cast<const f2*>(G);
             const f2* JW2 = reinterpret_cast<const f2*>(JW);
-            struct pacc {
-                float2 s, e;
-            };
-            auto pacc_fma = [](pacc& acc, pf2 a, pf2 b) {
-                const float2 pr = l_mul(a.hi, b.hi);
-                const float2 pe = l_fma(a.hi, b.hi, l_neg(pr));
-                const pf2 t = p_two_sum(acc.s, pr);
-                float2 e = l_add(acc.e, l_add(t.lo, pe));
-                e = l_fma(a.hi, b.lo, e);
-                e = l_fma(a.lo, b.hi, e);
-                acc.s = t.hi;
-                acc.e = e;
-            };
-            auto pacc_add = [](pacc& acc, pf2 a) {
-                const pf2 t = p_two_sum(acc.s, a.hi);
-                acc.s = t.hi;
-                acc.e = l_add(acc.e, l_add(t.lo, a.lo));
-            };
-            auto pack = [](f2 a, f2 b) { return pf2{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)}; };
-            for (int j = 2 * (int)threadIdx.x; j < ns; j += 2 * (int)blockDim.x) {
-                const bool has_b = j + 1 < ns;
-                const int a0 = SP[j] - c0, a1 = SP[j + 1] - c0;
-                const int b0 = has_b ? a1 : 0, b1 = has_b ? SP[j + 2] - c0 : 0;
-                const int na = a1 - a0, nb = b1 - b0, n = max(na, nb);
-                pacc sum[HH];
+            for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+                const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
+                const int32_t tgt = __ldcs(P.slot_target + s0 + j), mir = __ldcs(P.slot_mirror + s0 + j);
+                acc2 sum[HH];
 #pragma unroll
-                for (int k = 0; k < HH; ++k) sum[k] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
-                for (int p = 0; p < n; ++p) {
-                    const bool va = p < na, vb = p < nb;
-                    const int code_a = va ? CT[a0 + p] : 0, code_b = vb ? CT[b0 + p] : 0;
-                    const int idx_a = code_a >> 1, idx_b = code_b >> 1;
-                    const int el_a = idx_a / NL, el_b = idx_b / NL;
-                    int pa_a, pb_a, pa_b, pb_b;
-                    upper_pair<B>(idx_a - el_a * NL, pa_a, pb_a);
-                    upper_pair<B>(idx_b - el_b * NL, pa_b, pb_b);
-                    pacc A[D][D];
+                for (int k = 0; k < HH; ++k) sum[k] = {0.0f, 0.0f};
+                for (int p = p0; p < p1; ++p) {
+                    const int code = CT[p];
+                    const int idx = code >> 1;
+                    const int el = idx / NL;
+                    int pa, pb;
+                    upper_pair<B>(idx - el * NL, pa, pb);
+                    acc2 A[D][D];
 #pragma unroll
                     for (int r = 0; r < D; ++r)
 #pragma unroll
-                        for (int c = 0; c < D; ++c) A[r][c] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
+                        for (int c = 0; c < D; ++c) A[r][c] = {0.0f, 0.0f};
                     for (int q = 0; q < Q; ++q) {
-                        const f2* ga = G2 + (size_t)(el_a * Q + q) * B * D;
-                        const f2* gb = G2 + (size_t)(el_b * Q + q) * B * D;
-                        const f2 zero = {0.0f, 0.0f};
-                        const pf2 w = pack(va ? JW2[el_a * Q + q] : zero, vb ? JW2[el_b * Q + q] : zero);
-                        pf2 t[D];
+                        const f2* g = G2 + (size_t)(el * Q + q) * B * D;
+                        const f2 w = JW2[el * Q + q];
+                        f2 t[D];
 #pragma unroll
-                        for (int c = 0; c < D; ++c) t[c] = p_mul(w, pack(ga[pb_a * D + c], gb[pb_b * D + c]));
+                        for (int c = 0; c < D; ++c) t[c] = f2_mul(w, g[pb * D + c]);
 #pragma unroll
                         for (int r = 0; r < D; ++r) {
-                            const pf2 ar = pack(ga[pa_a * D + r], gb[pa_b * D + r]);
+                            const f2 ar = g[pa * D + r];
 #pragma unroll
-                            for (int c = 0; c < D; ++c) pacc_fma(A[r][c], ar, t[c]);
+                            for (int c = 0; c < D; ++c) acc_fma(A[r][c], ar, t[c]);
                         }
                     }
-                    const f2* ma = reinterpret_cast<const f2*>(LE + 2 * el_a);
-                    const f2* mb = reinterpret_cast<const f2*>(LE + 2 * el_b);
-                    const pf2 m0 = pack(ma[0], mb[0]), m1 = pack(ma[1], mb[1]);
-                    const float2 sc = make_float2(pow2f(SI[4 * el_a + 3]), pow2f(SI[4 * el_b + 3]));
-                    pf2 Av[D][D];
+                    const f2* m = reinterpret_cast<const f2*>(LE + 2 * el);
+                    const float sc = pow2f(SI[4 * el + 3]);
+                    f2 Av[D][D];
+#pragma unroll
+                    for (int r = 0; r < D; ++r)
+#pragma unroll
+                        for (int c = 0; c < D; ++c) Av[r][c] = acc_value(A[r][c]);
+                    f2 tr = Av[0][0];
+#pragma unroll
+                    for (int d = 1; d < D; ++d) tr = f2_add(tr, Av[d][d]);
+                    f2 blk[HH];
 #pragma unroll
                     for (int r = 0; r < D; ++r)
 #pragma unroll
                         for (int c = 0; c < D; ++c) {
-                            const pf2 v = p_fast_two_sum(A[r][c].s, A[r][c].e);
-                            Av[r][c] = v;
-                        }
-                    pf2 tr = Av[0][0];
-#pragma unroll
-                    for (int d = 1; d < D; ++d) tr = p_add(tr, Av[d][d]);
-                    pf2 blk[HH];
-#pragma unroll
-                    for (int r = 0; r < D; ++r)
-#pragma unroll
-                        for (int c = 0; c < D; ++c) {
-                            const pf2 u = r == c ? p_add(Av[c][r], tr) : Av[c][r];
-                            pf2 v = p_add(p_mul(m0, Av[r][c]), p_mul(m1, u));
-                            v.hi = l_mul(v.hi, sc);
-                            v.lo = l_mul(v.lo, sc);
+                            const f2 u = r == c ? f2_add(Av[c][r], tr) : Av[c][r];
+                            f2 v = f2_add(f2_mul(m[0], Av[r][c]), f2_mul(m[1], u));
+                            v.hi = __fmul_rn(v.hi, sc);
+                            v.lo = __fmul_rn(v.lo, sc);
                             blk[r * D + c] = v;
                         }
-                    // a transposed contribution adds the block's transpose
-                    const bool ta = code_a & 1, tb = code_b & 1;
+                    if (code & 1) {
 #pragma unroll
-                    for (int r = 0; r < D; ++r)
+                        for (int r = 0; r < D; ++r)
 #pragma unroll
-                        for (int c = 0; c < D; ++c) {
-                            const pf2 x = blk[r * D + c], y = blk[c * D + r];
-                            const pf2 v = {make_float2(ta ? y.hi.x : x.hi.x, tb ? y.hi.y : x.hi.y),
-                                           make_float2(ta ? y.lo.x : x.lo.x, tb ? y.lo.y : x.lo.y)};
-                            pacc_add(sum[r * D + c], v);
-                        }
+                            for (int c = 0; c < D; ++c) acc_add(sum[r * D + c], blk[c * D + r]);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < HH; ++k) acc_add(sum[k], blk[k]);
+                    }
                 }
-                R ea[HH], eb[HH];
+                R ae[HH];
 #pragma unroll
-                for (int k = 0; k < HH; ++k) {
-                    const pf2 v = p_fast_two_sum(sum[k].s, sum[k].e);
-                    ea[k] = (R)pair_to_double(v.hi.x, v.lo.x);
-                    eb[k] = (R)pair_to_double(v.hi.y, v.lo.y);
-                }
-                emit(__ldcs(P.slot_target + s0 + j), __ldcs(P.slot_mirror + s0 + j), R(0), R(0), ea);
-                if (has_b) emit(__ldcs(P.slot_target + s0 + j + 1), __ldcs(P.slot_mirror + s0 + j + 1), R(0), R(0), eb);
+                for (int k = 0; k < HH; ++k) ae[k] = (R)f2_to_double(acc_value(sum[k]));
+                emit(tgt, mir, R(0), R(0), ae);
             }
             return;
         }
