@@ -248,20 +248,96 @@ __device__ __forceinline__ int group_of(const int64_t* groups, int32_t G, int64_
 }
 
 // centroid of each element's vertices, ((x0 + x1) + x2 ...) / V in the
-// host's order, and its group's box
+// host's order, and its group's box.  Each thread keeps a running box of
+// its elements (flushed when the group changes); at the end a warp whose
+// lanes share one group reduces by shuffles, and a block whose warps share
+// one reduces in shared memory, so the box words see a few thousand
+// atomics rather than one per element and coordinate.  256 threads.
 template <int D>
-__global__ void k_centroids(const double* pts, const int32_t* conn, int64_t E, int32_t B, const int64_t* groups,
-                            int32_t G, double* cent, long long* box) {
+__global__ void __launch_bounds__(256) k_centroids(const double* pts, const int32_t* conn, int64_t E, int32_t B,
+                                                   const int64_t* groups, int32_t G, double* cent, long long* box) {
+    constexpr long long kHi = 0x7FFFFFFFFFFFFFFFLL, kLo = -kHi - 1;
+    int gc = -1;
+    long long mn[D], mx[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) mn[d] = kHi, mx[d] = kLo;
+    auto flush = [&](int g) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            atomicMin(box + (int64_t)g * 2 * D + d, mn[d]);
+            atomicMax(box + (int64_t)g * 2 * D + D + d, mx[d]);
+            mn[d] = kHi, mx[d] = kLo;
+        }
+    };
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x) {
         const int g = groups ? group_of(groups, G, e) : 0;
+        if (g != gc) {
+            if (gc >= 0) flush(gc);
+            gc = g;
+        }
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             double s = pts[(int64_t)conn[e * B] * D + d];
             for (int v = 1; v <= D; ++v) s = __dadd_rn(s, pts[(int64_t)conn[e * B + v] * D + d]);
             s = __ddiv_rn(s, (double)(D + 1));
             cent[e * D + d] = s;
-            atomicMin(box + (int64_t)g * 2 * D + d, ord_of(s));
-            atomicMax(box + (int64_t)g * 2 * D + D + d, ord_of(s));
+            mn[d] = min(mn[d], ord_of(s));
+            mx[d] = max(mx[d], ord_of(s));
+        }
+    }
+    // warp: one group among the lanes that hold a box (-1: none)
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int gw = gc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gw = max(gw, __shfl_xor_sync(full, gw, o));
+    const bool wuni = __all_sync(full, gc < 0 || gc == gw);
+    if (wuni) {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                mn[d] = min(mn[d], __shfl_xor_sync(full, mn[d], o));
+                mx[d] = max(mx[d], __shfl_xor_sync(full, mx[d], o));
+            }
+    } else if (gc >= 0) {
+        flush(gc);
+    }
+    // block: one group among the warps that still hold a box
+    __shared__ int wg[8];
+    __shared__ long long wmn[8][D], wmx[8][D];
+    if (lane == 0) {
+        wg[warp] = wuni ? gw : -1;
+#pragma unroll
+        for (int d = 0; d < D; ++d) wmn[warp][d] = mn[d], wmx[warp][d] = mx[d];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = blockDim.x >> 5;
+        int gb = -1;
+        bool buni = true;
+        for (int w = 0; w < nw; ++w)
+            if (wg[w] >= 0) {
+                if (gb < 0) gb = wg[w];
+                buni &= wg[w] == gb;
+            }
+        if (gb >= 0) {
+            if (buni) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) mn[d] = kHi, mx[d] = kLo;
+                for (int w = 0; w < nw; ++w)
+                    if (wg[w] >= 0)
+#pragma unroll
+                        for (int d = 0; d < D; ++d) mn[d] = min(mn[d], wmn[w][d]), mx[d] = max(mx[d], wmx[w][d]);
+                flush(gb);
+            } else {
+                for (int w = 0; w < nw; ++w)
+                    if (wg[w] >= 0) {
+#pragma unroll
+                        for (int d = 0; d < D; ++d) mn[d] = wmn[w][d], mx[d] = wmx[w][d];
+                        flush(wg[w]);
+                    }
+            }
         }
     }
 }
@@ -394,12 +470,13 @@ extern "C" int tm_morton_order_device(const double* points, int64_t n_points, in
     k_box_fill<<<dp_grid(G * 2 * dim, 256), 256, 0, st>>>(m.box, G, dim);
     if ((s = dp_status("tm_morton_order_device"))) return s;
     const int g = dp_grid(n_elements, 256);
+    const int gc = std::min(g, 152 * 4);                  // a few elements per thread: fewer box atomics
     if (dim == 2) {
-        k_centroids<2><<<g, 256, 0, st>>>(points, conn, n_elements, n_basis, groups, G, m.cent, m.box);
+        k_centroids<2><<<gc, 256, 0, st>>>(points, conn, n_elements, n_basis, groups, G, m.cent, m.box);
         if ((s = dp_status("tm_morton_order_device"))) return s;
         k_codes<2><<<g, 256, 0, st>>>(m.cent, n_elements, groups, G, m.box, m.rs.k0, m.rs.v0);
     } else {
-        k_centroids<3><<<g, 256, 0, st>>>(points, conn, n_elements, n_basis, groups, G, m.cent, m.box);
+        k_centroids<3><<<gc, 256, 0, st>>>(points, conn, n_elements, n_basis, groups, G, m.cent, m.box);
         if ((s = dp_status("tm_morton_order_device"))) return s;
         k_codes<3><<<g, 256, 0, st>>>(m.cent, n_elements, groups, G, m.box, m.rs.k0, m.rs.v0);
     }

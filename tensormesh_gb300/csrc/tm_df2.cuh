@@ -26,9 +26,11 @@ __device__ __forceinline__ float l_neg(float a) { return -a; }
 __device__ __forceinline__ float2 l_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 l_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 l_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 l_neg(float2 a) { return make_float2(-a.x, -a.y); }
-template <class L>
-__device__ __forceinline__ L l_sub(L a, L b) { return l_add(a, l_neg(b)); }
+// negation and subtraction on pairs as single paired instructions
+// (multiplication by -1 is exact; fma(b, -1, a) rounds a - b once)
+__device__ __forceinline__ float2 l_neg(float2 a) { return __fmul2_rn(a, make_float2(-1.0f, -1.0f)); }
+__device__ __forceinline__ float l_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float2 l_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
 
 template <class L> __device__ __forceinline__ L l_set(float v);
 template <> __device__ __forceinline__ float l_set<float>(float v) { return v; }
