@@ -12,6 +12,7 @@
 
 #include "../../include/tensormesh_gb300.h"
 #include "tm_df64.cuh"
+#include "tm_df2.cuh"
 #include "tm_element.cuh"
 #include "tm_reduce.cuh"
 #include "tm_status.h"
@@ -810,73 +811,109 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
             // each contribution's block from its (element, pair): A = sum_q
             // jw g_a g_b^T and lam A + mu (A^T + tr A I) in double-float on
             // the element's scaled values, scaled back by 2^S exactly, then
-            // a compensated sum per target in element order, rounded once
+            // a compensated sum per target in element order, rounded once.
+            // The block's entries go two by two through the paired FP32
+            // instructions: rows (r, 0), (r, 1) and, in 3-D, the column
+            // (0, 2), (1, 2) as pairs, (2, 2) alone.  Each lane performs the
+            // steps of the one-entry form, so the sums are bitwise those of
+            // one entry at a time.
             const f2* G2 = reinterpret_cast<const f2*>(G);
             const f2* JW2 = reinterpret_cast<const f2*>(JW);
+            using L2 = float2;
+            using P2 = ddv<L2>;
+            constexpr int NP = D == 3 ? 4 : 2;                 // entry pairs (and, in 3-D, (2, 2))
+            auto pair = [](f2 x, f2 y) { return P2{make_float2(x.hi, y.hi), make_float2(x.lo, y.lo)}; };
+            auto bcast = [](f2 x) { return P2{make_float2(x.hi, x.hi), make_float2(x.lo, x.lo)}; };
+            auto lane = [](P2 v, int k) { return k ? f2_make(v.hi.y, v.lo.y) : f2_make(v.hi.x, v.lo.x); };
             for (int j = threadIdx.x; j < ns; j += blockDim.x) {
                 const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
                 const int32_t tgt = __ldcs(P.slot_target + s0 + j), mir = __ldcs(P.slot_mirror + s0 + j);
-                acc2 sum[HH];
+                dacc<L2> sum[NP];
+                acc2 sum22 = {0.0f, 0.0f};
 #pragma unroll
-                for (int k = 0; k < HH; ++k) sum[k] = {0.0f, 0.0f};
+                for (int k = 0; k < NP; ++k) sum[k] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
                 for (int p = p0; p < p1; ++p) {
                     const int code = CT[p];
                     const int idx = code >> 1;
                     const int el = idx / NL;
                     int pa, pb;
                     upper_pair<B>(idx - el * NL, pa, pb);
-                    acc2 A[D][D];
+                    // A in pairs: {(r,0),(r,1)} for each row r, then (3-D) {(0,2),(1,2)}
+                    dacc<L2> A[NP];
+                    acc2 a22 = {0.0f, 0.0f};
 #pragma unroll
-                    for (int r = 0; r < D; ++r)
-#pragma unroll
-                        for (int c = 0; c < D; ++c) A[r][c] = {0.0f, 0.0f};
+                    for (int k = 0; k < NP; ++k) A[k] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
                     for (int q = 0; q < Q; ++q) {
                         const f2* g = G2 + (size_t)(el * Q + q) * B * D;
                         const f2 w = JW2[el * Q + q];
-                        f2 t[D];
+                        // t = w g_b: (t0, t1) paired, t2 alone
+                        const P2 t01 = p_mul(bcast(w), pair(g[pb * D], g[pb * D + 1]));
 #pragma unroll
-                        for (int c = 0; c < D; ++c) t[c] = f2_mul(w, g[pb * D + c]);
-#pragma unroll
-                        for (int r = 0; r < D; ++r) {
-                            const f2 ar = g[pa * D + r];
-#pragma unroll
-                            for (int c = 0; c < D; ++c) acc_fma(A[r][c], ar, t[c]);
+                        for (int r = 0; r < D; ++r) d_fma(A[r], bcast(g[pa * D + r]), t01);
+                        if constexpr (D == 3) {
+                            const f2 t2 = f2_mul(w, g[pb * D + 2]);
+                            d_fma(A[3], pair(g[pa * D], g[pa * D + 1]), bcast(t2));
+                            acc_fma(a22, g[pa * D + 2], t2);
                         }
                     }
+                    P2 V[NP];
+#pragma unroll
+                    for (int k = 0; k < NP; ++k) V[k] = d_value(A[k]);
+                    const f2 v22 = acc_value(a22);
+                    // trace ((A00 + A11) + A22) and A^T in the same pairs
+                    f2 tr = f2_add(lane(V[0], 0), lane(V[1], 1));
+                    if constexpr (D == 3) tr = f2_add(tr, v22);
+                    P2 T[NP];
+                    T[0] = pair(lane(V[0], 0), lane(V[1], 0));
+                    T[1] = pair(lane(V[0], 1), lane(V[1], 1));
+                    if constexpr (D == 3) {
+                        T[2] = V[3];
+                        T[3] = V[2];
+                    }
+                    // the block (or, for a transposed contribution, its
+                    // transpose): m0 X + m1 (Y + tr I), X = A and Y = A^T
+                    // (swapped when transposed), scaled by 2^S
+                    const bool tp = code & 1;
                     const f2* m = reinterpret_cast<const f2*>(LE + 2 * el);
                     const float sc = pow2f(SI[4 * el + 3]);
-                    f2 Av[D][D];
+                    const P2 m0 = bcast(m[0]), m1 = bcast(m[1]);
+                    const L2 sc2 = make_float2(sc, sc);
 #pragma unroll
-                    for (int r = 0; r < D; ++r)
-#pragma unroll
-                        for (int c = 0; c < D; ++c) Av[r][c] = acc_value(A[r][c]);
-                    f2 tr = Av[0][0];
-#pragma unroll
-                    for (int d = 1; d < D; ++d) tr = f2_add(tr, Av[d][d]);
-                    f2 blk[HH];
-#pragma unroll
-                    for (int r = 0; r < D; ++r)
-#pragma unroll
-                        for (int c = 0; c < D; ++c) {
-                            const f2 u = r == c ? f2_add(Av[c][r], tr) : Av[c][r];
-                            f2 v = f2_add(f2_mul(m[0], Av[r][c]), f2_mul(m[1], u));
-                            v.hi = __fmul_rn(v.hi, sc);
-                            v.lo = __fmul_rn(v.lo, sc);
-                            blk[r * D + c] = v;
+                    for (int k = 0; k < NP; ++k) {
+                        const P2 X = tp ? T[k] : V[k];
+                        P2 Y = tp ? V[k] : T[k];
+                        if (k < 2) {
+                            // the diagonal lane: (0,0) in pair 0, (1,1) in pair 1
+                            const P2 trk = k == 0 ? P2{make_float2(tr.hi, 0.0f), make_float2(tr.lo, 0.0f)}
+                                                  : P2{make_float2(0.0f, tr.hi), make_float2(0.0f, tr.lo)};
+                            Y = p_add(Y, trk);
                         }
-                    if (code & 1) {
-#pragma unroll
-                        for (int r = 0; r < D; ++r)
-#pragma unroll
-                            for (int c = 0; c < D; ++c) acc_add(sum[r * D + c], blk[c * D + r]);
-                    } else {
-#pragma unroll
-                        for (int k = 0; k < HH; ++k) acc_add(sum[k], blk[k]);
+                        P2 v = p_add(p_mul(m0, X), p_mul(m1, Y));
+                        v.hi = l_mul(v.hi, sc2);
+                        v.lo = l_mul(v.lo, sc2);
+                        d_add(sum[k], v);
+                    }
+                    if constexpr (D == 3) {
+                        f2 v = f2_add(f2_mul(m[0], v22), f2_mul(m[1], f2_add(v22, tr)));
+                        v.hi = __fmul_rn(v.hi, sc);
+                        v.lo = __fmul_rn(v.lo, sc);
+                        acc_add(sum22, v);
                     }
                 }
+                // back to row-major entries
                 R ae[HH];
+                P2 S[NP];
 #pragma unroll
-                for (int k = 0; k < HH; ++k) ae[k] = (R)f2_to_double(acc_value(sum[k]));
+                for (int k = 0; k < NP; ++k) S[k] = d_value(sum[k]);
+                if constexpr (D == 3) {
+                    const int src[9][2] = {{0, 0}, {0, 1}, {3, 0}, {1, 0}, {1, 1}, {3, 1}, {2, 0}, {2, 1}, {-1, 0}};
+#pragma unroll
+                    for (int k = 0; k < 9; ++k)
+                        ae[k] = (R)f2_to_double(src[k][0] < 0 ? acc_value(sum22) : lane(S[src[k][0]], src[k][1]));
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) ae[k] = (R)f2_to_double(lane(S[k >> 1], k & 1));
+                }
                 emit(tgt, mir, R(0), R(0), ae);
             }
             return;
@@ -967,6 +1004,27 @@ __global__ void __launch_bounds__(kThreads) k_matrix_finalize(const tm_matrix_ar
     R* oE = static_cast<R*>(a.out_elasticity);
     // launched as a programmatic dependent of k_matrix: wait for its results
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    if constexpr (ELAST) {
+        // a team of W lanes per shared target, lane k summing component k
+        // over the target's partials (in chunk order, as one thread per
+        // target would): a team's loads and stores cover W consecutive
+        // values, 32 / W teams per warp
+        constexpr int TPW = 32 / W;
+        const int lane = threadIdx.x & 31, team = lane / W, k = lane - team * W;
+        const int r = k / D, c = k - r * D;
+        const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+        const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+        if (team >= TPW) return;
+        for (int64_t sh = warp * TPW + team; sh < P.n_shared; sh += nwarp * TPW) {
+            const int q0 = P.shared_ptr[sh], q1 = P.shared_ptr[sh + 1];
+            const int64_t tgt = P.shared_target[sh], mir = P.shared_mirror[sh];
+            R acc = 0;
+            for (int q = q0; q < q1; ++q) acc += __ldcs(part + (int64_t)q * W + k);
+            oE[tgt * W + k] = acc;
+            if (mir != tgt) oE[mir * W + c * D + r] = acc;
+        }
+        return;
+    }
     for (int64_t sh = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sh < P.n_shared;
          sh += (int64_t)gridDim.x * blockDim.x) {
         const int q0 = P.shared_ptr[sh], q1 = P.shared_ptr[sh + 1];
@@ -1282,7 +1340,13 @@ int run_matrix_general(const tm_matrix_args& a, cudaStream_t st) {
         // while k_matrix drains and waits (griddepcontrol.wait) for its
         // results; not when an event separates the two launches
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(grid_for(a.plan.n_shared));
+        // (block forms: a team of D x D lanes per shared target, 32 / (D x D)
+        // teams per warp)
+        constexpr int DD = Traits<ET>::D * Traits<ET>::D;
+        const int64_t fin_threads = (FORMS & TM_FORM_ELASTICITY)
+                                        ? (a.plan.n_shared + 32 / DD - 1) / (32 / DD) * 32
+                                        : a.plan.n_shared;
+        cfg.gridDim = dim3(grid_for(fin_threads));
         cfg.blockDim = dim3(kThreads);
         cfg.dynamicSmemBytes = 0;
         cfg.stream = st;

@@ -176,6 +176,38 @@ __device__ __forceinline__ ddv<L> p_abs(ddv<L> a) {
     return {l_abs_sel(a.hi, a.hi), l_abs_sel(a.lo, a.hi)};
 }
 
+// an unnormalised double-float accumulator per lane: s + e, every term's
+// rounding error collected in e (TwoSum on the leading parts); the same
+// steps, lane by lane, as the single-lane acc2 of the double-float header
+template <class L>
+struct dacc {
+    L s, e;
+};
+
+// acc += a * b (a.lo * b.lo dropped: below 2^-96 of the product)
+template <class L>
+__device__ __forceinline__ void d_fma(dacc<L>& acc, ddv<L> a, ddv<L> b) {
+    const L p = l_mul(a.hi, b.hi);
+    const L pe = l_fma(a.hi, b.hi, l_neg(p));
+    const ddv<L> t = p_two_sum(acc.s, p);
+    L e = l_add(acc.e, l_add(t.lo, pe));
+    e = l_fma(a.hi, b.lo, e);
+    e = l_fma(a.lo, b.hi, e);
+    acc.s = t.hi;
+    acc.e = e;
+}
+
+// acc += a
+template <class L>
+__device__ __forceinline__ void d_add(dacc<L>& acc, ddv<L> a) {
+    const ddv<L> t = p_two_sum(acc.s, a.hi);
+    acc.s = t.hi;
+    acc.e = l_add(acc.e, l_add(t.lo, a.lo));
+}
+
+template <class L>
+__device__ __forceinline__ ddv<L> d_value(dacc<L> acc) { return p_fast_two_sum(acc.s, acc.e); }
+
 // ------------------------------------------------------------ conversions
 // double -> hi + lo on the integer pipe, without branches.  hi is x
 // truncated to 24 significant bits, lo the remaining 29 bits rounded to 24
