@@ -485,7 +485,10 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                 SI[4 * el] = sx;
             }
             __syncthreads();
-            for (int k = threadIdx.x; k < ne * Q; k += blockDim.x) {
+            // two threads per (element, point): both form J, its cofactors
+            // and determinant, each half of the gradients
+            for (int k2 = threadIdx.x; k2 < 2 * ne * Q; k2 += blockDim.x) {
+                const int k = k2 >> 1, half = k2 & 1;
                 const int el = k / Q, q = k - el * Q;
                 const f2* dp = DP2 + q * D * B;
                 const f2* xe = X2 + el * B * D;
@@ -523,16 +526,19 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                 if constexpr (DIFF || ELAST) {    // (mass needs only the weights)
                     f2* g = G2 + (size_t)k * B * D;
 #pragma unroll
-                    for (int b = 0; b < B; ++b)
+                    for (int bb = 0; bb < (B + 1) / 2; ++bb) {
+                        const int b = 2 * bb + half;
+                        if (b < B)
 #pragma unroll
-                        for (int c = 0; c < D; ++c) {
-                            acc2 t = {0.0f, 0.0f};
+                            for (int c = 0; c < D; ++c) {
+                                acc2 t = {0.0f, 0.0f};
 #pragma unroll
-                            for (int r = 0; r < D; ++r) acc_fma(t, dp[r * B + b], cof[r][c]);
-                            g[b * D + c] = f2_mul(acc_value(t), inv);
-                        }
+                                for (int r = 0; r < D; ++r) acc_fma(t, dp[r * B + b], cof[r][c]);
+                                g[b * D + c] = f2_mul(acc_value(t), inv);
+                            }
+                    }
                 }
-                JW2[k] = f2_mul(W2[q], adet);
+                if (half == 0) JW2[k] = f2_mul(W2[q], adet);
             }
             __syncthreads();
             auto fexp = [](f2 v) { return (int)((__float_as_uint(v.hi) >> 23) & 0xFF); };
@@ -540,23 +546,34 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                 const int e = biased_exponent(v);
                 return e == 0 ? 0 : e - 1022;
             };
-            for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+            // eight threads per element (a group of lanes of one warp) find
+            // and apply its scales; the group's first thread the rest
+            constexpr int GS = 8;
+            const int gi = threadIdx.x & (GS - 1);
+            const unsigned gmask = 0xFFu << ((threadIdx.x & 31) & ~(GS - 1));
+            for (int el = threadIdx.x / GS; el < ne; el += blockDim.x / GS) {
                 const int sx = SI[4 * el];
                 f2* g = G2 + (size_t)el * Q * B * D;
                 f2* w = JW2 + el * Q;
                 int fg = 126, fw = 0;    // (126: a mass-only kernel has no gradients to scale)
                 if constexpr (DIFF || ELAST) {
                     fg = 0;
-                    for (int t = 0; t < Q * B * D; ++t) fg = max(fg, fexp(g[t]));
+                    for (int t = gi; t < Q * B * D; t += GS) fg = max(fg, fexp(g[t]));
                 }
-                for (int q = 0; q < Q; ++q) fw = max(fw, fexp(w[q]));
+                for (int q = gi; q < Q; q += GS) fw = max(fw, fexp(w[q]));
+#pragma unroll
+                for (int o = GS / 2; o > 0; o >>= 1) {
+                    fg = max(fg, __shfl_xor_sync(gmask, fg, o));
+                    fw = max(fw, __shfl_xor_sync(gmask, fw, o));
+                }
                 // (float exponents in [2^-125, 2^124): the scale factors
                 // below stay normal floats)
                 ok = ok && fg >= 2 && fg <= 251 && fw >= 2 && fw <= 251;
                 const float cg = pow2f(126 - fg), cw = pow2f(126 - fw);    // max to [1/2, 1)
                 if constexpr (DIFF || ELAST)
-                    for (int t = 0; t < Q * B * D; ++t) g[t] = {__fmul_rn(g[t].hi, cg), __fmul_rn(g[t].lo, cg)};
-                for (int q = 0; q < Q; ++q) w[q] = {__fmul_rn(w[q].hi, cw), __fmul_rn(w[q].lo, cw)};
+                    for (int t = gi; t < Q * B * D; t += GS) g[t] = {__fmul_rn(g[t].hi, cg), __fmul_rn(g[t].lo, cg)};
+                for (int q = gi; q < Q; q += GS) w[q] = {__fmul_rn(w[q].hi, cw), __fmul_rn(w[q].lo, cw)};
+                if (gi != 0) continue;
                 const int sg = fg - 126 - sx, sw = fw - 126 + D * sx;
                 const int e = P.elem_perm[i0 + el];
                 int s2 = 0, s3 = 0;
