@@ -578,16 +578,19 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                 const int e = P.elem_perm[i0 + el];
                 int s2 = 0, s3 = 0;
                 if constexpr (ELAST) {
+                    // the element's weight E 2^S (S = 2 sg + sw + se): its
+                    // A, on scaled gradients and weights, times the weight
+                    // is A at true scale times E; lam and mu are E times the
+                    // call's two constants, applied once per target
                     const double Ey = (yng ? ldg(yng + e) : 1.0) * yscale;
-                    const double lam = Ey * clam, mu = Ey * cmu;
-                    const int ee = max(biased_exponent(lam), biased_exponent(mu));
+                    const int ee = biased_exponent(Ey);
                     const int se = ee == 0 ? 0 : ee - 1022;
                     s2 = se;
                     s3 = 2 * sg + sw + se;
-                    ok = ok && ee < 2047 && s3 > -70 && s3 < 100;
-                    f2* m = reinterpret_cast<f2*>(LE + 2 * el);
-                    m[0] = split_scaled(lam, se);
-                    m[1] = split_scaled(mu, se);
+                    ok = ok && ee > 0 && ee < 2047 && s3 > -70 && s3 < 100;
+                    const f2 wy = split_scaled(Ey, se);
+                    const float sc = pow2f(s3);
+                    reinterpret_cast<f2*>(LE + 2 * el)[0] = {__fmul_rn(wy.hi, sc), __fmul_rn(wy.lo, sc)};
                 }
                 if constexpr (DIFF) {
                     const double kv = (kap ? ldg(kap + e) : 1.0) * kscale;
@@ -825,15 +828,16 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
 
     if constexpr (DFE) {
         if (use_dfg) {
-            // each contribution's block from its (element, pair): A = sum_q
-            // jw g_a g_b^T and lam A + mu (A^T + tr A I) in double-float on
-            // the element's scaled values, scaled back by 2^S exactly, then
-            // a compensated sum per target in element order, rounded once.
-            // The block's entries go two by two through the paired FP32
+            // Per target, S = sum over its contributions of E_e X_e, X_e =
+            // A_e = sum_q jw g_a g_b^T of the contribution's (element, pair)
+            // (A_e^T for a transposed one), in double-float on the element's
+            // scaled values and weight E 2^S, as a compensated sum in
+            // element order; the target's block is then lam' S + mu' (S^T +
+            // tr S I) (lam = E lam', mu = E mu' for the call's Poisson
+            // ratio: the sum of the contributions' blocks), rounded once.
+            // The entries go two by two through the paired FP32
             // instructions: rows (r, 0), (r, 1) and, in 3-D, the column
-            // (0, 2), (1, 2) as pairs, (2, 2) alone.  Each lane performs the
-            // steps of the one-entry form, so the sums are bitwise those of
-            // one entry at a time.
+            // (0, 2), (1, 2) as pairs, (2, 2) alone.
             const f2* G2 = reinterpret_cast<const f2*>(G);
             const f2* JW2 = reinterpret_cast<const f2*>(JW);
             using L2 = float2;
@@ -842,6 +846,16 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
             auto pair = [](f2 x, f2 y) { return P2{make_float2(x.hi, y.hi), make_float2(x.lo, y.lo)}; };
             auto bcast = [](f2 x) { return P2{make_float2(x.hi, x.hi), make_float2(x.lo, x.lo)}; };
             auto lane = [](P2 v, int k) { return k ? f2_make(v.hi.y, v.lo.y) : f2_make(v.hi.x, v.lo.x); };
+            // the transpose in the same pairs
+            auto transp = [&](const P2* V, P2* T) {
+                T[0] = pair(lane(V[0], 0), lane(V[1], 0));
+                T[1] = pair(lane(V[0], 1), lane(V[1], 1));
+                if constexpr (D == 3) {
+                    T[2] = V[3];
+                    T[3] = V[2];
+                }
+            };
+            const f2 cl = split_double((double)clam), cm = split_double((double)cmu);
             for (int j = threadIdx.x; j < ns; j += blockDim.x) {
                 const int p0 = SP[j] - c0, p1 = SP[j + 1] - c0;
                 const int32_t tgt = __ldcs(P.slot_target + s0 + j), mir = __ldcs(P.slot_mirror + s0 + j);
@@ -873,63 +887,48 @@ __global__ void __launch_bounds__((matrix_threads<R, ET, FORMS>()), (matrix_min_
                             acc_fma(a22, g[pa * D + 2], t2);
                         }
                     }
-                    P2 V[NP];
+                    P2 V[NP], T[NP];
 #pragma unroll
                     for (int k = 0; k < NP; ++k) V[k] = d_value(A[k]);
-                    const f2 v22 = acc_value(a22);
-                    // trace ((A00 + A11) + A22) and A^T in the same pairs
-                    f2 tr = f2_add(lane(V[0], 0), lane(V[1], 1));
-                    if constexpr (D == 3) tr = f2_add(tr, v22);
-                    P2 T[NP];
-                    T[0] = pair(lane(V[0], 0), lane(V[1], 0));
-                    T[1] = pair(lane(V[0], 1), lane(V[1], 1));
-                    if constexpr (D == 3) {
-                        T[2] = V[3];
-                        T[3] = V[2];
-                    }
-                    // the block (or, for a transposed contribution, its
-                    // transpose): m0 X + m1 (Y + tr I), X = A and Y = A^T
-                    // (swapped when transposed), scaled by 2^S
+                    transp(V, T);
                     const bool tp = code & 1;
-                    const f2* m = reinterpret_cast<const f2*>(LE + 2 * el);
-                    const float sc = pow2f(SI[4 * el + 3]);
-                    const P2 m0 = bcast(m[0]), m1 = bcast(m[1]);
-                    const L2 sc2 = make_float2(sc, sc);
+                    const P2 wy = bcast(reinterpret_cast<const f2*>(LE + 2 * el)[0]);
 #pragma unroll
-                    for (int k = 0; k < NP; ++k) {
-                        const P2 X = tp ? T[k] : V[k];
-                        P2 Y = tp ? V[k] : T[k];
-                        if (k < 2) {
-                            // the diagonal lane: (0,0) in pair 0, (1,1) in pair 1
-                            const P2 trk = k == 0 ? P2{make_float2(tr.hi, 0.0f), make_float2(tr.lo, 0.0f)}
-                                                  : P2{make_float2(0.0f, tr.hi), make_float2(0.0f, tr.lo)};
-                            Y = p_add(Y, trk);
-                        }
-                        P2 v = p_add(p_mul(m0, X), p_mul(m1, Y));
-                        v.hi = l_mul(v.hi, sc2);
-                        v.lo = l_mul(v.lo, sc2);
-                        d_add(sum[k], v);
+                    for (int k = 0; k < NP; ++k) d_fma(sum[k], wy, tp ? T[k] : V[k]);
+                    if constexpr (D == 3) acc_fma(sum22, lane(wy, 0), acc_value(a22));
+                }
+                // the block: lam' S + mu' (S^T + tr S I)
+                P2 S[NP], ST[NP];
+#pragma unroll
+                for (int k = 0; k < NP; ++k) S[k] = d_value(sum[k]);
+                transp(S, ST);
+                const f2 s22 = acc_value(sum22);
+                f2 tr = f2_add(lane(S[0], 0), lane(S[1], 1));
+                if constexpr (D == 3) tr = f2_add(tr, s22);
+                const P2 CL = bcast(cl), CM = bcast(cm);
+                P2 K[NP];
+#pragma unroll
+                for (int k = 0; k < NP; ++k) {
+                    P2 Y = ST[k];
+                    if (k < 2) {
+                        // the diagonal lane: (0,0) in pair 0, (1,1) in pair 1
+                        const P2 trk = k == 0 ? P2{make_float2(tr.hi, 0.0f), make_float2(tr.lo, 0.0f)}
+                                              : P2{make_float2(0.0f, tr.hi), make_float2(0.0f, tr.lo)};
+                        Y = p_add(Y, trk);
                     }
-                    if constexpr (D == 3) {
-                        f2 v = f2_add(f2_mul(m[0], v22), f2_mul(m[1], f2_add(v22, tr)));
-                        v.hi = __fmul_rn(v.hi, sc);
-                        v.lo = __fmul_rn(v.lo, sc);
-                        acc_add(sum22, v);
-                    }
+                    K[k] = p_add(p_mul(CL, S[k]), p_mul(CM, Y));
                 }
                 // back to row-major entries
                 R ae[HH];
-                P2 S[NP];
-#pragma unroll
-                for (int k = 0; k < NP; ++k) S[k] = d_value(sum[k]);
                 if constexpr (D == 3) {
+                    const f2 k22 = f2_add(f2_mul(cl, s22), f2_mul(cm, f2_add(s22, tr)));
                     const int src[9][2] = {{0, 0}, {0, 1}, {3, 0}, {1, 0}, {1, 1}, {3, 1}, {2, 0}, {2, 1}, {-1, 0}};
 #pragma unroll
                     for (int k = 0; k < 9; ++k)
-                        ae[k] = (R)f2_to_double(src[k][0] < 0 ? acc_value(sum22) : lane(S[src[k][0]], src[k][1]));
+                        ae[k] = (R)f2_to_double(src[k][0] < 0 ? k22 : lane(K[src[k][0]], src[k][1]));
                 } else {
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) ae[k] = (R)f2_to_double(lane(S[k >> 1], k & 1));
+                    for (int k = 0; k < 4; ++k) ae[k] = (R)f2_to_double(lane(K[k >> 1], k & 1));
                 }
                 emit(tgt, mir, R(0), R(0), ae);
             }
