@@ -550,6 +550,38 @@ int tm_pcg_iterate(const tm_pcg_args* args, int32_t n_iter, tm_stream_t stream);
 int tm_pcg_iterate_until(const tm_pcg_args* args, int32_t max_iter, double rtol, tm_stream_t stream);
 
 /*
+ * Jacobi-preconditioned BiCGSTAB for general square systems, replacing the
+ * reference's bicgstab_py (sparse/solve/torch_solve.py:130-248; the CUDA
+ * fallback of spsolve, sparse/solve/__init__.py:195-246): right
+ * preconditioning by 1 / diag(A), a missing or |d| < 1e-12 diagonal taken
+ * as 1; breakdown when |r0^ . v| < 1e-12; omega = 0 when t . t < 1e-12 (the
+ * iteration then stops); stop when ||s|| or ||r|| <= max(atol, rtol ||b||).
+ * tm_bicgstab_start sets r = b - A x, r0^ = r, p = r and the scalars;
+ * tm_bicgstab_iterate runs n_iter iterations (11 launches each) without host
+ * synchronisation.  work: device [8 * n] of the value type (n = n_rows x
+ * block).  scalars: device double [16]: TM_BICG_RR (||r||^2), TM_BICG_BB
+ * (||b||^2), TM_BICG_ITER (iterations), TM_BICG_FLAG (0 running, 1
+ * converged, 2 breakdown).  Dot products in a fixed order: bitwise
+ * reproducible.
+ */
+#define TM_BICG_RR   5
+#define TM_BICG_BB   7
+#define TM_BICG_ITER 8
+#define TM_BICG_FLAG 9
+typedef struct tm_bicgstab_args {
+    tm_linear_operator A;
+    const void* b;
+    void* x;                   /* initial guess on entry, solution on exit */
+    void* work;
+    double* scalars;
+    double* partials;          /* device, tm_pcg_partials_bytes() */
+    double atol;
+    double rtol;
+} tm_bicgstab_args;
+int tm_bicgstab_start(const tm_bicgstab_args* args, tm_stream_t stream);
+int tm_bicgstab_iterate(const tm_bicgstab_args* args, int32_t n_iter, tm_stream_t stream);
+
+/*
  * Batched Jacobi-PCG over the diagonal blocks [system_offset[s],
  * system_offset[s+1]) of one block-diagonal CSR matrix (offset-concatenated
  * meshes), all systems in one launch; no counterpart in the reference, which

@@ -673,6 +673,53 @@ def reference_cg(values, row, col, n, b, atol, max_iter=100000):
     return x, it + 1
 
 
+def reference_bicgstab(values, row, col, n, b, atol, max_iter=10000):
+    """bicgstab_py (sparse/solve/torch_solve.py:130-248), restated: Jacobi
+    (right) preconditioning by 1 / diag, a missing or |d| < 1e-12 diagonal
+    taken as 1; stop when ||r|| < atol; breakdown when |r0^ . v| < 1e-12;
+    x += alpha p^ and stop when ||s|| < atol; omega = 0 when t . t < 1e-12,
+    and stop after that update.  Returns (x, iterations)."""
+    A = torch.sparse_coo_tensor(torch.stack([row.long(), col.long()]), values, (n, n)).coalesce().to_sparse_csr()
+    d = torch.ones(n, dtype=values.dtype, device=values.device)
+    diag = row.long() == col.long()
+    d[row.long()[diag]] = values[diag]
+    d = torch.where(d.abs() < 1e-12, torch.ones_like(d), d)
+    minv = 1.0 / d
+    x = torch.zeros_like(b)
+    r = b - A @ x
+    r0 = r.clone()
+    rho = torch.dot(r0, r)
+    p = r.clone()
+    it = 0
+    for it in range(max_iter):
+        if torch.norm(r) < atol:
+            break
+        ph = minv * p
+        v = A @ ph
+        den = torch.dot(r0, v)
+        if den.abs() < 1e-12:
+            break
+        alpha = rho / den
+        s = r - alpha * v
+        if torch.norm(s) < atol:
+            x = x + alpha * ph
+            break
+        sh = minv * s
+        t = A @ sh
+        tt = torch.dot(t, t)
+        omega = 0.0 if tt.abs() < 1e-12 else torch.dot(t, s) / tt
+        x = x + alpha * ph + omega * sh
+        r = s - omega * t
+        if torch.norm(r) < atol:
+            break
+        rho_new = torch.dot(r0, r)
+        if omega == 0:
+            break
+        p = r + (rho_new / rho) * (alpha / omega) * (p - omega * v)
+        rho = rho_new
+    return x, it + 1
+
+
 def reference_per_mesh_solve(points, conn, boundary, kappa, f, etype="triangle", qorder=2, rel=1e-10):
     """One mesh through the reference's path on the device of ``points``:
     pattern and slot map on the host, K(kappa) and b = int f v assembled by

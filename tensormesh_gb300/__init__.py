@@ -14,7 +14,7 @@ from .builtin import (LaplaceElementAssembler, DiffusionElementAssembler, MassEl
                       LinearElasticityElementAssembler, const_node_assembler, func_node_assembler,
                       LoadNodeAssembler)
 from .facet import FacetAssembler, LoadFacetAssembler, const_facet_assembler, func_facet_assembler
-from .solve import pcg_solve
+from .solve import bicgstab_solve, pcg_solve
 from .condense import Condenser
 from .adjoint import solve_diffusion
 from . import autotune
@@ -25,7 +25,7 @@ __all__ = [
     "Mesh", "gen_unit_square", "gen_unit_square_mixed", "gen_unit_cube", "Transformation", "ReduceProjector", "SparseProjector",
     "SparseMatrix", "ElementAssembler", "NodeAssembler", "assemble_forms", "LaplaceElementAssembler",
     "DiffusionElementAssembler", "MassElementAssembler", "LinearElasticityElementAssembler",
-    "const_node_assembler", "func_node_assembler", "LoadNodeAssembler", "pcg_solve",
+    "const_node_assembler", "func_node_assembler", "LoadNodeAssembler", "pcg_solve", "bicgstab_solve",
     "element_type2dimension", "element_type2order", "Condenser", "solve_diffusion",
     "FacetAssembler", "LoadFacetAssembler", "const_facet_assembler", "func_facet_assembler",
 ]

@@ -133,6 +133,11 @@ class PcgArgs(C.Structure):
                 ("scalars", C.c_void_p), ("partials", C.c_void_p)]
 
 
+class BicgstabArgs(C.Structure):
+    _fields_ = [("A", LinearOperator), ("b", C.c_void_p), ("x", C.c_void_p), ("work", C.c_void_p),
+                ("scalars", C.c_void_p), ("partials", C.c_void_p), ("atol", C.c_double), ("rtol", C.c_double)]
+
+
 class PcgStatus(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("flag", C.c_int32), ("relative_residual", C.c_double)]
 
@@ -145,6 +150,7 @@ class BatchedPcgArgs(C.Structure):
 
 
 TM_PCG_CONVERGED, TM_PCG_MAX_ITER, TM_PCG_BREAKDOWN = 1, 2, 3
+TM_BICG_RR, TM_BICG_BB, TM_BICG_ITER, TM_BICG_FLAG = 5, 7, 8, 9
 
 
 _SIGNATURES = {
@@ -191,6 +197,8 @@ _SIGNATURES = {
     "tm_batched_pcg": (C.c_int, [C.POINTER(BatchedPcgArgs), C.c_void_p]),
     "tm_pcg_partials_bytes": (C.c_size_t, []),
     "tm_pcg_start": (C.c_int, [C.POINTER(PcgArgs), C.c_void_p]),
+    "tm_bicgstab_start": (C.c_int, [C.POINTER(BicgstabArgs), C.c_void_p]),
+    "tm_bicgstab_iterate": (C.c_int, [C.POINTER(BicgstabArgs), C.c_int32, C.c_void_p]),
     "tm_pcg_iterate": (C.c_int, [C.POINTER(PcgArgs), C.c_int32, C.c_void_p]),
     "tm_pcg_iterate_until": (C.c_int, [C.POINTER(PcgArgs), C.c_int32, C.c_double, C.c_void_p]),
 }

@@ -121,22 +121,29 @@ class LoadAssembly(torch.autograd.Function):
 
 
 class SparseSolve(torch.autograd.Function):
-    """x = A^-1 b for a symmetric positive definite SparseMatrix A."""
+    """x = A^-1 b for a SparseMatrix A: Jacobi-PCG (``method="cg"``, A
+    symmetric positive definite) or Jacobi-BiCGSTAB (``"bicgstab"``).  The
+    backward solves A^T lam = dL/dx and returns dL/db = lam and dL/dA_ij =
+    -lam_i x_j (the reference's SparseSolveTorch.backward,
+    sparse/solve/torch_solve.py:262-270)."""
 
     @staticmethod
     def forward(ctx, values, b, A, kwargs):
-        from .solve import pcg_solve
-        x = pcg_solve(A.with_values(values.detach()), b.detach(), **kwargs)
-        ctx.A, ctx.kwargs = A, kwargs
+        from .solve import bicgstab_solve, pcg_solve
+        kw = dict(kwargs)
+        method = kw.pop("method", "cg")
+        solver = pcg_solve if method == "cg" else bicgstab_solve
+        x = solver(A.with_values(values.detach()), b.detach(), **kw)
+        ctx.A, ctx.kwargs, ctx.solver, ctx.method = A, kw, solver, method
         ctx.save_for_backward(values, x)
         return x
 
     @staticmethod
     def backward(ctx, gx):
-        from .solve import pcg_solve
         values, x = ctx.saved_tensors
         A = ctx.A.with_values(values.detach())
-        lam = pcg_solve(A, gx.detach(), **ctx.kwargs)
+        At = A if ctx.method == "cg" else A.transpose()
+        lam = ctx.solver(At, gx.detach(), **ctx.kwargs)
         gvals = None
         if ctx.needs_input_grad[0]:
             gvals = -lam[A.row_indices] * x[A.col_indices]

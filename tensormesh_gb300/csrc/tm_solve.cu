@@ -749,6 +749,285 @@ int pcg_iterate_until(const tm_pcg_args& a, int max_iter, double rtol, cudaStrea
     return pcg_iterate_until_l<R, H, 4>(a, max_iter, rtol, st);
 }
 
+// ---------------------------------------------------------------------------
+// Jacobi-preconditioned BiCGSTAB (right preconditioning, M^-1 = 1 / diag A)
+// for general square systems: the algorithm of the reference's bicgstab_py
+// (sparse/solve/torch_solve.py:130-248), with its safeguards: a missing or
+// |d| < 1e-12 diagonal counts as 1, |r0^ . v| < 1e-12 is a breakdown, omega
+// is 0 when t . t < 1e-12 (and the iteration stops after that update), and
+// the iteration stops when ||s|| or ||r|| reaches the threshold.  Scalars
+// stay on the device; every block takes the same decisions from the same
+// fixed-order sums, and one thread commits them at the end of an iteration.
+
+enum {
+    B_RHO = 0, B_DEN = 1, B_SS = 2, B_TT = 3, B_TS = 4, B_RR = 5, B_RHO_NEW = 6, B_BB = 7,
+    B_ITER = 8, B_FLAG = 9, B_THR2 = 10, B_ALPHA = 11, B_OMEGA = 12
+};
+
+// the decisions of the current iteration, identical in every block
+struct BicgState {
+    bool stop;      // the solve had ended before this iteration
+    bool brk;       // |r0^ . v| < 1e-12
+    bool sconv;     // ||s|| at the threshold: x += alpha p^ ends the solve
+    double alpha, omega;
+};
+__device__ __forceinline__ BicgState bicg_state(const double* sc) {
+    BicgState s;
+    s.stop = sc[B_FLAG] != 0.0;
+    const double den = sc[B_DEN];
+    s.brk = !(fabs(den) >= 1e-12);
+    s.alpha = s.brk ? 0.0 : sc[B_RHO] / den;
+    s.sconv = sc[B_SS] <= sc[B_THR2];
+    const double tt = sc[B_TT];
+    s.omega = !(fabs(tt) >= 1e-12) ? 0.0 : sc[B_TS] / tt;
+    return s;
+}
+
+// fixed-order block reduction of ND per-thread sums into partial[k * gridDim.x + blockIdx.x]
+template <int ND>
+__device__ __forceinline__ void block_partials(double (&v)[ND], double* partial) {
+    __shared__ double red[ND][kSolveThreads];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) red[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+#pragma unroll
+            for (int k = 0; k < ND; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < ND; ++k) partial[k * gridDim.x + blockIdx.x] = red[k][0];
+}
+
+// y = A x and the partials of w_k . y (w_k null: y . y); mode 0: skipped
+// once the solve has stopped, mode 1: also on breakdown or ||s|| converged
+template <typename R, int H, int ND>
+__global__ void __launch_bounds__(kSolveThreads) k_bicg_spmv(tm_linear_operator A, const R* x, R* y, const R* w0,
+                                                             const R* w1, double* partial, const double* sc,
+                                                             int mode) {
+    const int64_t n = A.n_rows * H;
+    const BicgState st = bicg_state(sc);
+    const bool skip = st.stop || (mode == 1 && (st.brk || st.sconv));
+    const R* w[2] = {w0, w1};
+    double acc[ND];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) acc[k] = 0.0;
+    auto take = [&](int64_t r, double s) {
+        y[r] = (R)s;
+#pragma unroll
+        for (int k = 0; k < ND; ++k) acc[k] += (w[k] ? (double)w[k][r] : s) * s;
+    };
+    if (!skip) {
+        if constexpr (H == 1) {
+            const int lane = threadIdx.x & 7, grp = threadIdx.x >> 3;
+            const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
+            for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
+                const int64_t r = base + grp < n ? base + grp : -1;
+                const double s = group_sum(r >= 0 ? row_partial<R, H>(A, x, r, lane) : 0.0);
+                if (r >= 0 && lane == 0) take(r, s);
+            }
+        } else {
+            constexpr int L = kBlockLanes;
+            const int lane = threadIdx.x & (L - 1), grp = threadIdx.x / L;
+            const int64_t nb = A.n_rows, groups_total = (int64_t)gridDim.x * (kSolveThreads / L);
+            for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / L); base < nb; base += groups_total) {
+                const int64_t bi = base + grp < nb ? base + grp : -1;
+                double s[H];
+                if (bi >= 0) {
+                    block_row_cg<R, H, L, false>(A, x, bi, lane, s);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < H; ++c) s[c] = 0;
+                }
+                const double u = group4_scatter<H>(s, lane);
+                if (bi >= 0 && lane < H) take(bi * H + lane, u);
+            }
+        }
+    }
+    block_partials<ND>(acc, partial);
+}
+
+// x0 given: minv, r = b - A x, r0^ = r, p = r; partials r.r (= rho) and b.b
+template <typename R, int H>
+__global__ void __launch_bounds__(kSolveThreads) k_bicg_start(tm_linear_operator A, const R* b, const R* x, R* r,
+                                                              R* r0h, R* p, R* minv, double* partial) {
+    const int64_t n = A.n_rows * H;
+    const R* val = static_cast<const R*>(A.values);
+    const int lane = threadIdx.x & 7, grp = threadIdx.x >> 3;
+    double acc[2] = {0.0, 0.0};
+    const int64_t groups_total = (int64_t)gridDim.x * (kSolveThreads / 8);
+    for (int64_t base = (int64_t)blockIdx.x * (kSolveThreads / 8); base < n; base += groups_total) {
+        const int64_t i = base + grp;
+        const double ax = group_sum(i < n ? row_partial<R, H>(A, x, i, lane) : 0.0);
+        if (i < n && lane == 0) {
+            const int64_t br = i / H;
+            const int a = (int)(i - br * H);
+            double d = 1.0;                              // a missing diagonal counts as 1
+            bool found = false;
+            for (int64_t q = A.row_ptr[br]; q < A.row_ptr[br + 1]; ++q)
+                if (A.col[q] == br) {
+                    d = found ? d + (double)val[q * H * H + a * H + a] : (double)val[q * H * H + a * H + a];
+                    found = true;
+                }
+            if (!(fabs(d) >= 1e-12)) d = 1.0;
+            minv[i] = (R)(1.0 / d);
+            const double ri = (double)b[i] - ax;
+            r[i] = (R)ri;
+            r0h[i] = (R)ri;
+            p[i] = (R)ri;
+            acc[0] += ri * ri;
+            acc[1] += (double)b[i] * (double)b[i];
+        }
+    }
+    block_partials<2>(acc, partial);
+}
+
+// fixed-order sum of the per-block partials of ND dots into sc[slot_k]; with
+// start set, also the initial scalars (threshold from atol, rtol and ||b||)
+template <int ND>
+__global__ void k_bicg_reduce(const double* partial, int n, double* sc, int s0, int s1, int start, double atol,
+                              double rtol) {
+    __shared__ double red[kSolveThreads];
+    const int slots[2] = {s0, s1};
+    for (int v = 0; v < ND; ++v) {
+        double s = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[v * n + i];
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) sc[slots[v]] = red[0];
+        __syncthreads();
+    }
+    if (start && threadIdx.x == 0) {
+        // rho = r0^ . r = r . r at the start; rr = r . r
+        sc[B_RR] = sc[B_RHO];
+        const double thr = fmax(atol, rtol * sqrt(sc[B_BB]));
+        sc[B_THR2] = thr * thr;
+        sc[B_ITER] = 0.0;
+        sc[B_DEN] = sc[B_SS] = sc[B_TT] = sc[B_TS] = 0.0;
+        sc[B_ALPHA] = sc[B_OMEGA] = 0.0;
+        sc[B_FLAG] = sc[B_RR] <= sc[B_THR2] ? 1.0 : 0.0;
+    }
+}
+
+// p^ = minv p
+template <typename R>
+__global__ void __launch_bounds__(kSolveThreads) k_bicg_phat(int64_t n, const R* p, const R* minv, R* ph,
+                                                             const double* sc) {
+    if (sc[B_FLAG] != 0.0) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        ph[i] = (R)((double)minv[i] * (double)p[i]);
+}
+
+// s = r - alpha v (into r), s^ = minv s; partial s . s
+template <typename R>
+__global__ void __launch_bounds__(kSolveThreads) k_bicg_s(int64_t n, R* r, const R* v, const R* minv, R* sh,
+                                                          double* partial, const double* sc) {
+    const BicgState st = bicg_state(sc);
+    double acc[1] = {0.0};
+    if (!st.stop && !st.brk)
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+            const double si = (double)r[i] - st.alpha * (double)v[i];
+            r[i] = (R)si;
+            sh[i] = (R)((double)minv[i] * si);
+            acc[0] += si * si;
+        }
+    block_partials<1>(acc, partial);
+}
+
+// x += alpha p^ (+ omega s^), r = s - omega t; partials r . r and r0^ . r
+template <typename R>
+__global__ void __launch_bounds__(kSolveThreads) k_bicg_x(int64_t n, R* x, R* r, const R* r0h, const R* ph,
+                                                          const R* sh, const R* t, double* partial, const double* sc) {
+    const BicgState st = bicg_state(sc);
+    const bool upd = !st.stop && !st.brk;
+    double acc[2] = {0.0, 0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double ri = (double)r[i];
+        if (upd) {
+            double xi = (double)x[i] + st.alpha * (double)ph[i];
+            if (!st.sconv) {
+                xi += st.omega * (double)sh[i];
+                ri -= st.omega * (double)t[i];
+                r[i] = (R)ri;
+            }
+            x[i] = (R)xi;
+        }
+        acc[0] += ri * ri;
+        acc[1] += (double)r0h[i] * ri;
+    }
+    block_partials<2>(acc, partial);
+}
+
+// p = r + beta (p - omega v)
+template <typename R>
+__global__ void __launch_bounds__(kSolveThreads) k_bicg_p(int64_t n, const R* r, R* p, const R* v, const double* sc) {
+    const BicgState st = bicg_state(sc);
+    if (st.stop || st.brk || st.sconv || sc[B_RR] <= sc[B_THR2] || st.omega == 0.0) return;
+    const double beta = (sc[B_RHO_NEW] / sc[B_RHO]) * (st.alpha / st.omega);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = (R)((double)r[i] + beta * ((double)p[i] - st.omega * (double)v[i]));
+}
+
+// the end of an iteration: flag (1 converged, 2 breakdown), rho, counter
+__global__ void k_bicg_commit(double* sc) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const BicgState st = bicg_state(sc);
+    if (st.stop) return;
+    sc[B_ITER] += 1.0;
+    sc[B_ALPHA] = st.alpha;
+    sc[B_OMEGA] = st.omega;
+    if (st.brk)
+        sc[B_FLAG] = 2.0;
+    else if (st.sconv || sc[B_RR] <= sc[B_THR2])
+        sc[B_FLAG] = 1.0;
+    else if (st.omega == 0.0)
+        sc[B_FLAG] = 2.0;
+    else
+        sc[B_RHO] = sc[B_RHO_NEW];
+}
+
+template <typename R, int H>
+int bicg_start(const tm_bicgstab_args& a, cudaStream_t st) {
+    const int64_t n = a.A.n_rows * H;
+    R* w = static_cast<R*>(a.work);
+    const int g = grid_rows(n);
+    k_bicg_start<R, H><<<g, kSolveThreads, 0, st>>>(a.A, static_cast<const R*>(a.b), static_cast<const R*>(a.x),
+                                                      w, w + n, w + 2 * n, w + 7 * n, a.partials);
+    k_bicg_reduce<2><<<1, kSolveThreads, 0, st>>>(a.partials, g, a.scalars, B_RHO, B_BB, 1, a.atol, a.rtol);
+    return status("tm_bicgstab_start");
+}
+
+template <typename R, int H>
+int bicg_iterate(const tm_bicgstab_args& a, int n_iter, cudaStream_t st) {
+    const int64_t n = a.A.n_rows * H;
+    R* w = static_cast<R*>(a.work);
+    R *r = w, *r0h = w + n, *p = w + 2 * n, *v = w + 3 * n, *ph = w + 4 * n, *sh = w + 5 * n, *t = w + 6 * n,
+      *minv = w + 7 * n;
+    R* x = static_cast<R*>(a.x);
+    const int gr = grid_rows(n), gv = grid_vec(n);
+    double* sc = a.scalars;
+    for (int it = 0; it < n_iter; ++it) {
+        k_bicg_phat<R><<<gv, kSolveThreads, 0, st>>>(n, p, minv, ph, sc);
+        k_bicg_spmv<R, H, 1><<<gr, kSolveThreads, 0, st>>>(a.A, ph, v, r0h, nullptr, a.partials, sc, 0);
+        k_bicg_reduce<1><<<1, kSolveThreads, 0, st>>>(a.partials, gr, sc, B_DEN, 0, 0, 0.0, 0.0);
+        k_bicg_s<R><<<gv, kSolveThreads, 0, st>>>(n, r, v, minv, sh, a.partials, sc);
+        k_bicg_reduce<1><<<1, kSolveThreads, 0, st>>>(a.partials, gv, sc, B_SS, 0, 0, 0.0, 0.0);
+        k_bicg_spmv<R, H, 2><<<gr, kSolveThreads, 0, st>>>(a.A, sh, t, nullptr, r, a.partials, sc, 1);
+        k_bicg_reduce<2><<<1, kSolveThreads, 0, st>>>(a.partials, gr, sc, B_TT, B_TS, 0, 0.0, 0.0);
+        k_bicg_x<R><<<gv, kSolveThreads, 0, st>>>(n, x, r, r0h, ph, sh, t, a.partials, sc);
+        k_bicg_reduce<2><<<1, kSolveThreads, 0, st>>>(a.partials, gv, sc, B_RR, B_RHO_NEW, 0, 0.0, 0.0);
+        k_bicg_p<R><<<gv, kSolveThreads, 0, st>>>(n, r, p, v, sc);
+        k_bicg_commit<<<1, 32, 0, st>>>(sc);
+    }
+    return status("tm_bicgstab_iterate");
+}
+
 int check_op(const tm_linear_operator& A) {
     if (A.n_rows < 0 || (A.n_rows > 0 && (!A.row_ptr || !A.values || !A.col)))
         return tm_set_error(TM_ERR_INVALID_ARG, "linear operator: null arrays");
@@ -814,5 +1093,26 @@ extern "C" int tm_pcg_iterate(const tm_pcg_args* a, int32_t n_iter, tm_stream_t 
     const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     return dispatch_op(a->A, [&](auto r, auto h) {
         return pcg_iterate<decltype(r), decltype(h)::value>(*a, n_iter, st);
+    });
+}
+
+extern "C" int tm_bicgstab_start(const tm_bicgstab_args* a, tm_stream_t stream) {
+    if (!a || !a->b || !a->x || !a->work || !a->scalars || !a->partials || !(a->atol >= 0.0) || !(a->rtol >= 0.0))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_bicgstab_start: bad argument");
+    int s = check_op(a->A);
+    if (s) return s;
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    return dispatch_op(a->A, [&](auto r, auto h) { return bicg_start<decltype(r), decltype(h)::value>(*a, st); });
+}
+
+extern "C" int tm_bicgstab_iterate(const tm_bicgstab_args* a, int32_t n_iter, tm_stream_t stream) {
+    if (!a || n_iter < 0 || !a->x || !a->work || !a->scalars || !a->partials)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_bicgstab_iterate: bad argument");
+    int s = check_op(a->A);
+    if (s) return s;
+    if (a->A.n_rows == 0 || n_iter == 0) return TM_OK;
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    return dispatch_op(a->A, [&](auto r, auto h) {
+        return bicg_iterate<decltype(r), decltype(h)::value>(*a, n_iter, st);
     });
 }

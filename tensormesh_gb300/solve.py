@@ -1,8 +1,9 @@
-"""SpMV and Jacobi-preconditioned CG over ``SparseMatrix`` (GPU kernels of
-``csrc/tm_solve.cu``).
+"""SpMV, Jacobi-preconditioned CG and Jacobi-preconditioned BiCGSTAB over
+``SparseMatrix`` (GPU kernels of ``csrc/tm_solve.cu``).
 
 ``pcg_solve`` replaces ``SparseMatrix.solve`` for the symmetric positive
-definite systems of the assembly path.  The reference inherits ``solve``
+definite systems of the assembly path; ``bicgstab_solve`` the reference's
+``bicgstab_py`` for general square systems.  The reference inherits ``solve``
 from torch-sla (direct solvers, or CG for large systems,
 docs/source/user_guide/batched_workflows.rst:124-131); its in-tree Krylov
 templates are ``cg_py`` / ``bicgstab_py`` (sparse/solve/torch_solve.py:70-248).
@@ -104,6 +105,54 @@ def pcg_solve(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, rtol: float
         done += k
     _lib.check(lib.tm_device_fault(), "pcg_solve")
     info = SolveInfo(int(host[5]), rel, rel <= rtol, flag == 2.0 and rel > rtol)
+    if return_info:
+        return x, info
+    return x
+
+
+def bicgstab_solve(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, atol: float = 1e-5,
+                   rtol: float = 0.0, max_iter: int = 10000, check_every: int = 50, return_info: bool = False):
+    """Solve A x = b for a general square A with Jacobi-preconditioned
+    BiCGSTAB (the reference's ``bicgstab_py``,
+    sparse/solve/torch_solve.py:130-248: right preconditioning by
+    1 / diag(A), its breakdown and omega safeguards) until
+    ||b - A x|| <= max(atol, rtol ||b||).
+
+    Iterations run on the device with every scalar there
+    (``tm_bicgstab_iterate``); the host reads the residual between batches
+    of ``check_every`` iterations.  Where the reference warns that it did
+    not converge, this returns the iterate as well (``return_info`` tells)."""
+    lib = _register()
+    _lib.require_cuda(A.values, "SparseMatrix values")
+    dev, dt = A.values.device, A.values.dtype
+    b = b.to(device=dev, dtype=dt).contiguous()
+    n = A.shape[0]
+    x = torch.zeros(n, dtype=dt, device=dev) if x0 is None else x0.to(device=dev, dtype=dt).reshape(-1).clone()
+    work = torch.empty(8, n, dtype=dt, device=dev)
+    scal = torch.zeros(16, dtype=torch.float64, device=dev)
+    partials = torch.empty(lib.tm_pcg_partials_bytes() // 8, dtype=torch.float64, device=dev)
+    op, keep = operator_of(A)
+    args = _lib.BicgstabArgs()
+    args.A = op
+    args.b, args.x, args.work = _lib.ptr(b), _lib.ptr(x), _lib.ptr(work)
+    args.scalars, args.partials = _lib.ptr(scal), _lib.ptr(partials)
+    args.atol, args.rtol = float(atol), float(rtol)
+    stream = _lib.stream_handle(dev)
+    _lib.check(lib.tm_bicgstab_start(C.byref(args), stream), "tm_bicgstab_start")
+    host = torch.empty(16, dtype=torch.float64, pin_memory=True)
+    done = 0
+    while True:
+        host.copy_(scal, non_blocking=True)
+        torch.cuda.current_stream(dev).synchronize()
+        flag = float(host[_lib.TM_BICG_FLAG])
+        if flag != 0.0 or done >= max_iter:
+            break
+        k = min(check_every, max_iter - done)
+        _lib.check(lib.tm_bicgstab_iterate(C.byref(args), k, stream), "tm_bicgstab_iterate")
+        done += k
+    rr, bb = float(host[_lib.TM_BICG_RR]), float(host[_lib.TM_BICG_BB])
+    rel = (rr / bb) ** 0.5 if bb > 0 else rr ** 0.5
+    info = SolveInfo(int(host[_lib.TM_BICG_ITER]), rel, flag == 1.0, flag == 2.0)
     if return_info:
         return x, info
     return x

@@ -218,14 +218,34 @@ class SparseMatrix:
             return self.matvec(x)
         return torch.stack([self.matvec(x[:, j].contiguous()) for j in range(x.shape[1])], 1)
 
-    def solve(self, b: torch.Tensor, **kwargs) -> torch.Tensor:
-        """x = A^-1 b (A symmetric positive definite) by Jacobi-PCG;
-        differentiable in the values and in b."""
+    def transpose(self) -> "SparseMatrix":
+        """A^T with the same values array (entry k of A is entry k of A^T;
+        its CSR view orders them when it is built)."""
+        if self._block > 1:
+            H = self._block
+            vals = self.values.reshape(-1, H, H).transpose(1, 2).reshape(-1)
+            return SparseMatrix(vals, self._col_src, self._row_src, (self.shape[1], self.shape[0]), _block=H,
+                                _block_row=self._block_col, _block_col=self._block_row, _sorted=False)
+        return SparseMatrix(self.values, self.col_indices, self.row_indices, (self.shape[1], self.shape[0]),
+                            _sorted=False)
+
+    @property
+    def T(self) -> "SparseMatrix":
+        return self.transpose()
+
+    def solve(self, b: torch.Tensor, method: str = "cg", **kwargs) -> torch.Tensor:
+        """x = A^-1 b: method "cg" (Jacobi-PCG, A symmetric positive
+        definite; keyword arguments of ``pcg_solve``) or "bicgstab"
+        (Jacobi-BiCGSTAB, any square A; keyword arguments of
+        ``bicgstab_solve``); differentiable in the values and in b (the
+        adjoint solves with A^T)."""
+        if method not in ("cg", "bicgstab"):
+            raise ValueError(f"solve: method must be 'cg' or 'bicgstab', not {method!r}")
         if torch.is_grad_enabled() and (self.values.requires_grad or b.requires_grad):
             from .adjoint import SparseSolve
-            return SparseSolve.apply(self.values, b, self, kwargs)
-        from .solve import pcg_solve
-        return pcg_solve(self, b, **kwargs)
+            return SparseSolve.apply(self.values, b, self, dict(kwargs, method=method))
+        from .solve import bicgstab_solve, pcg_solve
+        return (pcg_solve if method == "cg" else bicgstab_solve)(self, b, **kwargs)
 
     def __repr__(self):
         return (f"SparseMatrix(shape={self.shape}, nnz={self.nnz}, dtype={self.dtype}, "

@@ -4,7 +4,7 @@ CPU in float64.
 
 Usage (from the repository root, with the reference source tree available)::
 
-    python tests/golden/make_golden.py /path/to/TensorMesh [--only=facet|--only=quad|--only=full]
+    python tests/golden/make_golden.py /path/to/TensorMesh [--only=facet|--only=quad|--only=full|--only=krylov]
 
 Writes
 
@@ -21,6 +21,9 @@ Writes
   slot-map hashes, fingerprints (``checksum()`` of ``oracle/fem_oracle.py``)
   and 64 sign sketches (``sketch()``) of every value array
   (``--only=full`` writes this file alone).
+* ``tests/golden/small_krylov.npz``: the reference's Jacobi-BiCGSTAB and its
+  autograd wrapper on a small non-symmetric system (``--only=krylov``
+  writes this file alone).
 
 The reference's user-level forms are written exactly as its documentation
 and examples write them (a ``forward(gradu, gradv, kappa)`` diffusion form,
@@ -99,6 +102,53 @@ def facet_golden(tm, to_ref, quads=False):
     print("wrote", name)
 
 
+def krylov_golden():
+    """The reference's Jacobi-BiCGSTAB (sparse/solve/torch_solve.py:130-248)
+    and its autograd wrapper SparseSolveTorch (:252-270) on a small
+    non-symmetric system: a 5-point convection-diffusion operator on a
+    15 x 15 grid (upwind convection, so A != A^T), seeded right-hand side and
+    loss weights.  Writes small_krylov.npz."""
+    from tensormesh.sparse.solve.torch_solve import SparseSolveTorch, bicgstab_py
+    g, c = 15, 0.7
+    n = g * g
+    rows, cols, vals = [], [], []
+    for iy in range(g):
+        for ix in range(g):
+            i = iy * g + ix
+            ent = {i: 4.0 + 2.0 * c}
+            if ix > 0:
+                ent[i - 1] = -1.0 - 2.0 * c        # upwind: flow in +x and +y
+            if ix < g - 1:
+                ent[i + 1] = -1.0
+            if iy > 0:
+                ent[i - g] = -1.0 - 0.5 * c
+            if iy < g - 1:
+                ent[i + g] = -1.0 + 0.5 * c
+            for j in sorted(ent):
+                rows.append(i)
+                cols.append(j)
+                vals.append(ent[j])
+    row = torch.tensor(rows, dtype=torch.int64)
+    col = torch.tensor(cols, dtype=torch.int64)
+    values = torch.tensor(vals, dtype=torch.float64)
+    # right-hand side and loss weights of size 1e6: the reference's absolute
+    # safeguards (|r0^ . v| and t . t against 1e-12) then leave atol = 1e-6,
+    # a relative residual near 1e-12, as the criterion that ends the solve
+    rng = np.random.default_rng(71)
+    b = torch.from_numpy(rng.uniform(-1.0, 1.0, n) * 1e6)
+    w = torch.from_numpy(rng.uniform(-1.0, 1.0, n) * 1e6)
+    x = bicgstab_py(torch.stack([row, col], 0), values, n, n, b, atol=1e-6, max_iter=2000)
+    # (SparseSolveTorch's backward passes the transposed indices, no longer
+    # row-major, to a COO tensor declared coalesced; its gradients on this
+    # system are not finite, so the fixture keeps the forward solve and the
+    # weights, and the tests check gradients against direct solves)
+    u = SparseSolveTorch.apply(values, row, col, (n, n), b, None, 1e-6, 2000)
+    np.savez_compressed(os.path.join(HERE, "small_krylov.npz"), row=row.numpy(), col=col.numpy(),
+                        values=values.numpy(), b=b.numpy(), w=w.numpy(), x=x.detach().numpy(),
+                        x_autograd_forward=u.detach().numpy())
+    print("wrote small_krylov.npz")
+
+
 def main(reference_root, only=None):
     import refshim
     refshim.install(reference_root)
@@ -138,6 +188,9 @@ def main(reference_root, only=None):
 
     if only == "facet":
         facet_golden(tm, to_ref)
+        return
+    if only == "krylov":
+        krylov_golden()
         return
     if only == "full":
         full_golden(tm, to_ref, KappaDiffusion, ElasticityE, Source)
