@@ -455,6 +455,9 @@ int tm_quadrature_points(int32_t dtype, int64_t n_elements, const int32_t* conn,
  * it: with k_mode TM_ADJ_K_OUTER the weights dL/dK_ab = -lambda_a u_b are
  * formed per element from the solution u and the adjoint lambda.
  *   k_mode TM_ADJ_K_CSR:   weights[nnz] = dL/dvalues, slot_map [E*B*B] int64
+ *   k_mode TM_ADJ_M_CSR:   the same weights on a mass matrix M_e =
+ *                          kappa_scale |det J| Mhat (grad_kappa: dL/dM_e
+ *                          contracted with |det J| Mhat, per element)
  *   load_source:           adds the term of b = |det J| beta weighted by lam
  * Outputs (either may be NULL): grad_kappa [E] (dL/dkappa, element order),
  * grad_points [N*D] (dL/dx, reduced with the node plan).
@@ -462,6 +465,7 @@ int tm_quadrature_points(int32_t dtype, int64_t n_elements, const int32_t* conn,
 #define TM_ADJ_K_NONE   0
 #define TM_ADJ_K_CSR    1
 #define TM_ADJ_K_OUTER  2
+#define TM_ADJ_M_CSR    3
 #define TM_ADJ_LOAD_NONE  0
 #define TM_ADJ_LOAD_CONST 1
 #define TM_ADJ_LOAD_NODAL 2

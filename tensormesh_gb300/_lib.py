@@ -106,7 +106,7 @@ class AdjointArgs(C.Structure):
     ]
 
 
-TM_ADJ_K_NONE, TM_ADJ_K_CSR, TM_ADJ_K_OUTER = 0, 1, 2
+TM_ADJ_K_NONE, TM_ADJ_K_CSR, TM_ADJ_K_OUTER, TM_ADJ_M_CSR = 0, 1, 2, 3
 TM_ADJ_LOAD_NONE, TM_ADJ_LOAD_CONST, TM_ADJ_LOAD_NODAL = 0, 1, 2
 
 

@@ -7,6 +7,9 @@ docs/source/user_guide/differentiability.rst:34-56).  Here:
 * ``DiffusionAssembly`` -- the values of a P1 diffusion matrix as a function
   of node coordinates and per-element kappa; its backward runs the
   ``tm_adjoint_p1`` kernel on dL/dvalues (CSR weights through the slot map).
+* ``MassAssembly`` -- the values of a P1 mass matrix as a function of node
+  coordinates and its scalar density; its backward runs ``tm_adjoint_p1``
+  in its mass mode (d|det J| / dJ = |det J| J^-T per element).
 * ``LoadAssembly`` -- a P1 load vector as a function of node coordinates.
 * ``SparseSolve`` -- x = A^-1 b with Jacobi-PCG; backward solves A^T lambda =
   dL/dx (A symmetric) and returns dL/dvalues = -lambda_row x_col, dL/db = lambda.
@@ -97,6 +100,53 @@ class DiffusionAssembly(torch.autograd.Function):
                                want_points=ctx.needs_input_grad[0])
         return (gp.to(points.dtype) if gp is not None else None,
                 gk.to(kappa.dtype) if gk is not None else None, None, None)
+
+
+class MassAssembly(torch.autograd.Function):
+    """values = M(points, rho) of a mass form (float64, P1; rho a scalar)."""
+
+    @staticmethod
+    def forward(ctx, points, rho, asm, sd):
+        from .assemble import assemble_forms
+        sdd = {k: (v.detach() if torch.is_tensor(v) else v) for k, v in sd.items()}
+        (values,) = assemble_forms([asm], points.detach(), {}, sdd)
+        ctx.asm = asm
+        r = asm._tm_coefficients({}, sdd, asm._topology.n_elements).get("rho")
+        ctx.rho = 1.0 if r is None else float(r)            # the kernel's mass scale
+        ctx.save_for_backward(points, values)
+        ctx.has_rho = rho is not None
+        return values
+
+    @staticmethod
+    def backward(ctx, gvals):
+        points, values = ctx.saved_tensors
+        asm = ctx.asm
+        topo = asm._topology
+        _require_p1(topo)
+        et = asm.element_types[0]
+        slot = asm.projector[et].indices.to(points.device)
+        gp = None
+        if ctx.needs_input_grad[0]:
+            _, gp = _adjoint_call(topo, points, None, ctx.rho, _lib.TM_ADJ_M_CSR, weights=gvals, slot=slot,
+                                  want_kappa=False, want_points=True)
+            gp = gp.to(points.dtype)
+        grho = None
+        if ctx.has_rho and ctx.needs_input_grad[1]:
+            # M is linear in rho: dL/drho = sum_i gvals_i M_i / rho (rho != 0), else from rho = 1
+            if ctx.rho != 0.0:
+                grho = (gvals * values).sum() / ctx.rho
+            else:
+                (m1,) = _mass_unit(asm, points)
+                grho = (gvals * m1).sum()
+        return gp, grho, None, None
+
+
+def _mass_unit(asm, points):
+    """The mass values at unit density (the kernel's mass scale 1)."""
+    from .assemble import assemble_forms
+    from .builtin import MassElementAssembler
+    unit = MassElementAssembler.from_assembler(asm) if not isinstance(asm, MassElementAssembler) else asm
+    return assemble_forms([unit], points.detach(), {}, {"rho": 1.0})
 
 
 class LoadAssembly(torch.autograd.Function):

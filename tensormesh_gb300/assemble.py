@@ -390,6 +390,15 @@ class ElementAssembler(_AssemblerBase):
         et, points, ed, sd = self._prepare(points, point_data, element_data, scalar_data)
         if torch.is_grad_enabled() and (points.requires_grad or any(
                 torch.is_tensor(v) and v.requires_grad for v in list(ed.values()) + list(sd.values()))):
+            if form == "mass":
+                from .adjoint import MassAssembly
+                rho = self._tm_coefficients(ed, sd, self.elements[et].shape[0]).get("rho")
+                if torch.is_tensor(rho) and rho.numel() != 1:
+                    raise NotImplementedError("a per-element coefficient of the mass form is not assembled by "
+                                              "tensormesh_gb300 (a scalar one is)")
+                rho_t = rho if torch.is_tensor(rho) and rho.requires_grad else None
+                values = MassAssembly.apply(points, rho_t, self, dict(sd))
+                return self._build_output(values)
             if form != "diffusion":
                 raise NotImplementedError(f"gradients of the {form} form are not implemented")
             from .adjoint import DiffusionAssembly

@@ -1,5 +1,6 @@
-// Hand-written adjoint of the P1 diffusion assembly (and of the load vector)
-// with respect to the per-element coefficient and the node coordinates.
+// Hand-written adjoint of the P1 diffusion and mass assembly (and of the load
+// vector) with respect to the per-element coefficient and the node
+// coordinates.
 //
 // The reference obtains these gradients by letting torch autograd run
 // backwards through its assembly graph (index_add_, the integrand, the
@@ -16,7 +17,8 @@
 //     dL/dkappa = w |det J| tr(P)
 //     dL/dJ     = kappa w |det J| M^T (tr(P) I - 2 P)
 // The load vector b_a = |det J| beta_a (beta from the mass / load template)
-// weighted by lambda_a adds (sum_a lambda_a b_a) M^T to dL/dJ.  dL/dJ is
+// weighted by lambda_a adds (sum_a lambda_a b_a) M^T to dL/dJ; a mass matrix
+// s |det J| Mhat weighted by W adds s |det J| (W : Mhat) M^T.  dL/dJ is
 // spread to the nodes (row i to node i+1, minus the row sum to node 0) and
 // reduced per node with the node chunk plan (fixed order, no atomics on
 // values).  The weights come either from a CSR array dL/dvalues through the
@@ -87,7 +89,22 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(const tm_adjoint_args a
         for (int r = 0; r < D; ++r)
 #pragma unroll
             for (int k = 0; k < D; ++k) GJ[r][k] = 0.0;
-        if constexpr (KMODE != TM_ADJ_K_NONE) {
+        if constexpr (KMODE == TM_ADJ_M_CSR) {
+            // M = s |det J| Mhat: dL/ds-part sum_ab W_ab Mhat_ab, and
+            // d|det J| / dJ = |det J| J^-T
+            double wm = 0.0;
+#pragma unroll
+            for (int p = 0; p < B; ++p)
+#pragma unroll
+                for (int q = 0; q < B; ++q) wm += ldg(wcsr + a.slot_map[(e * B + p) * B + q]) * tab[TL.mhat + p * B + q];
+            if (gkap) gkap[e] = adet * wm;
+            const double f = a.kappa_scale * adet * wm;
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int k = 0; k < D; ++k) GJ[r][k] += f * M[k][r];
+        }
+        if constexpr (KMODE == TM_ADJ_K_CSR || KMODE == TM_ADJ_K_OUTER) {
             double W[B][B];
 #pragma unroll
             for (int p = 0; p < B; ++p)
@@ -224,6 +241,7 @@ int dispatch_kmode(const tm_adjoint_args& a, cudaStream_t st) {
         case TM_ADJ_K_NONE: return dispatch_load<ET, TM_ADJ_K_NONE>(a, st);
         case TM_ADJ_K_CSR: return dispatch_load<ET, TM_ADJ_K_CSR>(a, st);
         case TM_ADJ_K_OUTER: return dispatch_load<ET, TM_ADJ_K_OUTER>(a, st);
+        case TM_ADJ_M_CSR: return dispatch_load<ET, TM_ADJ_M_CSR>(a, st);
         default: return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_p1: unknown k_mode");
     }
 }
@@ -249,7 +267,7 @@ extern "C" int tm_adjoint_p1(const tm_adjoint_args* a, tm_stream_t stream) {
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_p1: expects a node plan of the mesh");
     if (!a->tables.packed || (a->plan.n_elements > 0 && !a->points))
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_p1: null tables or points");
-    if (a->k_mode == TM_ADJ_K_CSR && (!a->weights || !a->slot_map))
+    if ((a->k_mode == TM_ADJ_K_CSR || a->k_mode == TM_ADJ_M_CSR) && (!a->weights || !a->slot_map))
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_p1: CSR weights need weights and slot_map");
     if (a->k_mode == TM_ADJ_K_OUTER && (!a->u || !a->lam))
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_p1: outer-product weights need u and lam");
