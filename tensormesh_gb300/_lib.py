@@ -106,6 +106,14 @@ class AdjointArgs(C.Structure):
     ]
 
 
+class ElasticGradArgs(C.Structure):
+    _fields_ = [
+        ("n_points", C.c_int64), ("points", C.c_void_p), ("weights", C.c_void_p), ("slot_map", C.c_void_p),
+        ("young_scale", C.c_double), ("poisson", C.c_double), ("grad_young", C.c_void_p),
+        ("tables", ElementTables), ("plan", ChunkPlan),
+    ]
+
+
 TM_ADJ_K_NONE, TM_ADJ_K_CSR, TM_ADJ_K_OUTER, TM_ADJ_M_CSR = 0, 1, 2, 3
 TM_ADJ_LOAD_NONE, TM_ADJ_LOAD_CONST, TM_ADJ_LOAD_NODAL = 0, 1, 2
 
@@ -194,6 +202,7 @@ _SIGNATURES = {
                           C.c_void_p]),
     "tm_adjoint_workspace_bytes": (C.c_size_t, [C.POINTER(AdjointArgs)]),
     "tm_adjoint_p1": (C.c_int, [C.POINTER(AdjointArgs), C.c_void_p]),
+    "tm_elastic_grad_young": (C.c_int, [C.POINTER(ElasticGradArgs), C.c_void_p]),
     "tm_batched_pcg": (C.c_int, [C.POINTER(BatchedPcgArgs), C.c_void_p]),
     "tm_pcg_partials_bytes": (C.c_size_t, []),
     "tm_pcg_start": (C.c_int, [C.POINTER(PcgArgs), C.c_void_p]),

@@ -10,6 +10,9 @@ docs/source/user_guide/differentiability.rst:34-56).  Here:
 * ``MassAssembly`` -- the values of a P1 mass matrix as a function of node
   coordinates and its scalar density; its backward runs ``tm_adjoint_p1``
   in its mass mode (d|det J| / dJ = |det J| J^-T per element).
+* ``ElasticityAssembly`` -- the values of an isotropic elasticity matrix as
+  a function of its modulus (``tm_elastic_grad_young``: dL/dE_e is the
+  contraction of dL/dvalues with the element's blocks at unit modulus).
 * ``LoadAssembly`` -- a P1 load vector as a function of node coordinates.
 * ``SparseSolve`` -- x = A^-1 b with Jacobi-PCG; backward solves A^T lambda =
   dL/dx (A symmetric) and returns dL/dvalues = -lambda_row x_col, dL/db = lambda.
@@ -147,6 +150,53 @@ def _mass_unit(asm, points):
     from .builtin import MassElementAssembler
     unit = MassElementAssembler.from_assembler(asm) if not isinstance(asm, MassElementAssembler) else asm
     return assemble_forms([unit], points.detach(), {}, {"rho": 1.0})
+
+
+def elastic_grad_young(topo, points, gvals, slot, young_scale, poisson):
+    """dL/dE_e = young_scale sum_ab W[slot(e,a,b)] : K_e[a][b](E = 1), element
+    order (``tm_elastic_grad_young``)."""
+    lib = _lib.load()
+    dev = points.device
+    pts = points.detach().to(torch.float64).contiguous()
+    w = gvals.detach().to(torch.float64).contiguous()
+    plan = topo.node_plan(dev)
+    a = _lib.ElasticGradArgs()
+    a.n_points = topo.n_points
+    a.points, a.weights, a.slot_map = _lib.ptr(pts), _lib.ptr(w), _lib.ptr(slot)
+    a.young_scale, a.poisson = float(young_scale), float(poisson)
+    g = torch.empty(topo.n_elements, dtype=torch.float64, device=dev)
+    a.grad_young = _lib.ptr(g)
+    a.tables = topo.table_struct(dev)
+    a.plan = plan.struct()
+    _lib.check(lib.tm_elastic_grad_young(C.byref(a), _lib.stream_handle(dev)), "tm_elastic_grad_young")
+    return g
+
+
+class ElasticityAssembly(torch.autograd.Function):
+    """values = K(E) of an isotropic elasticity form (float64, any element
+    type) as a function of its modulus E (per element or a scalar tensor;
+    ``coefs``: the form's other kernel coefficients, nu and E_scale); the
+    backward runs ``tm_elastic_grad_young`` on dL/dvalues."""
+
+    @staticmethod
+    def forward(ctx, young, points, asm, coefs):
+        from .assemble import _assemble_on
+        c = dict(coefs, E=young.detach())
+        topo = asm._topology
+        (values,) = _assemble_on([asm], topo, points.detach(), {}, {}, None, None, _coefs=[c])
+        ctx.asm, ctx.nu, ctx.escale = asm, float(c.get("nu", 0.3)), float(c.get("E_scale", 1.0))
+        ctx.save_for_backward(points, young)
+        return values
+
+    @staticmethod
+    def backward(ctx, gvals):
+        points, young = ctx.saved_tensors
+        asm = ctx.asm
+        et = asm.element_types[0]
+        slot = asm.projector[et].indices.to(points.device)
+        g = elastic_grad_young(asm._topology, points, gvals, slot, ctx.escale, ctx.nu)
+        gy = g if young.dim() > 0 and young.numel() > 1 else g.sum().reshape(young.shape)
+        return gy.to(young.dtype), None, None, None
 
 
 class LoadAssembly(torch.autograd.Function):

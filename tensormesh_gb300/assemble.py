@@ -122,13 +122,26 @@ class _AssemblerBase(nn.Module):
 class RecognisedForm:
     """A user ``forward`` identified as a built-in family: ``form`` is
     "diffusion", "mass" or "elasticity", ``coef`` the name of its coefficient
-    argument (or None) and ``nu`` the Poisson ratio of an elasticity form."""
+    argument (or None) and ``nu`` the Poisson ratio of an elasticity form.
+    The family's modulus (kappa, rho or E) is ``scale * c`` for a form
+    linear in its coefficient c, else ``cmap(c)``: the form evaluated per
+    element on fixed probe arguments (``torch.func.vmap`` over c, as the
+    reference vmaps ``forward``), differentiable in c."""
 
-    def __init__(self, form: str, coef: Optional[str], nu: float = 0.3, scale: float = 1.0):
-        self.form, self.coef, self.nu, self.scale = form, coef, nu, scale
+    def __init__(self, form: str, coef: Optional[str], nu: float = 0.3, scale: float = 1.0, cmap=None):
+        self.form, self.coef, self.nu, self.scale, self.cmap = form, coef, nu, scale, cmap
+
+    def modulus(self, c):
+        """The family's modulus for the coefficient value(s) c."""
+        if self.cmap is not None:
+            return self.cmap(c)
+        if self.scale == 1.0:
+            return c
+        return c * self.scale if torch.is_tensor(c) else float(c) * self.scale
 
     def __repr__(self):
-        return f"RecognisedForm({self.form!r}, coef={self.coef!r}, nu={self.nu}, scale={self.scale})"
+        return (f"RecognisedForm({self.form!r}, coef={self.coef!r}, nu={self.nu}, scale={self.scale}, "
+                f"nonlinear={self.cmap is not None})")
 
 
 _FIELD_ARGS = ("gradu", "gradv", "u", "v", "x")
@@ -198,45 +211,113 @@ def _probe(asm) -> Optional[RecognisedForm]:
         with torch.no_grad():
             return torch.as_tensor(asm.forward(**kw))
 
-    if fields == {"u", "v"}:
-        for gu, gv, u, v, c in draws:
-            if not _close(call(gu, gv, u, v, c), (c if coef else 1.0) * u * v):
+    def scalar_map(base_of):
+        """s(c) per draw for out = s(c) base(args), checked on a second
+        argument set at the same c; the linear scale or a per-element map."""
+        svals = []
+        for k, (gu, gv, u, v, c) in enumerate(draws):
+            base = base_of(gu, gv, u, v)
+            if abs(float(base)) < 1e-3:
                 return None
-        return RecognisedForm("mass", coef)
+            sk = float(call(gu, gv, u, v, c)) / float(base)
+            gu2, gv2, u2, v2, _ = draws[(k + 1) % len(draws)]
+            if not _close(call(gu2, gv2, u2, v2, c), sk * base_of(gu2, gv2, u2, v2)):
+                return None
+            svals.append((c, sk))
+        return svals
+
+    def make_cmap(evaluate):
+        """c (a scalar or one value per element, on any device) -> the
+        modulus, with autograd; the probe arguments follow c's device."""
+        def cmap(c):
+            ct = torch.as_tensor(c, dtype=torch.float64)
+            ev = lambda ci: evaluate(ci, ct.device)
+            if ct.dim() == 0:
+                return ev(ct)
+            return torch.func.vmap(ev)(ct.reshape(-1))
+        return cmap
+
+    def classify(svals, family, base0, extra=None):
+        extra = extra or {}
+        if coef is None:
+            return RecognisedForm(family, None, scale=svals[0][1], **extra)
+        ratios = [sk / c for c, sk in svals]
+        if all(abs(r - ratios[0]) <= 1e-12 * max(1.0, abs(ratios[0])) for r in ratios):
+            return RecognisedForm(family, coef, scale=ratios[0], **extra)
+        return RecognisedForm(family, coef, cmap=make_cmap(base0), **extra)
+
+    if fields == {"u", "v"}:
+        svals = scalar_map(lambda gu, gv, u, v: u * v)
+        if svals is None:
+            return None
+        gu0, gv0, u0, v0, _ = draws[0]
+
+        def ev_mass(ci, dev):
+            u, v = u0.to(dev), v0.to(dev)
+            kw = {"u": u, "v": v}
+            if coef:
+                kw[coef] = ci
+            return asm.forward(**kw) / (u * v)
+        return classify(svals, "mass", ev_mass)
     if fields != {"gradu", "gradv"}:
         return None
     gu, gv, u, v, c = draws[0]
     out = call(gu, gv, u, v, c)
     if out.dim() == 0:
-        for gu, gv, u, v, c in draws:
-            if not _close(call(gu, gv, u, v, c), (c if coef else 1.0) * (gu @ gv)):
-                return None
-        return RecognisedForm("diffusion", coef)
+        svals = scalar_map(lambda gu, gv, u, v: gu @ gv)
+        if svals is None:
+            return None
+        gu0, gv0 = draws[0][0], draws[0][1]
+
+        def ev_diff(ci, dev):
+            gu, gv = gu0.to(dev), gv0.to(dev)
+            kw = {"gradu": gu, "gradv": gv}
+            if coef:
+                kw[coef] = ci
+            return asm.forward(**kw) / (gu @ gv)
+        return classify(svals, "diffusion", ev_diff)
     if tuple(out.shape) != (D, D):
         return None
 
     def basis(gu, gv):
         return torch.outer(gu, gv), torch.outer(gv, gu) + (gu @ gv) * torch.eye(D, dtype=torch.float64)
 
-    # lam and mu per unit coefficient from the first draw (least squares),
-    # then every draw must reproduce the block
-    a, b = basis(gu, gv)
-    scale = c if coef else 1.0
-    A = torch.stack([a.reshape(-1), b.reshape(-1)], 1) * scale
-    sol = torch.linalg.lstsq(A, out.reshape(-1, 1).to(torch.float64)).solution.reshape(-1)
-    lam, mu = float(sol[0]), float(sol[1])
-    if not (mu > 0 and lam + mu > 0):
-        return None
-    for gu, gv, u, v, c in draws:
+    # per draw: lam and mu of the block at that draw's coefficient (least
+    # squares on its gradients), checked on a second gradient pair at the
+    # same coefficient; lam / mu must be the same for every draw (one
+    # Poisson ratio), and the modulus per unit coefficient linear or a map
+    fits = []
+    for k, (gu, gv, u, v, c) in enumerate(draws):
         a, b = basis(gu, gv)
-        if not _close(call(gu, gv, u, v, c), (c if coef else 1.0) * (lam * a + mu * b)):
+        A = torch.stack([a.reshape(-1), b.reshape(-1)], 1)
+        sol = torch.linalg.lstsq(A, call(gu, gv, u, v, c).reshape(-1, 1).to(torch.float64)).solution.reshape(-1)
+        lam, mu = float(sol[0]), float(sol[1])
+        if not (mu > 0 and lam + mu > 0):
             return None
-    # the kernel's moduli: lam = E nu / ((1 + nu)(1 - 2 nu)), mu = E / (2 (1 + nu));
-    # E per unit coefficient is the form's scale
-    nu = lam / (2.0 * (lam + mu))
+        gu2, gv2 = draws[(k + 1) % len(draws)][:2]
+        a2, b2 = basis(gu2, gv2)
+        if not _close(call(gu2, gv2, u, v, c), lam * a2 + mu * b2):
+            return None
+        fits.append((c, lam, mu))
+    if any(abs(l / m - fits[0][1] / fits[0][2]) > 1e-12 * max(1.0, abs(fits[0][1] / fits[0][2]))
+           for _, l, m in fits):
+        return None
+    # the kernel's moduli: lam = E nu / ((1 + nu)(1 - 2 nu)), mu = E / (2 (1 + nu))
+    lam0, mu0 = fits[0][1], fits[0][2]
+    nu = lam0 / (2.0 * (lam0 + mu0))
     if not (-1.0 < nu < 0.5):
         return None
-    return RecognisedForm("elasticity", coef, nu, scale=2.0 * mu * (1.0 + nu))
+    svals = [(c, 2.0 * m * (1.0 + nu)) for c, _, m in fits]          # E at each draw
+    gu0, gv0 = draws[0][0], draws[0][1]
+    a0, b0 = basis(gu0, gv0)
+    pinv = torch.linalg.pinv(torch.stack([a0.reshape(-1), b0.reshape(-1)], 1))
+
+    def ev_el(ci, dev):
+        kw = {"gradu": gu0.to(dev), "gradv": gv0.to(dev)}
+        if coef:
+            kw[coef] = ci
+        return 2.0 * (1.0 + nu) * (pinv[1].to(dev) @ asm.forward(**kw).reshape(-1))
+    return classify(svals, "elasticity", ev_el, {"nu": nu})
 
 
 # ============================================================================
@@ -399,6 +480,22 @@ class ElementAssembler(_AssemblerBase):
                 rho_t = rho if torch.is_tensor(rho) and rho.requires_grad else None
                 values = MassAssembly.apply(points, rho_t, self, dict(sd))
                 return self._build_output(values)
+            if form == "elasticity":
+                if points.requires_grad:
+                    raise NotImplementedError("gradients of the elasticity form with respect to the node "
+                                              "coordinates are not implemented (with respect to the modulus "
+                                              "they are)")
+                c = self._tm_coefficients(ed, sd, self.elements[et].shape[0])
+                young = c.get("E")
+                if torch.is_tensor(c.get("nu")) and c["nu"].requires_grad:
+                    raise NotImplementedError("gradients with respect to the Poisson ratio are not implemented")
+                if torch.is_tensor(young) and young.requires_grad:
+                    from .adjoint import ElasticityAssembly
+                    rest = {k: v for k, v in c.items() if k != "E"}
+                    values = ElasticityAssembly.apply(young, points, self, rest)
+                    return self._build_output(values)
+                (values,) = assemble_forms([self], points, ed, sd)
+                return self._build_output(values)
             if form != "diffusion":
                 raise NotImplementedError(f"gradients of the {form} form are not implemented")
             from .adjoint import DiffusionAssembly
@@ -451,14 +548,15 @@ class ElementAssembler(_AssemblerBase):
             if c is None:
                 raise KeyError(f"{type(self).__name__}.forward takes {rec.coef!r}: pass it in element_data "
                                f"(one value per element) or scalar_data")
+        if rec.form == "mass" and torch.is_tensor(c) and c.dim() > 0 and c.numel() > 1:
+            raise NotImplementedError("a per-element coefficient of the mass form is not assembled by "
+                                      "tensormesh_gb300 (a scalar one is)")
+        m = rec.scale if c is None else rec.modulus(c)
         if rec.form == "diffusion":
-            return {"kappa": c}
+            return {"kappa": m}
         if rec.form == "mass":
-            if torch.is_tensor(c) and c.dim() > 0 and c.numel() > 1:
-                raise NotImplementedError("a per-element coefficient of the mass form is not assembled by "
-                                          "tensormesh_gb300 (a scalar one is)")
-            return {"rho": c}
-        return {"E": 1.0 if c is None else c, "nu": rec.nu, "E_scale": rec.scale}
+            return {"rho": m}
+        return {"E": m, "nu": rec.nu}
 
     def forward(self, *args, **kwargs):
         raise NotImplementedError("forward is not implemented")
@@ -563,8 +661,9 @@ def _assemble_mixed(assemblers, topo: "MixedTopology", points, ed, sd):
             for i in range(len(assemblers))]
 
 
-def _assemble_on(assemblers, topo: Topology, points, ed, sd, _events, _stats):
-    """The fused launches of ``assemble_forms`` on one element type."""
+def _assemble_on(assemblers, topo: Topology, points, ed, sd, _events, _stats, _coefs=None):
+    """The fused launches of ``assemble_forms`` on one element type
+    (``_coefs``: the assemblers' kernel coefficients, resolved already)."""
     E = topo.n_elements
     dev, dt = points.device, points.dtype
     pts = points.detach().contiguous()
@@ -595,7 +694,7 @@ def _assemble_on(assemblers, topo: Topology, points, ed, sd, _events, _stats):
             a = assemblers[i]
             f = forms[i]
             bits |= _FORM_BITS[f]
-            c = a._tm_coefficients(ed, sd, E)
+            c = _coefs[i] if _coefs is not None else a._tm_coefficients(ed, sd, E)
             if f == "diffusion":
                 t, s = _coef(c.get("kappa"), dt, dev, E, "kappa")
                 args.kappa, args.kappa_scale = _lib.ptr(t), s

@@ -233,19 +233,55 @@ class SparseMatrix:
     def T(self) -> "SparseMatrix":
         return self.transpose()
 
-    def solve(self, b: torch.Tensor, method: str = "cg", **kwargs) -> torch.Tensor:
-        """x = A^-1 b: method "cg" (Jacobi-PCG, A symmetric positive
+    # direct methods of the inherited solve (torch-sla); here iterative
+    # solves to a tight tolerance stand in for them
+    _DIRECT = ("lu", "cholesky", "ldlt", "umfpack", "superlu", "direct", "qr")
+    _DIRECT_BACKENDS = ("scipy", "cudss", "cupy", "eigen", "petsc")
+
+    def solve(self, b: torch.Tensor, method: Optional[str] = None, **kwargs) -> torch.Tensor:
+        """x = A^-1 b on the GPU: "cg" (Jacobi-PCG, A symmetric positive
         definite; keyword arguments of ``pcg_solve``) or "bicgstab"
         (Jacobi-BiCGSTAB, any square A; keyword arguments of
         ``bicgstab_solve``); differentiable in the values and in b (the
-        adjoint solves with A^T)."""
-        if method not in ("cg", "bicgstab"):
-            raise ValueError(f"solve: method must be 'cg' or 'bicgstab', not {method!r}")
+        adjoint solves with A^T).
+
+        The keywords of the solve the reference's SparseMatrix inherits
+        (torch-sla: ``backend``, ``method``, ``preconditioner``, ``tol``,
+        ``atol``, ``max_iter``, ``x0``, ``is_spd``, ``verbose``) are
+        accepted: the kernels of this library run on the matrix's device
+        whatever the ``backend``, the preconditioner is Jacobi, ``tol`` is
+        the relative residual, and a direct method or ``method=None``
+        selects CG for an SPD matrix (``is_spd``, default True) and BiCGSTAB
+        otherwise; a direct method, or no method with a backend whose
+        default is direct (``"scipy"``, ``"cudss"``, ...), solves to a
+        relative residual of 1e-12 unless ``tol`` says otherwise."""
+        kw = dict(kwargs)
+        backend = str(kw.pop("backend", "auto") or "auto").lower()
+        kw.pop("verbose", None)
+        kw.pop("preconditioner", None)
+        is_spd = bool(kw.pop("is_spd", True))
+        tol = kw.pop("tol", None)
+        m = (method or "auto").lower()
+        # a direct method, or a backend whose default is one, asks for a
+        # solution accurate to rounding
+        direct = m in self._DIRECT or (method is None and backend in self._DIRECT_BACKENDS)
+        if m in ("auto", "default") or direct:
+            m = "cg" if is_spd else "bicgstab"
+        if m not in ("cg", "bicgstab"):
+            raise ValueError(f"solve: method must be 'cg', 'bicgstab', a direct method or None, not {method!r}")
+        if tol is None and direct and "rtol" not in kw and "atol" not in kw:
+            tol = 1e-12
+        if tol is not None:
+            kw["rtol"] = float(tol)
+            if m == "bicgstab":
+                kw.setdefault("atol", 0.0)
+        if m == "cg":
+            kw.pop("atol", None)
         if torch.is_grad_enabled() and (self.values.requires_grad or b.requires_grad):
             from .adjoint import SparseSolve
-            return SparseSolve.apply(self.values, b, self, dict(kwargs, method=method))
+            return SparseSolve.apply(self.values, b, self, dict(kw, method=m))
         from .solve import bicgstab_solve, pcg_solve
-        return (pcg_solve if method == "cg" else bicgstab_solve)(self, b, **kwargs)
+        return (pcg_solve if m == "cg" else bicgstab_solve)(self, b, **kw)
 
     def __repr__(self):
         return (f"SparseMatrix(shape={self.shape}, nnz={self.nnz}, dtype={self.dtype}, "

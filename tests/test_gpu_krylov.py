@@ -91,3 +91,23 @@ def test_bicgstab_float32(cuda):
     assert x.dtype == torch.float32 and info.converged
     xs = spl.spsolve(As.tocsc(), d["b"])
     assert np.linalg.norm(x.double().cpu().numpy() - xs) <= 1e-4 * np.linalg.norm(xs)
+
+
+def test_solve_accepts_the_inherited_keywords(cuda):
+    """SparseMatrix.solve with the keywords of the solve the reference's
+    SparseMatrix inherits (as its examples call it: ``K.solve(F,
+    backend="scipy")``, ``method="lu"``, ``is_spd=False``)."""
+    m = tg.gen_unit_square(16, jitter=0.2, seed=82).to(cuda)
+    K = tg.LaplaceElementAssembler.from_mesh(m)(m.points)
+    b = tg.const_node_assembler(1.0).from_mesh(m)(m.points)
+    Ki, bi = tg.Condenser(m.boundary_mask)(K, b)
+    ref = tg.pcg_solve(Ki, bi, rtol=1e-13)
+    for kw in ({"backend": "scipy"}, {"method": "lu"}, {"method": "cholesky", "backend": "cudss"},
+               {"method": "cg", "preconditioner": "jacobi", "tol": 1e-12, "verbose": True}):
+        x = Ki.solve(bi, **kw)
+        assert rel_fro(x, ref) <= 1e-9, kw
+    d, A, As, n = _fixture(cuda)
+    b2 = torch.from_numpy(d["b"]).to(cuda)
+    x = A.solve(b2, is_spd=False, tol=1e-12)
+    xs = spl.spsolve(As.tocsc(), d["b"])
+    assert np.linalg.norm(x.cpu().numpy() - xs) <= 1e-10 * np.linalg.norm(xs)

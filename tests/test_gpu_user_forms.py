@@ -10,7 +10,9 @@ them, assemble through the kernels and match the reference's golden values
 * a mass form ``forward(u, v) = u * v`` (builtin.py:99-100): golden ``q*_M``.
 * an elasticity form ``forward(gradu, gradv, E)`` returning the isotropic
   block with nu = 0.3: golden ``q*_El`` (the reference's Ba^T C(E) Bb).
-A form that is none of these still raises NotImplementedError."""
+A form whose modulus is a nonlinear function of its coefficient assembles
+through the same kernels; a form that is none of these still raises
+NotImplementedError."""
 import pytest
 import torch
 
@@ -50,6 +52,11 @@ class SquaredKappa(tg.ElementAssembler):
         return kappa * kappa * (gradu @ gradv)
 
 
+class Anisotropic(tg.ElementAssembler):
+    def forward(self, gradu, gradv, kappa):
+        return kappa * gradu[0] * gradv[0]
+
+
 @pytest.mark.parametrize("case", list(ETYPE))
 def test_user_forms_match_reference(case, cuda):
     g = load_golden(case)
@@ -75,7 +82,15 @@ def test_recognition(cuda):
     assert recognise_form(PlainMass.from_mesh(mesh)).form == "mass"
     r = recognise_form(IsotropicElasticity.from_mesh(mesh, nu=0.25))
     assert r.form == "elasticity" and abs(r.nu - 0.25) < 1e-14
-    bad = SquaredKappa.from_mesh(mesh)
+    # a modulus nonlinear in the coefficient: kappa^2 per element
+    sq = SquaredKappa.from_mesh(mesh)
+    r = recognise_form(sq)
+    assert r.form == "diffusion" and r.cmap is not None
+    k = torch.linspace(0.5, 2.0, mesh.n_elements, dtype=torch.float64, device=cuda)
+    K2 = sq(mesh.points, element_data={"kappa": k})
+    K1 = SIMPLaplace.from_assembler(sq)(mesh.points, element_data={"kappa": k * k})
+    assert rel_fro(K2.values, K1.values) <= 1e-14
+    bad = Anisotropic.from_mesh(mesh)
     assert recognise_form(bad) is None
     with pytest.raises(NotImplementedError):
         bad(mesh.points, element_data={"kappa": torch.ones(mesh.n_elements, dtype=torch.float64, device=cuda)})
