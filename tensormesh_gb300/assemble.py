@@ -145,6 +145,7 @@ class RecognisedForm:
 
 
 _FIELD_ARGS = ("gradu", "gradv", "u", "v", "x")
+_MODULUS_KEY = "_tm_modulus"          # element data: a modulus derived from a per-node coefficient
 _UNSET = object()
 
 
@@ -449,7 +450,30 @@ class ElementAssembler(_AssemblerBase):
                 assert value.shape[0] == E, f"the shape of {key} should be [{E}, ...], but got {tuple(value.shape)}"
                 ed[key] = value
         sd = dict(scalar_data or {})
+        rec = recognise_form(self)
+        if point_data and rec is not None and rec.coef is not None and rec.coef in point_data \
+                and rec.coef not in ed:
+            ed[_MODULUS_KEY] = self._nodal_modulus(rec, point_data[rec.coef], et, points)
         return et, points, ed, sd
+
+    def _nodal_modulus(self, rec, c_nodes, et, points):
+        """The per-element modulus of a form whose coefficient is given per
+        node (point_data), interpolated to the quadrature points as the
+        reference does (the nodal value times phi at each point): on P1
+        elements, whose gradients are constant, the element matrix is the
+        unit-modulus one times sum_q w_q m(c(x_q)) / sum_q w_q."""
+        if et not in ("triangle", "tetra") or rec.form == "mass":
+            raise NotImplementedError("a per-node coefficient is assembled for diffusion and elasticity forms "
+                                      "on P1 triangles and tetrahedra")
+        tab = element_tables(et, self.transformation[et].quadrature_order)
+        dev = points.device
+        w = torch.from_numpy(tab["w"]).to(device=dev, dtype=torch.float64)
+        phi = torch.from_numpy(tab["phi"]).to(device=dev, dtype=torch.float64)
+        c = torch.as_tensor(c_nodes).to(device=dev, dtype=torch.float64).reshape(-1)
+        conn = self.elements[et].to(dev).long()
+        cq = c[conn] @ phi.T                                          # [E, Q]
+        mq = rec.modulus(cq.reshape(-1)).reshape(cq.shape) if (rec.cmap is not None or rec.scale != 1.0) else cq
+        return (mq @ w) / w.sum()
 
     def __call__(self, points: Optional[torch.Tensor] = None, func: Optional[Callable] = None,
                  point_data=None, element_data=None, scalar_data=None, batch_size: int = -1):
@@ -542,6 +566,9 @@ class ElementAssembler(_AssemblerBase):
         rec = recognise_form(self)
         if rec is None:
             return {}
+        if _MODULUS_KEY in ed:                       # from a per-node coefficient, mapped already
+            m = ed[_MODULUS_KEY]
+            return {"kappa": m} if rec.form == "diffusion" else {"E": m, "nu": rec.nu}
         c = None
         if rec.coef is not None:
             c = ed.get(rec.coef, sd.get(rec.coef))

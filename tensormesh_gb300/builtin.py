@@ -26,6 +26,8 @@ class LaplaceElementAssembler(ElementAssembler):
         return gradu @ gradv
 
     def _tm_coefficients(self, ed, sd, E):
+        if "_tm_modulus" in ed:                      # a per-node kappa, interpolated (assemble.py)
+            return {"kappa": ed["_tm_modulus"]}
         return {"kappa": ed.get("kappa", sd.get("kappa"))}
 
 

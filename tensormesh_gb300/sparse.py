@@ -218,6 +218,26 @@ class SparseMatrix:
             return self.matvec(x)
         return torch.stack([self.matvec(x[:, j].contiguous()) for j in range(x.shape[1])], 1)
 
+    # the dtype / device conversions of a torch tensor (the reference's
+    # SparseMatrix is one), on the values; the layout is shared
+    def to(self, *args, **kwargs) -> "SparseMatrix":
+        v = self.values.to(*args, **kwargs)
+        if v.device != self.values.device:
+            m = SparseMatrix(v, self._row_src.to(v.device), self._col_src.to(v.device), self.shape,
+                             _topology=self._topology, _block=self._block,
+                             _block_row=None if self._block_row is None else self._block_row.to(v.device),
+                             _block_col=None if self._block_col is None else self._block_col.to(v.device),
+                             _sorted=self._sorted)
+            m._hash = self._hash
+            return m
+        return self if v is self.values else self.with_values(v)
+
+    def double(self) -> "SparseMatrix":
+        return self.to(torch.float64)
+
+    def float(self) -> "SparseMatrix":
+        return self.to(torch.float32)
+
     def transpose(self) -> "SparseMatrix":
         """A^T with the same values array (entry k of A is entry k of A^T;
         its CSR view orders them when it is built)."""
