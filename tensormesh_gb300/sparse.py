@@ -218,6 +218,55 @@ class SparseMatrix:
             return self.matvec(x)
         return torch.stack([self.matvec(x[:, j].contiguous()) for j in range(x.shape[1])], 1)
 
+    # ------------------------------------------------------------ arithmetic
+    # (the reference's SparseMatrix inherits them from torch-sla's sparse
+    # tensor: time integrators write M + dt * K); differentiable in the values
+    def _same_layout(self, other: "SparseMatrix") -> bool:
+        if self.shape != other.shape or self._block != other._block or self.nnz != other.nnz:
+            return False
+        if self._topology is not None and self._topology is other._topology:
+            return True
+        if self._row_src is other._row_src and self._col_src is other._col_src:
+            return True
+        return self.layout_hash == other.layout_hash
+
+    def __mul__(self, s) -> "SparseMatrix":
+        if isinstance(s, SparseMatrix) or (torch.is_tensor(s) and s.numel() != 1):
+            return NotImplemented
+        return self.with_values(self.values * s)
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, s) -> "SparseMatrix":
+        if isinstance(s, SparseMatrix) or (torch.is_tensor(s) and s.numel() != 1):
+            return NotImplemented
+        return self.with_values(self.values / s)
+
+    def __neg__(self) -> "SparseMatrix":
+        return self.with_values(-self.values)
+
+    def __add__(self, other) -> "SparseMatrix":
+        if not isinstance(other, SparseMatrix):
+            return NotImplemented
+        if self.shape != other.shape:
+            raise ValueError(f"cannot add sparse matrices of shapes {self.shape} and {other.shape}")
+        if self._same_layout(other):
+            return self.with_values(self.values + other.values.to(self.values.dtype))
+        # different patterns: the union, entries summed (scalar COO, row-major)
+        dev = self.values.device
+        row = torch.cat([self.row_indices.to(dev), other.row_indices.to(dev)])
+        col = torch.cat([self.col_indices.to(dev), other.col_indices.to(dev)])
+        val = torch.cat([self.values.reshape(-1), other.values.to(dev, self.values.dtype).reshape(-1)])
+        key = row * self.shape[1] + col
+        uniq, inv = torch.unique(key, sorted=True, return_inverse=True)
+        out = torch.zeros(uniq.numel(), dtype=val.dtype, device=dev).index_add(0, inv, val)
+        return SparseMatrix(out, uniq // self.shape[1], uniq % self.shape[1], self.shape, _sorted=True)
+
+    def __sub__(self, other) -> "SparseMatrix":
+        if not isinstance(other, SparseMatrix):
+            return NotImplemented
+        return self + (-other)
+
     # the dtype / device conversions of a torch tensor (the reference's
     # SparseMatrix is one), on the values; the layout is shared
     def to(self, *args, **kwargs) -> "SparseMatrix":
