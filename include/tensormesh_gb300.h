@@ -494,27 +494,31 @@ size_t tm_adjoint_workspace_bytes(const tm_adjoint_args* args);
 int tm_adjoint_p1(const tm_adjoint_args* args, tm_stream_t stream);
 
 /*
- * dL/dE per element of an isotropic linear-elasticity matrix (float64, any
- * element type): replaces autograd through the reference's elasticity
- * integrand with respect to a per-element modulus (functional/
- * elasticity.py:132-284, assemble/element_assembler.py:390-445).  weights =
- * dL/dvalues as [nnz, D, D] blocks; slot_map [E*B*B] int64 (element order);
- * grad_young[e] = young_scale * sum_ab W[slot(e,a,b)] : K_e[a][b](E = 1)
- * (element order), K_e(1) the element's blocks at unit modulus for the
- * given Poisson ratio.  plan: a plan of the mesh (its conn and elem_perm).
+ * dL/dc per element of a diffusion matrix (c = kappa) or an isotropic
+ * linear-elasticity matrix (c = E), float64, any element type: replaces
+ * autograd through the reference's integrand with respect to a per-element
+ * coefficient (assemble/element_assembler.py:390-445; for elasticity
+ * functional/elasticity.py:132-284).  form: TM_FORM_DIFFUSION (weights =
+ * dL/dvalues [nnz]) or TM_FORM_ELASTICITY (weights [nnz, D, D] blocks,
+ * poisson the call's Poisson ratio); slot_map [E*B*B] int64 (element
+ * order); grad[e] = scale * sum_ab W[slot(e,a,b)] : K_e[a][b](c = 1)
+ * (element order), K_e(1) the element's matrix at unit coefficient.
+ * plan: a plan of the mesh (its conn and elem_perm).
  */
-typedef struct tm_elastic_grad_args {
+typedef struct tm_coef_grad_args {
+    int32_t form;                  /* TM_FORM_DIFFUSION or TM_FORM_ELASTICITY */
+    int32_t reserved;
     int64_t n_points;
     const void* points;            /* device [N*D] float64 */
-    const void* weights;           /* device [nnz*D*D] float64 */
+    const void* weights;           /* device [nnz] or [nnz*D*D] float64 */
     const int64_t* slot_map;       /* device [E*B*B] */
-    double young_scale;
+    double scale;
     double poisson;
-    void* grad_young;              /* device [E] float64 */
+    void* grad;                    /* device [E] float64 */
     tm_element_tables tables;
     tm_chunk_plan plan;
-} tm_elastic_grad_args;
-int tm_elastic_grad_young(const tm_elastic_grad_args* args, tm_stream_t stream);
+} tm_coef_grad_args;
+int tm_coef_grad(const tm_coef_grad_args* args, tm_stream_t stream);
 
 /* ---- sparse linear algebra (SparseMatrix @ and solve) ------------------- */
 /*

@@ -106,10 +106,11 @@ class AdjointArgs(C.Structure):
     ]
 
 
-class ElasticGradArgs(C.Structure):
+class CoefGradArgs(C.Structure):
     _fields_ = [
+        ("form", C.c_int32), ("reserved", C.c_int32),
         ("n_points", C.c_int64), ("points", C.c_void_p), ("weights", C.c_void_p), ("slot_map", C.c_void_p),
-        ("young_scale", C.c_double), ("poisson", C.c_double), ("grad_young", C.c_void_p),
+        ("scale", C.c_double), ("poisson", C.c_double), ("grad", C.c_void_p),
         ("tables", ElementTables), ("plan", ChunkPlan),
     ]
 
@@ -202,7 +203,7 @@ _SIGNATURES = {
                           C.c_void_p]),
     "tm_adjoint_workspace_bytes": (C.c_size_t, [C.POINTER(AdjointArgs)]),
     "tm_adjoint_p1": (C.c_int, [C.POINTER(AdjointArgs), C.c_void_p]),
-    "tm_elastic_grad_young": (C.c_int, [C.POINTER(ElasticGradArgs), C.c_void_p]),
+    "tm_coef_grad": (C.c_int, [C.POINTER(CoefGradArgs), C.c_void_p]),
     "tm_batched_pcg": (C.c_int, [C.POINTER(BatchedPcgArgs), C.c_void_p]),
     "tm_pcg_partials_bytes": (C.c_size_t, []),
     "tm_pcg_start": (C.c_int, [C.POINTER(PcgArgs), C.c_void_p]),

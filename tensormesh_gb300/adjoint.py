@@ -11,7 +11,7 @@ docs/source/user_guide/differentiability.rst:34-56).  Here:
   coordinates and its scalar density; its backward runs ``tm_adjoint_p1``
   in its mass mode (d|det J| / dJ = |det J| J^-T per element).
 * ``ElasticityAssembly`` -- the values of an isotropic elasticity matrix as
-  a function of its modulus (``tm_elastic_grad_young``: dL/dE_e is the
+  a function of its modulus (``tm_coef_grad``: dL/dE_e is the
   contraction of dL/dvalues with the element's blocks at unit modulus).
 * ``LoadAssembly`` -- a P1 load vector as a function of node coordinates.
 * ``SparseSolve`` -- x = A^-1 b with Jacobi-PCG; backward solves A^T lambda =
@@ -78,10 +78,10 @@ class DiffusionAssembly(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, points, kappa, asm, kappa_scale):
-        from .assemble import assemble_forms
-        ed = {} if kappa is None else {"kappa": kappa.detach()}
-        sd = {} if kappa is not None else {"kappa": kappa_scale}
-        (values,) = assemble_forms([asm], points.detach(), ed, sd)
+        from .assemble import _assemble_on
+        # the kernel's coefficient as given (already the form's modulus)
+        c = {"kappa": kappa_scale if kappa is None else kappa.detach()}
+        (values,) = _assemble_on([asm], asm._topo(True), points.detach(), {}, {}, None, None, _coefs=[c])
         ctx.asm = asm
         ctx.kappa_scale = kappa_scale if kappa is not None else kappa_scale
         ctx.save_for_backward(points, kappa if kappa is not None else torch.empty(0))
@@ -93,14 +93,26 @@ class DiffusionAssembly(torch.autograd.Function):
         points, kappa = ctx.saved_tensors
         asm = ctx.asm
         topo = asm._topology
-        _require_p1(topo)
         et = asm.element_types[0]
         slot = asm.projector[et].indices.to(points.device)
+        want_k = ctx.has_kappa and ctx.needs_input_grad[1]
+        scalar_k = ctx.has_kappa and kappa.dim() == 0
+        if topo.etype not in ("triangle", "tetra") or scalar_k:
+            # the coefficient alone (any element type): the contraction of
+            # dL/dvalues with the unit-coefficient element matrices
+            if ctx.needs_input_grad[0]:
+                _require_p1(topo)
+                if scalar_k:
+                    raise NotImplementedError("gradients with respect to both the node coordinates and a "
+                                              "scalar kappa are not implemented")
+            gk = None
+            if want_k:
+                g = coef_grad(topo, points, gvals, slot, _lib.TM_FORM_DIFFUSION, 1.0)
+                gk = g.sum().reshape(()) if scalar_k else g
+            return None, (gk.to(kappa.dtype) if gk is not None else None), None, None
         kap = kappa if ctx.has_kappa else None
-        gk, gp = _adjoint_call(topo, points, kap, ctx.kappa_scale if ctx.has_kappa else ctx.kappa_scale,
-                               _lib.TM_ADJ_K_CSR, weights=gvals, slot=slot,
-                               want_kappa=ctx.has_kappa and ctx.needs_input_grad[1],
-                               want_points=ctx.needs_input_grad[0])
+        gk, gp = _adjoint_call(topo, points, kap, ctx.kappa_scale, _lib.TM_ADJ_K_CSR, weights=gvals, slot=slot,
+                               want_kappa=want_k, want_points=ctx.needs_input_grad[0])
         return (gp.to(points.dtype) if gp is not None else None,
                 gk.to(kappa.dtype) if gk is not None else None, None, None)
 
@@ -125,11 +137,11 @@ class MassAssembly(torch.autograd.Function):
         points, values = ctx.saved_tensors
         asm = ctx.asm
         topo = asm._topology
-        _require_p1(topo)
         et = asm.element_types[0]
         slot = asm.projector[et].indices.to(points.device)
         gp = None
         if ctx.needs_input_grad[0]:
+            _require_p1(topo)
             _, gp = _adjoint_call(topo, points, None, ctx.rho, _lib.TM_ADJ_M_CSR, weights=gvals, slot=slot,
                                   want_kappa=False, want_points=True)
             gp = gp.to(points.dtype)
@@ -152,23 +164,24 @@ def _mass_unit(asm, points):
     return assemble_forms([unit], points.detach(), {}, {"rho": 1.0})
 
 
-def elastic_grad_young(topo, points, gvals, slot, young_scale, poisson):
-    """dL/dE_e = young_scale sum_ab W[slot(e,a,b)] : K_e[a][b](E = 1), element
-    order (``tm_elastic_grad_young``)."""
+def coef_grad(topo, points, gvals, slot, form, scale, poisson=0.3):
+    """dL/dc_e = scale sum_ab W[slot(e,a,b)] : K_e[a][b](c = 1), element
+    order (``tm_coef_grad``; form TM_FORM_DIFFUSION or TM_FORM_ELASTICITY)."""
     lib = _lib.load()
     dev = points.device
     pts = points.detach().to(torch.float64).contiguous()
     w = gvals.detach().to(torch.float64).contiguous()
     plan = topo.node_plan(dev)
-    a = _lib.ElasticGradArgs()
+    a = _lib.CoefGradArgs()
+    a.form = form
     a.n_points = topo.n_points
     a.points, a.weights, a.slot_map = _lib.ptr(pts), _lib.ptr(w), _lib.ptr(slot)
-    a.young_scale, a.poisson = float(young_scale), float(poisson)
+    a.scale, a.poisson = float(scale), float(poisson)
     g = torch.empty(topo.n_elements, dtype=torch.float64, device=dev)
-    a.grad_young = _lib.ptr(g)
+    a.grad = _lib.ptr(g)
     a.tables = topo.table_struct(dev)
     a.plan = plan.struct()
-    _lib.check(lib.tm_elastic_grad_young(C.byref(a), _lib.stream_handle(dev)), "tm_elastic_grad_young")
+    _lib.check(lib.tm_coef_grad(C.byref(a), _lib.stream_handle(dev)), "tm_coef_grad")
     return g
 
 
@@ -176,14 +189,13 @@ class ElasticityAssembly(torch.autograd.Function):
     """values = K(E) of an isotropic elasticity form (float64, any element
     type) as a function of its modulus E (per element or a scalar tensor;
     ``coefs``: the form's other kernel coefficients, nu and E_scale); the
-    backward runs ``tm_elastic_grad_young`` on dL/dvalues."""
+    backward runs ``tm_coef_grad`` on dL/dvalues."""
 
     @staticmethod
     def forward(ctx, young, points, asm, coefs):
         from .assemble import _assemble_on
         c = dict(coefs, E=young.detach())
-        topo = asm._topology
-        (values,) = _assemble_on([asm], topo, points.detach(), {}, {}, None, None, _coefs=[c])
+        (values,) = _assemble_on([asm], asm._topo(True), points.detach(), {}, {}, None, None, _coefs=[c])
         ctx.asm, ctx.nu, ctx.escale = asm, float(c.get("nu", 0.3)), float(c.get("E_scale", 1.0))
         ctx.save_for_backward(points, young)
         return values
@@ -194,7 +206,7 @@ class ElasticityAssembly(torch.autograd.Function):
         asm = ctx.asm
         et = asm.element_types[0]
         slot = asm.projector[et].indices.to(points.device)
-        g = elastic_grad_young(asm._topology, points, gvals, slot, ctx.escale, ctx.nu)
+        g = coef_grad(asm._topology, points, gvals, slot, _lib.TM_FORM_ELASTICITY, ctx.escale, ctx.nu)
         gy = g if young.dim() > 0 and young.numel() > 1 else g.sum().reshape(young.shape)
         return gy.to(young.dtype), None, None, None
 

@@ -524,7 +524,8 @@ class ElementAssembler(_AssemblerBase):
                 raise NotImplementedError(f"gradients of the {form} form are not implemented")
             from .adjoint import DiffusionAssembly
             kap = self._tm_coefficients(ed, sd, self.elements[et].shape[0]).get("kappa")
-            if torch.is_tensor(kap) and kap.dim() > 0:
+            if torch.is_tensor(kap) and (kap.dim() > 0 or kap.requires_grad):
+                kap = kap.reshape(-1) if kap.numel() > 1 else kap.reshape(())
                 values = DiffusionAssembly.apply(points, kap, self, 1.0)
             else:
                 values = DiffusionAssembly.apply(points, None, self, 1.0 if kap is None else float(kap))

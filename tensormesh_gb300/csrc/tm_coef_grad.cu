@@ -1,5 +1,9 @@
-// Gradient of an isotropic linear-elasticity matrix with respect to the
-// per-element Young's modulus (float64).
+// Gradient of a diffusion or isotropic linear-elasticity matrix with respect
+// to its per-element coefficient (float64, any element type).
+//
+// Diffusion: K_e = kappa_e sum_q jw_q g_a . g_b, so for weights W =
+// dL/dvalues ([nnz]) dL/dkappa_e = s sum_{a,b} W[slot(e,a,b)] sum_q jw_q
+// g_a . g_b.
 //
 // The reference differentiates its elasticity assembly with autograd through
 // the vmap'd integrand B_a^T C B_b (functional/elasticity.py:132-284,
@@ -40,8 +44,8 @@ __host__ __device__ inline size_t eg_smem(int Q) {
            sizeof(double) * kEgSub * kEgPer;
 }
 
-template <int ET>
-__global__ void __launch_bounds__(kEgThreads) k_elastic_grad(const tm_elastic_grad_args a) {
+template <int ET, bool ELAST>
+__global__ void __launch_bounds__(kEgThreads) k_coef_grad(const tm_coef_grad_args a) {
     using T = Traits<ET>;
     constexpr int D = T::D, B = T::B;
     const tm_chunk_plan& P = a.plan;
@@ -58,7 +62,7 @@ __global__ void __launch_bounds__(kEgThreads) k_elastic_grad(const tm_elastic_gr
     const double clam = nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), cmu = 1.0 / (2.0 * (1.0 + nu));
     const double* pts = static_cast<const double*>(a.points);
     const double* W = static_cast<const double*>(a.weights);
-    double* gE = static_cast<double*>(a.grad_young);
+    double* gE = static_cast<double*>(a.grad);
     const int64_t i0 = (int64_t)blockIdx.x * CH;
     const int ne = (int)min((int64_t)CH, P.n_elements - i0);
     for (int s0 = 0; s0 < ne; s0 += kEgSub) {
@@ -110,6 +114,19 @@ __global__ void __launch_bounds__(kEgThreads) k_elastic_grad(const tm_elastic_gr
                 const double* ge = G + (size_t)el * Q * B * D;
                 for (int p = t; p < B * B; p += kEgPer) {
                     const int pa = p / B, pb = p - pa * B;
+                    if constexpr (!ELAST) {
+                        const double w = W[a.slot_map[(e * B + pa) * B + pb]];
+                        double s = 0.0;
+                        for (int q = 0; q < Q; ++q) {
+                            const double* gq = ge + (size_t)q * B * D;
+                            double dd = 0.0;
+#pragma unroll
+                            for (int r = 0; r < D; ++r) dd += gq[pa * D + r] * gq[pb * D + r];
+                            s += JW[el * Q + q] * dd;
+                        }
+                        acc += w * s;
+                        continue;
+                    }
                     const double* w = W + a.slot_map[(e * B + pa) * B + pb] * (D * D);
                     double Wm[D][D];
                     double trw = 0.0;
@@ -146,7 +163,7 @@ __global__ void __launch_bounds__(kEgThreads) k_elastic_grad(const tm_elastic_gr
             double s = 0.0;
 #pragma unroll
             for (int t = 0; t < kEgPer; ++t) s += part[el * kEgPer + t];
-            gE[P.elem_perm[i0 + s0 + el]] = a.young_scale * s;
+            gE[P.elem_perm[i0 + s0 + el]] = a.scale * s;
         }
         __syncthreads();
     }
@@ -162,40 +179,48 @@ inline int eg_status(const char* what) {
     return TM_OK;
 }
 
-template <int ET>
-int run_elastic_grad(const tm_elastic_grad_args& a, cudaStream_t st) {
-    using T = Traits<ET>;
-    if (a.plan.n_basis != T::B)
-        return tm_set_error(TM_ERR_INVALID_ARG, "tm_elastic_grad_young: plan of another element type");
+template <int ET, bool ELAST>
+int run_coef_grad_form(const tm_coef_grad_args& a, cudaStream_t st) {
     const size_t smem = eg_smem<ET>(a.tables.n_quad);
-    if (smem > 227 * 1024) return tm_set_error(TM_ERR_TOO_LARGE, "tm_elastic_grad_young: too many quadrature points");
-    if (a.plan.n_chunks == 0) return TM_OK;
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_elastic_grad<ET>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        cudaFuncSetAttribute(k_coef_grad<ET, ELAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
         return eg_status("cudaFuncSetAttribute");
-    k_elastic_grad<ET><<<a.plan.n_chunks, kEgThreads, smem, st>>>(a);
-    return eg_status("k_elastic_grad");
+    k_coef_grad<ET, ELAST><<<a.plan.n_chunks, kEgThreads, smem, st>>>(a);
+    return eg_status("k_coef_grad");
+}
+
+template <int ET>
+int run_coef_grad(const tm_coef_grad_args& a, cudaStream_t st) {
+    using T = Traits<ET>;
+    if (a.plan.n_basis != T::B) return tm_set_error(TM_ERR_INVALID_ARG, "tm_coef_grad: plan of another element type");
+    if (eg_smem<ET>(a.tables.n_quad) > 227 * 1024)
+        return tm_set_error(TM_ERR_TOO_LARGE, "tm_coef_grad: too many quadrature points");
+    if (a.plan.n_chunks == 0) return TM_OK;
+    return a.form == TM_FORM_ELASTICITY ? run_coef_grad_form<ET, true>(a, st) : run_coef_grad_form<ET, false>(a, st);
 }
 
 }  // namespace tmk
 
 using namespace tmk;
 
-extern "C" int tm_elastic_grad_young(const tm_elastic_grad_args* a, tm_stream_t stream) {
-    if (!a) return tm_set_error(TM_ERR_INVALID_ARG, "tm_elastic_grad_young: null args");
-    if (a->plan.n_elements > 0 && (!a->points || !a->weights || !a->slot_map || !a->grad_young ||
+extern "C" int tm_coef_grad(const tm_coef_grad_args* a, tm_stream_t stream) {
+    if (!a) return tm_set_error(TM_ERR_INVALID_ARG, "tm_coef_grad: null args");
+    if (a->form != TM_FORM_ELASTICITY && a->form != TM_FORM_DIFFUSION)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_coef_grad: form must be TM_FORM_DIFFUSION or TM_FORM_ELASTICITY");
+    if (a->plan.n_elements > 0 && (!a->points || !a->weights || !a->slot_map || !a->grad ||
                                    !a->tables.packed || !a->plan.conn || !a->plan.elem_perm))
-        return tm_set_error(TM_ERR_INVALID_ARG, "tm_elastic_grad_young: null pointer");
-    if (!(a->poisson > -1.0 && a->poisson < 0.5))
-        return tm_set_error(TM_ERR_INVALID_ARG, "tm_elastic_grad_young: Poisson ratio outside (-1, 0.5)");
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_coef_grad: null pointer");
+    if (a->form == TM_FORM_ELASTICITY && !(a->poisson > -1.0 && a->poisson < 0.5))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_coef_grad: Poisson ratio outside (-1, 0.5)");
     const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     switch (a->tables.element_type) {
-        case TM_TRI3: return run_elastic_grad<TM_TRI3>(*a, st);
-        case TM_TET4: return run_elastic_grad<TM_TET4>(*a, st);
-        case TM_TRI6: return run_elastic_grad<TM_TRI6>(*a, st);
-        case TM_TET10: return run_elastic_grad<TM_TET10>(*a, st);
-        case TM_QUAD4: return run_elastic_grad<TM_QUAD4>(*a, st);
-        case TM_QUAD9: return run_elastic_grad<TM_QUAD9>(*a, st);
-        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_elastic_grad_young: unknown element type");
+        case TM_TRI3: return run_coef_grad<TM_TRI3>(*a, st);
+        case TM_TET4: return run_coef_grad<TM_TET4>(*a, st);
+        case TM_TRI6: return run_coef_grad<TM_TRI6>(*a, st);
+        case TM_TET10: return run_coef_grad<TM_TET10>(*a, st);
+        case TM_QUAD4: return run_coef_grad<TM_QUAD4>(*a, st);
+        case TM_QUAD9: return run_coef_grad<TM_QUAD9>(*a, st);
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_coef_grad: unknown element type");
     }
 }

@@ -1,5 +1,6 @@
 """Gradients of isotropic elasticity matrices with respect to the modulus
-(``ElasticityAssembly``: the ``tm_elastic_grad_young`` kernel) against the
+(``ElasticityAssembly``: the ``tm_coef_grad`` kernel), and of diffusion
+matrices with respect to their coefficient on every element type, against the
 oracle's autograd through the reference's op sequence (Voigt B^T C B,
 quadrature einsum, index_add_), for every element type, within 1e-10
 relative; and the reference's compliance-minimisation workflow (a SIMP
@@ -101,3 +102,38 @@ def test_simp_compliance_gradient(cuda):
     (F[free] * uo).sum().backward()
     assert rel_fro(u.detach().cpu(), uo.detach()) <= 1e-8
     assert rel_fro(rho.grad.cpu(), ro.grad) <= 1e-7
+
+
+class ExpDiffusion(tg.ElementAssembler):
+    def forward(self, gradu, gradv, s):
+        return torch.exp(s) * (gradu @ gradv)
+
+
+@pytest.mark.parametrize("etype", list(MESHES))
+def test_diffusion_coefficient_gradient_every_element(etype, cuda):
+    """dL/dkappa per element on every element type (tm_coef_grad for P2 and
+    quadrilaterals, the P1 adjoint kernel for P1), and through a nonlinear
+    coefficient map (kappa = exp(s)), against the oracle's autograd."""
+    mesh = MESHES[etype]()
+    rng = np.random.default_rng(69)
+    s0 = torch.from_numpy(rng.uniform(-0.5, 0.5, mesh.n_elements))
+    gm = mesh.to(cuda)
+    asm = ExpDiffusion.from_mesh(gm)
+    W = torch.from_numpy(rng.uniform(-1.0, 1.0, asm.edges.shape[1]))
+    s = s0.clone().to(cuda).requires_grad_(True)
+    K = asm(gm.points, element_data={"s": s})
+    (K.values * W.to(cuda)).sum().backward()
+    so = s0.clone().requires_grad_(True)
+    _, _, Ko = O.assemble_matrix(mesh.points, mesh.elements().long(), mesh.n_points,
+                                 lambda p, c, kappa: O.element_locals_diffusion(p, c, etype, kappa, 2),
+                                 kappa=torch.exp(so))
+    assert rel_fro(K.values.detach().cpu(), Ko.detach()) <= 1e-12
+    (Ko * W).sum().backward()
+    assert rel_fro(s.grad.cpu(), so.grad) <= 1e-10
+    # a scalar coefficient tensor
+    k = torch.tensor(1.3, dtype=torch.float64, device=cuda, requires_grad=True)
+    K2 = tg.LaplaceElementAssembler.from_assembler(asm)(gm.points, scalar_data={"kappa": k})
+    (K2.values * W.to(cuda)).sum().backward()
+    _, _, K1 = O.assemble_matrix(mesh.points, mesh.elements().long(), mesh.n_points,
+                                 lambda p, c: O.element_locals_diffusion(p, c, etype, None, 2))
+    assert abs(float(k.grad) - float((K1 * W).sum())) <= 1e-10 * abs(float((K1 * W).sum()))
