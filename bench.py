@@ -324,8 +324,33 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and ws == 1 and not args.no_batched:
         # the metric's second half: batched solves/s (C5), with its own clocks
         line["batched"] = batched_summary(args, dev)
+    if rank == 0 and ws == 1 and not args.no_secondary:
+        line["secondary"] = secondary_summary(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def secondary_summary(args, local):
+    """The other rows' figures, each with its own clock samples (a few
+    steps each): C1 Poisson solve, C3 elasticity assembly pass and solve,
+    C4 adjoint cost ratio."""
+    import copy
+    a = copy.copy(args)
+    a.steps, a.warmup = 5, 2
+    out = {}
+    p = poisson_line(a, local)
+    out["poisson_c1"] = {k: p[k] for k in ("value", "unit", "ms_per_step", "assembly_ms", "iterations",
+                                           "l2_relative_error", "reference_l2_relative_error", "clocks")}
+    e = elasticity_line(a, 1, local)
+    out["elasticity_c3"] = {"pass_ms": e["ms_per_step"], "elements_per_s": e["value"],
+                            "element_kernel_ms": e["roofline"]["k_matrix_ms"],
+                            "fp64_frac": e["roofline"]["fp64_frac"], "e2e_ms": e["e2e"]["ms_per_step"],
+                            "pcg_ms_per_iteration": e["solve"]["ms_per_iteration"],
+                            "pcg_iterations": e["solve"]["iterations"], "clocks": e["clocks"]}
+    i = inverse_line(a, local)
+    out["inverse_c4"] = {k: i[k] for k in ("value", "unit", "forward_ms", "backward_ms", "adjoint_kernel_ms",
+                                           "assembly_ms", "clocks")}
+    return out
 
 
 def run_reference(args, ws, rank, local):
@@ -408,6 +433,12 @@ def _time_ms(fn, dev):
 
 
 def run_inverse(args, ws, rank, local):
+    line = inverse_line(args, local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def inverse_line(args, local):
     """C4: P1 tets 48^3 x 6, loss ||u(kappa) - u_target||^2, forward solve vs
     the adjoint backward (one adjoint PCG solve + the adjoint element pass)."""
     import tensormesh_gb300 as tg
@@ -450,11 +481,16 @@ def run_inverse(args, ws, rank, local):
             "config": {"workload": "inverse_diffusion_tet_48: 663,552 P1 tets, f = 1, zero Dirichlet, PCG rtol 1e-10"},
             "forward_ms": f, "backward_ms": b, "adjoint_kernel_ms": statistics.median(t_adj),
             "assembly_ms": statistics.median(t_asm), "clocks": clocks}
+    return line
+
+
+def run_poisson(args, ws, rank, local):
+    line = poisson_line(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
-def run_poisson(args, ws, rank, local):
+def poisson_line(args, local):
     """C1: P1 triangles on the unit square, 256 x 256 cells x 2 (131,072
     elements, 66,049 nodes), f = 2 pi^2 sin(pi x) sin(pi y), zero Dirichlet
     data.  One step = the whole solve through the public API: K and b
@@ -503,8 +539,7 @@ def run_poisson(args, ws, rank, local):
             "assembly_ms": statistics.median(asm_times), "iterations": info.iterations,
             "converged": info.converged, "l2_relative_error": err,
             "reference_l2_relative_error": 3.7935219e-05, "clocks": clocks}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
 
 
 def _elastic_name(n):
@@ -527,6 +562,12 @@ ELASTIC_FLOPS_PER_ELEMENT = 13000.0
 
 
 def run_elasticity(args, ws, rank, local):
+    line = elasticity_line(args, ws, local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def elasticity_line(args, ws, local):
     """C3: one step = the 3x3 block values of K(E) for 196,608 P2 tets
     (FP64).  Also times the set-up (from_mesh), the end-to-end call with host
     buffers, and the solve that follows in the reference's examples:
@@ -637,8 +678,7 @@ def run_elasticity(args, ws, rank, local):
                       "hbm_frac_per_iteration": it_bytes / (it_ms * 1e-3) / 1e9 / peak,
                       "unknowns": n_c, "nnz": nnz_c},
             "clocks": clocks, "gpu_launches": 2 * args.steps}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
 
 
 def _elastic_system(n, dev):
@@ -873,6 +913,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-gpu-reference", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="leave the batched solves out of the default line")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="leave the C1 / C3 / C4 summaries out of the default line")
     ap.add_argument("--cubes", type=int, default=64, help="cubes per side of the Kuhn-split cube (64: 1,572,864 elements)")
     ap.add_argument("--workload", default="diffusion_mass",
                     choices=["diffusion_mass", "poisson", "elasticity", "spmv", "inverse", "batched"])
