@@ -492,6 +492,13 @@ typedef struct tm_adjoint_args {
 } tm_adjoint_args;
 size_t tm_adjoint_workspace_bytes(const tm_adjoint_args* args);
 int tm_adjoint_p1(const tm_adjoint_args* args, tm_stream_t stream);
+/*
+ * The same gradients on any element type (P2 triangles and tetrahedra,
+ * quadrilaterals, and P1), per quadrature point, for k_mode TM_ADJ_K_CSR
+ * (diffusion: grad_kappa and grad_points) or TM_ADJ_M_CSR (mass:
+ * grad_points); no outer-product weights or load term.
+ */
+int tm_adjoint_general(const tm_adjoint_args* args, tm_stream_t stream);
 
 /*
  * dL/dc per element of a diffusion matrix (c = kappa) or an isotropic

@@ -203,6 +203,7 @@ _SIGNATURES = {
                           C.c_void_p]),
     "tm_adjoint_workspace_bytes": (C.c_size_t, [C.POINTER(AdjointArgs)]),
     "tm_adjoint_p1": (C.c_int, [C.POINTER(AdjointArgs), C.c_void_p]),
+    "tm_adjoint_general": (C.c_int, [C.POINTER(AdjointArgs), C.c_void_p]),
     "tm_coef_grad": (C.c_int, [C.POINTER(CoefGradArgs), C.c_void_p]),
     "tm_batched_pcg": (C.c_int, [C.POINTER(BatchedPcgArgs), C.c_void_p]),
     "tm_pcg_partials_bytes": (C.c_size_t, []),

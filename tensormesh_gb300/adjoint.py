@@ -34,6 +34,8 @@ from .element import element_tables
 def _adjoint_call(topo, points, kappa, kappa_scale, k_mode, weights=None, slot=None, u=None, lam=None,
                   load_source=_lib.TM_ADJ_LOAD_NONE, load_const=0.0, load_values=None,
                   want_kappa=True, want_points=True):
+    """``tm_adjoint_p1`` on P1 elements, ``tm_adjoint_general`` (per
+    quadrature point; diffusion and mass weights only) on the others."""
     lib = _lib.load()
     dev = points.device
     pts = points.detach().to(torch.float64).contiguous()
@@ -64,7 +66,10 @@ def _adjoint_call(topo, points, kappa, kappa_scale, k_mode, weights=None, slot=N
     a.tables = topo.table_struct(dev)
     ws = torch.empty(max(1, lib.tm_adjoint_workspace_bytes(C.byref(a))), dtype=torch.uint8, device=dev)
     a.workspace = _lib.ptr(ws)
-    _lib.check(lib.tm_adjoint_p1(C.byref(a), _lib.stream_handle(dev)), "tm_adjoint_p1")
+    if topo.etype in ("triangle", "tetra"):
+        _lib.check(lib.tm_adjoint_p1(C.byref(a), _lib.stream_handle(dev)), "tm_adjoint_p1")
+    else:
+        _lib.check(lib.tm_adjoint_general(C.byref(a), _lib.stream_handle(dev)), "tm_adjoint_general")
     return gk, gp
 
 
@@ -97,14 +102,12 @@ class DiffusionAssembly(torch.autograd.Function):
         slot = asm.projector[et].indices.to(points.device)
         want_k = ctx.has_kappa and ctx.needs_input_grad[1]
         scalar_k = ctx.has_kappa and kappa.dim() == 0
-        if topo.etype not in ("triangle", "tetra") or scalar_k:
+        if scalar_k or (topo.etype not in ("triangle", "tetra") and not ctx.needs_input_grad[0]):
             # the coefficient alone (any element type): the contraction of
             # dL/dvalues with the unit-coefficient element matrices
             if ctx.needs_input_grad[0]:
-                _require_p1(topo)
-                if scalar_k:
-                    raise NotImplementedError("gradients with respect to both the node coordinates and a "
-                                              "scalar kappa are not implemented")
+                raise NotImplementedError("gradients with respect to both the node coordinates and a "
+                                          "scalar kappa are not implemented")
             gk = None
             if want_k:
                 g = coef_grad(topo, points, gvals, slot, _lib.TM_FORM_DIFFUSION, 1.0)
@@ -141,7 +144,6 @@ class MassAssembly(torch.autograd.Function):
         slot = asm.projector[et].indices.to(points.device)
         gp = None
         if ctx.needs_input_grad[0]:
-            _require_p1(topo)
             _, gp = _adjoint_call(topo, points, None, ctx.rho, _lib.TM_ADJ_M_CSR, weights=gvals, slot=slot,
                                   want_kappa=False, want_points=True)
             gp = gp.to(points.dtype)

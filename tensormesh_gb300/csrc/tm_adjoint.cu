@@ -191,6 +191,182 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(const tm_adjoint_args a
     if (a.grad_points) node_reduce<double, D>(P, LV, static_cast<double*>(a.grad_points), a.workspace);
 }
 
+inline int adj_status(const char* what);
+
+// The same derivatives on elements whose Jacobian varies (P2 triangles and
+// tetrahedra, quadrilaterals), per quadrature point: with M = J_q^-1 and the
+// reference gradients dphi(q) [D x B], a diffusion weight W gives S =
+// dphi sym(W) dphi^T, P = M S M^T and dL/dJ_q = kappa w_q |det J_q| M^T
+// (tr(P) I - 2 P), dL/dkappa = sum_q w_q |det J_q| tr(P); a mass weight gives
+// dL/dJ_q = s w_q |det J_q| (sum_ab W_ab phi_a(q) phi_b(q)) M^T.  Node c of
+// the element receives sum_q sum_r dL/dJ_q[r][d] dphi(q)[r][c].
+template <int ET, bool MASS>
+__global__ void __launch_bounds__(kAdjThreads) k_adjoint_gen(const tm_adjoint_args a) {
+    using T = Traits<ET>;
+    constexpr int D = T::D, B = T::B;
+    const tm_chunk_plan& P = a.plan;
+    const int CH = P.chunk_elems, Q = a.tables.n_quad;
+    const TableLayout TL = table_layout(Q, B, D);
+    extern __shared__ __align__(16) unsigned char sm[];
+    double* tab = reinterpret_cast<double*>(sm);
+    double* LV = reinterpret_cast<double*>(sm + align16(sizeof(double) * TL.total));
+    for (int k = threadIdx.x; k < TL.total; k += blockDim.x) tab[k] = a.tables.packed[k];
+    __syncthreads();
+    const int64_t i0 = (int64_t)blockIdx.x * CH;
+    const int ne = (int)min((int64_t)CH, P.n_elements - i0);
+    const double* pts = static_cast<const double*>(a.points);
+    const double* kap = static_cast<const double*>(a.kappa);
+    const double* wcsr = static_cast<const double*>(a.weights);
+    double* gkap = static_cast<double*>(a.grad_kappa);
+    for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+        const int64_t i = i0 + el;
+        const int64_t e = P.elem_perm[i];
+        double X[B][D];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const int64_t node = P.conn[i * B + b];
+#pragma unroll
+            for (int d = 0; d < D; ++d) X[b][d] = ldg(pts + node * D + d);
+        }
+        const int64_t* slot = a.slot_map + e * B * B;
+        const double kv = (!MASS && kap ? ldg(kap + e) : 1.0) * a.kappa_scale;
+        double lv[B][D];
+#pragma unroll
+        for (int b = 0; b < B; ++b)
+#pragma unroll
+            for (int d = 0; d < D; ++d) lv[b][d] = 0.0;
+        double gk = 0.0;
+        for (int q = 0; q < Q; ++q) {
+            const double* dp = tab + TL.dphi + q * D * B;
+            double J[D][D];
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    double t = 0.0;
+#pragma unroll
+                    for (int b = 0; b < B; ++b) t += dp[r * B + b] * X[b][d];
+                    J[r][d] = t;
+                }
+            double cof[D][D];
+            const double det = cofactors<double>(J, cof);
+            const double inv = 1.0 / det, adet = fabs(det);
+            double M[D][D];                   // M = J^-1, M[k][r] = cof[r][k] / det
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int k = 0; k < D; ++k) M[k][r] = cof[r][k] * inv;
+            const double wq = tab[TL.w + q];
+            double GJ[D][D];
+            if constexpr (MASS) {
+                const double* ph = tab + TL.phi + q * B;
+                double wm = 0.0;
+                for (int pa = 0; pa < B; ++pa)
+#pragma unroll
+                    for (int pb = 0; pb < B; ++pb) wm += ldg(wcsr + slot[pa * B + pb]) * ph[pa] * ph[pb];
+                const double f = kv * wq * adet * wm;
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int k = 0; k < D; ++k) GJ[r][k] = f * M[k][r];
+            } else {
+                double S[D][D];
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int k = 0; k < D; ++k) S[r][k] = 0.0;
+                for (int pa = 0; pa < B; ++pa)
+#pragma unroll
+                    for (int pb = 0; pb < B; ++pb) {
+                        const double w = 0.5 * (ldg(wcsr + slot[pa * B + pb]) + ldg(wcsr + slot[pb * B + pa]));
+#pragma unroll
+                        for (int r = 0; r < D; ++r)
+#pragma unroll
+                            for (int k = 0; k < D; ++k) S[r][k] += w * dp[r * B + pa] * dp[k * B + pb];
+                    }
+                double MS[D][D], Pm[D][D];
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        double t = 0.0;
+#pragma unroll
+                        for (int m = 0; m < D; ++m) t += M[r][m] * S[m][k];
+                        MS[r][k] = t;
+                    }
+                double tr = 0.0;
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        double t = 0.0;
+#pragma unroll
+                        for (int m = 0; m < D; ++m) t += MS[r][m] * M[k][m];
+                        Pm[r][k] = t;
+                        if (r == k) tr += t;
+                    }
+                gk += wq * adet * tr;
+                const double f = kv * wq * adet;
+#pragma unroll
+                for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        double t = 0.0;
+#pragma unroll
+                        for (int m = 0; m < D; ++m) t += M[m][r] * ((m == k ? tr : 0.0) - 2.0 * Pm[m][k]);
+                        GJ[r][k] = f * t;
+                    }
+            }
+#pragma unroll
+            for (int c = 0; c < B; ++c)
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    double t = 0.0;
+#pragma unroll
+                    for (int r = 0; r < D; ++r) t += GJ[r][d] * dp[r * B + c];
+                    lv[c][d] += t;
+                }
+        }
+        if (gkap) gkap[e] = MASS ? 0.0 : gk * a.kappa_scale;
+        double* out = LV + (size_t)el * B * D;
+#pragma unroll
+        for (int b = 0; b < B; ++b)
+#pragma unroll
+            for (int d = 0; d < D; ++d) out[b * D + d] = lv[b][d];
+    }
+    __syncthreads();
+    if (a.grad_points) node_reduce<double, D>(P, LV, static_cast<double*>(a.grad_points), a.workspace);
+}
+
+template <int ET, bool MASS>
+int run_adjoint_gen(const tm_adjoint_args& a, cudaStream_t st) {
+    using T = Traits<ET>;
+    const TableLayout TL = table_layout(a.tables.n_quad, T::B, T::D);
+    const size_t smem = align16(sizeof(double) * TL.total) + sizeof(double) * (size_t)a.plan.chunk_elems * T::B * T::D;
+    if (smem > 227 * 1024) return tm_set_error(TM_ERR_TOO_LARGE, "tm_adjoint_general: chunk too large for shared memory");
+    if (a.grad_points) {
+        if (cudaMemsetAsync(a.grad_points, 0, sizeof(double) * (size_t)a.n_points * T::D, st) != cudaSuccess)
+            return adj_status("cudaMemsetAsync");
+        if (a.plan.n_shared > 0) {
+            void* counters = static_cast<unsigned char*>(a.workspace) + node_counters_offset<double>(a.plan, T::D);
+            if (cudaMemsetAsync(counters, 0, sizeof(int32_t) * (size_t)a.plan.n_shared, st) != cudaSuccess)
+                return adj_status("cudaMemsetAsync");
+        }
+    }
+    if (a.plan.n_chunks == 0) return TM_OK;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_adjoint_gen<ET, MASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+        return adj_status("cudaFuncSetAttribute");
+    k_adjoint_gen<ET, MASS><<<a.plan.n_chunks, kAdjThreads, smem, st>>>(a);
+    return adj_status("k_adjoint_gen");
+}
+
+template <int ET>
+int dispatch_gen(const tm_adjoint_args& a, cudaStream_t st) {
+    return a.k_mode == TM_ADJ_M_CSR ? run_adjoint_gen<ET, true>(a, st) : run_adjoint_gen<ET, false>(a, st);
+}
+
 inline int adj_status(const char* what) {
     const cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) {
@@ -252,7 +428,8 @@ using namespace tmk;
 
 extern "C" size_t tm_adjoint_workspace_bytes(const tm_adjoint_args* a) {
     if (!a) return 0;
-    const int D = a->tables.element_type == TM_TRI3 ? 2 : 3;
+    const int et = a->tables.element_type;
+    const int D = (et == TM_TET4 || et == TM_TET10) ? 3 : 2;
     return node_counters_offset<double>(a->plan, D) + sizeof(int32_t) * (size_t)a->plan.n_shared;
 }
 
@@ -279,4 +456,27 @@ extern "C" int tm_adjoint_p1(const tm_adjoint_args* a, tm_stream_t stream) {
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_p1: workspace is null");
     const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     return et == TM_TRI3 ? dispatch_kmode<TM_TRI3>(*a, st) : dispatch_kmode<TM_TET4>(*a, st);
+}
+
+extern "C" int tm_adjoint_general(const tm_adjoint_args* a, tm_stream_t stream) {
+    if (!a) return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_general: null args");
+    if (a->dtype != TM_F64) return tm_set_error(TM_ERR_UNSUPPORTED, "tm_adjoint_general: float64 only");
+    if (a->k_mode != TM_ADJ_K_CSR && a->k_mode != TM_ADJ_M_CSR)
+        return tm_set_error(TM_ERR_UNSUPPORTED, "tm_adjoint_general: k_mode TM_ADJ_K_CSR or TM_ADJ_M_CSR only");
+    if (a->load_source != TM_ADJ_LOAD_NONE)
+        return tm_set_error(TM_ERR_UNSUPPORTED, "tm_adjoint_general: no load term");
+    if (!a->weights || !a->slot_map || !a->tables.packed || (a->plan.n_elements > 0 && !a->points))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_general: null weights, slot map, tables or points");
+    if (a->grad_points && a->plan.n_shared > 0 && !a->workspace)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_general: workspace is null");
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    switch (a->tables.element_type) {
+        case TM_TRI3: return dispatch_gen<TM_TRI3>(*a, st);
+        case TM_TET4: return dispatch_gen<TM_TET4>(*a, st);
+        case TM_TRI6: return dispatch_gen<TM_TRI6>(*a, st);
+        case TM_TET10: return dispatch_gen<TM_TET10>(*a, st);
+        case TM_QUAD4: return dispatch_gen<TM_QUAD4>(*a, st);
+        case TM_QUAD9: return dispatch_gen<TM_QUAD9>(*a, st);
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_adjoint_general: unknown element type");
+    }
 }
