@@ -466,6 +466,7 @@ int tm_quadrature_points(int32_t dtype, int64_t n_elements, const int32_t* conn,
 #define TM_ADJ_K_CSR    1
 #define TM_ADJ_K_OUTER  2
 #define TM_ADJ_M_CSR    3
+#define TM_ADJ_E_CSR    4
 #define TM_ADJ_LOAD_NONE  0
 #define TM_ADJ_LOAD_CONST 1
 #define TM_ADJ_LOAD_NODAL 2
@@ -489,14 +490,18 @@ typedef struct tm_adjoint_args {
     void* workspace;           /* >= tm_adjoint_workspace_bytes() */
     tm_element_tables tables;
     tm_chunk_plan plan;        /* node plan of the mesh */
+    double poisson;            /* TM_ADJ_E_CSR: the Poisson ratio */
 } tm_adjoint_args;
 size_t tm_adjoint_workspace_bytes(const tm_adjoint_args* args);
 int tm_adjoint_p1(const tm_adjoint_args* args, tm_stream_t stream);
 /*
  * The same gradients on any element type (P2 triangles and tetrahedra,
  * quadrilaterals, and P1), per quadrature point, for k_mode TM_ADJ_K_CSR
- * (diffusion: grad_kappa and grad_points) or TM_ADJ_M_CSR (mass:
- * grad_points); no outer-product weights or load term.
+ * (diffusion: grad_kappa and grad_points), TM_ADJ_M_CSR (mass:
+ * grad_points), TM_ADJ_E_CSR (isotropic elasticity, weights [nnz, D, D]
+ * blocks, kappa the per-element modulus, poisson the ratio: grad_points) or
+ * TM_ADJ_K_NONE; a load term (constant or nodal source, weighted by lam)
+ * with any k_mode but TM_ADJ_E_CSR; no outer-product weights.
  */
 int tm_adjoint_general(const tm_adjoint_args* args, tm_stream_t stream);
 

@@ -102,7 +102,7 @@ class AdjointArgs(C.Structure):
         ("weights", C.c_void_p), ("slot_map", C.c_void_p), ("u", C.c_void_p), ("lam", C.c_void_p),
         ("load_const", C.c_double), ("load_values", C.c_void_p), ("grad_kappa", C.c_void_p),
         ("grad_points", C.c_void_p), ("workspace", C.c_void_p),
-        ("tables", ElementTables), ("plan", ChunkPlan),
+        ("tables", ElementTables), ("plan", ChunkPlan), ("poisson", C.c_double),
     ]
 
 
@@ -115,7 +115,7 @@ class CoefGradArgs(C.Structure):
     ]
 
 
-TM_ADJ_K_NONE, TM_ADJ_K_CSR, TM_ADJ_K_OUTER, TM_ADJ_M_CSR = 0, 1, 2, 3
+TM_ADJ_K_NONE, TM_ADJ_K_CSR, TM_ADJ_K_OUTER, TM_ADJ_M_CSR, TM_ADJ_E_CSR = 0, 1, 2, 3, 4
 TM_ADJ_LOAD_NONE, TM_ADJ_LOAD_CONST, TM_ADJ_LOAD_NODAL = 0, 1, 2
 
 

@@ -13,7 +13,8 @@ docs/source/user_guide/differentiability.rst:34-56).  Here:
 * ``ElasticityAssembly`` -- the values of an isotropic elasticity matrix as
   a function of its modulus (``tm_coef_grad``: dL/dE_e is the
   contraction of dL/dvalues with the element's blocks at unit modulus).
-* ``LoadAssembly`` -- a P1 load vector as a function of node coordinates.
+* ``LoadAssembly`` -- a load vector (any element type) as a function of
+  node coordinates and of its constant or nodal source.
 * ``SparseSolve`` -- x = A^-1 b with Jacobi-PCG; backward solves A^T lambda =
   dL/dx (A symmetric) and returns dL/dvalues = -lambda_row x_col, dL/db = lambda.
 * ``solve_diffusion`` -- the fused form for losses through a Dirichlet
@@ -33,9 +34,10 @@ from .element import element_tables
 
 def _adjoint_call(topo, points, kappa, kappa_scale, k_mode, weights=None, slot=None, u=None, lam=None,
                   load_source=_lib.TM_ADJ_LOAD_NONE, load_const=0.0, load_values=None,
-                  want_kappa=True, want_points=True):
+                  want_kappa=True, want_points=True, poisson=0.3):
     """``tm_adjoint_p1`` on P1 elements, ``tm_adjoint_general`` (per
-    quadrature point; diffusion and mass weights only) on the others."""
+    quadrature point; diffusion, mass and elasticity weights only) on the
+    others and for elasticity on every element type."""
     lib = _lib.load()
     dev = points.device
     pts = points.detach().to(torch.float64).contiguous()
@@ -59,6 +61,7 @@ def _adjoint_call(topo, points, kappa, kappa_scale, k_mode, weights=None, slot=N
     a.load_const = float(load_const)
     lv = None if load_values is None else load_values.detach().to(torch.float64).contiguous()
     a.load_values = _lib.ptr(lv)
+    a.poisson = float(poisson)
     gk = torch.empty(E, dtype=torch.float64, device=dev) if want_kappa else None
     gp = torch.empty(topo.n_points, topo.info.dim, dtype=torch.float64, device=dev) if want_points else None
     a.grad_kappa, a.grad_points = _lib.ptr(gk), _lib.ptr(gp)
@@ -66,7 +69,7 @@ def _adjoint_call(topo, points, kappa, kappa_scale, k_mode, weights=None, slot=N
     a.tables = topo.table_struct(dev)
     ws = torch.empty(max(1, lib.tm_adjoint_workspace_bytes(C.byref(a))), dtype=torch.uint8, device=dev)
     a.workspace = _lib.ptr(ws)
-    if topo.etype in ("triangle", "tetra"):
+    if topo.etype in ("triangle", "tetra") and k_mode != _lib.TM_ADJ_E_CSR:
         _lib.check(lib.tm_adjoint_p1(C.byref(a), _lib.stream_handle(dev)), "tm_adjoint_p1")
     else:
         _lib.check(lib.tm_adjoint_general(C.byref(a), _lib.stream_handle(dev)), "tm_adjoint_general")
@@ -188,10 +191,12 @@ def coef_grad(topo, points, gvals, slot, form, scale, poisson=0.3):
 
 
 class ElasticityAssembly(torch.autograd.Function):
-    """values = K(E) of an isotropic elasticity form (float64, any element
-    type) as a function of its modulus E (per element or a scalar tensor;
-    ``coefs``: the form's other kernel coefficients, nu and E_scale); the
-    backward runs ``tm_coef_grad`` on dL/dvalues."""
+    """values = K(E, points) of an isotropic elasticity form (float64, any
+    element type) as a function of its modulus E (per element or a scalar
+    tensor; ``coefs``: the form's other kernel coefficients, nu and E_scale)
+    and of the node coordinates; the backward runs ``tm_coef_grad`` (dL/dE)
+    and ``tm_adjoint_general`` in elasticity mode (dL/dpoints) on
+    dL/dvalues."""
 
     @staticmethod
     def forward(ctx, young, points, asm, coefs):
@@ -208,30 +213,73 @@ class ElasticityAssembly(torch.autograd.Function):
         asm = ctx.asm
         et = asm.element_types[0]
         slot = asm.projector[et].indices.to(points.device)
-        g = coef_grad(asm._topology, points, gvals, slot, _lib.TM_FORM_ELASTICITY, ctx.escale, ctx.nu)
-        gy = g if young.dim() > 0 and young.numel() > 1 else g.sum().reshape(young.shape)
-        return gy.to(young.dtype), None, None, None
+        topo = asm._topology
+        per_element = young.dim() > 0 and young.numel() > 1
+        gy = gp = None
+        if ctx.needs_input_grad[0]:
+            g = coef_grad(topo, points, gvals, slot, _lib.TM_FORM_ELASTICITY, ctx.escale, ctx.nu)
+            gy = (g if per_element else g.sum().reshape(young.shape)).to(young.dtype)
+        if ctx.needs_input_grad[1]:
+            ey = young.detach().reshape(-1) if per_element else None
+            scale = ctx.escale * (1.0 if per_element else float(young.detach().reshape(())))
+            _, gp = _adjoint_call(topo, points, ey, scale, _lib.TM_ADJ_E_CSR, weights=gvals, slot=slot,
+                                  want_kappa=False, want_points=True, poisson=ctx.nu)
+            gp = gp.to(points.dtype)
+        return gy, gp, None, None
 
 
 class LoadAssembly(torch.autograd.Function):
-    """b(points) for a constant or nodal source (float64, P1)."""
+    """b(points, s) = sum_q w_q |det J_q| phi_a(q) f(q) for a constant
+    (``src`` [W]) or nodal (``src`` [N, W]) source, any element type.
+    dL/dpoints runs the load term of ``tm_adjoint_p1`` / ``tm_adjoint_general``
+    (one call per component for a nodal source; for a constant one the
+    components fold into one weight lam . c); dL/dsrc is linear: the load
+    vector of the nodal source lam (the mass matrix applied to lam), or
+    lam_k . b(c = 1) per constant component."""
 
     @staticmethod
-    def forward(ctx, points, topo, source, const, values, run):
-        ctx.topo, ctx.source, ctx.const = topo, source, const
-        ctx.save_for_backward(points, values if values is not None else torch.empty(0))
-        ctx.has_values = values is not None
-        return run()
+    def forward(ctx, points, src, topo, source, width):
+        from .assemble import _run_vector
+        ctx.topo, ctx.source, ctx.width = topo, source, width
+        s = src.detach()
+        ctx.save_for_backward(points, s)
+        pts = points.detach().contiguous()
+        if source == _lib.TM_SOURCE_CONST:
+            return _run_vector(topo, pts, source, None, s.reshape(-1).tolist(), width)
+        vals = s.reshape(topo.n_points, width).to(device=pts.device, dtype=pts.dtype).contiguous()
+        return _run_vector(topo, pts, source, vals, None, width)
 
     @staticmethod
     def backward(ctx, gb):
-        points, values = ctx.saved_tensors
-        _require_p1(ctx.topo)
-        load = _lib.TM_ADJ_LOAD_CONST if ctx.source == _lib.TM_SOURCE_CONST else _lib.TM_ADJ_LOAD_NODAL
-        _, gp = _adjoint_call(ctx.topo, points, None, 1.0, _lib.TM_ADJ_K_NONE, lam=gb.reshape(-1),
-                              load_source=load, load_const=ctx.const,
-                              load_values=values if ctx.has_values else None, want_kappa=False)
-        return gp.to(points.dtype), None, None, None, None, None
+        from .assemble import _run_vector
+        points, s = ctx.saved_tensors
+        topo, W, N = ctx.topo, ctx.width, ctx.topo.n_points
+        pts = points.detach().contiguous()
+        lam = gb.detach().reshape(N, W)
+        gp = gs = None
+        if ctx.needs_input_grad[0]:
+            if ctx.source == _lib.TM_SOURCE_CONST:
+                c = s.reshape(W).to(device=lam.device, dtype=torch.float64)
+                _, gp = _adjoint_call(topo, points, None, 1.0, _lib.TM_ADJ_K_NONE,
+                                      lam=lam.to(torch.float64) @ c, load_source=_lib.TM_ADJ_LOAD_CONST,
+                                      load_const=1.0, want_kappa=False)
+            else:
+                f = s.reshape(N, W).to(device=lam.device, dtype=torch.float64)
+                for k in range(W):
+                    _, g = _adjoint_call(topo, points, None, 1.0, _lib.TM_ADJ_K_NONE, lam=lam[:, k],
+                                         load_source=_lib.TM_ADJ_LOAD_NODAL, load_values=f[:, k],
+                                         want_kappa=False)
+                    gp = g if gp is None else gp + g
+            gp = gp.to(points.dtype)
+        if ctx.needs_input_grad[1]:
+            lt = lam.to(pts.dtype).contiguous()
+            if ctx.source == _lib.TM_SOURCE_CONST:
+                b1 = _run_vector(topo, pts, ctx.source, None, [1.0] * W, W).reshape(N, W)
+                gs = (lt * b1).sum(0)
+            else:
+                gs = _run_vector(topo, pts, _lib.TM_SOURCE_NODAL, lt, None, W)
+            gs = gs.reshape(s.shape).to(device=s.device, dtype=s.dtype)
+        return gp, gs, None, None, None
 
 
 class SparseSolve(torch.autograd.Function):

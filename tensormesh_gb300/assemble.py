@@ -505,16 +505,15 @@ class ElementAssembler(_AssemblerBase):
                 values = MassAssembly.apply(points, rho_t, self, dict(sd))
                 return self._build_output(values)
             if form == "elasticity":
-                if points.requires_grad:
-                    raise NotImplementedError("gradients of the elasticity form with respect to the node "
-                                              "coordinates are not implemented (with respect to the modulus "
-                                              "they are)")
                 c = self._tm_coefficients(ed, sd, self.elements[et].shape[0])
                 young = c.get("E")
                 if torch.is_tensor(c.get("nu")) and c["nu"].requires_grad:
                     raise NotImplementedError("gradients with respect to the Poisson ratio are not implemented")
-                if torch.is_tensor(young) and young.requires_grad:
+                if points.requires_grad or (torch.is_tensor(young) and young.requires_grad):
                     from .adjoint import ElasticityAssembly
+                    if not torch.is_tensor(young):
+                        young = torch.tensor(1.0 if young is None else float(young), dtype=torch.float64,
+                                             device=points.device)
                     rest = {k: v for k, v in c.items() if k != "E"}
                     values = ElasticityAssembly.apply(young, points, self, rest)
                     return self._build_output(values)
@@ -925,25 +924,20 @@ def assemble_linear_form(asm: NodeAssembler, fn: Callable, points: torch.Tensor,
     needs_grad = torch.is_grad_enabled() and (points.requires_grad or any(
         torch.is_tensor(v) and v.requires_grad for v in list(point_data.values()) + list(scalar_data.values())))
     if source is not None and source[0] == "const":
-        c = torch.as_tensor(source[1], dtype=torch.float64).reshape(-1)
-        run = lambda: _run_vector(topo, pts, _lib.TM_SOURCE_CONST, None, c.tolist(), int(c.numel()))
-        if needs_grad:
-            if c.numel() != 1 or not points.requires_grad:
-                raise NotImplementedError("gradients of vector-valued loads are not implemented")
+        c = source[1] if torch.is_tensor(source[1]) else torch.as_tensor(source[1], dtype=torch.float64)
+        c = c.reshape(-1)
+        if needs_grad or (torch.is_grad_enabled() and c.requires_grad):
             from .adjoint import LoadAssembly
-            return LoadAssembly.apply(points, topo, _lib.TM_SOURCE_CONST, float(c[0]), None, run)
-        return run()
+            return LoadAssembly.apply(points, c, topo, _lib.TM_SOURCE_CONST, int(c.numel()))
+        return _run_vector(topo, pts, _lib.TM_SOURCE_CONST, None, c.tolist(), int(c.numel()))
     if source is not None and source[0] == "nodal" and source[1] in point_data:
         f = point_data[source[1]].to(device=dev, dtype=dt)
         width = 1 if f.dim() == 1 else int(np.prod(f.shape[1:]))
-        fv = f.detach().reshape(f.shape[0], width).contiguous()
-        run = lambda: _run_vector(topo, pts, _lib.TM_SOURCE_NODAL, fv, None, width)
         if needs_grad:
-            if width != 1 or f.requires_grad:
-                raise NotImplementedError("gradients with respect to the nodal source are not implemented")
             from .adjoint import LoadAssembly
-            return LoadAssembly.apply(points, topo, _lib.TM_SOURCE_NODAL, 0.0, fv.reshape(-1), run)
-        return run()
+            return LoadAssembly.apply(points, f, topo, _lib.TM_SOURCE_NODAL, width)
+        fv = f.detach().reshape(f.shape[0], width).contiguous()
+        return _run_vector(topo, pts, _lib.TM_SOURCE_NODAL, fv, None, width)
     if needs_grad:
         raise NotImplementedError("gradients of general linear forms are not implemented")
     # general source g(x, data) * v: evaluate g at the quadrature points

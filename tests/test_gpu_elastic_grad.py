@@ -48,6 +48,57 @@ def test_young_gradient_matches_oracle_autograd(etype, cuda):
     assert rel_fro(E.grad.cpu(), Eo.grad) <= 1e-10
 
 
+@pytest.mark.parametrize("etype", list(MESHES))
+@pytest.mark.parametrize("per_element", [True, False])
+def test_point_gradient_matches_oracle_autograd(etype, per_element, cuda):
+    """dL/dpoints of L = sum W : K(points, E) (the elasticity mode of
+    ``tm_adjoint_general``) together with dL/dE, against the oracle's
+    autograd, per-element and scalar modulus."""
+    mesh = MESHES[etype]()
+    rng = np.random.default_rng(69)
+    E0 = torch.from_numpy(rng.uniform(0.5, 2.0, mesh.n_elements)) if per_element else torch.tensor(1.7,
+                                                                                                  dtype=torch.float64)
+    gm = mesh.to(cuda)
+    asm = tg.LinearElasticityElementAssembler.from_mesh(gm, nu=0.27)
+    D = mesh.points.shape[1]
+    W = torch.from_numpy(rng.uniform(-1.0, 1.0, (asm.edges.shape[1], D, D)))
+    P = gm.points.clone().requires_grad_(True)
+    E = E0.clone().to(cuda).requires_grad_(True)
+    K = asm(P, element_data={"E": E}) if per_element else asm(P, scalar_data={"E": E})
+    vals = K.values.reshape(-1, D, D)
+    (vals * W.to(cuda)).sum().backward()
+    Po = mesh.points.clone().requires_grad_(True)
+    Eo = E0.clone().requires_grad_(True)
+    Ef = Eo if per_element else Eo.expand(mesh.n_elements)
+    conn = mesh.elements().long()
+    _, _, Ko = O.assemble_matrix(Po, conn, mesh.n_points,
+                                 lambda p, c, E: O.element_locals_elasticity(p, c, etype, E, 0.27, 2), E=Ef)
+    assert rel_fro(vals.detach().cpu(), Ko.detach()) <= 1e-12
+    (Ko * W).sum().backward()
+    assert rel_fro(P.grad.cpu(), Po.grad) <= 1e-10
+    assert rel_fro(E.grad.cpu(), Eo.grad) <= 1e-10
+
+
+def test_point_gradient_constant_modulus(cuda):
+    """Points alone requiring grad, the modulus a plain number of the
+    assembler (E = 3, nu = 0.2)."""
+    mesh = MESHES["tetra"]()
+    gm = mesh.to(cuda)
+    asm = tg.LinearElasticityElementAssembler.from_mesh(gm, E=3.0, nu=0.2)
+    rng = np.random.default_rng(70)
+    W = torch.from_numpy(rng.uniform(-1.0, 1.0, (asm.edges.shape[1], 3, 3)))
+    P = gm.points.clone().requires_grad_(True)
+    vals = asm(P).values.reshape(-1, 3, 3)
+    (vals * W.to(cuda)).sum().backward()
+    Po = mesh.points.clone().requires_grad_(True)
+    conn = mesh.elements().long()
+    Ef = torch.full((mesh.n_elements,), 3.0, dtype=torch.float64)
+    _, _, Ko = O.assemble_matrix(Po, conn, mesh.n_points,
+                                 lambda p, c, E: O.element_locals_elasticity(p, c, "tetra", E, 0.2, 2), E=Ef)
+    (Ko * W).sum().backward()
+    assert rel_fro(P.grad.cpu(), Po.grad) <= 1e-10
+
+
 class SIMPElastic(tg.ElementAssembler):
     """The plane-stress SIMP form of the reference's compliance example
     (examples/inverse_design/compliance_topology.py:31-110), restated."""
