@@ -285,6 +285,24 @@ def run_ours(args, ws, rank, local):
     h2d = pts_h.numel() * 8 + kap_h.numel() * 8
     d2h = 2 * nnz * 8
 
+    # the host link's own rate for the same bytes: the two result copies
+    # alone (device to pinned host), which bound e2e from below
+    K0, M0 = tg.assemble_forms([K_asm, M_asm], mesh.points, ed)
+    K_h0, M_h0 = bufs[0][2], bufs[0][3]
+    for _ in range(3):
+        K_h0.copy_(K0, non_blocking=True)
+        M_h0.copy_(M0, non_blocking=True)
+    torch.cuda.synchronize()
+    l_s, l_e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l_s.record(cur)
+    for _ in range(args.steps):
+        K_h0.copy_(K0, non_blocking=True)
+        M_h0.copy_(M0, non_blocking=True)
+    l_e.record(cur)
+    torch.cuda.synchronize()
+    d2h_ms = l_s.elapsed_time(l_e) / args.steps
+    del K0, M0
+
     peak, peak_kind = _peaks()
     abytes = algorithmic_bytes(N, E, nnz)
     achieved = abytes / (ms * 1e-3) / 1e9
@@ -306,7 +324,9 @@ def run_ours(args, ws, rank, local):
                    "quadrature_order": 2, "l2": "flushed between steps (512 MB write)",
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": E * ws / (e2e_ms * 1e-3), "unit": "elements/s", "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "d2h_copy_ms": d2h_ms, "d2h_link_gbs": d2h / (d2h_ms * 1e-3) / 1e9,
+                "link_frac": d2h_ms / e2e_ms},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_p1df + k_p1df_finalize (one assembly pass)",
