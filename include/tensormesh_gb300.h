@@ -661,6 +661,26 @@ typedef struct tm_batched_pcg_args {
 } tm_batched_pcg_args;
 int tm_batched_pcg(const tm_batched_pcg_args* args, tm_stream_t stream);
 
+/*
+ * The same batch (float64 matrix) by mixed-precision iterative refinement:
+ * per system, the float64 residual r = b - A x, a float32 Jacobi-PCG solve
+ * of A d = r / ||r|| until its residual falls by inner_rtol, x += ||r|| d in
+ * float64, until the true residual meets ||b - A x|| <= rtol ||b|| (the
+ * convergence test of tm_batched_pcg) or max_outer corrections or
+ * base.max_iter inner iterations in all.  base.work: device [5 * n_rows]
+ * float64 (the float64 residual and six float32 vectors); values32: device
+ * float [nnz], written by the call.  status.iterations counts the inner
+ * iterations; status.relative_residual is the true float64 residual.
+ */
+typedef struct tm_batched_mixed_args {
+    tm_batched_pcg_args base;
+    void* values32;
+    double inner_rtol;         /* e.g. 1e-4 */
+    int32_t max_outer;
+    int32_t reserved;
+} tm_batched_mixed_args;
+int tm_batched_pcg_mixed(const tm_batched_mixed_args* args, tm_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -158,6 +158,11 @@ class BatchedPcgArgs(C.Structure):
                 ("status", C.c_void_p), ("order", C.c_void_p)]
 
 
+class BatchedMixedArgs(C.Structure):
+    _fields_ = [("base", BatchedPcgArgs), ("values32", C.c_void_p), ("inner_rtol", C.c_double),
+                ("max_outer", C.c_int32), ("reserved", C.c_int32)]
+
+
 TM_PCG_CONVERGED, TM_PCG_MAX_ITER, TM_PCG_BREAKDOWN = 1, 2, 3
 TM_BICG_RR, TM_BICG_BB, TM_BICG_ITER, TM_BICG_FLAG = 5, 7, 8, 9
 
@@ -206,6 +211,7 @@ _SIGNATURES = {
     "tm_adjoint_general": (C.c_int, [C.POINTER(AdjointArgs), C.c_void_p]),
     "tm_coef_grad": (C.c_int, [C.POINTER(CoefGradArgs), C.c_void_p]),
     "tm_batched_pcg": (C.c_int, [C.POINTER(BatchedPcgArgs), C.c_void_p]),
+    "tm_batched_pcg_mixed": (C.c_int, [C.POINTER(BatchedMixedArgs), C.c_void_p]),
     "tm_pcg_partials_bytes": (C.c_size_t, []),
     "tm_pcg_start": (C.c_int, [C.POINTER(PcgArgs), C.c_void_p]),
     "tm_bicgstab_start": (C.c_int, [C.POINTER(BicgstabArgs), C.c_void_p]),

@@ -15,6 +15,12 @@ With ``autotune=True`` the elements per chunk of the stiffness and load
 launches are timed over the candidate sizes on the batch itself
 (``autotune.tune_matrix`` / ``tune_vector``) before anything is captured;
 ``chunks`` holds the sizes used.
+
+``precision="mixed"`` (float64 batches) solves by mixed-precision iterative
+refinement instead (``tm_batched_pcg_mixed``): float64 residuals and
+corrections around float32 Jacobi-PCG inner solves, to the same test on the
+true float64 residual, ||b - A x|| <= rtol ||b||.  GB300 runs float64 at
+1/64 of the float32 rate, and the float64 PCG of a system is bound by it.
 """
 import ctypes as C
 from dataclasses import dataclass
@@ -76,6 +82,7 @@ class BatchedDiffusion:
         self.order = torch.from_numpy(np.argsort(-sizes, kind="stable").astype(np.int32)).to(dev)
         self.dirichlet = bnd.to(dev).to(torch.uint8)
         self._graph = None
+        self._values32 = None
         if autotune:
             from . import autotune as tuner
             pts = self.mesh.points.to(dtype)
@@ -103,7 +110,8 @@ class BatchedDiffusion:
 
     # ------------------------------------------------------------------
     def _solve_into(self, kappa: torch.Tensor, f: torch.Tensor, x: torch.Tensor, work: torch.Tensor,
-                    queue: torch.Tensor, status: torch.Tensor, rtol: float, max_iter: int):
+                    queue: torch.Tensor, status: torch.Tensor, rtol: float, max_iter: int,
+                    precision: str = "float64", inner_rtol: float = 1e-4, max_outer: int = 30):
         from .assemble import assemble_forms
         lib = _lib.load()
         (values,) = assemble_forms([self.K_asm], self.mesh.points, {"kappa": kappa})
@@ -126,7 +134,21 @@ class BatchedDiffusion:
         a.queue, a.status = _lib.ptr(queue), _lib.ptr(status)
         a.order = _lib.ptr(self.order)
         x.zero_()
-        _lib.check(lib.tm_batched_pcg(C.byref(a), _lib.stream_handle(self.device)), "tm_batched_pcg")
+        if precision == "mixed":
+            if values.dtype != torch.float64:
+                raise ValueError("precision='mixed' refines float64 batches")
+            if self._values32 is None or self._values32.numel() != values.numel():
+                self._values32 = torch.empty(values.numel(), dtype=torch.float32, device=self.device)
+            m = _lib.BatchedMixedArgs()
+            m.base = a
+            m.values32 = _lib.ptr(self._values32)
+            m.inner_rtol, m.max_outer = float(inner_rtol), int(max_outer)
+            _lib.check(lib.tm_batched_pcg_mixed(C.byref(m), _lib.stream_handle(self.device)),
+                       "tm_batched_pcg_mixed")
+        elif precision == "float64":
+            _lib.check(lib.tm_batched_pcg(C.byref(a), _lib.stream_handle(self.device)), "tm_batched_pcg")
+        else:
+            raise ValueError(f"precision must be 'float64' or 'mixed', not {precision!r}")
         return values, b
 
     def _buffers(self):
@@ -141,18 +163,23 @@ class BatchedDiffusion:
         dbl = raw.view(torch.float64).reshape(self.n_systems, 2)
         return BatchStatus(ints[:, 0].clone(), ints[:, 1].clone(), dbl[:, 1].clone())
 
-    def solve(self, kappa: torch.Tensor, f: torch.Tensor, rtol: float = 1e-10, max_iter: int = 100000):
+    def solve(self, kappa: torch.Tensor, f: torch.Tensor, rtol: float = 1e-10, max_iter: int = 100000,
+              precision: str = "float64", inner_rtol: float = 1e-4, max_outer: int = 30):
         """Assemble every system and solve them all; returns (u [n_points]
-        concatenated, BatchStatus)."""
+        concatenated, BatchStatus).  ``precision="mixed"``: iterative
+        refinement with float32 inner solves (``inner_rtol``: their residual
+        reduction; at most ``max_outer`` corrections)."""
         kappa = kappa.to(device=self.device, dtype=self.dtype).contiguous()
         f = f.to(device=self.device, dtype=self.dtype).contiguous()
         x, work, queue, status = self._buffers()
-        self._solve_into(kappa, f, x, work, queue, status, rtol, max_iter)
+        self._solve_into(kappa, f, x, work, queue, status, rtol, max_iter, precision, inner_rtol, max_outer)
         return x, self._status(status)
 
     # ------------------------------------------------------------------
-    def capture(self, rtol: float = 1e-10, max_iter: int = 100000):
+    def capture(self, rtol: float = 1e-10, max_iter: int = 100000, precision: str = "float64",
+                inner_rtol: float = 1e-4, max_outer: int = 30):
         """Record assembly + load + batched solve as one CUDA graph."""
+        opts = (precision, inner_rtol, max_outer)
         dev = self.device
         self._kappa = torch.ones(self.n_elements, dtype=self.dtype, device=dev)
         self._f = torch.zeros(self.n_points, dtype=self.dtype, device=dev)
@@ -160,13 +187,14 @@ class BatchedDiffusion:
         side = torch.cuda.Stream(dev)
         side.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(side):                    # warm-up: plans, tables, allocator pools
-            self._solve_into(self._kappa, self._f, self._x, self._work, self._queue, self._status_raw, rtol, 1)
+            self._solve_into(self._kappa, self._f, self._x, self._work, self._queue, self._status_raw, rtol, 1,
+                             *opts)
         torch.cuda.current_stream(dev).wait_stream(side)
         torch.cuda.synchronize(dev)
         self._graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self._graph):
             self._solve_into(self._kappa, self._f, self._x, self._work, self._queue, self._status_raw,
-                             rtol, max_iter)
+                             rtol, max_iter, *opts)
         return self
 
     def replay(self, kappa: torch.Tensor, f: torch.Tensor):

@@ -402,6 +402,8 @@ __global__ void __launch_bounds__(p1_threads<NE>(), 2) k_p1df(const tm_matrix_ar
             // lane x: the stiffness sum, lane y: the sum of |det| rho; TwoSum
             // on the leading parts, the error terms and low parts summed
             float2 acc = make_float2(0.0f, 0.0f), err = make_float2(0.0f, 0.0f);
+            // unrolled so that the next contributions' loads issue early
+#pragma unroll 4
             for (int p = p0; p < p1; ++p) {
                 const unsigned idx = (unsigned)CT[p] >> 1;
                 const unsigned e = idx / (unsigned)NL;       // record e, entry idx - e NL

@@ -87,3 +87,46 @@ def test_batched_other_element_types(order, cell, cuda):
     assert st.all_converged
     for m, k, f, ui in zip(meshes, kappas, fs, batch.split(u)):
         assert rel_fro(ui, _oracle_solution(m, k, f)) <= 1e-9
+
+
+def test_mixed_precision_refinement_matches_per_mesh(cuda):
+    """precision="mixed": float32 inner Jacobi-PCG solves inside float64
+    refinement reach the same test on the true float64 residual; solutions
+    against the oracle's direct solves, bitwise reproducible, and the graph
+    replay equal to the eager call."""
+    sizes = [1, 3, 7, 16, 5, 24, 11, 40]
+    meshes, kappas, fs = _batch(sizes, seed=57)
+    batch = BatchedDiffusion([m.to(cuda) for m in meshes])
+    kap, f = torch.cat(kappas), torch.cat(fs)
+    u, st = batch.solve(kap, f, rtol=1e-12, precision="mixed")
+    assert st.all_converged, st.flag
+    assert float(st.relative_residual.max()) <= 1e-12
+    for m, k, fi, ui in zip(meshes, kappas, fs, batch.split(u)):
+        ref = _oracle_solution(m, k, fi)
+        if float(ref.norm()) == 0.0:
+            assert float(ui.abs().max()) == 0.0
+        else:
+            assert rel_fro(ui, ref) <= 1e-9
+    u2, _ = batch.solve(kap, f, rtol=1e-12, precision="mixed")
+    assert torch.equal(u, u2)
+    u64, st64 = batch.solve(kap, f, rtol=1e-12)
+    assert rel_fro(u, u64) <= 1e-9
+    g = BatchedDiffusion([m.to(cuda) for m in meshes]).capture(rtol=1e-12, precision="mixed")
+    ug, stg = g.replay(kap, f)
+    torch.cuda.synchronize()
+    assert stg.all_converged and torch.equal(ug, u)
+
+
+def test_mixed_precision_limits(cuda):
+    """An inner tolerance outside (0, 1) and a float32 batch are refused;
+    max_outer = 0 stops before any correction (flag max_iter)."""
+    meshes, kappas, fs = _batch([6, 9], seed=58)
+    batch = BatchedDiffusion([m.to(cuda) for m in meshes])
+    kap, f = torch.cat(kappas), torch.cat(fs)
+    with pytest.raises(RuntimeError):
+        batch.solve(kap, f, precision="mixed", inner_rtol=1.5)
+    _, st = batch.solve(kap, f, precision="mixed", max_outer=0)
+    assert bool((st.flag == 2).all())
+    b32 = BatchedDiffusion([m.to(cuda) for m in meshes], dtype=torch.float32)
+    with pytest.raises(ValueError):
+        b32.solve(kap, f, precision="mixed")
