@@ -515,18 +515,23 @@ int tm_adjoint_general(const tm_adjoint_args* args, tm_stream_t stream);
  * poisson the call's Poisson ratio); slot_map [E*B*B] int64 (element
  * order); grad[e] = scale * sum_ab W[slot(e,a,b)] : K_e[a][b](c = 1)
  * (element order), K_e(1) the element's matrix at unit coefficient.
- * plan: a plan of the mesh (its conn and elem_perm).
+ * plan: a plan of the mesh (its conn and elem_perm).  flags
+ * TM_COEF_GRAD_LAME_PARTS (elasticity): grad [2E], grad[e] the contraction
+ * with the unit-lam part of K_e (sum_q jw g_a g_b^T) and grad[E + e] with
+ * the unit-mu part (sum_q jw (g_b g_a^T + g_a . g_b I)), each times scale;
+ * for dL/dnu through lam' = nu / ((1 + nu)(1 - 2 nu)), mu' = 1 / (2 (1 + nu)).
  */
+#define TM_COEF_GRAD_LAME_PARTS 1
 typedef struct tm_coef_grad_args {
     int32_t form;                  /* TM_FORM_DIFFUSION or TM_FORM_ELASTICITY */
-    int32_t reserved;
+    int32_t flags;                 /* 0 or TM_COEF_GRAD_LAME_PARTS */
     int64_t n_points;
     const void* points;            /* device [N*D] float64 */
     const void* weights;           /* device [nnz] or [nnz*D*D] float64 */
     const int64_t* slot_map;       /* device [E*B*B] */
     double scale;
     double poisson;
-    void* grad;                    /* device [E] float64 */
+    void* grad;                    /* device [E] (or [2E], TM_COEF_GRAD_LAME_PARTS) float64 */
     tm_element_tables tables;
     tm_chunk_plan plan;
 } tm_coef_grad_args;

@@ -108,7 +108,7 @@ class AdjointArgs(C.Structure):
 
 class CoefGradArgs(C.Structure):
     _fields_ = [
-        ("form", C.c_int32), ("reserved", C.c_int32),
+        ("form", C.c_int32), ("flags", C.c_int32),
         ("n_points", C.c_int64), ("points", C.c_void_p), ("weights", C.c_void_p), ("slot_map", C.c_void_p),
         ("scale", C.c_double), ("poisson", C.c_double), ("grad", C.c_void_p),
         ("tables", ElementTables), ("plan", ChunkPlan),
@@ -164,6 +164,7 @@ class BatchedMixedArgs(C.Structure):
 
 
 TM_PCG_CONVERGED, TM_PCG_MAX_ITER, TM_PCG_BREAKDOWN = 1, 2, 3
+TM_COEF_GRAD_LAME_PARTS = 1
 TM_BICG_RR, TM_BICG_BB, TM_BICG_ITER, TM_BICG_FLAG = 5, 7, 8, 9
 
 

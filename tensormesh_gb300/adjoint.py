@@ -169,9 +169,11 @@ def _mass_unit(asm, points):
     return assemble_forms([unit], points.detach(), {}, {"rho": 1.0})
 
 
-def coef_grad(topo, points, gvals, slot, form, scale, poisson=0.3):
+def coef_grad(topo, points, gvals, slot, form, scale, poisson=0.3, lame_parts=False):
     """dL/dc_e = scale sum_ab W[slot(e,a,b)] : K_e[a][b](c = 1), element
-    order (``tm_coef_grad``; form TM_FORM_DIFFUSION or TM_FORM_ELASTICITY)."""
+    order (``tm_coef_grad``; form TM_FORM_DIFFUSION or TM_FORM_ELASTICITY).
+    ``lame_parts`` (elasticity): [2E], the contractions with the unit-lam and
+    the unit-mu parts of K_e apart."""
     lib = _lib.load()
     dev = points.device
     pts = points.detach().to(torch.float64).contiguous()
@@ -182,7 +184,8 @@ def coef_grad(topo, points, gvals, slot, form, scale, poisson=0.3):
     a.n_points = topo.n_points
     a.points, a.weights, a.slot_map = _lib.ptr(pts), _lib.ptr(w), _lib.ptr(slot)
     a.scale, a.poisson = float(scale), float(poisson)
-    g = torch.empty(topo.n_elements, dtype=torch.float64, device=dev)
+    a.flags = _lib.TM_COEF_GRAD_LAME_PARTS if lame_parts else 0
+    g = torch.empty((2 if lame_parts else 1) * topo.n_elements, dtype=torch.float64, device=dev)
     a.grad = _lib.ptr(g)
     a.tables = topo.table_struct(dev)
     a.plan = plan.struct()
@@ -191,19 +194,20 @@ def coef_grad(topo, points, gvals, slot, form, scale, poisson=0.3):
 
 
 class ElasticityAssembly(torch.autograd.Function):
-    """values = K(E, points) of an isotropic elasticity form (float64, any
-    element type) as a function of its modulus E (per element or a scalar
-    tensor; ``coefs``: the form's other kernel coefficients, nu and E_scale)
-    and of the node coordinates; the backward runs ``tm_coef_grad`` (dL/dE)
-    and ``tm_adjoint_general`` in elasticity mode (dL/dpoints) on
-    dL/dvalues."""
+    """values = K(E, nu, points) of an isotropic elasticity form (float64,
+    any element type) as a function of its modulus E (per element or a
+    scalar tensor), its Poisson ratio nu (a scalar tensor) and the node
+    coordinates (``coefs``: the form's other kernel coefficients, E_scale);
+    the backward runs ``tm_coef_grad`` (dL/dE, and for dL/dnu its unit-lam
+    and unit-mu parts apart: K = E (lam'(nu) K_lam + mu'(nu) K_mu)) and
+    ``tm_adjoint_general`` in elasticity mode (dL/dpoints) on dL/dvalues."""
 
     @staticmethod
-    def forward(ctx, young, points, asm, coefs):
+    def forward(ctx, young, nu, points, asm, coefs):
         from .assemble import _assemble_on
-        c = dict(coefs, E=young.detach())
+        c = dict(coefs, E=young.detach(), nu=float(nu))
         (values,) = _assemble_on([asm], asm._topo(True), points.detach(), {}, {}, None, None, _coefs=[c])
-        ctx.asm, ctx.nu, ctx.escale = asm, float(c.get("nu", 0.3)), float(c.get("E_scale", 1.0))
+        ctx.asm, ctx.nu, ctx.escale = asm, float(nu), float(c.get("E_scale", 1.0))
         ctx.save_for_backward(points, young)
         return values
 
@@ -215,17 +219,28 @@ class ElasticityAssembly(torch.autograd.Function):
         slot = asm.projector[et].indices.to(points.device)
         topo = asm._topology
         per_element = young.dim() > 0 and young.numel() > 1
-        gy = gp = None
-        if ctx.needs_input_grad[0]:
-            g = coef_grad(topo, points, gvals, slot, _lib.TM_FORM_ELASTICITY, ctx.escale, ctx.nu)
-            gy = (g if per_element else g.sum().reshape(young.shape)).to(young.dtype)
+        gy = gnu = gp = None
         if ctx.needs_input_grad[1]:
+            nu = ctx.nu
+            parts = coef_grad(topo, points, gvals, slot, _lib.TM_FORM_ELASTICITY, ctx.escale, nu, lame_parts=True)
+            pl, pm = parts[:topo.n_elements], parts[topo.n_elements:]
+            lam, mu = nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), 1.0 / (2.0 * (1.0 + nu))
+            dlam = (1.0 + 2.0 * nu * nu) / ((1.0 + nu) ** 2 * (1.0 - 2.0 * nu) ** 2)
+            dmu = -1.0 / (2.0 * (1.0 + nu) ** 2)
+            ey = young.detach().reshape(-1).to(parts.device, torch.float64)
+            gnu = (ey * (dlam * pl + dmu * pm)).sum().reshape(()).to(torch.float64)
+            g = lam * pl + mu * pm
+        elif ctx.needs_input_grad[0]:
+            g = coef_grad(topo, points, gvals, slot, _lib.TM_FORM_ELASTICITY, ctx.escale, ctx.nu)
+        if ctx.needs_input_grad[0]:
+            gy = (g if per_element else g.sum().reshape(young.shape)).to(young.dtype)
+        if ctx.needs_input_grad[2]:
             ey = young.detach().reshape(-1) if per_element else None
             scale = ctx.escale * (1.0 if per_element else float(young.detach().reshape(())))
             _, gp = _adjoint_call(topo, points, ey, scale, _lib.TM_ADJ_E_CSR, weights=gvals, slot=slot,
                                   want_kappa=False, want_points=True, poisson=ctx.nu)
             gp = gp.to(points.dtype)
-        return gy, gp, None, None
+        return gy, gnu, gp, None, None
 
 
 class LoadAssembly(torch.autograd.Function):

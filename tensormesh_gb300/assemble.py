@@ -506,16 +506,19 @@ class ElementAssembler(_AssemblerBase):
                 return self._build_output(values)
             if form == "elasticity":
                 c = self._tm_coefficients(ed, sd, self.elements[et].shape[0])
-                young = c.get("E")
-                if torch.is_tensor(c.get("nu")) and c["nu"].requires_grad:
-                    raise NotImplementedError("gradients with respect to the Poisson ratio are not implemented")
-                if points.requires_grad or (torch.is_tensor(young) and young.requires_grad):
+                young, nu = c.get("E"), c.get("nu", 0.3)
+                nu_grad = torch.is_tensor(nu) and nu.requires_grad
+                if nu_grad and nu.numel() != 1:
+                    raise NotImplementedError("a per-element Poisson ratio is not assembled by tensormesh_gb300")
+                if points.requires_grad or nu_grad or (torch.is_tensor(young) and young.requires_grad):
                     from .adjoint import ElasticityAssembly
                     if not torch.is_tensor(young):
                         young = torch.tensor(1.0 if young is None else float(young), dtype=torch.float64,
                                              device=points.device)
-                    rest = {k: v for k, v in c.items() if k != "E"}
-                    values = ElasticityAssembly.apply(young, points, self, rest)
+                    if not torch.is_tensor(nu):
+                        nu = torch.tensor(float(nu), dtype=torch.float64)
+                    rest = {k: v for k, v in c.items() if k not in ("E", "nu")}
+                    values = ElasticityAssembly.apply(young, nu.reshape(()), points, self, rest)
                     return self._build_output(values)
                 (values,) = assemble_forms([self], points, ed, sd)
                 return self._build_output(values)

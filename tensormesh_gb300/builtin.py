@@ -57,7 +57,8 @@ class LinearElasticityElementAssembler(ElementAssembler):
         raise NotImplementedError("assembled by the elasticity kernel")
 
     def _tm_coefficients(self, ed, sd, E):
-        return {"E": ed.get("E", sd.get("E", self.E)), "nu": float(sd.get("nu", self.nu))}
+        nu = sd.get("nu", self.nu)
+        return {"E": ed.get("E", sd.get("E", self.E)), "nu": nu if torch.is_tensor(nu) else float(nu)}
 
 
 def const_node_assembler(c=1):

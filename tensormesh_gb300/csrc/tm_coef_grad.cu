@@ -16,6 +16,10 @@
 // with lam' = nu / ((1 + nu)(1 - 2 nu)), mu' = 1 / (2 (1 + nu)) and s the
 // modulus scale of the call, that is, per quadrature point
 //     jw_q (lam' g_a^T W g_b + mu' (g_b^T W g_a + tr(W) g_a . g_b)).
+// With flags TM_COEF_GRAD_LAME_PARTS the two parts come back apart, grad[e] =
+// s sum jw_q g_a^T W g_b (unit lam) and grad[E + e] = s sum jw_q (g_b^T W
+// g_a + tr(W) g_a . g_b) (unit mu), for the derivative with respect to the
+// Poisson ratio through lam'(nu) and mu'(nu).
 // One CTA per chunk of the plan, in sub-batches of 32 elements: one thread
 // per (element, quadrature point) computes the Jacobian, its cofactors and
 // the gradients into shared memory; four threads per element then take its
@@ -41,7 +45,7 @@ __host__ __device__ inline size_t eg_smem(int Q) {
     using T = Traits<ET>;
     const TableLayout TL = table_layout(Q, T::B, T::D);
     return align16(sizeof(double) * TL.total) + sizeof(double) * (size_t)kEgSub * Q * (T::B * T::D + 1) +
-           sizeof(double) * kEgSub * kEgPer;
+           2 * sizeof(double) * kEgSub * kEgPer;
 }
 
 template <int ET, bool ELAST>
@@ -60,6 +64,7 @@ __global__ void __launch_bounds__(kEgThreads) k_coef_grad(const tm_coef_grad_arg
     __syncthreads();
     const double nu = a.poisson;
     const double clam = nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), cmu = 1.0 / (2.0 * (1.0 + nu));
+    const bool split = ELAST && (a.flags & TM_COEF_GRAD_LAME_PARTS) != 0;
     const double* pts = static_cast<const double*>(a.points);
     const double* W = static_cast<const double*>(a.weights);
     double* gE = static_cast<double*>(a.grad);
@@ -108,7 +113,7 @@ __global__ void __launch_bounds__(kEgThreads) k_coef_grad(const tm_coef_grad_arg
         // pairs: kEgPer threads per element, pair p = t, t + kEgPer, ...
         {
             const int el = threadIdx.x / kEgPer, t = threadIdx.x - el * kEgPer;
-            double acc = 0.0;
+            double acc = 0.0, acc_mu = 0.0;     // (acc_mu: the unit-mu part when split)
             if (el < ns) {
                 const int64_t e = P.elem_perm[i0 + s0 + el];
                 const double* ge = G + (size_t)el * Q * B * D;
@@ -151,19 +156,30 @@ __global__ void __launch_bounds__(kEgThreads) k_coef_grad(const tm_coef_grad_arg
                                 s2 += gb[r] * Wm[r][c] * ga[c];
                             }
                         }
-                        acc += JW[el * Q + q] * (clam * s1 + cmu * (s2 + trw * dd));
+                        if (split) {
+                            acc += JW[el * Q + q] * s1;
+                            acc_mu += JW[el * Q + q] * (s2 + trw * dd);
+                        } else {
+                            acc += JW[el * Q + q] * (clam * s1 + cmu * (s2 + trw * dd));
+                        }
                     }
                 }
             }
             part[el * kEgPer + t] = acc;
+            part[kEgSub * kEgPer + el * kEgPer + t] = acc_mu;
         }
         __syncthreads();
         if (threadIdx.x < ns) {
             const int el = threadIdx.x;
-            double s = 0.0;
+            double s = 0.0, sm = 0.0;
 #pragma unroll
-            for (int t = 0; t < kEgPer; ++t) s += part[el * kEgPer + t];
-            gE[P.elem_perm[i0 + s0 + el]] = a.scale * s;
+            for (int t = 0; t < kEgPer; ++t) {
+                s += part[el * kEgPer + t];
+                sm += part[kEgSub * kEgPer + el * kEgPer + t];
+            }
+            const int64_t e = P.elem_perm[i0 + s0 + el];
+            gE[e] = a.scale * s;
+            if (split) gE[P.n_elements + e] = a.scale * sm;
         }
         __syncthreads();
     }

@@ -79,6 +79,36 @@ def test_point_gradient_matches_oracle_autograd(etype, per_element, cuda):
     assert rel_fro(E.grad.cpu(), Eo.grad) <= 1e-10
 
 
+@pytest.mark.parametrize("etype", ["triangle", "tetra10", "quad9"])
+def test_poisson_ratio_gradient_matches_oracle_autograd(etype, cuda):
+    """dL/dnu (and dL/dE, dL/dpoints in the same backward) of L = sum W :
+    K(points, E, nu) with nu = 0.27 passed as a tensor in scalar_data,
+    against the oracle's autograd through its Voigt C(E, nu)."""
+    mesh = MESHES[etype]()
+    rng = np.random.default_rng(71)
+    E0 = torch.from_numpy(rng.uniform(0.5, 2.0, mesh.n_elements))
+    gm = mesh.to(cuda)
+    asm = tg.LinearElasticityElementAssembler.from_mesh(gm)
+    D = mesh.points.shape[1]
+    W = torch.from_numpy(rng.uniform(-1.0, 1.0, (asm.edges.shape[1], D, D)))
+    P = gm.points.clone().requires_grad_(True)
+    E = E0.clone().to(cuda).requires_grad_(True)
+    nu = torch.tensor(0.27, dtype=torch.float64, requires_grad=True)
+    K = asm(P, element_data={"E": E}, scalar_data={"nu": nu})
+    vals = K.values.reshape(-1, D, D)
+    (vals * W.to(cuda)).sum().backward()
+    Po = mesh.points.clone().requires_grad_(True)
+    Eo = E0.clone().requires_grad_(True)
+    nuo = torch.tensor(0.27, dtype=torch.float64, requires_grad=True)
+    _, _, Ko = O.assemble_matrix(Po, mesh.elements().long(), mesh.n_points,
+                                 lambda p, c, E: O.element_locals_elasticity(p, c, etype, E, nuo, 2), E=Eo)
+    assert rel_fro(vals.detach().cpu(), Ko.detach()) <= 1e-12
+    (Ko * W).sum().backward()
+    assert abs(float(nu.grad) - float(nuo.grad)) <= 1e-10 * abs(float(nuo.grad))
+    assert rel_fro(E.grad.cpu(), Eo.grad) <= 1e-10
+    assert rel_fro(P.grad.cpu(), Po.grad) <= 1e-10
+
+
 def test_point_gradient_constant_modulus(cuda):
     """Points alone requiring grad, the modulus a plain number of the
     assembler (E = 3, nu = 0.2)."""
