@@ -62,6 +62,7 @@ class SparseMatrix:
         self._sorted = _sorted
         self._csr = None
         self._order = None
+        self._tstruct = {}     # the transpose's CSR view, shared by matrices of this layout
 
     # ------------------------------------------------------------ attributes
     @property
@@ -164,7 +165,7 @@ class SparseMatrix:
                          _block=self._block, _block_row=self._block_row, _block_col=self._block_col,
                          _sorted=self._sorted)
         m._hash, m._row64, m._col64, m._csr = self._hash, self._row64, self._col64, self._csr
-        m._order = self._order
+        m._order, m._tstruct = self._order, self._tstruct
         return m
 
     # ------------------------------------------------------------ CSR view
@@ -210,7 +211,14 @@ class SparseMatrix:
 
     def matvec(self, x: torch.Tensor, out: Optional[torch.Tensor] = None, alpha: float = 1.0,
                beta: float = 0.0) -> torch.Tensor:
+        """A x (``out = alpha A x + beta out`` with ``out``).  Without ``out``
+        the product is differentiable in the values and in x, as the
+        reference's torch sparse product is: dL/dx = A^T dL/dy and dL/dA_ij =
+        dL/dy_i x_j."""
         from .solve import spmv
+        if out is None and alpha == 1.0 and torch.is_grad_enabled() and (
+                self.values.requires_grad or (torch.is_tensor(x) and x.requires_grad)):
+            return _SparseMatVec.apply(self.values, x, self)
         return spmv(self, x, out=out, alpha=alpha, beta=beta)
 
     def __matmul__(self, x: torch.Tensor) -> torch.Tensor:
@@ -289,14 +297,24 @@ class SparseMatrix:
 
     def transpose(self) -> "SparseMatrix":
         """A^T with the same values array (entry k of A is entry k of A^T;
-        its CSR view orders them when it is built)."""
+        its CSR view orders them when it is built, once per layout)."""
         if self._block > 1:
             H = self._block
             vals = self.values.reshape(-1, H, H).transpose(1, 2).reshape(-1)
-            return SparseMatrix(vals, self._col_src, self._row_src, (self.shape[1], self.shape[0]), _block=H,
-                                _block_row=self._block_col, _block_col=self._block_row, _sorted=False)
-        return SparseMatrix(self.values, self.col_indices, self.row_indices, (self.shape[1], self.shape[0]),
-                            _sorted=False)
+            m = SparseMatrix(vals, self._col_src, self._row_src, (self.shape[1], self.shape[0]), _block=H,
+                             _block_row=self._block_col, _block_col=self._block_row, _sorted=False)
+        else:
+            m = SparseMatrix(self.values, self.col_indices, self.row_indices, (self.shape[1], self.shape[0]),
+                             _sorted=False)
+        key = str(self.values.device)
+        hold = self._tstruct.get(key)
+        if hold is None:
+            m._csr_structure()
+            m._row_order()
+            self._tstruct[key] = (m._csr, m._order)
+        else:
+            m._csr, m._order = hold
+        return m
 
     @property
     def T(self) -> "SparseMatrix":
@@ -355,3 +373,39 @@ class SparseMatrix:
     def __repr__(self):
         return (f"SparseMatrix(shape={self.shape}, nnz={self.nnz}, dtype={self.dtype}, "
                 f"device={self.device}{', block=%d' % self._block if self._block > 1 else ''})")
+
+
+class _SparseMatVec(torch.autograd.Function):
+    """y = A x through the SpMV kernel, differentiable in A's values and in
+    x: dL/dx = A^T g (the transpose's own CSR view, built once per layout),
+    dL/dvalues = g_row x_col per stored entry (per block entry, g of the
+    block's rows times x of its columns, for block matrices)."""
+
+    @staticmethod
+    def forward(ctx, values, x, A):
+        from .solve import spmv
+        ctx.A = A
+        ctx.x_dtype = x.dtype
+        ctx.save_for_backward(x)
+        return spmv(A, x.detach())
+
+    @staticmethod
+    def backward(ctx, g):
+        from .solve import spmv
+        (x,) = ctx.saved_tensors
+        A = ctx.A
+        g = g.to(A.values.dtype).contiguous()
+        gv = gx = None
+        if ctx.needs_input_grad[1]:
+            gx = spmv(A.transpose(), g).to(ctx.x_dtype)
+        if ctx.needs_input_grad[0]:
+            xd = x.detach().to(device=g.device, dtype=g.dtype)
+            H = A._block
+            if H > 1:
+                br = A._block_row.to(g.device).long()
+                bc = A._block_col.to(g.device).long()
+                gv = g.view(-1, H)[br][:, :, None] * xd.reshape(-1, H)[bc][:, None, :]
+            else:
+                gv = g[A._row_src.to(g.device).long()] * xd[A._col_src.to(g.device).long()]
+            gv = gv.reshape(A.values.shape)
+        return gv, gx, None
