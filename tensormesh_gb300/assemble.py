@@ -544,11 +544,49 @@ class ElementAssembler(_AssemblerBase):
         _lib.require_cuda(points, "points")
         self.type(points.dtype).to(points.device)
         ed = dict(element_data or {})
-        if torch.is_grad_enabled() and (points.requires_grad or any(
-                torch.is_tensor(v) and v.requires_grad for v in ed.values())):
-            raise NotImplementedError("gradients on meshes with several element types are not implemented")
-        (values,) = assemble_forms([self], points, ed, dict(scalar_data or {}))
+        sd = dict(scalar_data or {})
+        pd = dict(point_data or {})
+        leaves = [points] + [v for v in list(ed.values()) + list(sd.values()) + list(pd.values())
+                             if torch.is_tensor(v)]
+        leaves += [t for v in ed.values() if isinstance(v, dict) for t in v.values() if torch.is_tensor(t)]
+        if pd or (torch.is_grad_enabled() and any(t.requires_grad for t in leaves)):
+            # each type on its own pattern through the single-type path
+            # (per-node coefficients, the adjoint kernels), summed into the
+            # union pattern by a differentiable combine
+            per_type = _split_element_data(self._topology, ed)
+            parts = []
+            for et in self._topology.types:
+                Kt = self._type_view(et)(points, point_data=pd, element_data=per_type[et], scalar_data=sd)
+                H = Kt._block
+                parts.append(Kt.values.reshape(-1, H, H) if H > 1 else Kt.values)
+            return self._build_output(_CombineParts.apply(self._topology, "matrix", *parts))
+        (values,) = assemble_forms([self], points, ed, sd)
         return self._build_output(values)
+
+    def _type_view(self, et: str) -> "ElementAssembler":
+        """This assembler restricted to element type ``et`` of a mixed mesh,
+        on that type's own pattern (its Topology, slot map and edges), so
+        that the single-type path runs on it; kept per type."""
+        views = self.__dict__.setdefault("_tm_type_views", {})
+        if et not in views:
+            import copy
+            topo = self._topology.topos[et]
+            sub = copy.copy(self)
+            object.__setattr__(sub, "_modules", dict(self._modules))
+            object.__setattr__(sub, "_buffers", dict(self._buffers))
+            object.__setattr__(sub, "_parameters", dict(self._parameters))
+            E, B = self.elements[et].shape
+            dev = self.elements[et].device
+            sub.projector = nn.ModuleDict({et: ReduceProjector(indices=topo.slot, from_shape=(E, B, B),
+                                                               to_shape=(topo.nnz,)).to(dev)})
+            sub.transformation = nn.ModuleDict({et: self.transformation[et]})
+            sub.elements = BufferDict({et: self.elements[et]})
+            sub._buffers["edges"] = topo.edges.to(dev)
+            sub.element_types = [et]
+            sub._topology = topo
+            sub.__dict__.pop("_tm_type_views", None)
+            views[et] = sub
+        return views[et]
 
     def _build_output(self, values: torch.Tensor) -> SparseMatrix:
         topo = self._topo(True)
@@ -682,6 +720,28 @@ def _combine(topo: "MixedTopology", kind: str, parts, dev, dt) -> torch.Tensor:
     _lib.check(lib.tm_project_reduce(_lib.dtype_code(dt), n_to, width, _lib.ptr(seg), _lib.ptr(src), _lib.ptr(x),
                                      _lib.ptr(out), _lib.stream_handle(dev)), "tm_project_reduce")
     return out
+
+
+class _CombineParts(torch.autograd.Function):
+    """``_combine`` with its gradient: each entry of a part receives the
+    gradient of the union position ("matrix") or node ("node") it is summed
+    into."""
+
+    @staticmethod
+    def forward(ctx, topo, kind, *parts):
+        ctx.topo, ctx.kind = topo, kind
+        ctx.shapes = [p.shape for p in parts]
+        return _combine(topo, kind, [p.detach() for p in parts], parts[0].device, parts[0].dtype)
+
+    @staticmethod
+    def backward(ctx, g):
+        grads = []
+        for et, shape in zip(ctx.topo.types, ctx.shapes):
+            if ctx.kind == "matrix":
+                grads.append(g[ctx.topo.map_tensor(et, g.device)].reshape(shape))
+            else:
+                grads.append(g.reshape(shape))
+        return (None, None, *grads)
 
 
 def _assemble_mixed(assemblers, topo: "MixedTopology", points, ed, sd):
@@ -894,17 +954,12 @@ class NodeAssembler(_AssemblerBase):
         fn = self.forward if func is None else func
         topo = self._topology
         if isinstance(topo, MixedTopology):
-            if torch.is_grad_enabled() and (points.requires_grad or any(
-                    torch.is_tensor(v) and v.requires_grad for v in list(point_data.values()) +
-                    list(scalar_data.values()))):
-                raise NotImplementedError("gradients on meshes with several element types are not implemented")
             for et in self.element_types[1:]:
                 self.transformation[et].update_points(points)
             parts = [assemble_linear_form(self, fn, points, point_data, scalar_data, topo=topo.topos[et])
                      for et in topo.types]
             width = parts[0].numel() // topo.n_points
-            return _combine(topo, "node", [p.reshape(topo.n_points, width) for p in parts], points.device,
-                            points.dtype).reshape(-1)
+            return _CombineParts.apply(topo, "node", *[p.reshape(topo.n_points, width) for p in parts]).reshape(-1)
         return assemble_linear_form(self, fn, points, point_data, scalar_data)
 
 

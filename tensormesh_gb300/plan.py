@@ -545,6 +545,13 @@ class MixedTopology:
             self._seg[key] = (torch.from_numpy(seg).to(device), torch.from_numpy(src).to(device))
         return self._seg[key]
 
+    def map_tensor(self, et: str, device: torch.device) -> torch.Tensor:
+        """``maps[et]`` (type et's CSR positions -> union positions) on a device."""
+        key = ("map", et, device)
+        if key not in self._seg:
+            self._seg[key] = torch.from_numpy(self.maps[et]).to(device)
+        return self._seg[key]
+
     def row_ptr(self, device: torch.device) -> torch.Tensor:
         """CSR row pointer of the union pattern."""
         if device not in self._row_ptr:

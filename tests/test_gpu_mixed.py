@@ -55,3 +55,61 @@ def test_mixed_quad_triangle_mesh(cuda):
     assert info.converged
     uo = O.solve_dirichlet(Ko, edges[0], edges[1], m.n_points, m.boundary_mask, bo)
     assert rel_fro(cond.recover(ui), uo) <= 1e-10
+
+
+def test_mixed_mesh_gradients(cuda):
+    """Gradients on a quad + triangle mesh (each type through its own
+    adjoint kernels, summed by the differentiable combine): dL/dpoints and
+    dL/dkappa of diffusion (kappa one tensor over all elements), dL/dpoints
+    of mass, dL/dE (a per-type dict) and dL/dpoints of elasticity, and
+    dL/dpoints, dL/df of the nodal load, against the oracle's per-type
+    assembly under autograd."""
+    m = tg.gen_unit_square_mixed(6, jitter=0.2, seed=43)
+    g = m.to(cuda)
+    rng = np.random.default_rng(44)
+    types = list(m.cells)
+    k0 = torch.from_numpy(rng.lognormal(0.0, 1.0, sum(c.shape[0] for c in m.cells.values())))
+    E0 = {et: torch.from_numpy(rng.uniform(0.5, 2.0, c.shape[0])) for et, c in m.cells.items()}
+    f0 = torch.from_numpy(rng.uniform(-1.0, 1.0, m.n_points))
+    asm = tg.LaplaceElementAssembler.from_mesh(g)
+    nnz = asm.edges.shape[1]
+    W = torch.from_numpy(rng.uniform(-1.0, 1.0, nnz))
+    W3 = torch.from_numpy(rng.uniform(-1.0, 1.0, (nnz, 2, 2)))
+    wb = torch.from_numpy(rng.uniform(-1.0, 1.0, m.n_points))
+
+    P = g.points.clone().requires_grad_(True)
+    kap = k0.clone().to(cuda).requires_grad_(True)
+    Ed = {et: e.clone().to(cuda).requires_grad_(True) for et, e in E0.items()}
+    f = f0.clone().to(cuda).requires_grad_(True)
+    K = asm(P, element_data={"kappa": kap})
+    M = tg.MassElementAssembler.from_assembler(asm)(P)
+    El = tg.LinearElasticityElementAssembler.from_assembler(asm, nu=0.3)(P, element_data={"E": Ed})
+    b = tg.LoadNodeAssembler.from_mesh(g)(P, point_data={"f": f})
+    loss = ((K.values * W.to(cuda)).sum() + (M.values * W.to(cuda)).sum()
+            + (El.values.reshape(-1, 2, 2) * W3.to(cuda)).sum() + (b * wb.to(cuda)).sum())
+    loss.backward()
+
+    Po = m.points.clone().requires_grad_(True)
+    ko = k0.clone().requires_grad_(True)
+    Eo = {et: e.clone().requires_grad_(True) for et, e in E0.items()}
+    fo = f0.clone().requires_grad_(True)
+    kparts, o = {}, 0
+    for et in types:
+        n = m.cells[et].shape[0]
+        kparts[et] = ko[o:o + n]
+        o += n
+    _, Ko = O.assemble_mixed(Po, m.cells, m.n_points, {
+        et: (lambda p, c, et=et: O.element_locals_diffusion(p, c, et, kparts[et], 2)) for et in types})
+    _, Mo = O.assemble_mixed(Po, m.cells, m.n_points,
+                             {et: (lambda p, c, et=et: O.element_locals_mass(p, c, et, 2)) for et in types})
+    _, Elo = O.assemble_mixed(Po, m.cells, m.n_points, {
+        et: (lambda p, c, et=et: O.element_locals_elasticity(p, c, et, Eo[et], 0.3, 2)) for et in types})
+    bo = sum(O.assemble_load(Po, c, et, m.n_points, f_nodes=fo) for et, c in m.cells.items())
+    lo = (Ko * W).sum() + (Mo * W).sum() + (Elo.reshape(-1, 2, 2) * W3).sum() + (bo * wb).sum()
+    lo.backward()
+    assert abs(float(loss.detach()) - float(lo.detach())) <= 1e-12 * abs(float(lo.detach()))
+    assert rel_fro(P.grad.cpu(), Po.grad) <= 1e-10
+    assert rel_fro(kap.grad.cpu(), ko.grad) <= 1e-10
+    for et in types:
+        assert rel_fro(Ed[et].grad.cpu(), Eo[et].grad) <= 1e-10
+    assert rel_fro(f.grad.cpu(), fo.grad) <= 1e-10
