@@ -470,6 +470,7 @@ int tm_quadrature_points(int32_t dtype, int64_t n_elements, const int32_t* conn,
 #define TM_ADJ_LOAD_NONE  0
 #define TM_ADJ_LOAD_CONST 1
 #define TM_ADJ_LOAD_NODAL 2
+#define TM_ADJ_LOAD_QUAD  3   /* tm_adjoint_general only: f given per quadrature point */
 typedef struct tm_adjoint_args {
     int32_t dtype;             /* TM_F64 */
     int32_t k_mode;
@@ -484,7 +485,7 @@ typedef struct tm_adjoint_args {
     const void* u;             /* TM_ADJ_K_OUTER: [N] */
     const void* lam;           /* TM_ADJ_K_OUTER and load term: [N] */
     double load_const;         /* TM_ADJ_LOAD_CONST */
-    const void* load_values;   /* TM_ADJ_LOAD_NODAL: [N] */
+    const void* load_values;   /* TM_ADJ_LOAD_NODAL: [N]; TM_ADJ_LOAD_QUAD: [E*Q], element order */
     void* grad_kappa;          /* [E] or NULL */
     void* grad_points;         /* [N*D] or NULL */
     void* workspace;           /* >= tm_adjoint_workspace_bytes() */

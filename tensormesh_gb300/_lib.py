@@ -116,7 +116,7 @@ class CoefGradArgs(C.Structure):
 
 
 TM_ADJ_K_NONE, TM_ADJ_K_CSR, TM_ADJ_K_OUTER, TM_ADJ_M_CSR, TM_ADJ_E_CSR = 0, 1, 2, 3, 4
-TM_ADJ_LOAD_NONE, TM_ADJ_LOAD_CONST, TM_ADJ_LOAD_NODAL = 0, 1, 2
+TM_ADJ_LOAD_NONE, TM_ADJ_LOAD_CONST, TM_ADJ_LOAD_NODAL, TM_ADJ_LOAD_QUAD = 0, 1, 2, 3
 
 
 class CondenseArgs(C.Structure):

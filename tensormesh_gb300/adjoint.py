@@ -69,7 +69,7 @@ def _adjoint_call(topo, points, kappa, kappa_scale, k_mode, weights=None, slot=N
     a.tables = topo.table_struct(dev)
     ws = torch.empty(max(1, lib.tm_adjoint_workspace_bytes(C.byref(a))), dtype=torch.uint8, device=dev)
     a.workspace = _lib.ptr(ws)
-    if topo.etype in ("triangle", "tetra") and k_mode != _lib.TM_ADJ_E_CSR:
+    if topo.etype in ("triangle", "tetra") and k_mode != _lib.TM_ADJ_E_CSR and load_source != _lib.TM_ADJ_LOAD_QUAD:
         _lib.check(lib.tm_adjoint_p1(C.byref(a), _lib.stream_handle(dev)), "tm_adjoint_p1")
     else:
         _lib.check(lib.tm_adjoint_general(C.byref(a), _lib.stream_handle(dev)), "tm_adjoint_general")
@@ -295,6 +295,89 @@ class LoadAssembly(torch.autograd.Function):
                 gs = _run_vector(topo, pts, _lib.TM_SOURCE_NODAL, lt, None, W)
             gs = gs.reshape(s.shape).to(device=s.device, dtype=s.dtype)
         return gp, gs, None, None, None
+
+
+def _jxw(topo, points) -> torch.Tensor:
+    """w_q |det J_q| per (element, quadrature point), element order."""
+    lib = _lib.load()
+    dev = points.device
+    pts = points.detach().to(torch.float64).contiguous()
+    conn = topo.conn32(dev)
+    tb = topo.table_struct(dev)
+    E, Q, B, D = topo.n_elements, tb.n_quad, topo.info.n_basis, topo.info.dim
+    grad = torch.empty(E, Q, B, D, dtype=torch.float64, device=dev)
+    jxw = torch.empty(E, Q, dtype=torch.float64, device=dev)
+    _lib.check(lib.tm_shape_grad_jxw(E, _lib.ptr(conn), _lib.ptr(pts), tb, _lib.ptr(grad), _lib.ptr(jxw),
+                                     _lib.stream_handle(dev)), "tm_shape_grad_jxw")
+    return jxw
+
+
+def _phi(topo, device) -> torch.Tensor:
+    from .element import element_tables
+    return torch.from_numpy(element_tables(topo.etype, topo.quadrature_order)["phi"]).to(device=device,
+                                                                                     dtype=torch.float64)
+
+
+class QuadLoadAssembly(torch.autograd.Function):
+    """b(points, fq)_a = sum_e sum_q w_q |det J_q| phi_a(q) fq[e, q, k]: a
+    source given at the quadrature points (``func`` sources, evaluated in
+    torch on the quadrature points).  dL/dfq = w_q |det J_q| lam(x_q)
+    (lam interpolated with phi); dL/dpoints through |det J_q| by the
+    quadrature-point load term of ``tm_adjoint_general``, per component."""
+
+    @staticmethod
+    def forward(ctx, points, fq, topo, width):
+        from .assemble import _run_vector
+        ctx.topo, ctx.width = topo, width
+        f = fq.detach().contiguous()
+        ctx.save_for_backward(points, f)
+        return _run_vector(topo, points.detach().contiguous(), _lib.TM_SOURCE_QUAD, f, None, width)
+
+    @staticmethod
+    def backward(ctx, gb):
+        points, f = ctx.saved_tensors
+        topo, W = ctx.topo, ctx.width
+        dev = gb.device
+        lam = gb.detach().to(torch.float64).reshape(topo.n_points, W)
+        gp = gf = None
+        if ctx.needs_input_grad[1]:
+            conn = topo.conn32(dev).long()
+            lamq = torch.einsum("ebk,qb->eqk", lam[conn], _phi(topo, dev))
+            gf = (_jxw(topo, points)[..., None] * lamq).reshape(f.shape).to(f.dtype)
+        if ctx.needs_input_grad[0]:
+            E = topo.n_elements
+            fk = f.to(torch.float64).reshape(E, -1, W)
+            for k in range(W):
+                _, g = _adjoint_call(topo, points, None, 1.0, _lib.TM_ADJ_K_NONE, lam=lam[:, k],
+                                     load_source=_lib.TM_ADJ_LOAD_QUAD, load_values=fk[:, :, k].reshape(-1),
+                                     want_kappa=False)
+                gp = g if gp is None else gp + g
+            gp = gp.to(points.dtype)
+        return gp, gf, None, None
+
+
+class QuadPoints(torch.autograd.Function):
+    """x_q = sum_b phi_b(q) x_b per (element, quadrature point)
+    (``tm_quadrature_points``); dL/dx_b = sum_(e,q) phi_b(q) dL/dx_q, formed
+    as the load vector of the quadrature values dL/dx_q / (w_q |det J_q|)."""
+
+    @staticmethod
+    def forward(ctx, points, topo):
+        from .assemble import quadrature_points
+        ctx.topo = topo
+        ctx.save_for_backward(points)
+        return quadrature_points(topo, points.detach().contiguous())
+
+    @staticmethod
+    def backward(ctx, gx):
+        from .assemble import _run_vector
+        (points,) = ctx.saved_tensors
+        topo = ctx.topo
+        D = gx.shape[-1]
+        jxw = _jxw(topo, points)
+        vals = (gx.detach().to(torch.float64) / jxw[..., None]).contiguous()
+        gp = _run_vector(topo, points.detach().to(torch.float64).contiguous(), _lib.TM_SOURCE_QUAD, vals, None, D)
+        return gp.reshape(points.shape).to(points.dtype), None
 
 
 class SparseSolve(torch.autograd.Function):

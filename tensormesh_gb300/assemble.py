@@ -996,13 +996,16 @@ def assemble_linear_form(asm: NodeAssembler, fn: Callable, points: torch.Tensor,
             return LoadAssembly.apply(points, f, topo, _lib.TM_SOURCE_NODAL, width)
         fv = f.detach().reshape(f.shape[0], width).contiguous()
         return _run_vector(topo, pts, _lib.TM_SOURCE_NODAL, fv, None, width)
-    if needs_grad:
-        raise NotImplementedError("gradients of general linear forms are not implemented")
-    # general source g(x, data) * v: evaluate g at the quadrature points
+    # general source g(x, data) * v: evaluate g at the quadrature points (in
+    # torch, so that gradients flow through g to x_q and to its data)
     args = {}
     need_x = "x" in params
     if need_x or any(p.startswith("grad") for p in params):
-        xq = quadrature_points(topo, pts)                     # [E, Q, D]
+        if needs_grad and points.requires_grad:
+            from .adjoint import QuadPoints
+            xq = QuadPoints.apply(points, topo)               # [E, Q, D], differentiable
+        else:
+            xq = quadrature_points(topo, pts)                 # [E, Q, D]
     phi = torch.from_numpy(element_tables(topo.etype, topo.quadrature_order)["phi"]).to(device=dev, dtype=dt)
     conn = topo.conn32(dev).long()
     for p in params:
@@ -1026,6 +1029,9 @@ def assemble_linear_form(asm: NodeAssembler, fn: Callable, points: torch.Tensor,
         g = g.expand(E, Q, *trailing)
     width = int(np.prod(trailing)) if len(trailing) else 1
     fq = g.reshape(E, Q, width).contiguous()
+    if needs_grad or (torch.is_grad_enabled() and fq.requires_grad):    # (tensors captured by the function too)
+        from .adjoint import QuadLoadAssembly
+        return QuadLoadAssembly.apply(points, fq, topo, width)
     return _run_vector(topo, pts, _lib.TM_SOURCE_QUAD, fq, None, width)
 
 

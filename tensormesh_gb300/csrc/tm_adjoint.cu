@@ -332,7 +332,8 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint_gen(const tm_adjoint_ar
             }
             if (lsrc != TM_ADJ_LOAD_NONE) {
                 const double* ph = tab + TL.phi + q * B;
-                double lq = 0.0, fq = lsrc == TM_ADJ_LOAD_CONST ? a.load_const : 0.0;
+                double lq = 0.0, fq = lsrc == TM_ADJ_LOAD_CONST ? a.load_const
+                                    : lsrc == TM_ADJ_LOAD_QUAD ? ldg(fnod + e * Q + q) : 0.0;
 #pragma unroll
                 for (int b = 0; b < B; ++b) {
                     const int64_t node = P.conn[i * B + b];
@@ -658,6 +659,8 @@ extern "C" int tm_adjoint_p1(const tm_adjoint_args* a, tm_stream_t stream) {
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_p1: the load term needs lam");
     if (a->load_source == TM_ADJ_LOAD_NODAL && !a->load_values)
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_p1: nodal load needs load_values");
+    if (a->load_source == TM_ADJ_LOAD_QUAD)
+        return tm_set_error(TM_ERR_UNSUPPORTED, "tm_adjoint_p1: quadrature-point loads go to tm_adjoint_general");
     if (a->grad_points && a->plan.n_shared > 0 && !a->workspace)
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_p1: workspace is null");
     const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -674,12 +677,13 @@ extern "C" int tm_adjoint_general(const tm_adjoint_args* a, tm_stream_t stream) 
     if (a->k_mode == TM_ADJ_E_CSR && !(a->poisson > -1.0 && a->poisson < 0.5))
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_general: Poisson ratio outside (-1, 0.5)");
     if (a->load_source != TM_ADJ_LOAD_NONE && a->load_source != TM_ADJ_LOAD_CONST &&
-        a->load_source != TM_ADJ_LOAD_NODAL)
+        a->load_source != TM_ADJ_LOAD_NODAL && a->load_source != TM_ADJ_LOAD_QUAD)
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_general: unknown load source");
     if (a->load_source != TM_ADJ_LOAD_NONE && a->k_mode == TM_ADJ_E_CSR)
         return tm_set_error(TM_ERR_UNSUPPORTED, "tm_adjoint_general: no load term with elasticity weights");
     if (a->load_source != TM_ADJ_LOAD_NONE && a->plan.n_elements > 0 &&
-        (!a->lam || (a->load_source == TM_ADJ_LOAD_NODAL && !a->load_values)))
+        (!a->lam || ((a->load_source == TM_ADJ_LOAD_NODAL || a->load_source == TM_ADJ_LOAD_QUAD) &&
+                     !a->load_values)))
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_general: a load term needs lam (and load_values)");
     if (a->k_mode != TM_ADJ_K_NONE && (!a->weights || !a->slot_map))
         return tm_set_error(TM_ERR_INVALID_ARG, "tm_adjoint_general: null weights or slot map");

@@ -85,3 +85,45 @@ def test_source_gradient_alone(cuda):
     bo = O.assemble_load(mesh.points, mesh.elements().long(), "quad9", mesh.n_points, f_nodes=fo)
     (bo ** 2).sum().backward()
     assert rel_fro(f.grad.cpu(), fo.grad) <= 1e-10
+
+
+@pytest.mark.parametrize("etype", ["triangle", "tetra", "triangle6", "quad9"])
+def test_function_source_gradients(etype, cuda):
+    """A source given as a function of the quadrature-point coordinates and
+    of a nodal field and a captured tensor: dL/dpoints (through x_q and the
+    measure), dL/dnodal field and dL/dcaptured, against the oracle's
+    restatement under autograd."""
+    mesh = MESHES[etype]()
+    rng = np.random.default_rng(86)
+    a0 = torch.tensor(1.3, dtype=torch.float64)
+    h0 = torch.from_numpy(rng.uniform(0.5, 1.5, mesh.n_points))
+    W = torch.from_numpy(rng.uniform(-1.0, 1.0, mesh.n_points))
+    gm = mesh.to(cuda)
+    a = a0.clone().to(cuda).requires_grad_(True)
+
+    class Src(tg.NodeAssembler):
+        def forward(self, x, v, h):
+            return a * torch.sin(3.0 * x[..., 0]) * (1.0 + x[..., 1] ** 2) * h * v
+
+    P = gm.points.clone().requires_grad_(True)
+    h = h0.clone().to(cuda).requires_grad_(True)
+    b = Src.from_mesh(gm)(P, point_data={"h": h})
+    (b * W.to(cuda)).sum().backward()
+
+    Po = mesh.points.clone().requires_grad_(True)
+    ao = a0.clone().requires_grad_(True)
+    ho = h0.clone().requires_grad_(True)
+    conn = mesh.elements().long()
+    # the oracle integrates func(x_q) * v; the nodal field enters as h(x_q)
+    _, phi, _ = O.shape_tables(etype, 2)
+    hq = torch.einsum("eb,qb->eq", ho[conn], phi)
+    xq = torch.einsum("ebd,qb->eqd", Po[conn], phi)
+    fq = ao * torch.sin(3.0 * xq[..., 0]) * (1.0 + xq[..., 1] ** 2) * hq
+    _, jxw = O.shape_grad_jxw(Po, conn, etype, 2)
+    loc = torch.einsum("qb,eq,eq->eb", phi, fq, jxw)
+    bo = O.reduce_project(conn.reshape(-1), loc.reshape(-1), mesh.n_points)
+    assert rel_fro(b.detach().cpu(), bo.detach()) <= 1e-12
+    (bo * W).sum().backward()
+    assert rel_fro(P.grad.cpu(), Po.grad) <= 1e-10
+    assert rel_fro(h.grad.cpu(), ho.grad) <= 1e-10
+    assert abs(float(a.grad) - float(ao.grad)) <= 1e-10 * abs(float(ao.grad))
