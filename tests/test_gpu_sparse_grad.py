@@ -101,5 +101,5 @@ def test_residual_loss_back_to_kappa(cuda):
         (edges[0].long(), edges[1].long()), Ko, accumulate=True)
     lo = ((Kd @ u0) ** 2).sum()
     lo.backward()
-    assert abs(float(loss) - float(lo)) <= 1e-12 * float(lo)
+    assert abs(float(loss.detach()) - float(lo.detach())) <= 1e-12 * float(lo.detach())
     assert rel_fro(kap.grad.cpu(), ko.grad) <= 1e-10
