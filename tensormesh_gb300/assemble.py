@@ -568,7 +568,8 @@ class ElementAssembler(_AssemblerBase):
         on that type's own pattern (its Topology, slot map and edges), so
         that the single-type path runs on it; kept per type."""
         views = self.__dict__.setdefault("_tm_type_views", {})
-        if et not in views:
+        key = (et, self.elements[et].device)
+        if key not in views:
             import copy
             topo = self._topology.topos[et]
             sub = copy.copy(self)
@@ -585,8 +586,8 @@ class ElementAssembler(_AssemblerBase):
             sub.element_types = [et]
             sub._topology = topo
             sub.__dict__.pop("_tm_type_views", None)
-            views[et] = sub
-        return views[et]
+            views[key] = sub
+        return views[key]
 
     def _build_output(self, values: torch.Tensor) -> SparseMatrix:
         topo = self._topo(True)
