@@ -387,6 +387,24 @@ size_t tm_facet_vector_workspace_bytes(const tm_facet_vector_args* args);
 int tm_assemble_facet_vector(const tm_facet_vector_args* args, tm_stream_t stream);
 
 /*
+ * Gradients of a facet load (float64) for L = sum_i lam_i . out_i: the
+ * node coordinates through the facet measure (grad_points [n_points*D],
+ * overwritten) and, for a source given per point, dL/dvalues = w_q |F_q|
+ * lam(t_q) (grad_values [n_items*Q*width], item order); base as for
+ * tm_assemble_facet_vector (its out is not used; its workspace sized by
+ * tm_facet_adjoint_workspace_bytes).  Replaces autograd through
+ * assemble/facet_assembler.py:123-277.
+ */
+typedef struct tm_facet_adjoint_args {
+    tm_facet_vector_args base;
+    const void* lam;           /* [n_points, width] */
+    void* grad_points;         /* [n_points, D] or NULL */
+    void* grad_values;         /* TM_SOURCE_QUAD: [n_items, Q, width] or NULL */
+} tm_facet_adjoint_args;
+size_t tm_facet_adjoint_workspace_bytes(const tm_facet_adjoint_args* args);
+int tm_facet_adjoint(const tm_facet_adjoint_args* args, tm_stream_t stream);
+
+/*
  * Physical shape gradients and |det J| w per element and quadrature point
  * (Transformation.batch_shape_grad_jxw, element/transformation.py:1219-1276).
  * grad [E*Q*B*D], jxw [E*Q], element order, float64.

@@ -95,6 +95,11 @@ class FacetVectorArgs(C.Structure):
     ]
 
 
+class FacetAdjointArgs(C.Structure):
+    _fields_ = [("base", FacetVectorArgs), ("lam", C.c_void_p), ("grad_points", C.c_void_p),
+                ("grad_values", C.c_void_p)]
+
+
 class AdjointArgs(C.Structure):
     _fields_ = [
         ("dtype", C.c_int32), ("k_mode", C.c_int32), ("load_source", C.c_int32), ("reserved", C.c_int32),
@@ -202,6 +207,8 @@ _SIGNATURES = {
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "tm_facet_vector_workspace_bytes": (C.c_size_t, [C.POINTER(FacetVectorArgs)]),
     "tm_assemble_facet_vector": (C.c_int, [C.POINTER(FacetVectorArgs), C.c_void_p]),
+    "tm_facet_adjoint_workspace_bytes": (C.c_size_t, [C.POINTER(FacetAdjointArgs)]),
+    "tm_facet_adjoint": (C.c_int, [C.POINTER(FacetAdjointArgs), C.c_void_p]),
     "tm_condense": (C.c_int, [C.POINTER(CondenseArgs), C.c_void_p]),
     "tm_project_reduce": (C.c_int, [C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -203,6 +203,164 @@ int facet_type(const tm_facet_vector_args& a, cudaStream_t st) {
     }
 }
 
+// The adjoint of the facet loads for L = sum_i lam_i . b_i (float64): per
+// item and facet quadrature point, with s = sum_w lam_w(t_q) g_w(t_q) (lam
+// interpolated with psi), L_q = w_q |F| s; d|F|/dF_0 = F_0 / |F| for lines,
+// d|F|/dF_0 = (F_1 x c) / |F| and d|F|/dF_1 = (c x F_0) / |F| with c = F_0 x
+// F_1 for triangles; node b of the item receives sum_c w_q s d|F|/dF_c
+// dpsi_b/dt_c (node-plan reduction).  grad_values (a source given per
+// point): w_q |F| lam_w(t_q) per (item, point, component), item order.
+template <int FT, int SRC, int W>
+__global__ void __launch_bounds__(kFacetThreads) k_facet_adjoint(const tm_facet_adjoint_args a) {
+    using T = FacetTraits<FT>;
+    constexpr int FD = T::FD, B = T::B, D = FD + 1;
+    const tm_facet_vector_args& v = a.base;
+    const tm_chunk_plan& P = v.plan;
+    const int CH = P.chunk_elems, Q = v.tables.n_quad;
+    extern __shared__ __align__(16) unsigned char sm[];
+    double* tab = reinterpret_cast<double*>(sm);
+    double* LV = reinterpret_cast<double*>(sm + align16(sizeof(double) * (size_t)Q * (1 + B + FD * B)));
+    const double* tw = tab;
+    const double* tpsi = tab + Q;
+    const double* tdpsi = tab + Q + Q * B;
+    const int n_tab = Q * (1 + B + FD * B);
+    for (int k = threadIdx.x; k < n_tab; k += blockDim.x) tab[k] = v.tables.packed[k];
+    __syncthreads();
+    const int64_t i0 = (int64_t)blockIdx.x * CH;
+    const int ne = (int)min((int64_t)CH, P.n_elements - i0);
+    const double* pts = static_cast<const double*>(v.points);
+    const double* val = static_cast<const double*>(v.values);
+    const double* lam = static_cast<const double*>(a.lam);
+    double* gq = static_cast<double*>(a.grad_values);
+    for (int el = threadIdx.x; el < ne; el += blockDim.x) {
+        const int64_t i = i0 + el;
+        const int64_t item = P.elem_perm[i];
+        int64_t node[B];
+        double X[B][D];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            node[b] = P.conn[i * B + b];
+#pragma unroll
+            for (int d = 0; d < D; ++d) X[b][d] = pts[node[b] * D + d];
+        }
+        double lv[B][D];
+#pragma unroll
+        for (int b = 0; b < B; ++b)
+#pragma unroll
+            for (int d = 0; d < D; ++d) lv[b][d] = 0.0;
+        for (int q = 0; q < Q; ++q) {
+            double F[FD][D];
+#pragma unroll
+            for (int c = 0; c < FD; ++c)
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    double t = 0.0;
+#pragma unroll
+                    for (int b = 0; b < B; ++b) t += tdpsi[(q * FD + c) * B + b] * X[b][d];
+                    F[c][d] = t;
+                }
+            double m, dm[FD][D];
+            if constexpr (FD == 1) {
+                m = sqrt(F[0][0] * F[0][0] + F[0][1] * F[0][1]);
+                dm[0][0] = F[0][0] / m;
+                dm[0][1] = F[0][1] / m;
+            } else {
+                const double c[3] = {F[0][1] * F[1][2] - F[0][2] * F[1][1], F[0][2] * F[1][0] - F[0][0] * F[1][2],
+                                     F[0][0] * F[1][1] - F[0][1] * F[1][0]};
+                m = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+                const double im = 1.0 / m;
+                // F_1 x c and c x F_0
+                dm[0][0] = (F[1][1] * c[2] - F[1][2] * c[1]) * im;
+                dm[0][1] = (F[1][2] * c[0] - F[1][0] * c[2]) * im;
+                dm[0][2] = (F[1][0] * c[1] - F[1][1] * c[0]) * im;
+                dm[1][0] = (c[1] * F[0][2] - c[2] * F[0][1]) * im;
+                dm[1][1] = (c[2] * F[0][0] - c[0] * F[0][2]) * im;
+                dm[1][2] = (c[0] * F[0][1] - c[1] * F[0][0]) * im;
+            }
+            double s = 0.0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                double lw = 0.0, g = 0.0;
+#pragma unroll
+                for (int b = 0; b < B; ++b) lw += tpsi[q * B + b] * lam[node[b] * W + w];
+                if constexpr (SRC == TM_SOURCE_CONST) {
+                    g = v.const_value[w];
+                } else if constexpr (SRC == TM_SOURCE_NODAL) {
+#pragma unroll
+                    for (int b = 0; b < B; ++b) g += tpsi[q * B + b] * val[node[b] * W + w];
+                } else {
+                    g = val[(item * Q + q) * W + w];
+                }
+                s += lw * g;
+                if (gq) gq[(item * Q + q) * W + w] = tw[q] * m * lw;
+            }
+            const double f = tw[q] * s;
+#pragma unroll
+            for (int b = 0; b < B; ++b)
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    double t = 0.0;
+#pragma unroll
+                    for (int c = 0; c < FD; ++c) t += dm[c][d] * tdpsi[(q * FD + c) * B + b];
+                    lv[b][d] += f * t;
+                }
+        }
+        double* out = LV + (size_t)el * B * D;
+#pragma unroll
+        for (int b = 0; b < B; ++b)
+#pragma unroll
+            for (int d = 0; d < D; ++d) out[b * D + d] = lv[b][d];
+    }
+    __syncthreads();
+    if (a.grad_points) node_reduce<double, D>(P, LV, static_cast<double*>(a.grad_points), v.workspace);
+}
+
+template <int FT, int SRC, int W>
+int run_facet_adjoint(const tm_facet_adjoint_args& a, cudaStream_t st) {
+    using T = FacetTraits<FT>;
+    constexpr int D = T::FD + 1;
+    const tm_facet_vector_args& v = a.base;
+    const size_t smem = align16(sizeof(double) * (size_t)v.tables.n_quad * (1 + T::B + T::FD * T::B)) +
+                        sizeof(double) * (size_t)v.plan.chunk_elems * T::B * D;
+    if (smem > 227 * 1024) return tm_set_error(TM_ERR_TOO_LARGE, "tm_facet_adjoint: chunk too large");
+    if (a.grad_points) {
+        if (cudaMemsetAsync(a.grad_points, 0, sizeof(double) * (size_t)v.n_points * D, st) != cudaSuccess)
+            return status("cudaMemsetAsync");
+        if (v.plan.n_shared > 0) {
+            void* counters = static_cast<unsigned char*>(v.workspace) + node_counters_offset<double>(v.plan, D);
+            if (cudaMemsetAsync(counters, 0, sizeof(int32_t) * (size_t)v.plan.n_shared, st) != cudaSuccess)
+                return status("cudaMemsetAsync");
+        }
+    }
+    if (v.plan.n_chunks == 0) return TM_OK;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_facet_adjoint<FT, SRC, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+        return status("cudaFuncSetAttribute");
+    k_facet_adjoint<FT, SRC, W><<<v.plan.n_chunks, kFacetThreads, smem, st>>>(a);
+    return status("k_facet_adjoint");
+}
+
+template <int FT, int SRC>
+int adjoint_width(const tm_facet_adjoint_args& a, cudaStream_t st) {
+    switch (a.base.width) {
+        case 1: return run_facet_adjoint<FT, SRC, 1>(a, st);
+        case 2: return run_facet_adjoint<FT, SRC, 2>(a, st);
+        case 3: return run_facet_adjoint<FT, SRC, 3>(a, st);
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_facet_adjoint: width must be 1..3");
+    }
+}
+
+template <int FT>
+int adjoint_source(const tm_facet_adjoint_args& a, cudaStream_t st) {
+    switch (a.base.source) {
+        case TM_SOURCE_CONST: return adjoint_width<FT, TM_SOURCE_CONST>(a, st);
+        case TM_SOURCE_NODAL: return adjoint_width<FT, TM_SOURCE_NODAL>(a, st);
+        case TM_SOURCE_QUAD: return adjoint_width<FT, TM_SOURCE_QUAD>(a, st);
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_facet_adjoint: unknown source kind");
+    }
+}
+
 int facet_basis(int ft) {
     switch (ft) {
         case TM_FACET_LINE2: return 2;
@@ -246,4 +404,37 @@ extern "C" int tm_assemble_facet_vector(const tm_facet_vector_args* a, tm_stream
     if (a->dtype == TM_F64) return facet_type<double>(*a, st);
     if (a->dtype == TM_F32) return facet_type<float>(*a, st);
     return tm_set_error(TM_ERR_INVALID_ARG, "tm_assemble_facet_vector: dtype must be TM_F64 or TM_F32");
+}
+
+extern "C" size_t tm_facet_adjoint_workspace_bytes(const tm_facet_adjoint_args* a) {
+    if (!a) return 0;
+    const int D = (a->base.tables.facet_type == TM_FACET_TRI3 || a->base.tables.facet_type == TM_FACET_TRI6) ? 3 : 2;
+    return node_counters_offset<double>(a->base.plan, D) + sizeof(int32_t) * (size_t)a->base.plan.n_shared;
+}
+
+extern "C" int tm_facet_adjoint(const tm_facet_adjoint_args* a, tm_stream_t stream) {
+    if (!a) return tm_set_error(TM_ERR_INVALID_ARG, "tm_facet_adjoint: null args");
+    const tm_facet_vector_args& v = a->base;
+    if (v.dtype != TM_F64) return tm_set_error(TM_ERR_UNSUPPORTED, "tm_facet_adjoint: float64 only");
+    const int B = facet_basis(v.tables.facet_type);
+    if (B < 0) return tm_set_error(TM_ERR_UNSUPPORTED, "tm_facet_adjoint: unknown facet type");
+    const tm_chunk_plan& P = v.plan;
+    if (P.n_basis != B || P.n_local != B)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_facet_adjoint: plan is not a node plan over this facet type");
+    if (P.chunk_elems < 1 || P.chunk_elems > 4096 || v.width < 1 || v.width > 3 || v.n_points < 0)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_facet_adjoint: bad chunk size, width or n_points");
+    if (P.n_elements > 0 && (!v.points || !a->lam || !v.tables.packed || !P.elem_perm || !P.conn))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_facet_adjoint: null points, lam, tables or plan");
+    if ((v.source == TM_SOURCE_NODAL || v.source == TM_SOURCE_QUAD) && P.n_elements > 0 && !v.values)
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_facet_adjoint: values is null");
+    if (a->grad_points && P.n_shared > 0 && (!P.shared_ptr || !P.shared_target || !v.workspace))
+        return tm_set_error(TM_ERR_INVALID_ARG, "tm_facet_adjoint: shared arrays or workspace is null");
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    switch (v.tables.facet_type) {
+        case TM_FACET_LINE2: return adjoint_source<TM_FACET_LINE2>(*a, st);
+        case TM_FACET_LINE3: return adjoint_source<TM_FACET_LINE3>(*a, st);
+        case TM_FACET_TRI3: return adjoint_source<TM_FACET_TRI3>(*a, st);
+        case TM_FACET_TRI6: return adjoint_source<TM_FACET_TRI6>(*a, st);
+        default: return tm_set_error(TM_ERR_UNSUPPORTED, "tm_facet_adjoint: unknown facet type");
+    }
 }

@@ -150,42 +150,114 @@ class FacetAssembler(nn.Module):
         if form is None:
             self.forward()                       # raises: no built-in form
         dev, dt = points.device, points.dtype
-        pts = points.detach().contiguous()
         kind, arg = form
+        # the source as a tensor: constant [W], nodal [N, W] or per point
+        # [items, Q, W] (a function of the points' quadrature coordinates)
+        if kind == "const":
+            src = arg if torch.is_tensor(arg) else torch.as_tensor(arg, dtype=torch.float64)
+            src = src.reshape(-1)
+        elif kind == "nodal":
+            f = point_data[arg].to(device=dev, dtype=dt)
+            src = f.reshape(self.n_points, -1)
+        else:
+            grad_x = torch.is_grad_enabled() and points.requires_grad
+            xq = self.quadrature_points(points if grad_x else points.detach())
+            src = torch.as_tensor(arg(xq), device=dev, dtype=dt)
+            src = src.reshape(self.n_items, xq.shape[1], -1)
+        if torch.is_grad_enabled() and (points.requires_grad or src.requires_grad):
+            return FacetLoad.apply(points, src, self, kind)
+        return self._run(points.detach(), kind, src.detach())
+
+    def _args(self, pts: torch.Tensor, kind: str, src: torch.Tensor):
+        dev, dt = pts.device, pts.dtype
         a = _lib.FacetVectorArgs()
         a.dtype = _lib.dtype_code(dt)
         a.n_points = self.n_points
         a.points = _lib.ptr(pts)
         keep = [pts]
         if kind == "const":
-            c = torch.as_tensor(arg, dtype=torch.float64).reshape(-1)
+            c = src.detach().to(torch.float64).reshape(-1)
             if c.numel() > 3:
                 raise ValueError("a constant facet load has 1..3 components")
             a.source, a.width = _lib.TM_SOURCE_CONST, c.numel()
             for i in range(c.numel()):
                 a.const_value[i] = float(c[i])
         elif kind == "nodal":
-            f = point_data[arg].to(device=dev, dtype=dt)
-            f2 = f.reshape(self.n_points, -1).contiguous()
+            f2 = src.detach().to(device=dev, dtype=dt).contiguous()
             a.source, a.width, a.values = _lib.TM_SOURCE_NODAL, f2.shape[1], _lib.ptr(f2)
             keep.append(f2)
         else:
-            xq = self.quadrature_points(pts)
-            g = arg(xq)
-            g2 = torch.as_tensor(g, device=dev, dtype=dt).reshape(self.n_items, xq.shape[1], -1).contiguous()
+            g2 = src.detach().to(device=dev, dtype=dt).contiguous()
             a.source, a.width, a.values = _lib.TM_SOURCE_QUAD, g2.shape[2], _lib.ptr(g2)
             keep.append(g2)
         if not 1 <= a.width <= 3:
             raise ValueError(f"facet loads have 1..3 components, got {a.width}")
-        plan = self._plan(dev)
-        a.plan = plan.struct()
+        a.plan = self._plan(dev).struct()
         a.tables = self._table_struct(dev)
+        return a, keep
+
+    def _run(self, pts: torch.Tensor, kind: str, src: torch.Tensor) -> torch.Tensor:
+        dev, dt = pts.device, pts.dtype
+        pts = pts.contiguous()
+        a, keep = self._args(pts, kind, src)
         lib = _lib.load()
         ws = torch.empty(max(1, lib.tm_facet_vector_workspace_bytes(C.byref(a))), dtype=torch.uint8, device=dev)
         out = torch.empty(self.n_points, a.width, dtype=dt, device=dev)
         a.workspace, a.out = _lib.ptr(ws), _lib.ptr(out)
         _lib.check(lib.tm_assemble_facet_vector(C.byref(a), _lib.stream_handle(dev)), "tm_assemble_facet_vector")
         return out.reshape(-1)
+
+
+class FacetLoad(torch.autograd.Function):
+    """A facet load vector as a function of the node coordinates and of its
+    source (constant [W], nodal [N, W] or per point [items, Q, W]): the
+    backward runs ``tm_facet_adjoint`` (the points through the facet
+    measure; dL/dvalues of a per-point source) and, for constant and nodal
+    sources, the forward kernel (dL/dc_w = lam_w . b(c = 1); dL/df = the
+    facet load of the nodal source lam)."""
+
+    @staticmethod
+    def forward(ctx, points, src, fa, kind):
+        ctx.fa, ctx.kind = fa, kind
+        ctx.save_for_backward(points, src)
+        return fa._run(points.detach(), kind, src.detach())
+
+    @staticmethod
+    def backward(ctx, gb):
+        points, src = ctx.saved_tensors
+        fa, kind = ctx.fa, ctx.kind
+        dev = gb.device
+        pts = points.detach().to(torch.float64).contiguous()
+        s64 = src.detach().to(device=dev, dtype=torch.float64)
+        W = (s64.numel() if kind == "const" else s64.shape[-1])
+        lam = gb.detach().to(torch.float64).reshape(fa.n_points, W).contiguous()
+        gp = gs = None
+        want_q = kind == "func" and ctx.needs_input_grad[1]
+        if ctx.needs_input_grad[0] or want_q:
+            base, keep = fa._args(pts, kind, s64)
+            a = _lib.FacetAdjointArgs()
+            a.base = base
+            a.lam = _lib.ptr(lam)
+            D = points.shape[1]
+            gpts = torch.empty(fa.n_points, D, dtype=torch.float64, device=dev) if ctx.needs_input_grad[0] else None
+            # (contiguous: the kernel writes [items, Q, W] in order, whatever
+            # the source's strides)
+            gq = torch.empty(s64.shape, dtype=torch.float64, device=dev) if want_q else None
+            a.grad_points, a.grad_values = _lib.ptr(gpts), _lib.ptr(gq)
+            lib = _lib.load()
+            ws = torch.empty(max(1, lib.tm_facet_adjoint_workspace_bytes(C.byref(a))), dtype=torch.uint8, device=dev)
+            a.base.workspace = _lib.ptr(ws)
+            _lib.check(lib.tm_facet_adjoint(C.byref(a), _lib.stream_handle(dev)), "tm_facet_adjoint")
+            if gpts is not None:
+                gp = gpts.to(points.dtype)
+            if gq is not None:
+                gs = gq.to(src.dtype)
+        if ctx.needs_input_grad[1] and kind == "const":
+            b1 = fa._run(pts, "const", torch.ones(W, dtype=torch.float64)).reshape(fa.n_points, W)
+            gs = (lam * b1).sum(0).reshape(src.shape).to(device=src.device, dtype=src.dtype)
+        elif ctx.needs_input_grad[1] and kind == "nodal":
+            gs = fa._run(pts, "nodal", lam).reshape(src.shape).to(src.dtype)
+        return gp, gs, None, None
 
 
 def const_facet_assembler(c=1):

@@ -76,3 +76,60 @@ def test_facet_multichunk_deterministic_and_float32(cuda):
     assert rel_fro(b32.double(), ref) <= 1e-5
     with pytest.raises(NotImplementedError):
         tg.FacetAssembler.from_mesh(dm)(dm.points)
+
+
+FGRAD_MESHES = {
+    "triangle": lambda: tg.gen_unit_square(5, jitter=0.2, seed=131),
+    "triangle6": lambda: tg.gen_unit_square(3, order=2, jitter=0.1, seed=132),
+    "quad9": lambda: tg.gen_unit_square(3, order=2, jitter=0.1, seed=133, cell="quad"),
+    "tetra": lambda: tg.gen_unit_cube(3, jitter=0.2, seed=134),
+    "tetra10": lambda: tg.gen_unit_cube(2, order=2, jitter=0.1, seed=135),
+}
+
+
+@pytest.mark.parametrize("etype", list(FGRAD_MESHES))
+@pytest.mark.parametrize("kind", ["const", "nodal", "func"])
+def test_facet_load_gradients(etype, kind, cuda):
+    """dL/dpoints (through the facet measure, tm_facet_adjoint, and for a
+    function source through x_q) and dL/dsource of L = w . b_facet, against
+    the oracle's facet load under autograd (1e-10)."""
+    mesh = FGRAD_MESHES[etype]()
+    gm = mesh.to(cuda)
+    rng = np.random.default_rng(136)
+    N = mesh.n_points
+    c0 = torch.tensor([0.7, -1.1], dtype=torch.float64)
+    f0 = torch.from_numpy(rng.uniform(-1.0, 1.0, N))
+    a0 = torch.tensor(1.4, dtype=torch.float64)
+    width = 2 if kind == "const" else 1
+    W = torch.from_numpy(rng.uniform(-1.0, 1.0, N * width))
+    P = gm.points.clone().requires_grad_(True)
+    if kind == "const":
+        c = c0.clone().requires_grad_(True)
+        b = tg.const_facet_assembler(c).from_mesh(gm)(P)
+        src = c
+    elif kind == "nodal":
+        f = f0.clone().to(cuda).requires_grad_(True)
+        b = tg.LoadFacetAssembler.from_mesh(gm)(P, point_data={"f": f})
+        src = f
+    else:
+        a = a0.clone().to(cuda).requires_grad_(True)
+        b = tg.func_facet_assembler(lambda x: a * torch.sin(2.0 * x[..., 0]) * (1 + x[..., 1] ** 2)).from_mesh(gm)(P)
+        src = a
+    (b * W.to(cuda)).sum().backward()
+
+    Po = mesh.points.clone().requires_grad_(True)
+    conn = mesh.elements()
+    if kind == "const":
+        so = c0.clone().requires_grad_(True)
+        bo = O.assemble_facet_load(Po, conn, etype, mesh.boundary_mask, N, 2, const=so).reshape(-1)
+    elif kind == "nodal":
+        so = f0.clone().requires_grad_(True)
+        bo = O.assemble_facet_load(Po, conn, etype, mesh.boundary_mask, N, 2, f_nodes=so)
+    else:
+        so = a0.clone().requires_grad_(True)
+        bo = O.assemble_facet_load(Po, conn, etype, mesh.boundary_mask, N, 2,
+                                   func=lambda x: so * torch.sin(2.0 * x[..., 0]) * (1 + x[..., 1] ** 2))
+    assert rel_fro(b.detach().cpu(), bo.detach()) <= 1e-12
+    (bo * W).sum().backward()
+    assert rel_fro(P.grad.cpu(), Po.grad) <= 1e-10
+    assert rel_fro(src.grad.detach().cpu().reshape(-1), so.grad.reshape(-1)) <= 1e-10
