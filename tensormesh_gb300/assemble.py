@@ -671,6 +671,15 @@ def assemble_forms(assemblers, points: Optional[torch.Tensor] = None, element_da
     for a in assemblers[1:]:
         if a._topology is not first._topology:
             raise ValueError("fused assembly needs assemblers that share a topology (from_assembler)")
+    leaves = [points] + list((element_data or {}).values()) + list((scalar_data or {}).values())
+    leaves += [t for v in (element_data or {}).values() if isinstance(v, dict) for t in v.values()]
+    if torch.is_grad_enabled() and any(torch.is_tensor(t) and t.requires_grad for t in leaves):
+        # differentiable: each form through its own call (its adjoint kernels)
+        out = []
+        for a in assemblers:
+            m = a(points, element_data=element_data, scalar_data=scalar_data)
+            out.append(m.values.reshape(-1, m._block, m._block) if m._block > 1 else m.values)
+        return out
     et = first.element_types[0]
     trans = first.transformation[et]
     if points is None:

@@ -169,6 +169,9 @@ class BatchedDiffusion:
         concatenated, BatchStatus).  ``precision="mixed"``: iterative
         refinement with float32 inner solves (``inner_rtol``: their residual
         reduction; at most ``max_outer`` corrections)."""
+        if torch.is_grad_enabled() and (kappa.requires_grad or f.requires_grad):
+            raise NotImplementedError("batched solves are not differentiable; use the per-mesh path "
+                                      "(assembler, Condenser, SparseMatrix.solve) for gradients")
         kappa = kappa.to(device=self.device, dtype=self.dtype).contiguous()
         f = f.to(device=self.device, dtype=self.dtype).contiguous()
         x, work, queue, status = self._buffers()
@@ -200,6 +203,9 @@ class BatchedDiffusion:
     def replay(self, kappa: torch.Tensor, f: torch.Tensor):
         if self._graph is None:
             raise RuntimeError("call capture() first")
+        if torch.is_grad_enabled() and (kappa.requires_grad or f.requires_grad):
+            raise NotImplementedError("batched solves are not differentiable; use the per-mesh path "
+                                      "(assembler, Condenser, SparseMatrix.solve) for gradients")
         self._kappa.copy_(kappa.to(self._kappa.dtype), non_blocking=True)
         self._f.copy_(f.to(self._f.dtype), non_blocking=True)
         self._graph.replay()

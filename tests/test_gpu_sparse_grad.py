@@ -103,3 +103,24 @@ def test_residual_loss_back_to_kappa(cuda):
     lo.backward()
     assert abs(float(loss.detach()) - float(lo.detach())) <= 1e-12 * float(lo.detach())
     assert rel_fro(kap.grad.cpu(), ko.grad) <= 1e-10
+
+
+def test_fused_assembly_with_gradients(cuda):
+    """assemble_forms with a coefficient requiring grad runs each form's
+    differentiable call: the same values, gradients equal to the
+    assemblers' own."""
+    mesh = tg.gen_unit_cube(3, jitter=0.2, seed=87).to(cuda)
+    rng = np.random.default_rng(88)
+    k0 = torch.from_numpy(rng.lognormal(0.0, 1.0, mesh.n_elements)).to(cuda)
+    K_asm = tg.LaplaceElementAssembler.from_mesh(mesh)
+    M_asm = tg.MassElementAssembler.from_assembler(K_asm)
+    W = torch.from_numpy(rng.uniform(-1.0, 1.0, K_asm.edges.shape[1])).to(cuda)
+    with torch.no_grad():
+        K0, M0 = tg.assemble_forms([K_asm, M_asm], mesh.points, {"kappa": k0})
+    k1 = k0.clone().requires_grad_(True)
+    K1, M1 = tg.assemble_forms([K_asm, M_asm], mesh.points, {"kappa": k1})
+    assert rel_fro(K1.detach(), K0) <= 1e-13 and rel_fro(M1.detach(), M0) <= 1e-13
+    ((K1 + M1) * W).sum().backward()
+    k2 = k0.clone().requires_grad_(True)
+    (K_asm(mesh.points, element_data={"kappa": k2}).values * W).sum().backward()
+    assert rel_fro(k1.grad, k2.grad) <= 1e-14
