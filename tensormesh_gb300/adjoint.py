@@ -392,8 +392,13 @@ class SparseSolve(torch.autograd.Function):
         from .solve import bicgstab_solve, pcg_solve
         kw = dict(kwargs)
         method = kw.pop("method", "cg")
+        info_out = kw.pop("_info_out", None)       # a list that receives the forward solve's SolveInfo
+        kw.pop("return_info", None)
         solver = pcg_solve if method == "cg" else bicgstab_solve
-        x = solver(A.with_values(values.detach()), b.detach(), **kw)
+        x, info = solver(A.with_values(values.detach()), b.detach(), return_info=True, **kw)
+        if info_out is not None:
+            info_out.append(info)
+        kw.pop("x0", None)
         ctx.A, ctx.kwargs, ctx.solver, ctx.method = A, kw, solver, method
         ctx.save_for_backward(values, x)
         return x

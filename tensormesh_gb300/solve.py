@@ -56,6 +56,15 @@ def spmv(A, x: torch.Tensor, out: Optional[torch.Tensor] = None, alpha: float = 
     return out
 
 
+def _differentiable(A, b, return_info, **kw):
+    """A solve whose values or right-hand side require grad: through
+    ``SparseSolve`` (the adjoint solve with A^T in the backward)."""
+    from .adjoint import SparseSolve
+    out = []
+    x = SparseSolve.apply(A.values, b, A, dict(kw, _info_out=out))
+    return (x, out[0]) if return_info else x
+
+
 @dataclass
 class SolveInfo:
     iterations: int
@@ -72,6 +81,9 @@ def pcg_solve(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, rtol: float
     (``tm_pcg_iterate_until``: grid barriers between phases, stop on the
     device at convergence); a batch is at most ``max(check_every, 2000)``
     iterations, and the host reads the scalars between batches."""
+    if torch.is_grad_enabled() and (A.values.requires_grad or (torch.is_tensor(b) and b.requires_grad)):
+        return _differentiable(A, b, return_info, method="cg", x0=x0, rtol=rtol, max_iter=max_iter,
+                               check_every=check_every)
     lib = _register()
     _lib.require_cuda(A.values, "SparseMatrix values")
     dev, dt = A.values.device, A.values.dtype
@@ -122,6 +134,9 @@ def bicgstab_solve(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, atol: 
     (``tm_bicgstab_iterate``); the host reads the residual between batches
     of ``check_every`` iterations.  Where the reference warns that it did
     not converge, this returns the iterate as well (``return_info`` tells)."""
+    if torch.is_grad_enabled() and (A.values.requires_grad or (torch.is_tensor(b) and b.requires_grad)):
+        return _differentiable(A, b, return_info, method="bicgstab", x0=x0, atol=atol, rtol=rtol,
+                               max_iter=max_iter, check_every=check_every)
     lib = _register()
     _lib.require_cuda(A.values, "SparseMatrix values")
     dev, dt = A.values.device, A.values.dtype

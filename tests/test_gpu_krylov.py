@@ -111,3 +111,29 @@ def test_solve_accepts_the_inherited_keywords(cuda):
     x = A.solve(b2, is_spd=False, tol=1e-12)
     xs = spl.spsolve(As.tocsc(), d["b"])
     assert np.linalg.norm(x.cpu().numpy() - xs) <= 1e-10 * np.linalg.norm(xs)
+
+
+def test_direct_solver_calls_are_differentiable(cuda):
+    """pcg_solve / bicgstab_solve with a right-hand side or values that
+    require grad go through the adjoint solve (as SparseMatrix.solve does):
+    the same gradients, and return_info still reports the forward solve."""
+    mesh = tg.gen_unit_square(10, jitter=0.2, seed=91).to(cuda)
+    K = tg.LaplaceElementAssembler.from_mesh(mesh)(mesh.points)
+    b = tg.const_node_assembler(1.0).from_mesh(mesh)(mesh.points)
+    Kc, bc = tg.Condenser(mesh.boundary_mask)(K, b)
+    w = torch.linspace(-1.0, 1.0, bc.numel(), dtype=torch.float64, device=cuda)
+    grads = []
+    # (BiCGSTAB keeps the reference's absolute breakdown thresholds, 1e-12:
+    # its right-hand side and the loss weights are scaled up; dL/db does not
+    # depend on b and is linear in the weights)
+    for solve, scale in ((lambda A, r: tg.pcg_solve(A, r, rtol=1e-13, return_info=True), 1.0),
+                         (lambda A, r: tg.bicgstab_solve(A, r, atol=0.0, rtol=1e-9, return_info=True), 1e6),
+                         (lambda A, r: (A.solve(r, rtol=1e-13), None), 1.0)):
+        r = (bc.detach() * scale).requires_grad_(True)
+        x, info = solve(Kc, r)
+        if info is not None:
+            assert info.relative_residual <= 1e-7
+        (x * w * scale).sum().backward()
+        grads.append(r.grad.clone() / scale)
+    assert rel_fro(grads[0], grads[2]) <= 1e-10
+    assert rel_fro(grads[1], grads[2]) <= 1e-6
