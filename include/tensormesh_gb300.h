@@ -686,7 +686,9 @@ typedef struct tm_batched_pcg_args {
 int tm_batched_pcg(const tm_batched_pcg_args* args, tm_stream_t stream);
 
 /*
- * The same batch (float64 matrix) by mixed-precision iterative refinement:
+ * The same batch (float64 matrix) by mixed-precision iterative refinement
+ * (no counterpart in the reference, whose per-mesh solves run the Jacobi
+ * CG of sparse/solve/torch_solve.py:70-127 in the matrix's precision):
  * per system, the float64 residual r = b - A x, a float32 Jacobi-PCG solve
  * of A d = r / ||r|| until its residual falls by inner_rtol, x += ||r|| d in
  * float64, until the true residual meets ||b - A x|| <= rtol ||b|| (the
